@@ -1,0 +1,305 @@
+/*
+ * pk_oracle.c -- CPU restatement of PaKman's k-mer counting, frequency-histogram
+ * cutoff and macro-node construction, used as the CHECKER for the GPU path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only the tests, the smoke check and the bench's CPU
+ * baseline load this library; the GPU product never links or calls it.  It is
+ * pinned against the reference's own binaries (built from the reference sources by
+ * oracle/ref/Makefile) on the committed fixtures under tests/golden/.
+ *
+ * Semantics restated (file:line refer to the reference tree):
+ *  - record layout: the buffer is scanned from its first '>'; every record is a
+ *    header line starting with '>' followed by exactly one sequence line
+ *    (src/kmer_counting.cpp:2920-2935, 3144).  A record start that is not '>' is
+ *    an assertion failure in the reference; here it returns PKO_EFORMAT.  Once a
+ *    sequence line would start with fewer than k bytes left in the buffer, the
+ *    reference stops (src/kmer_counting.cpp:2935) -- no later record is checked.
+ *  - base codes: code(c) = (c >> 1) & 7 (char_to_el, includes/distribute_kmers.h:
+ *    784-786): A=0 C=1 T=2 G=3, lowercase alike, 'N' = 7.  The window is rolled as
+ *    kmer = ((kmer << 2) | code) & KMER_MASK (kmer_shift, :798-805), so an 'N' ORs
+ *    into the previous base's low bit and windows spanning 'N' are still counted.
+ *    No reverse complement is taken anywhere.
+ *  - every window of k bytes inside one sequence line is one k-mer instance
+ *    (src/kmer_counting.cpp:2967-3017).  The table is sorted ascending by k-mer
+ *    and unique, with the number of instances as its count (transfer_kmers +
+ *    SortAndAggregate, src/kmer_counting.cpp:254-352, 169-250).
+ *  - drop_n (an extension used for the long-k workload): windows containing
+ *    'N' or 'n' are skipped.  It equals running the reference on the same reads
+ *    split into separate records at every 'N'.
+ *  - histogram: hist[c] = #entries with count c, for c < t; cutoff = position of
+ *    the first minimum of hist[1..t) (std::min_element, src/kmer_histogram.cpp:
+ *    84-115); t == 1 gives cutoff 1.  Entries with count >= cutoff are kept
+ *    (src/kmer_histogram.cpp:140).  No kept entry -> PKO_EEMPTY (the reference
+ *    calls MPI_Abort, src/kmer_histogram.cpp:189-200).
+ *  - macro-nodes: node set = sorted unique {x >> 2, x & SUCC_MASK} over kept x
+ *    (src/mn_construct.cpp:225-285; the "^1" at :234 is shifted out).  Node P gets
+ *    a suffix entry (ext = last base of x, count) for each kept x with x >> 2 == P
+ *    (:346-391); node S gets a prefix entry (ext = first base of x, count) for each
+ *    kept x with x & SUCC_MASK == S (:407-457).  Suffixes come out in ascending ext
+ *    order in the reference; prefix order is unspecified there (unstable sort by
+ *    suffix only, :303) and is ascending ext here.  Output per node: key and four
+ *    u32 counts per side indexed by ext, 0 meaning absent.
+ *  - visit value (:75-79) = ceil(count / coverage), exact in integers.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef unsigned __int128 u128;
+
+typedef struct {
+  uint64_t lo, hi;
+} pko_key;
+
+enum { PKO_OK = 0, PKO_EFORMAT = -1, PKO_EARG = -2, PKO_ENOMEM = -3, PKO_EEMPTY = -4 };
+
+static inline u128 key_mask(int bits) {
+  return bits >= 128 ? ~(u128)0 : (((u128)1 << bits) - 1);
+}
+
+/* ---------------------------------------------------------------- sorting ---- */
+/* Stable LSD radix sort of (key, aux) records on the low `bits` bits of key. */
+typedef struct {
+  u128 key;
+  uint32_t aux;
+} rec_t;
+
+static int radix_sort_recs(rec_t* a, size_t n, int bits) {
+  if (n < 2 || bits <= 0) return PKO_OK;
+  rec_t* b = (rec_t*)malloc(n * sizeof(rec_t));
+  if (!b) return PKO_ENOMEM;
+  size_t* cnt = (size_t*)malloc(65536 * sizeof(size_t));
+  if (!cnt) { free(b); return PKO_ENOMEM; }
+  rec_t *src = a, *dst = b;
+  for (int sh = 0; sh < bits; sh += 16) {
+    memset(cnt, 0, 65536 * sizeof(size_t));
+    for (size_t i = 0; i < n; i++) cnt[(unsigned)(src[i].key >> sh) & 0xffff]++;
+    size_t s = 0;
+    for (int d = 0; d < 65536; d++) { size_t c = cnt[d]; cnt[d] = s; s += c; }
+    for (size_t i = 0; i < n; i++) dst[cnt[(unsigned)(src[i].key >> sh) & 0xffff]++] = src[i];
+    rec_t* t = src; src = dst; dst = t;
+  }
+  if (src != a) memcpy(a, src, n * sizeof(rec_t));
+  free(b);
+  free(cnt);
+  return PKO_OK;
+}
+
+static int radix_sort_u64(uint64_t* a, size_t n, int bits) {
+  if (n < 2 || bits <= 0) return PKO_OK;
+  uint64_t* b = (uint64_t*)malloc(n * sizeof(uint64_t));
+  size_t* cnt = (size_t*)malloc(65536 * sizeof(size_t));
+  if (!b || !cnt) { free(b); free(cnt); return PKO_ENOMEM; }
+  uint64_t *src = a, *dst = b;
+  for (int sh = 0; sh < bits; sh += 16) {
+    memset(cnt, 0, 65536 * sizeof(size_t));
+    for (size_t i = 0; i < n; i++) cnt[(src[i] >> sh) & 0xffff]++;
+    size_t s = 0;
+    for (int d = 0; d < 65536; d++) { size_t c = cnt[d]; cnt[d] = s; s += c; }
+    for (size_t i = 0; i < n; i++) dst[cnt[(src[i] >> sh) & 0xffff]++] = src[i];
+    uint64_t* t = src; src = dst; dst = t;
+  }
+  if (src != a) memcpy(a, src, n * sizeof(uint64_t));
+  free(b);
+  free(cnt);
+  return PKO_OK;
+}
+
+/* ------------------------------------------------------------ extraction ---- */
+/*
+ * Walk the records exactly as the reference's sliding window does and hand every
+ * k-mer instance to `emit`.  Returns PKO_OK or PKO_EFORMAT.
+ */
+typedef void (*emit_fn)(void* ctx, u128 kmer);
+
+static int walk_kmers(const uint8_t* buf, size_t n, int k, int drop_n, emit_fn emit, void* ctx,
+                      size_t* n_reads) {
+  const u128 mask = key_mask(2 * k);
+  size_t p = 0, reads = 0;
+  while (p < n && buf[p] != '>') p++;
+  for (size_t i = p; i < n; i++) reads += (buf[i] == '>');
+  if (n_reads) *n_reads = reads;
+  while (p < n) {
+    if (buf[p] != '>') return PKO_EFORMAT;
+    while (p < n && buf[p] != '\n') p++; /* skip the header line */
+    p++;
+    if (p + (size_t)k > n) break;
+    u128 kmer = 0;
+    int run = 0; /* bases since the last dropped 'N' (drop_n only) */
+    for (int i = 0; i < k - 1 && buf[p] != '\n'; i++, p++) {
+      uint8_t c = buf[p];
+      kmer = ((kmer << 2) | (u128)((c >> 1) & 7)) & mask;
+      run = (drop_n && (c == 'N' || c == 'n')) ? 0 : run + 1;
+    }
+    while (p < n && buf[p] != '\n') {
+      uint8_t c = buf[p++];
+      kmer = ((kmer << 2) | (u128)((c >> 1) & 7)) & mask;
+      run = (drop_n && (c == 'N' || c == 'n')) ? 0 : run + 1;
+      if (!drop_n || run >= k) emit(ctx, kmer);
+    }
+    p++; /* skip the newline */
+  }
+  return PKO_OK;
+}
+
+typedef struct {
+  uint64_t* k64;
+  rec_t* k128;
+  size_t n, cap;
+  int wide;
+  int oom;
+} collect_t;
+
+static void collect_emit(void* c_, u128 kmer) {
+  collect_t* c = (collect_t*)c_;
+  if (c->oom) return;
+  if (c->n == c->cap) {
+    size_t nc = c->cap ? 2 * c->cap : (1u << 20);
+    void* p = c->wide ? realloc(c->k128, nc * sizeof(rec_t)) : realloc(c->k64, nc * sizeof(uint64_t));
+    if (!p) { c->oom = 1; return; }
+    if (c->wide) c->k128 = (rec_t*)p; else c->k64 = (uint64_t*)p;
+    c->cap = nc;
+  }
+  if (c->wide) { c->k128[c->n].key = kmer; c->k128[c->n].aux = 0; }
+  else c->k64[c->n] = (uint64_t)kmer;
+  c->n++;
+}
+
+static void count_emit(void* c_, u128 kmer) {
+  (void)kmer;
+  (*(size_t*)c_)++;
+}
+
+/* Number of k-mer instances (windows) without building the table. */
+int pko_count_windows(const uint8_t* buf, size_t n, int k, int drop_n, size_t* n_windows,
+                      size_t* n_reads) {
+  if (k < 2 || k > 64) return PKO_EARG;
+  size_t w = 0;
+  int rc = walk_kmers(buf, n, k, drop_n, count_emit, &w, n_reads);
+  *n_windows = w;
+  return rc;
+}
+
+/*
+ * Build the sorted unique (k-mer, count) table.  keys/counts are malloc'd here and
+ * released with pko_free.
+ */
+int pko_count(const uint8_t* buf, size_t n, int k, int drop_n, pko_key** keys_out,
+              uint32_t** counts_out, size_t* n_unique, size_t* n_windows, size_t* n_reads) {
+  if (k < 2 || k > 64) return PKO_EARG;
+  collect_t c;
+  memset(&c, 0, sizeof(c));
+  c.wide = k > 32;
+  int rc = walk_kmers(buf, n, k, drop_n, collect_emit, &c, n_reads);
+  if (c.oom) rc = PKO_ENOMEM;
+  if (rc != PKO_OK) { free(c.k64); free(c.k128); return rc; }
+  *n_windows = c.n;
+  if (c.wide) rc = radix_sort_recs(c.k128, c.n, 2 * k);
+  else rc = radix_sort_u64(c.k64, c.n, 2 * k);
+  if (rc != PKO_OK) { free(c.k64); free(c.k128); return rc; }
+  /* run-length aggregation (SortAndAggregate_InPlace, src/kmer_counting.cpp:169-190) */
+  size_t u = 0;
+  pko_key* keys = (pko_key*)malloc((c.n ? c.n : 1) * sizeof(pko_key));
+  uint32_t* cnts = (uint32_t*)malloc((c.n ? c.n : 1) * sizeof(uint32_t));
+  if (!keys || !cnts) { free(keys); free(cnts); free(c.k64); free(c.k128); return PKO_ENOMEM; }
+  for (size_t i = 0; i < c.n;) {
+    u128 key = c.wide ? c.k128[i].key : (u128)c.k64[i];
+    size_t j = i + 1;
+    while (j < c.n && (c.wide ? c.k128[j].key : (u128)c.k64[j]) == key) j++;
+    keys[u].lo = (uint64_t)key;
+    keys[u].hi = (uint64_t)(key >> 64);
+    cnts[u] = (uint32_t)(j - i);
+    u++;
+    i = j;
+  }
+  free(c.k64);
+  free(c.k128);
+  *keys_out = keys;
+  *counts_out = cnts;
+  *n_unique = u;
+  return PKO_OK;
+}
+
+/* Frequency histogram over [0, t) and the first-minimum cutoff over [1, t). */
+int pko_cutoff(const uint32_t* counts, size_t u, int t, uint64_t* hist, int* cutoff) {
+  if (t < 1) return PKO_EARG;
+  memset(hist, 0, (size_t)t * sizeof(uint64_t));
+  for (size_t i = 0; i < u; i++)
+    if (counts[i] < (uint32_t)t) hist[counts[i]]++;
+  int best = 1;
+  for (int c = 2; c < t; c++)
+    if (hist[c] < hist[best]) best = c;
+  *cutoff = best; /* t == 1: empty range, std::min_element returns the end -> 1 */
+  return PKO_OK;
+}
+
+/*
+ * Macro-nodes from the table.  node_keys: M keys; suf/pre: 4*M counts indexed by
+ * ext code (0 = absent).  Returns PKO_EEMPTY when no entry reaches the cutoff.
+ */
+int pko_macro_nodes(const pko_key* keys, const uint32_t* counts, size_t u, int k,
+                    uint32_t cutoff, pko_key** node_keys, uint32_t** suf_out, uint32_t** pre_out,
+                    size_t* n_nodes, size_t* n_kept) {
+  if (k < 2 || k > 64) return PKO_EARG;
+  const int nb = 2 * (k - 1);
+  const u128 succ_mask = key_mask(nb);
+  size_t v = 0;
+  for (size_t i = 0; i < u; i++) v += counts[i] >= cutoff;
+  *n_kept = v;
+  if (v == 0) return PKO_EEMPTY;
+  /* suffix-side items in key order (grouped by x >> 2, ext ascending) */
+  rec_t* sfx = (rec_t*)malloc(v * sizeof(rec_t));
+  rec_t* pfx = (rec_t*)malloc(v * sizeof(rec_t));
+  uint32_t* sc = (uint32_t*)malloc(v * sizeof(uint32_t));
+  uint32_t* pc = (uint32_t*)malloc(v * sizeof(uint32_t));
+  if (!sfx || !pfx || !sc || !pc) { free(sfx); free(pfx); free(sc); free(pc); return PKO_ENOMEM; }
+  size_t j = 0;
+  for (size_t i = 0; i < u; i++) {
+    if (counts[i] < cutoff) continue;
+    u128 x = ((u128)keys[i].hi << 64) | keys[i].lo;
+    sfx[j].key = x >> 2;
+    sfx[j].aux = (uint32_t)(x & 3); /* last base */
+    sc[j] = counts[i];
+    pfx[j].key = x & succ_mask;
+    pfx[j].aux = (uint32_t)(x >> nb) | ((uint32_t)j << 2); /* first base, original slot */
+    j++;
+  }
+  /* prefix-side items sorted by suffix (k-1)-mer; stable, so ties stay in ext order */
+  int rc = radix_sort_recs(pfx, v, nb);
+  if (rc != PKO_OK) { free(sfx); free(pfx); free(sc); free(pc); return rc; }
+  for (size_t i = 0; i < v; i++) pc[i] = sc[pfx[i].aux >> 2];
+  /* merge the two key-ordered streams into nodes */
+  pko_key* nk = (pko_key*)malloc(2 * v * sizeof(pko_key));
+  uint32_t* ns = (uint32_t*)calloc(8 * v, sizeof(uint32_t));
+  uint32_t* np = (uint32_t*)calloc(8 * v, sizeof(uint32_t));
+  if (!nk || !ns || !np) {
+    free(sfx); free(pfx); free(sc); free(pc); free(nk); free(ns); free(np);
+    return PKO_ENOMEM;
+  }
+  size_t a = 0, b = 0, m = 0;
+  while (a < v || b < v) {
+    u128 ka = a < v ? sfx[a].key : ~(u128)0;
+    u128 kb = b < v ? pfx[b].key : ~(u128)0;
+    u128 node = (a < v && (b >= v || ka <= kb)) ? ka : kb;
+    nk[m].lo = (uint64_t)node;
+    nk[m].hi = (uint64_t)(node >> 64);
+    while (a < v && sfx[a].key == node) { ns[4 * m + sfx[a].aux] = sc[a]; a++; }
+    while (b < v && pfx[b].key == node) { np[4 * m + (pfx[b].aux & 3)] = pc[b]; b++; }
+    m++;
+  }
+  free(sfx); free(pfx); free(sc); free(pc);
+  *node_keys = nk;
+  *suf_out = ns;
+  *pre_out = np;
+  *n_nodes = m;
+  return PKO_OK;
+}
+
+/* visit value (src/mn_construct.cpp:75-79): (int)ceil((double)count / coverage). */
+int pko_visit(int count, int coverage) {
+  int q = count / coverage, r = count % coverage;
+  if (r != 0 && ((r > 0) == (coverage > 0))) q++;
+  return q;
+}
+
+void pko_free(void* p) { free(p); }
