@@ -1,0 +1,341 @@
+#!/usr/bin/env python3
+"""Throughput of PaKman's k-mer counting -> histogram cutoff -> macro-node path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload bacterial|plain|longk] [--scale S]
+
+One step = one pass of the whole path (count, cutoff, macro-nodes) over one read
+set.  The default workload is the 4.6 Mbp genome / 80x / 100 bp / k=32 read set
+(seeded synthetic reads, ~254M k-mer windows).  `value` is k-mer windows per
+second with the FASTA bytes already resident in HBM; `e2e` is the same metric
+through the C ABI with the FASTA in pinned host memory and the macro-node table
+copied back every step.  Under torchrun each rank runs an independent replica
+(the path has no cross-device exchange on one GPU per job); value = all ranks'
+windows / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k-mers/sec count+macro-node on 1 GB300 (% HBM roofline); served p50/p99 latency"
+UNIT = "k-mers/s"
+KERNELS_PER_STEP = 9  # line scan, tile prefix, bucket count, column prefix, bucket prefix,
+#                       scatter, bucket table, cutoff, macro-nodes
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["bacterial", "plain", "longk"], default="bacterial")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-windows", type=int, default=60_000_000)
+    return ap.parse_args()
+
+
+def workload(name: str, scale: float):
+    from pakman_plus_gb300 import synth
+    return {"bacterial": synth.config2, "plain": synth.config1, "longk": synth.config3}[name](scale)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, bus_id):
+        self.lines = []
+        self.proc = None
+        self.bus_id = bus_id
+
+    def start(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.bus_id:
+            cmd += ["-i", self.bus_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=5)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def stage_bytes(stage: str, F: int, N: int, U: int, M: int, W: int, t: int, B: int, G: int) -> int:
+    """Algorithmic bytes one launch of a stage must move (read + write)."""
+    return {
+        "line_scan": F,
+        "bucket_count": F + 4 * G * B,
+        "bucket_offsets": 3 * 4 * G * B,
+        "scatter": F + N * W,
+        "bucket_table": N * W + U * (W + 4),
+        "cutoff": 8 * t,
+        "macro_nodes": 2 * U * (W + 4) + M * (W + 32),
+    }.get(stage, 0)
+
+
+def pipeline_bytes(F, N, U, V, M, W):
+    """Whole-path model: F + 2NW + 2U(W+4) + 4U + 4V(W+4) + M(W+32)."""
+    return F + 2 * N * W + 2 * U * (W + 4) + 4 * U + 4 * V * (W + 4) + M * (W + 32)
+
+
+def cpu_baseline(rs, sample_windows: int):
+    """Oracle port (single thread) on the first reads of the same workload."""
+    from oracle import pk_oracle as po
+    lines = rs.fasta.split(b"\n")
+    per_read = max(1, rs.read_len - rs.k + 1)
+    reads = min(rs.n_reads, max(1, sample_windows // per_read))
+    sample = b"\n".join(lines[: 2 * reads]) + b"\n"
+    t0 = time.perf_counter()
+    pipe = po.run(sample, rs.k, rs.t, rs.drop_n)
+    dt = time.perf_counter() - t0
+    n = pipe.table.n_windows
+    return {"value": n / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"first {reads} reads ({n} k-mer windows) of the same read set, "
+                      f"count + cutoff + macro-nodes, {dt:.2f} s"}
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    rs = workload(args.workload, args.scale)
+    from oracle import pk_oracle as po
+    per_read = max(1, rs.read_len - rs.k + 1)
+    reads = min(rs.n_reads, max(1, args.cpu_sample_windows // per_read))
+    lines = rs.fasta.split(b"\n")
+    sample = b"\n".join(lines[: 2 * reads]) + b"\n"
+    exe = po.build_reference(rs.k) if os.path.isdir(po.REFERENCE_TREE) else None
+    if exe is None:
+        exe_path = os.path.join(po.REF_OUT, f"pakman_ref_k{rs.k}")
+        exe = exe_path if os.path.exists(exe_path) and os.access(exe_path, os.X_OK) else None
+    kind = "reference" if exe else "port"
+    threads = os.cpu_count() or 1
+    times, n_windows = [], 0
+    for step in range(args.warmup + args.steps):
+        if kind == "reference":
+            r = po.run_reference(sample, rs.k, rs.read_len, rs.coverage, rs.t, threads=threads,
+                                 want_mn=False)
+            dt = r.seconds.get("count_s", 0.0) + r.seconds.get("mn_s", 0.0)
+            n_windows = int(r.table_counts.sum())
+        else:
+            t0 = time.perf_counter()
+            pipe = po.run(sample, rs.k, rs.t, rs.drop_n)
+            dt = time.perf_counter() - t0
+            n_windows = pipe.table.n_windows
+        if step >= args.warmup:
+            times.append(dt)
+    ms = 1000.0 * sum(times) / len(times)
+    value = n_windows / (ms / 1000.0)
+    cores = threads if kind == "reference" else 1
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64" if rs.k <= 32 else "u128",
+            "data": "synthetic",
+            "config": {"workload": rs.name, "reads": rs.n_reads, "read_len": rs.read_len, "k": rs.k,
+                       "t": rs.t, "sample_reads": reads},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": f"first {reads} reads ({n_windows} k-mer windows) per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+
+    import numpy as np
+    import torch
+
+    import pakman_plus_gb300 as pk
+    from pakman_plus_gb300 import build as pkbuild
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pkbuild.build()
+    rs = workload(args.workload, args.scale)
+    F = len(rs.fasta)
+    host = torch.frombuffer(bytearray(rs.fasta), dtype=torch.uint8)
+    d_fa = host.to(f"cuda:{local}")
+    ctx = pk.Context(local)
+    stream = torch.cuda.Stream(device=local)
+    job = pk.Job(ctx, stream=stream.cuda_stream)
+    params = pk.default_params(k=rs.k, num_buckets=rs.t, coverage=rs.coverage, read_length=rs.read_len,
+                               drop_n=int(rs.drop_n), batch_kmers=rs.batch)
+    job.enable_timing(True)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        s = job.run_device(d_fa.data_ptr(), F, params)
+    props = torch.cuda.get_device_properties(local)
+    bus = None
+    try:
+        bus = "%08x:%02x:%02x.0" % (props.pci_domain_id, props.pci_bus_id, props.pci_device_id)
+    except AttributeError:
+        pass
+    sampler = ClockSampler(bus)
+    stage_acc = {}
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        s = job.run_device(d_fa.data_ptr(), F, params)
+        for name, ms in job.stage_times().items():
+            stage_acc[name] = stage_acc.get(name, 0.0) + ms
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms_step = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms_step], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = s.n_windows * world / (ms_step / 1000.0)
+
+    # end to end through the C ABI: pinned host FASTA in, macro-node table out
+    e2e = None
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 10))
+    pinned = torch.empty(F, dtype=torch.uint8, pin_memory=True)
+    pinned.copy_(host)
+    pin_np = pinned.numpy()
+    W = 8 if rs.k <= 32 else 16
+    job.run(pin_np, params)
+    job.macro_nodes()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        se = job.run(pin_np, params)
+        mn = job.macro_nodes()
+    t1 = time.perf_counter()
+    e2e_ms = 1000.0 * (t1 - t0) / e2e_steps
+    if dist:
+        t = torch.tensor([e2e_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": se.n_windows * world / (e2e_ms / 1000.0), "unit": UNIT,
+           "h2d_bytes_per_step": F, "d2h_bytes_per_step": int(mn.keys.nbytes + mn.suffix_counts.nbytes
+                                                                + mn.prefix_counts.nbytes + 48),
+           "ms_per_step": e2e_ms, "steps": e2e_steps}
+
+    if rank == 0:
+        peak, peak_kind = peaks()
+        U, V, M, N = s.n_unique, s.n_kept, s.n_nodes, s.n_windows
+        B = 1 << 15
+        G = props.multi_processor_count
+        avg = {k: v / args.steps for k, v in stage_acc.items()}
+        kern = {k: v for k, v in avg.items() if k != "h2d" and v > 0}
+        dom = max(kern, key=kern.get)
+        dom_bytes = stage_bytes(dom, F, N, U, M, W, rs.t, B, G)
+        achieved = dom_bytes / (kern[dom] / 1000.0) / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tp):
+            tj = json.load(open(tp))
+            ent = tj.get(rs.name, {}).get(dom)
+            if ent:
+                traffic = ent.get("dram_bytes_per_launch")
+        pb = pipeline_bytes(F, N, U, V, M, W)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64" if rs.k <= 32 else "u128",
+            "data": "synthetic",
+            "config": {"workload": rs.name, "genome_bp": rs.genome_len, "reads": rs.n_reads,
+                       "read_len": rs.read_len, "k": rs.k, "t": rs.t, "coverage": rs.coverage,
+                       "fasta_bytes": F, "kmer_windows": N, "distinct_kmers": U, "kept_kmers": V,
+                       "macro_nodes": M, "cutoff": s.cutoff, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (FASTA and key buffers > 126 MB)",
+                       "pipeline_bytes_model": pb,
+                       "pipeline_hbm_frac": pb / (ms_step / 1000.0) / 1e9 / peak,
+                       "stage_ms": {k: round(v, 4) for k, v in avg.items()}},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"},
+            "e2e": e2e,
+            "gpu_launches": KERNELS_PER_STEP * args.steps,
+            "clocks": clocks,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(rs, args.cpu_sample_windows)
+        print(json.dumps(line), flush=True)
+    job.close()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

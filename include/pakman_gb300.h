@@ -1,0 +1,157 @@
+/*
+ * pakman_gb300.h -- C ABI of the GB300 k-mer counting / histogram cutoff /
+ * macro-node construction path of PaKman.
+ *
+ * Plain C types only (pointers, sizes, fixed-width integers); no CUDA or torch
+ * types appear in any signature (a CUDA stream is passed as `void*`).  Every
+ * call returns a pk_status; the text of the last failure on the calling thread
+ * is available from pk_last_error().  There is no CPU fallback: without a CUDA
+ * device pk_ctx_create() fails with PK_ERR_NO_DEVICE.
+ *
+ * Which reference interface each entry point replaces (paths inside the PaKman
+ * tree):
+ *   pk_count / pk_count_device   perform_kmer_counting(const char*, size_t)
+ *                                 src/kmer_counting.cpp:3351 (fills kmer_proc_buf,
+ *                                 src/distribute_kmers.cpp:87, sorted and unique)
+ *   pk_copy_table_packed          the kmer_proc_buf contents as packed KmerPairs
+ *                                 (includes/distribute_kmers.h:702-714)
+ *   pk_cutoff                     construct_kmer_histogram, src/kmer_histogram.cpp:72-115
+ *                                 (histogram of counts < t, first-minimum cutoff)
+ *   pk_build_macro_nodes          construct_macro_nodes / begin_mnode_construction,
+ *                                 src/mn_construct.cpp:212-532
+ *   pk_copy_macro_nodes           the MN_map contents (MacroNode suffix/prefix counts,
+ *                                 includes/distribute_kmers.h:533-658)
+ *   pk_run / pk_run_device        the driver sequence src/distribute_kmers.cpp:147-168
+ */
+#ifndef PAKMAN_GB300_H
+#define PAKMAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pk_status {
+  PK_OK = 0,
+  PK_ERR_INVALID = 1,   /* bad argument (k outside 2..64, t < 1, null pointer, ...) */
+  PK_ERR_FORMAT = 2,    /* a record start is not '>' (the reference asserts in its
+                           l-mer and k-mer passes, src/kmer_counting.cpp:407, 2920) */
+  PK_ERR_EMPTY = 3,     /* no k-mer reaches the cutoff (the reference calls
+                           MPI_Abort, src/kmer_histogram.cpp:189-200) */
+  PK_ERR_NOMEM = 4,     /* HBM budget of the context exceeded or allocation failed */
+  PK_ERR_CUDA = 5,      /* CUDA runtime error */
+  PK_ERR_STATE = 6,     /* call out of order (e.g. macro-nodes before counting) */
+  PK_ERR_LIMIT = 7,     /* input beyond a documented limit (>= 2^32 k-mer windows) */
+  PK_ERR_DEVICE = 8,    /* a kernel reported failure (bounded wait expired,
+                           on-chip capacity exceeded); results are not valid */
+  PK_ERR_BUSY = 9,      /* serving: no capacity right now, retry later */
+  PK_ERR_NO_DEVICE = 10 /* no usable CUDA device */
+} pk_status;
+
+typedef struct pk_ctx pk_ctx;
+typedef struct pk_job pk_job;
+
+/* Run parameters.  Field meanings follow the reference's command line
+ * (src/distribute_kmers.cpp:217-313) and build knobs (Makefile:1-20). */
+typedef struct pk_params {
+  int32_t k;            /* k-mer length (ksize; WINDW_SIZE = k-1), 2..64 */
+  int32_t lmer_length;  /* LMER_LENGTH, default 8 */
+  int32_t num_buckets;  /* -t: histogram bins, default 21 */
+  int32_t coverage;     /* -c: visit count = ceil(count / coverage); non-zero */
+  int32_t read_length;  /* -r: accepted and passed through; the counter does not use it */
+  int32_t drop_n;       /* 0: reference behaviour (an 'N' is code 7 OR-ed into the
+                           window); 1: windows containing 'N'/'n' are skipped */
+  uint64_t batch_kmers; /* -b: MAX_KMER_COUNT; the table is the same for any value */
+  int32_t bucket_bits;  /* partition digits (leading key bits); 0 = automatic */
+  int32_t reserved[7];
+} pk_params;
+
+/* Counts reported by a run. */
+typedef struct pk_summary {
+  uint64_t n_reads;     /* '>' bytes in the buffer (the reference's "Total number of reads") */
+  uint64_t n_windows;   /* k-mer instances counted (sum of the table's counts) */
+  uint64_t n_unique;    /* distinct k-mers (table rows) */
+  uint64_t n_kept;      /* rows with count >= cutoff */
+  uint64_t n_nodes;     /* macro-nodes */
+  uint32_t cutoff;      /* histogram cutoff (first minimum over [1, t)) */
+  int32_t key_bytes;    /* 8 for k <= 32, 16 for k <= 64 */
+} pk_summary;
+
+void pk_params_default(pk_params* p);
+const char* pk_status_string(pk_status s);
+/* Text of the last failure on the calling thread ("" if none). */
+const char* pk_last_error(void);
+
+/* ---- context: one device, one HBM budget ------------------------------------- */
+pk_status pk_ctx_create(int device, uint64_t hbm_budget_bytes, pk_ctx** out);
+void pk_ctx_destroy(pk_ctx* ctx);
+pk_status pk_ctx_memory(pk_ctx* ctx, uint64_t* used_bytes, uint64_t* budget_bytes);
+
+/* ---- job: one read set; device buffers are held until reset/destroy ------------ */
+/* stream: a cudaStream_t to run on, or NULL for a stream owned by the job. */
+pk_status pk_job_create(pk_ctx* ctx, void* stream, pk_job** out);
+void pk_job_destroy(pk_job* job);
+pk_status pk_job_reset(pk_job* job);
+pk_status pk_job_sync(pk_job* job);
+/* Bytes of device memory the job holds now. */
+pk_status pk_job_memory(pk_job* job, uint64_t* bytes);
+
+/* ---- counting: replaces perform_kmer_counting -------------------------------------
+ * fasta/d_fasta: one or more records, each a '>' header line followed by exactly one
+ * sequence line (the reference's layout).  d_fasta must be 16-byte aligned device
+ * memory; it is read, never written, and must stay valid until the job is synced.
+ * Returns once the table is enqueued; the table stays resident on the device. */
+pk_status pk_count(pk_job* job, const char* fasta, uint64_t n, const pk_params* p);
+pk_status pk_count_device(pk_job* job, const void* d_fasta, uint64_t n, const pk_params* p);
+pk_status pk_table_info(pk_job* job, uint64_t* n_unique, uint64_t* n_windows, uint64_t* n_reads);
+/* Table rows ascending by k-mer: keys as uint64 (k <= 32) or {uint64 lo, hi}
+ * (k > 32), counts as uint32.  capacity = rows the buffers hold. */
+pk_status pk_copy_table(pk_job* job, void* keys, uint32_t* counts, uint64_t capacity);
+/* Same rows as packed KmerPairs {kmer_t seq; int k_count;} (12 or 20 bytes). */
+pk_status pk_copy_table_packed(pk_job* job, void* pairs, uint64_t capacity);
+/* Device pointers of the resident table (valid until reset/destroy). */
+pk_status pk_table_device(pk_job* job, const void** d_keys, const uint32_t** d_counts);
+
+/* ---- histogram cutoff: replaces construct_kmer_histogram ----------------------------
+ * hist (optional) receives num_buckets bins.  Returns PK_ERR_EMPTY when no row
+ * reaches the cutoff (cutoff, hist and n_kept are still filled in). */
+pk_status pk_cutoff(pk_job* job, int32_t num_buckets, uint32_t* cutoff, uint64_t* hist,
+                    uint64_t* n_kept);
+
+/* ---- macro-nodes: replaces construct_macro_nodes ----------------------------------
+ * min_count = 0 uses the cutoff from pk_cutoff; otherwise rows with count >=
+ * min_count are kept.  Node keys are the (k-1)-mers ascending; per node four suffix
+ * counts and four prefix counts indexed by extension base code (A=0 C=1 T=2 G=3),
+ * 0 meaning absent.  Visit values are ceil(count / coverage). */
+pk_status pk_build_macro_nodes(pk_job* job, uint32_t min_count, uint64_t* n_nodes);
+pk_status pk_copy_macro_nodes(pk_job* job, void* keys, uint32_t* suffix_counts,
+                              uint32_t* prefix_counts, uint64_t capacity);
+pk_status pk_macro_nodes_device(pk_job* job, const void** d_keys, const uint32_t** d_suffix,
+                                const uint32_t** d_prefix);
+
+/* ---- whole path --------------------------------------------------------------------
+ * count -> cutoff (p->num_buckets) -> macro-nodes, synchronised at the end. */
+pk_status pk_run(pk_job* job, const char* fasta, uint64_t n, const pk_params* p, pk_summary* out);
+pk_status pk_run_device(pk_job* job, const void* d_fasta, uint64_t n, const pk_params* p,
+                        pk_summary* out);
+pk_status pk_summary_get(pk_job* job, pk_summary* out);
+
+/* ---- per-kernel timing (CUDA events on the job's stream) ---------------------------- */
+pk_status pk_job_enable_timing(pk_job* job, int on);
+/* Milliseconds per stage of the last run; n_stages receives the stage count. */
+pk_status pk_job_stage_times(pk_job* job, float* ms, int capacity, int* n_stages);
+const char* pk_stage_name(int stage);
+
+/* Pinned host memory for fast transfers (cudaHostAlloc). */
+pk_status pk_host_alloc(uint64_t bytes, void** out);
+void pk_host_free(void* p);
+
+/* Library version string. */
+const char* pk_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PAKMAN_GB300_H */

@@ -1,0 +1,332 @@
+"""Python host mirror of PaKman's counting / histogram / macro-node interface.
+
+Two layers over the C ABI:
+
+* :class:`Context` / :class:`Job` -- thin owners of ``pk_ctx`` / ``pk_job``.
+* :class:`PakmanSession` -- the reference's phase functions with the reference's
+  names and argument meanings: ``perform_kmer_counting(read_data)``
+  (src/kmer_counting.cpp:3351) fills ``kmer_proc_buf`` (a sorted, unique
+  KmerPairs table, src/distribute_kmers.cpp:87), ``construct_kmer_histogram()``
+  (src/kmer_histogram.cpp:72) returns the histogram and ``min_bucket``, and
+  ``begin_mnode_construction()`` (src/mn_construct.cpp:479) returns the macro-node
+  map.  Failure modes follow the reference: a record start that is not '>' raises
+  :class:`FormatError` (the reference asserts), no k-mer surviving the cutoff raises
+  :class:`EmptyAfterCutoff` (the reference calls MPI_Abort).
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_float, c_int, c_uint32, c_uint64, c_void_p
+from dataclasses import dataclass
+from typing import Dict, Optional, Tuple
+
+import numpy as np
+
+from . import capi
+from .capi import EmptyAfterCutoff, FormatError, PakmanError, check, default_params  # noqa: F401
+
+KEY128 = np.dtype([("lo", "<u8"), ("hi", "<u8")])
+KMERPAIRS64 = np.dtype([("seq", "<u8"), ("k_count", "<i4")])  # packed, 12 bytes
+KMERPAIRS128 = np.dtype([("seq_lo", "<u8"), ("seq_hi", "<u8"), ("k_count", "<i4")])  # 20 bytes
+
+
+def key_dtype(k: int):
+    return np.dtype("<u8") if k <= 32 else KEY128
+
+
+def to_key128(keys: np.ndarray) -> np.ndarray:
+    """Keys of either width as the (lo, hi) structured layout."""
+    if keys.dtype == KEY128:
+        return keys
+    out = np.empty(keys.size, KEY128)
+    out["lo"] = keys
+    out["hi"] = 0
+    return out
+
+
+class Context:
+    """One device and an HBM budget (0 = unlimited)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        L = capi.lib()
+        h = c_void_p()
+        check(L.pk_ctx_create(device, hbm_budget, byref(h)), "pk_ctx_create")
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def memory(self) -> Tuple[int, int]:
+        u, b = c_uint64(), c_uint64()
+        check(capi.lib().pk_ctx_memory(self._h, byref(u), byref(b)), "pk_ctx_memory")
+        return u.value, b.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.lib().pk_ctx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class Summary:
+    n_reads: int
+    n_windows: int
+    n_unique: int
+    n_kept: int
+    n_nodes: int
+    cutoff: int
+    key_bytes: int
+
+    @staticmethod
+    def from_c(s: capi.PkSummary) -> "Summary":
+        return Summary(s.n_reads, s.n_windows, s.n_unique, s.n_kept, s.n_nodes, s.cutoff, s.key_bytes)
+
+
+@dataclass
+class MacroNodeTable:
+    """Macro-nodes as columns: (k-1)-mer keys ascending, suffix/prefix counts by
+    extension base code (A=0 C=1 T=2 G=3), 0 = absent; visit = ceil(count/coverage)."""
+    keys: np.ndarray
+    suffix_counts: np.ndarray
+    prefix_counts: np.ndarray
+    coverage: int
+    k: int
+
+    def __len__(self):
+        return int(self.keys.size)
+
+    @property
+    def suffix_visits(self) -> np.ndarray:
+        return _visit(self.suffix_counts, self.coverage)
+
+    @property
+    def prefix_visits(self) -> np.ndarray:
+        return _visit(self.prefix_counts, self.coverage)
+
+    def node(self, i: int) -> Dict:
+        """One node in the reference MacroNode's terms (k_1_mer bases, suffixes,
+        suffix_count pairs, prefixes, prefix_count pairs)."""
+        key = self.keys[i]
+        v = (int(key["hi"]) << 64 | int(key["lo"])) if self.keys.dtype == KEY128 else int(key)
+        nb = self.k - 1
+        bases = [(v >> (2 * (nb - 1 - p))) & 3 for p in range(nb)]
+        sv, pv = self.suffix_visits[i], self.prefix_visits[i]
+        suf = [(e, int(self.suffix_counts[i, e]), int(sv[e])) for e in range(4) if self.suffix_counts[i, e]]
+        pre = [(e, int(self.prefix_counts[i, e]), int(pv[e])) for e in range(4) if self.prefix_counts[i, e]]
+        return {"k_1_mer": bases, "suffixes": [s[0] for s in suf],
+                "suffix_count": [(s[1], s[2]) for s in suf], "prefixes": [p[0] for p in pre],
+                "prefix_count": [(p[1], p[2]) for p in pre]}
+
+
+def _visit(counts: np.ndarray, coverage: int) -> np.ndarray:
+    c = counts.astype(np.int64)
+    cov = int(coverage)
+    q = np.floor_divide(c, cov)
+    q += (c - q * cov) != 0
+    return np.where(c != 0, q, 0)
+
+
+class Job:
+    """One read set on the device: count -> cutoff -> macro-nodes; buffers stay
+    resident until :meth:`reset` or :meth:`close`."""
+
+    def __init__(self, ctx: Context, stream: Optional[int] = None):
+        self.ctx = ctx
+        h = c_void_p()
+        check(capi.lib().pk_job_create(ctx.handle, c_void_p(stream) if stream else None, byref(h)),
+              "pk_job_create")
+        self._h = h
+        self.params: Optional[capi.PkParams] = None
+        self._pin = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- counting
+    def count(self, fasta, params: capi.PkParams):
+        buf = _as_bytes_ptr(fasta)
+        self.params = params
+        check(capi.lib().pk_count(self._h, buf[0], buf[1], byref(params)), "pk_count")
+
+    def count_device(self, ptr: int, n: int, params: capi.PkParams):
+        self.params = params
+        check(capi.lib().pk_count_device(self._h, c_void_p(ptr), n, byref(params)), "pk_count_device")
+
+    def table_info(self) -> Tuple[int, int, int]:
+        u, w, r = c_uint64(), c_uint64(), c_uint64()
+        check(capi.lib().pk_table_info(self._h, byref(u), byref(w), byref(r)), "pk_table_info")
+        return u.value, w.value, r.value
+
+    def table(self) -> Tuple[np.ndarray, np.ndarray]:
+        u, _, _ = self.table_info()
+        keys = np.empty(u, key_dtype(self.params.k))
+        cnts = np.empty(u, np.uint32)
+        check(capi.lib().pk_copy_table(self._h, keys.ctypes.data, cnts.ctypes.data, u), "pk_copy_table")
+        return keys, cnts
+
+    def table_packed(self) -> np.ndarray:
+        u, _, _ = self.table_info()
+        out = np.empty(u, KMERPAIRS64 if self.params.k <= 32 else KMERPAIRS128)
+        check(capi.lib().pk_copy_table_packed(self._h, out.ctypes.data, u), "pk_copy_table_packed")
+        return out
+
+    def table_device(self) -> Tuple[int, int]:
+        k, c = c_void_p(), c_void_p()
+        check(capi.lib().pk_table_device(self._h, byref(k), byref(c)), "pk_table_device")
+        return k.value, c.value
+
+    # -- histogram cutoff
+    def cutoff(self, num_buckets: int) -> Tuple[int, np.ndarray, int]:
+        cut, kept = c_uint32(), c_uint64()
+        hist = np.zeros(num_buckets, np.uint64)
+        check(capi.lib().pk_cutoff(self._h, num_buckets, byref(cut), hist.ctypes.data, byref(kept)),
+              "pk_cutoff")
+        return cut.value, hist, kept.value
+
+    # -- macro-nodes
+    def build_macro_nodes(self, min_count: int = 0) -> int:
+        m = c_uint64()
+        check(capi.lib().pk_build_macro_nodes(self._h, min_count, byref(m)), "pk_build_macro_nodes")
+        return m.value
+
+    def macro_nodes(self, coverage: Optional[int] = None) -> MacroNodeTable:
+        s = self.summary()
+        m = s.n_nodes
+        keys = np.empty(m, key_dtype(self.params.k))
+        suf = np.empty((m, 4), np.uint32)
+        pre = np.empty((m, 4), np.uint32)
+        check(capi.lib().pk_copy_macro_nodes(self._h, keys.ctypes.data, suf.ctypes.data,
+                                             pre.ctypes.data, m), "pk_copy_macro_nodes")
+        cov = coverage if coverage is not None else self.params.coverage
+        return MacroNodeTable(keys, suf, pre, cov, self.params.k)
+
+    # -- whole path
+    def run(self, fasta, params: capi.PkParams) -> Summary:
+        buf = _as_bytes_ptr(fasta)
+        self.params = params
+        s = capi.PkSummary()
+        check(capi.lib().pk_run(self._h, buf[0], buf[1], byref(params), byref(s)), "pk_run")
+        return Summary.from_c(s)
+
+    def run_device(self, ptr: int, n: int, params: capi.PkParams) -> Summary:
+        self.params = params
+        s = capi.PkSummary()
+        check(capi.lib().pk_run_device(self._h, c_void_p(ptr), n, byref(params), byref(s)),
+              "pk_run_device")
+        return Summary.from_c(s)
+
+    def summary(self) -> Summary:
+        s = capi.PkSummary()
+        check(capi.lib().pk_summary_get(self._h, byref(s)), "pk_summary_get")
+        return Summary.from_c(s)
+
+    def sync(self):
+        check(capi.lib().pk_job_sync(self._h), "pk_job_sync")
+
+    def memory(self) -> int:
+        b = c_uint64()
+        check(capi.lib().pk_job_memory(self._h, byref(b)), "pk_job_memory")
+        return b.value
+
+    def enable_timing(self, on: bool = True):
+        check(capi.lib().pk_job_enable_timing(self._h, int(on)), "pk_job_enable_timing")
+
+    def stage_times(self) -> Dict[str, float]:
+        arr = (c_float * 16)()
+        n = c_int()
+        check(capi.lib().pk_job_stage_times(self._h, arr, 16, byref(n)), "pk_job_stage_times")
+        return {capi.lib().pk_stage_name(i).decode(): float(arr[i]) for i in range(n.value)}
+
+    def reset(self):
+        check(capi.lib().pk_job_reset(self._h), "pk_job_reset")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.lib().pk_job_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _as_bytes_ptr(fasta):
+    """(pointer, length) of a bytes-like or numpy uint8 host buffer (kept alive by caller)."""
+    if isinstance(fasta, np.ndarray):
+        a = np.ascontiguousarray(fasta, dtype=np.uint8)
+        return c_void_p(a.ctypes.data), a.size
+    if isinstance(fasta, (bytes, bytearray, memoryview)):
+        mv = memoryview(fasta)
+        if mv.readonly:
+            buf = ctypes.c_char_p(bytes(mv))
+            return ctypes.cast(buf, c_void_p), mv.nbytes
+        arr = (ctypes.c_char * mv.nbytes).from_buffer(mv)
+        return ctypes.cast(arr, c_void_p), mv.nbytes
+    raise TypeError("fasta must be bytes or a uint8 numpy array")
+
+
+class PakmanSession:
+    """The reference's counting / histogram / macro-node phases under the
+    reference's names, with its globals (k, LMER_LENGTH, -t, -c, -r, -b) as
+    attributes."""
+
+    def __init__(self, k: int = 32, lmer_length: int = 8, num_buckets: int = 21, coverage: int = 1,
+                 read_length: int = 100, batch: int = 100_000_000, drop_n: bool = False,
+                 ctx: Optional[Context] = None, device: int = 0):
+        self.ctx = ctx or Context(device)
+        self.job = Job(self.ctx)
+        self.params = default_params(k=k, lmer_length=lmer_length, num_buckets=num_buckets,
+                                     coverage=coverage, read_length=read_length, batch_kmers=batch,
+                                     drop_n=int(drop_n))
+        self.min_bucket: Optional[int] = None
+
+    def perform_kmer_counting(self, read_data) -> None:
+        """Count every k-mer window of the FASTA buffer (device), table stays resident."""
+        self.job.count(read_data, self.params)
+        self.job.table_info()  # surfaces format errors now, as the reference's assert would
+
+    @property
+    def kmer_proc_buf(self) -> np.ndarray:
+        """Sorted unique (k-mer, count) table as packed KmerPairs records."""
+        return self.job.table_packed()
+
+    def construct_kmer_histogram(self) -> Tuple[np.ndarray, int]:
+        cut, hist, kept = None, None, None
+        try:
+            cut, hist, kept = self.job.cutoff(self.params.num_buckets)
+        finally:
+            pass
+        self.min_bucket = cut
+        return hist, cut
+
+    def begin_mnode_construction(self) -> MacroNodeTable:
+        if self.min_bucket is None:
+            self.construct_kmer_histogram()
+        self.job.build_macro_nodes(0)
+        return self.job.macro_nodes(self.params.coverage)
+
+    def close(self):
+        self.job.close()

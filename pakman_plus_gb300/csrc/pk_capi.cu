@@ -1,0 +1,687 @@
+// Host runtime behind the C ABI (include/pakman_gb300.h): contexts with an HBM
+// budget, jobs that own their device buffers, and the stream-ordered launch
+// sequence of the counting -> cutoff -> macro-node path.  No CPU fallback: every
+// result comes from the kernels in pk_kernels.cu.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/pakman_gb300.h"
+#include "pk_internal.h"
+
+using namespace pk;
+
+// ------------------------------------------------------------------ errors ------
+static thread_local std::string t_last_error;
+
+static pk_status fail(pk_status s, const std::string& msg) {
+  t_last_error = msg;
+  return s;
+}
+
+#define PK_CUDA(call)                                                                     \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(e_ == cudaErrorMemoryAllocation ? PK_ERR_NOMEM : PK_ERR_CUDA,           \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                     \
+  } while (0)
+
+#define PK_TRY(expr)              \
+  do {                            \
+    pk_status s_ = (expr);        \
+    if (s_ != PK_OK) return s_;   \
+  } while (0)
+
+// ---------------------------------------------------------------- context -------
+struct pk_ctx {
+  int device = 0;
+  uint64_t budget = 0;
+  std::atomic<uint64_t> used{0};
+  cudaMemPool_t pool = nullptr;
+  int sms = 0;
+};
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+enum Stage {
+  ST_H2D = 0,
+  ST_LINES,
+  ST_BUCKET_COUNT,
+  ST_OFFSETS,
+  ST_SCATTER,
+  ST_TABLE,
+  ST_CUTOFF,
+  ST_MN,
+  ST_COUNT_
+};
+static const char* kStageNames[ST_COUNT_] = {"h2d",     "line_scan", "bucket_count", "bucket_offsets",
+                                             "scatter", "bucket_table", "cutoff", "macro_nodes"};
+
+struct pk_job {
+  pk_ctx* ctx = nullptr;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  pk_params params{};
+  int wide = 0;
+  int bbits = 0;
+  int grid = 0;
+  unsigned long long chunk = 0;
+  uint64_t F = 0, N = 0;
+  int t_hist = 0;
+  int stage = 0;  // 0 none, 1 counted, 2 cutoff, 3 macro-nodes
+  uint64_t mn_cap = 0;
+  Scalars* d_sc = nullptr;
+  Scalars* h_sc = nullptr;  // pinned mirror
+  DevBuf fasta, tile_nl, counts, bstart, keys, tkeys, tcounts, tb, tsub, flags_b, flags_m, hist,
+      hist2, nkeys, nsuf, npre, packed;
+  bool timing = false;
+  cudaEvent_t ev0[ST_COUNT_] = {}, ev1[ST_COUNT_] = {};
+  bool ev_rec[ST_COUNT_] = {};
+};
+
+static pk_status set_device(pk_ctx* c) {
+  PK_CUDA(cudaSetDevice(c->device));
+  return PK_OK;
+}
+
+static pk_status job_alloc(pk_job* j, DevBuf& b, size_t bytes) {
+  if (b.p && b.bytes >= bytes) return PK_OK;
+  if (b.p) {
+    PK_CUDA(cudaFreeAsync(b.p, j->stream));
+    j->ctx->used -= b.bytes;
+    b.p = nullptr;
+    b.bytes = 0;
+  }
+  if (bytes == 0) bytes = 16;
+  bytes = (bytes + 255) & ~(size_t)255;
+  uint64_t now = j->ctx->used.fetch_add(bytes) + bytes;
+  if (j->ctx->budget && now > j->ctx->budget) {
+    j->ctx->used -= bytes;
+    return fail(PK_ERR_NOMEM, "HBM budget exceeded: need " + std::to_string(bytes) + " more bytes, " +
+                                  std::to_string(now - bytes) + " of " + std::to_string(j->ctx->budget) +
+                                  " in use");
+  }
+  cudaError_t e = cudaMallocFromPoolAsync(&b.p, bytes, j->ctx->pool, j->stream);
+  if (e != cudaSuccess) {
+    j->ctx->used -= bytes;
+    b.p = nullptr;
+    return fail(PK_ERR_NOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+  }
+  b.bytes = bytes;
+  return PK_OK;
+}
+
+static void job_free(pk_job* j, DevBuf& b) {
+  if (b.p) {
+    cudaFreeAsync(b.p, j->stream);
+    j->ctx->used -= b.bytes;
+  }
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+static void job_free_all(pk_job* j) {
+  DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->keys,  &j->tkeys,
+                   &j->tcounts, &j->tb,    &j->tsub,    &j->flags_b, &j->flags_m, &j->hist,
+                   &j->hist2,  &j->nkeys,  &j->nsuf,    &j->npre,    &j->packed};
+  for (DevBuf* b : all) job_free(j, *b);
+}
+
+// per-stage CUDA events on the job's stream (begin/end pairs, so host-side gaps
+// between stages are not charged to a kernel)
+static void mark_begin(pk_job* j, int st) {
+  if (j->timing) cudaEventRecord(j->ev0[st], j->stream);
+}
+static void mark_end(pk_job* j, int st) {
+  if (j->timing) {
+    cudaEventRecord(j->ev1[st], j->stream);
+    j->ev_rec[st] = true;
+  }
+}
+
+// ---------------------------------------------------------------- C ABI ---------
+extern "C" {
+
+void pk_params_default(pk_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->k = 32;
+  p->lmer_length = 8;
+  p->num_buckets = 21;
+  p->coverage = 1;
+  p->read_length = 100;
+  p->drop_n = 0;
+  p->batch_kmers = 100000000ull;
+  p->bucket_bits = 0;
+}
+
+const char* pk_status_string(pk_status s) {
+  switch (s) {
+    case PK_OK: return "ok";
+    case PK_ERR_INVALID: return "invalid argument";
+    case PK_ERR_FORMAT: return "FASTA record does not start with '>'";
+    case PK_ERR_EMPTY: return "no k-mer reaches the histogram cutoff";
+    case PK_ERR_NOMEM: return "out of device memory or HBM budget";
+    case PK_ERR_CUDA: return "CUDA error";
+    case PK_ERR_STATE: return "call out of order";
+    case PK_ERR_LIMIT: return "input beyond supported size";
+    case PK_ERR_DEVICE: return "device-side failure";
+    case PK_ERR_BUSY: return "busy";
+    case PK_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+const char* pk_last_error(void) { return t_last_error.c_str(); }
+
+const char* pk_version(void) { return "pakman-gb300 0.1 (sm_103a)"; }
+
+pk_status pk_ctx_create(int device, uint64_t budget, pk_ctx** out) {
+  if (!out) return fail(PK_ERR_INVALID, "out is null");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n <= 0)
+    return fail(PK_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= n) return fail(PK_ERR_INVALID, "device index out of range");
+  PK_CUDA(cudaSetDevice(device));
+  pk_ctx* c = new pk_ctx();
+  c->device = device;
+  c->budget = budget;
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  e = cudaMemPoolCreate(&c->pool, &props);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(PK_ERR_CUDA, std::string("cudaMemPoolCreate: ") + cudaGetErrorString(e));
+  }
+  uint64_t thr = ~0ull;
+  cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+  *out = c;
+  return PK_OK;
+}
+
+void pk_ctx_destroy(pk_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaDeviceSynchronize();
+  if (c->pool) cudaMemPoolDestroy(c->pool);
+  delete c;
+}
+
+pk_status pk_ctx_memory(pk_ctx* c, uint64_t* used, uint64_t* budget) {
+  if (!c) return fail(PK_ERR_INVALID, "ctx is null");
+  if (used) *used = c->used.load();
+  if (budget) *budget = c->budget;
+  return PK_OK;
+}
+
+pk_status pk_job_create(pk_ctx* c, void* stream, pk_job** out) {
+  if (!c || !out) return fail(PK_ERR_INVALID, "null argument");
+  PK_TRY(set_device(c));
+  pk_job* j = new pk_job();
+  j->ctx = c;
+  if (stream) {
+    j->stream = (cudaStream_t)stream;
+  } else {
+    cudaError_t e = cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete j;
+      return fail(PK_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    j->own_stream = true;
+  }
+  cudaError_t e = cudaMalloc(&j->d_sc, sizeof(Scalars));
+  if (e == cudaSuccess) e = cudaHostAlloc(&j->h_sc, sizeof(Scalars), cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    if (j->d_sc) cudaFree(j->d_sc);
+    if (j->own_stream) cudaStreamDestroy(j->stream);
+    delete j;
+    return fail(PK_ERR_NOMEM, std::string("job scalars: ") + cudaGetErrorString(e));
+  }
+  memset(j->h_sc, 0, sizeof(Scalars));
+  for (int i = 0; i < ST_COUNT_; i++) {
+    cudaEventCreate(&j->ev0[i]);
+    cudaEventCreate(&j->ev1[i]);
+  }
+  *out = j;
+  return PK_OK;
+}
+
+void pk_job_destroy(pk_job* j) {
+  if (!j) return;
+  cudaSetDevice(j->ctx->device);
+  cudaStreamSynchronize(j->stream);
+  job_free_all(j);
+  cudaStreamSynchronize(j->stream);
+  for (int i = 0; i < ST_COUNT_; i++) {
+    if (j->ev0[i]) cudaEventDestroy(j->ev0[i]);
+    if (j->ev1[i]) cudaEventDestroy(j->ev1[i]);
+  }
+  if (j->d_sc) cudaFree(j->d_sc);
+  if (j->h_sc) cudaFreeHost(j->h_sc);
+  if (j->own_stream) cudaStreamDestroy(j->stream);
+  delete j;
+}
+
+pk_status pk_job_reset(pk_job* j) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  PK_TRY(set_device(j->ctx));
+  job_free_all(j);
+  j->stage = 0;
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  return PK_OK;
+}
+
+pk_status pk_job_sync(pk_job* j) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  PK_TRY(set_device(j->ctx));
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  return PK_OK;
+}
+
+pk_status pk_job_memory(pk_job* j, uint64_t* bytes) {
+  if (!j || !bytes) return fail(PK_ERR_INVALID, "null argument");
+  DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->keys,  &j->tkeys,
+                   &j->tcounts, &j->tb,    &j->tsub,    &j->flags_b, &j->flags_m, &j->hist,
+                   &j->hist2,  &j->nkeys,  &j->nsuf,    &j->npre,    &j->packed};
+  uint64_t s = 0;
+  for (DevBuf* b : all) s += b->bytes;
+  *bytes = s;
+  return PK_OK;
+}
+
+pk_status pk_job_enable_timing(pk_job* j, int on) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  j->timing = on != 0;
+  return PK_OK;
+}
+
+pk_status pk_job_stage_times(pk_job* j, float* ms, int cap, int* n) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  PK_TRY(set_device(j->ctx));
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  if (n) *n = ST_COUNT_;
+  for (int s = 0; s < ST_COUNT_ && s < cap; s++) {
+    float v = 0.f;
+    if (j->ev_rec[s]) cudaEventElapsedTime(&v, j->ev0[s], j->ev1[s]);
+    ms[s] = v;
+  }
+  return PK_OK;
+}
+
+const char* pk_stage_name(int s) { return (s >= 0 && s < ST_COUNT_) ? kStageNames[s] : ""; }
+
+pk_status pk_host_alloc(uint64_t bytes, void** out) {
+  if (!out) return fail(PK_ERR_INVALID, "out is null");
+  PK_CUDA(cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault));
+  return PK_OK;
+}
+
+void pk_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+static pk_status check_params(const pk_params* p) {
+  if (!p) return fail(PK_ERR_INVALID, "params is null");
+  if (p->k < 2 || p->k > 64) return fail(PK_ERR_INVALID, "k must be in 2..64");
+  if (p->lmer_length < 1 || p->lmer_length > 32) return fail(PK_ERR_INVALID, "lmer_length must be in 1..32");
+  if (p->num_buckets < 1) return fail(PK_ERR_INVALID, "num_buckets (-t) must be >= 1");
+  if (p->bucket_bits < 0 || p->bucket_bits > 15) return fail(PK_ERR_INVALID, "bucket_bits must be in 0..15");
+  return PK_OK;
+}
+
+static int auto_bucket_bits(uint64_t F, int k, int wide) {
+  // leading-key-bit partition sized so an average bucket fills about half of the
+  // on-chip hash table of the per-bucket kernel
+  const double per_bucket = wide ? 2048.0 : 4096.0;
+  const double est = 0.7 * (double)F;  // k-mer windows per input byte for ~100 bp reads
+  int b = 2;
+  while (b < 15 && est / (double)(1u << b) > per_bucket) b++;
+  int cap = 2 * k - 2;
+  if (cap > 15) cap = 15;
+  return std::max(2, std::min(b, cap));
+}
+
+// Stages 1-5: device FASTA -> sorted (k-mer, count) table, resident.
+static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_params* p) {
+  const int k = p->k;
+  j->params = *p;
+  j->wide = k > 32;
+  j->F = n;
+  j->stage = 0;
+  const int W = j->wide ? 16 : 8;
+  const int bb = p->bucket_bits ? std::min(p->bucket_bits, std::min(15, 2 * k - 2))
+                                : auto_bucket_bits(n, k, j->wide);
+  j->bbits = std::max(2, bb);
+  const int B = 1 << j->bbits;
+  const uint64_t ntiles = (n + kTileBytes - 1) / kTileBytes;
+  int grid = (int)std::min<uint64_t>((uint64_t)j->ctx->sms, std::max<uint64_t>(ntiles, 1));
+  unsigned long long chunk = (ntiles + grid - 1) / grid * (unsigned long long)kTileBytes;
+  if (chunk == 0) chunk = kTileBytes;
+  grid = (int)std::max<uint64_t>(1, (n + chunk - 1) / chunk);
+  j->grid = grid;
+  j->chunk = chunk;
+
+  PK_TRY(job_alloc(j, j->tile_nl, sizeof(uint32_t) * (ntiles + 1)));
+  PK_TRY(job_alloc(j, j->counts, sizeof(uint32_t) * (size_t)grid * B));
+  PK_TRY(job_alloc(j, j->bstart, sizeof(uint32_t) * (B + 1)));
+  Scalars init{};
+  memset(&init, 0, sizeof(init));
+  init.s0 = ~0ull;
+  *j->h_sc = init;
+  PK_CUDA(cudaMemcpyAsync(j->d_sc, j->h_sc, sizeof(Scalars), cudaMemcpyHostToDevice, j->stream));
+
+  CountArgs a{};
+  a.fasta = (const uint8_t*)d_fasta;
+  a.F = n;
+  a.k = k;
+  a.lmer_m = std::min(k, p->lmer_length);
+  a.drop_n = p->drop_n ? 1 : 0;
+  a.bbits = j->bbits;
+  a.grid = grid;
+  a.chunk = chunk;
+  a.tile_nl = (uint32_t*)j->tile_nl.p;
+  a.counts = (uint32_t*)j->counts.p;
+  a.bstart = (uint32_t*)j->bstart.p;
+  a.sc = j->d_sc;
+
+  mark_begin(j, ST_LINES);
+  PK_CUDA(launch_line_scan(a, j->stream));
+  mark_end(j, ST_LINES);
+  mark_begin(j, ST_BUCKET_COUNT);
+  PK_CUDA(launch_bucket_count(a, j->wide, j->stream));
+  mark_end(j, ST_BUCKET_COUNT);
+  mark_begin(j, ST_OFFSETS);
+  PK_CUDA(launch_bucket_offsets(a, j->stream));
+  mark_end(j, ST_OFFSETS);
+  // the key buffer is sized by the exact window count
+  PK_CUDA(cudaMemcpyAsync(j->h_sc, j->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost, j->stream));
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  if (j->h_sc->err & ERR_FORMAT)
+    return fail(PK_ERR_FORMAT, "a FASTA record start is not '>' (one '>' header line and one "
+                               "sequence line per record expected)");
+  const uint64_t N = j->h_sc->n_windows;
+  if (N >= (1ull << 32) - 1)
+    return fail(PK_ERR_LIMIT, "more than 2^32-2 k-mer windows in one job; split the input");
+  j->N = N;
+  PK_TRY(job_alloc(j, j->keys, (size_t)W * N));
+  a.n_keys = N;
+  PK_TRY(job_alloc(j, j->tkeys, (size_t)W * N));
+  PK_TRY(job_alloc(j, j->tcounts, sizeof(uint32_t) * N));
+  PK_TRY(job_alloc(j, j->tb, sizeof(uint32_t) * (B + 1)));
+  PK_TRY(job_alloc(j, j->tsub, sizeof(uint32_t) * 3 * (size_t)B));
+  PK_TRY(job_alloc(j, j->flags_b, sizeof(unsigned long long) * B));
+  const int t = p->num_buckets;
+  PK_TRY(job_alloc(j, j->hist, sizeof(unsigned long long) * (size_t)t));
+  PK_CUDA(cudaMemsetAsync(j->flags_b.p, 0, sizeof(unsigned long long) * B, j->stream));
+  PK_CUDA(cudaMemsetAsync(j->hist.p, 0, sizeof(unsigned long long) * (size_t)t, j->stream));
+  PK_CUDA(cudaMemsetAsync(j->tb.p, 0, sizeof(uint32_t) * (B + 1), j->stream));
+  j->t_hist = t;
+
+  mark_begin(j, ST_SCATTER);
+  PK_CUDA(launch_scatter(a, j->keys.p, j->wide, j->stream));
+  mark_end(j, ST_SCATTER);
+  mark_begin(j, ST_TABLE);
+  BucketArgs b{};
+  b.keys = j->keys.p;
+  b.bstart = (const uint32_t*)j->bstart.p;
+  b.tkeys = j->tkeys.p;
+  b.tcounts = (uint32_t*)j->tcounts.p;
+  b.tb = (uint32_t*)j->tb.p;
+  b.tsub = (uint32_t*)j->tsub.p;
+  b.flags = (unsigned long long*)j->flags_b.p;
+  b.hist = (unsigned long long*)j->hist.p;
+  b.t = t;
+  b.k = k;
+  b.bbits = j->bbits;
+  b.cap = N;
+  b.sc = j->d_sc;
+  PK_CUDA(launch_bucket_table(b, j->wide, 0, j->stream));
+  mark_end(j, ST_TABLE);
+  j->stage = 1;
+  return PK_OK;
+}
+
+pk_status pk_count_device(pk_job* j, const void* d_fasta, uint64_t n, const pk_params* p) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  PK_TRY(check_params(p));
+  if (n && !d_fasta) return fail(PK_ERR_INVALID, "d_fasta is null");
+  if (((uintptr_t)d_fasta & 15) != 0) return fail(PK_ERR_INVALID, "d_fasta must be 16-byte aligned");
+  PK_TRY(set_device(j->ctx));
+  for (int i = 0; i < ST_COUNT_; i++) j->ev_rec[i] = false;
+  return count_impl(j, d_fasta, n, p);
+}
+
+pk_status pk_count(pk_job* j, const char* fasta, uint64_t n, const pk_params* p) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  PK_TRY(check_params(p));
+  if (n && !fasta) return fail(PK_ERR_INVALID, "fasta is null");
+  PK_TRY(set_device(j->ctx));
+  for (int i = 0; i < ST_COUNT_; i++) j->ev_rec[i] = false;
+  PK_TRY(job_alloc(j, j->fasta, (size_t)n + 16));
+  mark_begin(j, ST_H2D);
+  if (n) PK_CUDA(cudaMemcpyAsync(j->fasta.p, fasta, n, cudaMemcpyHostToDevice, j->stream));
+  mark_end(j, ST_H2D);
+  return count_impl(j, j->fasta.p, n, p);
+}
+
+static pk_status sync_scalars(pk_job* j) {
+  PK_CUDA(cudaMemcpyAsync(j->h_sc, j->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost, j->stream));
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  const uint32_t err = j->h_sc->err;
+  if (err & ERR_FORMAT) return fail(PK_ERR_FORMAT, "a FASTA record start is not '>'");
+  if (err & ERR_LOOKBACK) return fail(PK_ERR_DEVICE, "a bounded look-back wait expired");
+  if (err & ERR_BUCKET) return fail(PK_ERR_DEVICE, "a bucket could not be split to fit on chip");
+  if (err & ERR_MN_CAPACITY) return fail(PK_ERR_DEVICE, "a macro-node segment exceeded on-chip capacity");
+  if (err & ERR_BOUNDS) return fail(PK_ERR_DEVICE, "an index fell outside its buffer (write skipped)");
+  return PK_OK;
+}
+
+pk_status pk_table_info(pk_job* j, uint64_t* u, uint64_t* w, uint64_t* r) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  if (j->stage < 1) return fail(PK_ERR_STATE, "no table: call pk_count first");
+  PK_TRY(set_device(j->ctx));
+  PK_TRY(sync_scalars(j));
+  if (u) *u = j->h_sc->n_unique;
+  if (w) *w = j->h_sc->n_windows;
+  if (r) *r = j->h_sc->n_reads;
+  return PK_OK;
+}
+
+pk_status pk_copy_table(pk_job* j, void* keys, uint32_t* counts, uint64_t cap) {
+  uint64_t u = 0;
+  PK_TRY(pk_table_info(j, &u, nullptr, nullptr));
+  if (cap < u) return fail(PK_ERR_INVALID, "capacity smaller than the table");
+  const size_t W = j->wide ? 16 : 8;
+  if (u && keys) PK_CUDA(cudaMemcpyAsync(keys, j->tkeys.p, W * u, cudaMemcpyDeviceToHost, j->stream));
+  if (u && counts)
+    PK_CUDA(cudaMemcpyAsync(counts, j->tcounts.p, 4 * u, cudaMemcpyDeviceToHost, j->stream));
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  return PK_OK;
+}
+
+pk_status pk_copy_table_packed(pk_job* j, void* pairs, uint64_t cap) {
+  uint64_t u = 0;
+  PK_TRY(pk_table_info(j, &u, nullptr, nullptr));
+  if (cap < u) return fail(PK_ERR_INVALID, "capacity smaller than the table");
+  if (!u) return PK_OK;
+  const size_t rec = j->wide ? 20 : 12;
+  PK_TRY(job_alloc(j, j->packed, rec * u));
+  PK_CUDA(launch_pack_pairs(j->tkeys.p, (const uint32_t*)j->tcounts.p, u, j->wide, j->packed.p, j->stream));
+  PK_CUDA(cudaMemcpyAsync(pairs, j->packed.p, rec * u, cudaMemcpyDeviceToHost, j->stream));
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  job_free(j, j->packed);
+  return PK_OK;
+}
+
+pk_status pk_table_device(pk_job* j, const void** k, const uint32_t** c) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  if (j->stage < 1) return fail(PK_ERR_STATE, "no table: call pk_count first");
+  if (k) *k = j->tkeys.p;
+  if (c) *c = (const uint32_t*)j->tcounts.p;
+  return PK_OK;
+}
+
+// cutoff on the device; no host synchronisation
+static pk_status cutoff_enqueue(pk_job* j, int t) {
+  const unsigned long long* hist = (const unsigned long long*)j->hist.p;
+  if (t != j->t_hist) {
+    // histogram for a different -t than the one fused into counting
+    PK_TRY(sync_scalars(j));
+    PK_TRY(job_alloc(j, j->hist2, sizeof(unsigned long long) * (size_t)t));
+    PK_CUDA(cudaMemsetAsync(j->hist2.p, 0, sizeof(unsigned long long) * (size_t)t, j->stream));
+    PK_CUDA(launch_histogram((const uint32_t*)j->tcounts.p, j->h_sc->n_unique, t,
+                             (unsigned long long*)j->hist2.p, j->stream));
+    hist = (const unsigned long long*)j->hist2.p;
+  }
+  mark_begin(j, ST_CUTOFF);
+  PK_CUDA(launch_cutoff(hist, t, j->d_sc, j->stream));
+  mark_end(j, ST_CUTOFF);
+  j->stage = 2;
+  return PK_OK;
+}
+
+pk_status pk_cutoff(pk_job* j, int32_t t, uint32_t* cutoff, uint64_t* hist, uint64_t* kept) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  if (t < 1) return fail(PK_ERR_INVALID, "num_buckets must be >= 1");
+  if (j->stage < 1) return fail(PK_ERR_STATE, "no table: call pk_count first");
+  PK_TRY(set_device(j->ctx));
+  PK_TRY(cutoff_enqueue(j, t));
+  const void* hsrc = t == j->t_hist ? j->hist.p : j->hist2.p;
+  if (hist) PK_CUDA(cudaMemcpyAsync(hist, hsrc, sizeof(uint64_t) * (size_t)t, cudaMemcpyDeviceToHost, j->stream));
+  PK_TRY(sync_scalars(j));
+  if (cutoff) *cutoff = j->h_sc->cutoff;
+  if (kept) *kept = j->h_sc->n_kept;
+  if (j->h_sc->n_kept == 0)
+    return fail(PK_ERR_EMPTY, "no k-mer reaches the cutoff " + std::to_string(j->h_sc->cutoff) +
+                                  "; macro-node construction cannot proceed");
+  return PK_OK;
+}
+
+static pk_status mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
+  const int B = 1 << j->bbits;
+  const size_t W = j->wide ? 16 : 8;
+  uint64_t cap = 2 * kept_bound;
+  if (cap == 0) cap = 1;
+  PK_TRY(job_alloc(j, j->nkeys, W * cap));
+  PK_TRY(job_alloc(j, j->nsuf, 16 * cap));
+  PK_TRY(job_alloc(j, j->npre, 16 * cap));
+  PK_TRY(job_alloc(j, j->flags_m, sizeof(unsigned long long) * B));
+  PK_CUDA(cudaMemsetAsync(j->flags_m.p, 0, sizeof(unsigned long long) * B, j->stream));
+  PK_CUDA(cudaMemsetAsync(&j->d_sc->ticket_mn, 0, sizeof(uint32_t), j->stream));
+  PK_CUDA(cudaMemsetAsync(&j->d_sc->n_nodes, 0, sizeof(unsigned long long), j->stream));
+  if (min_count) PK_CUDA(cudaMemcpyAsync(&j->d_sc->cutoff, &min_count, sizeof(uint32_t), cudaMemcpyHostToDevice, j->stream));
+  j->mn_cap = cap;
+  MnArgs m{};
+  m.tkeys = j->tkeys.p;
+  m.tcounts = (const uint32_t*)j->tcounts.p;
+  m.tb = (const uint32_t*)j->tb.p;
+  m.tsub = (const uint32_t*)j->tsub.p;
+  m.flags = (unsigned long long*)j->flags_m.p;
+  m.nkeys = j->nkeys.p;
+  m.nsuf = (uint32_t*)j->nsuf.p;
+  m.npre = (uint32_t*)j->npre.p;
+  m.cap = cap;
+  m.k = j->params.k;
+  m.bbits = j->bbits;
+  m.sc = j->d_sc;
+  mark_begin(j, ST_MN);
+  PK_CUDA(launch_macro_nodes(m, j->wide, 0, j->stream));
+  mark_end(j, ST_MN);
+  j->stage = 3;
+  return PK_OK;
+}
+
+pk_status pk_build_macro_nodes(pk_job* j, uint32_t min_count, uint64_t* n_nodes) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  if (j->stage < 1 || (min_count == 0 && j->stage < 2))
+    return fail(PK_ERR_STATE, "call pk_count and pk_cutoff (or pass min_count) first");
+  PK_TRY(set_device(j->ctx));
+  PK_TRY(sync_scalars(j));
+  uint64_t bound = min_count ? j->h_sc->n_unique : j->h_sc->n_kept;
+  if (bound == 0)
+    return fail(PK_ERR_EMPTY, "no k-mer reaches the cutoff; macro-node construction cannot proceed");
+  PK_TRY(mn_enqueue(j, min_count, bound));
+  PK_TRY(sync_scalars(j));
+  if (n_nodes) *n_nodes = j->h_sc->n_nodes;
+  return PK_OK;
+}
+
+pk_status pk_copy_macro_nodes(pk_job* j, void* keys, uint32_t* suf, uint32_t* pre, uint64_t cap) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  if (j->stage < 3) return fail(PK_ERR_STATE, "no macro-nodes: call pk_build_macro_nodes first");
+  PK_TRY(set_device(j->ctx));
+  PK_TRY(sync_scalars(j));
+  const uint64_t m = j->h_sc->n_nodes;
+  if (cap < m) return fail(PK_ERR_INVALID, "capacity smaller than the node count");
+  const size_t W = j->wide ? 16 : 8;
+  if (m && keys) PK_CUDA(cudaMemcpyAsync(keys, j->nkeys.p, W * m, cudaMemcpyDeviceToHost, j->stream));
+  if (m && suf) PK_CUDA(cudaMemcpyAsync(suf, j->nsuf.p, 16 * m, cudaMemcpyDeviceToHost, j->stream));
+  if (m && pre) PK_CUDA(cudaMemcpyAsync(pre, j->npre.p, 16 * m, cudaMemcpyDeviceToHost, j->stream));
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  return PK_OK;
+}
+
+pk_status pk_macro_nodes_device(pk_job* j, const void** k, const uint32_t** s, const uint32_t** p) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  if (j->stage < 3) return fail(PK_ERR_STATE, "no macro-nodes: call pk_build_macro_nodes first");
+  if (k) *k = j->nkeys.p;
+  if (s) *s = (const uint32_t*)j->nsuf.p;
+  if (p) *p = (const uint32_t*)j->npre.p;
+  return PK_OK;
+}
+
+pk_status pk_summary_get(pk_job* j, pk_summary* o) {
+  if (!j || !o) return fail(PK_ERR_INVALID, "null argument");
+  PK_TRY(set_device(j->ctx));
+  PK_TRY(sync_scalars(j));
+  o->n_reads = j->h_sc->n_reads;
+  o->n_windows = j->h_sc->n_windows;
+  o->n_unique = j->stage >= 1 ? j->h_sc->n_unique : 0;
+  o->n_kept = j->stage >= 2 ? j->h_sc->n_kept : 0;
+  o->n_nodes = j->stage >= 3 ? j->h_sc->n_nodes : 0;
+  o->cutoff = j->stage >= 2 ? j->h_sc->cutoff : 0;
+  o->key_bytes = j->wide ? 16 : 8;
+  return PK_OK;
+}
+
+static pk_status run_rest(pk_job* j, const pk_params* p, pk_summary* out) {
+  PK_TRY(cutoff_enqueue(j, p->num_buckets));
+  PK_TRY(sync_scalars(j));
+  if (j->h_sc->n_kept == 0) {
+    if (out) pk_summary_get(j, out);
+    return fail(PK_ERR_EMPTY, "no k-mer reaches the cutoff " + std::to_string(j->h_sc->cutoff) +
+                                  "; macro-node construction cannot proceed");
+  }
+  PK_TRY(mn_enqueue(j, 0, j->h_sc->n_kept));
+  if (out) return pk_summary_get(j, out);
+  return sync_scalars(j);
+}
+
+pk_status pk_run(pk_job* j, const char* fasta, uint64_t n, const pk_params* p, pk_summary* out) {
+  PK_TRY(pk_count(j, fasta, n, p));
+  return run_rest(j, p, out);
+}
+
+pk_status pk_run_device(pk_job* j, const void* d_fasta, uint64_t n, const pk_params* p, pk_summary* out) {
+  PK_TRY(pk_count_device(j, d_fasta, n, p));
+  return run_rest(j, p, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,107 @@
+// Internal launcher interface between the C-ABI host runtime (pk_capi.cpp) and the
+// sm_103a kernels (pk_kernels.cu).  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pk {
+
+// Device error word bits (pk_job error flag).
+enum : uint32_t {
+  ERR_FORMAT = 1u,        // a record start is not '>' (reference asserts)
+  ERR_LOOKBACK = 2u,      // a bounded look-back wait ran out
+  ERR_BUCKET = 4u,        // a bucket could not be split small enough for on-chip counting
+  ERR_MN_CAPACITY = 8u,   // a macro-node segment exceeded on-chip capacity
+  ERR_TICKET = 16u,       // work ticket overrun (should not happen)
+  ERR_BOUNDS = 32u,       // a computed index fell outside its buffer (write skipped)
+};
+
+constexpr int kTileBytes = 65536;   // line-scan tile; chunk boundaries are multiples of it
+constexpr int kExtractThreads = 512;
+constexpr int kSegBytes = 64;       // bytes per thread per extraction step
+constexpr int kBucketThreads = 512;
+constexpr int kMnThreads = 512;
+constexpr int kMnCap = 4096;        // items (k-mer records) per macro-node segment on chip
+constexpr int kHistSmem = 1024;     // count-histogram bins kept in shared memory
+
+struct Scalars {                    // device-side scalars of one job
+  unsigned long long s0;            // index of the first '>' (F if none)
+  unsigned long long n_windows;     // number of k-mer instances
+  unsigned long long n_reads;       // number of '>' bytes from s0 on
+  uint32_t nl_before_s0;            // newlines in [0, s0)
+  uint32_t err;                     // ERR_* bits
+  uint32_t ticket_bucket;           // work tickets
+  uint32_t ticket_mn;
+  uint32_t cutoff;                  // histogram cutoff
+  uint32_t pad;
+  unsigned long long n_unique;      // U
+  unsigned long long n_kept;        // V
+  unsigned long long n_nodes;       // M
+};
+
+struct CountArgs {
+  const uint8_t* fasta;
+  unsigned long long F;
+  int k;
+  int lmer_m;        // min(k, LMER_LENGTH): record-start checks follow the l-mer pass
+  int drop_n;
+  int bbits;         // bucket bits (top bits of the 2k-bit key)
+  int grid;          // extraction CTAs (chunks)
+  unsigned long long chunk;  // bytes per chunk (multiple of kTileBytes)
+  uint32_t* tile_nl;         // ceil(F / kTileBytes) + 1, exclusive newline prefix
+  uint32_t* counts;          // grid x 2^bbits  (per-chunk bucket counts, then prefixes)
+  uint32_t* bstart;          // 2^bbits + 1 bucket starts
+  unsigned long long n_keys; // capacity of the bucketed key buffer (scatter pass)
+  Scalars* sc;
+};
+
+struct BucketArgs {
+  const void* keys;          // bucketed keys (uint64 or u128), N entries
+  const uint32_t* bstart;    // 2^bbits + 1
+  void* tkeys;               // table keys out
+  uint32_t* tcounts;         // table counts out
+  uint32_t* tb;              // 2^bbits + 1 table bucket starts out
+  uint32_t* tsub;            // 3 * 2^bbits: table index where next-2-bit digit 1,2,3 starts
+  unsigned long long* flags; // 2^bbits look-back words (zeroed)
+  unsigned long long* hist;  // t bins (zeroed)
+  int t;
+  int k;
+  int bbits;
+  unsigned long long cap;    // table capacity (rows)
+  Scalars* sc;
+};
+
+struct MnArgs {
+  const void* tkeys;
+  const uint32_t* tcounts;
+  const uint32_t* tb;
+  const uint32_t* tsub;
+  unsigned long long* flags; // 2^bbits look-back words (zeroed)
+  void* nkeys;               // node keys out (capacity cap)
+  uint32_t* nsuf;            // 4 * cap
+  uint32_t* npre;            // 4 * cap
+  unsigned long long cap;
+  int k;
+  int bbits;
+  Scalars* sc;
+};
+
+// Launchers (all stream-ordered, no host synchronisation).
+cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st);
+cudaError_t launch_bucket_count(const CountArgs& a, int wide, cudaStream_t st);
+cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st);
+cudaError_t launch_scatter(const CountArgs& a, void* keys_out, int wide, cudaStream_t st);
+cudaError_t launch_bucket_table(const BucketArgs& a, int wide, int grid, cudaStream_t st);
+cudaError_t launch_histogram(const uint32_t* tcounts, unsigned long long u, int t,
+                             unsigned long long* hist, cudaStream_t st);
+cudaError_t launch_cutoff(const unsigned long long* hist, int t, Scalars* sc, cudaStream_t st);
+cudaError_t launch_macro_nodes(const MnArgs& a, int wide, int grid, cudaStream_t st);
+cudaError_t launch_pack_pairs(const void* tkeys, const uint32_t* tcounts, unsigned long long u,
+                              int wide, void* out, cudaStream_t st);
+
+size_t bucket_smem_bytes(int wide);
+size_t mn_smem_bytes(int wide);
+int bucket_ctas_per_sm(int wide);
+int mn_ctas_per_sm(int wide);
+
+}  // namespace pk

@@ -1,0 +1,1163 @@
+// sm_103a kernels for PaKman's k-mer counting -> histogram cutoff -> macro-node path.
+//
+// Pipeline for one read set (FASTA bytes resident in HBM):
+//   k_line_scan      newline count per 64 KB tile, first '>' and '>' count
+//   k_tile_prefix    exclusive newline prefix over tiles, newlines before the first '>'
+//   k_extract<..,0>  per chunk: roll every k-mer window, histogram of bucket ids (smem)
+//   k_col_prefix     per bucket: prefix over chunks; k_bucket_prefix: bucket starts
+//   k_extract<..,1>  per chunk: roll again, scatter each key to its bucket slot
+//   k_bucket_table   per bucket: hash-aggregate in smem, radix-sort the distinct
+//                    keys, write the sorted (k-mer, count) table with a decoupled
+//                    look-back over buckets, count histogram and next-digit offsets
+//   k_cutoff         first minimum of the count histogram over [1, t)
+//   k_macro_nodes    per (k-1)-mer bucket: merge the suffix-side and prefix-side
+//                    streams of kept k-mers into macro-node records
+//
+// A bucket is the leading `bbits` bits of the 2k-bit key, so buckets in index order
+// are the table in key order and no global merge is needed.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pk_internal.h"
+
+namespace pk {
+
+typedef unsigned __int128 u128;
+
+#define FULLMASK 0xffffffffu
+
+// ----------------------------------------------------------------- key helpers ----
+template <typename K>
+struct KeyOps;
+
+template <>
+struct KeyOps<uint64_t> {
+  static constexpr int W = 8;
+  __device__ __forceinline__ static uint64_t mask(int bits) {
+    return bits >= 64 ? ~0ull : ((1ull << bits) - 1ull);
+  }
+  __device__ __forceinline__ static uint64_t shr(uint64_t x, int s) { return s >= 64 ? 0ull : x >> s; }
+  __device__ __forceinline__ static uint64_t shl(uint64_t x, int s) { return s >= 64 ? 0ull : x << s; }
+  __device__ __forceinline__ static uint32_t low32(uint64_t x) { return (uint32_t)x; }
+  __device__ __forceinline__ static uint64_t hash(uint64_t x) { return x * 0x9E3779B97F4A7C15ull; }
+  __device__ __forceinline__ static unsigned match(unsigned m, uint64_t x) {
+    return __match_any_sync(m, (unsigned long long)x);
+  }
+  __device__ __forceinline__ static uint64_t cas(uint64_t* p, uint64_t cmp, uint64_t val) {
+    return atomicCAS(reinterpret_cast<unsigned long long*>(p), (unsigned long long)cmp,
+                     (unsigned long long)val);
+  }
+};
+
+template <>
+struct KeyOps<u128> {
+  static constexpr int W = 16;
+  __device__ __forceinline__ static u128 mask(int bits) {
+    return bits >= 128 ? ~(u128)0 : (((u128)1 << bits) - 1);
+  }
+  __device__ __forceinline__ static u128 shr(u128 x, int s) { return s >= 128 ? (u128)0 : x >> s; }
+  __device__ __forceinline__ static u128 shl(u128 x, int s) { return s >= 128 ? (u128)0 : x << s; }
+  __device__ __forceinline__ static uint32_t low32(u128 x) { return (uint32_t)(uint64_t)x; }
+  __device__ __forceinline__ static uint64_t hash(u128 x) {
+    uint64_t lo = (uint64_t)x, hi = (uint64_t)(x >> 64);
+    return (lo ^ (hi * 0xC2B2AE3D27D4EB4Full)) * 0x9E3779B97F4A7C15ull;
+  }
+  __device__ __forceinline__ static unsigned match(unsigned m, u128 x) {
+    return __match_any_sync(m, (unsigned long long)x) &
+           __match_any_sync(m, (unsigned long long)(x >> 64));
+  }
+  __device__ __forceinline__ static u128 cas(u128* p, u128 cmp, u128 val) { return atomicCAS(p, cmp, val); }
+};
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned r;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Decoupled look-back words: status in bits 62-63 (1 = aggregate, 2 = inclusive).
+constexpr unsigned long long kLbAgg = 1ull << 62;
+constexpr unsigned long long kLbIncl = 2ull << 62;
+constexpr unsigned long long kLbVal = (1ull << 62) - 1;
+constexpr int kLbSpinLimit = 1 << 24;  // ~1-2 s with the back-off below
+
+// Exclusive prefix of `flags[0..idx)`; called by one thread.  Every wait is bounded:
+// on expiry the error bit is set and the partial sum is returned.
+__device__ unsigned long long lookback_exclusive(unsigned long long* flags, int idx, uint32_t* err) {
+  unsigned long long sum = 0;
+  for (int j = idx - 1; j >= 0; --j) {
+    unsigned long long f = 0;
+    int spins = 0;
+    while (true) {
+      f = ld_acquire(&flags[j]);
+      if (f >> 62) break;
+      if (++spins >= kLbSpinLimit) {
+        atomicOr(err, ERR_LOOKBACK);
+        return sum;
+      }
+      __nanosleep(spins < 64 ? 32 : 256);
+    }
+    sum += f & kLbVal;
+    if ((f & ~kLbVal) == kLbIncl) break;
+  }
+  return sum;
+}
+
+// Block-wide exclusive sum over `nthreads` (multiple of 32, <= 1024) threads.
+__device__ __forceinline__ uint32_t block_exclusive_sum(uint32_t v, uint32_t* s_warp, uint32_t& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(FULLMASK, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < nw ? s_warp[lane] : 0;
+    uint32_t ws = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(FULLMASK, ws, o);
+      if (lane >= o) ws += y;
+    }
+    if (lane < nw) s_warp[lane] = ws - w;
+    if (lane == 31) s_warp[32] = ws;
+  }
+  __syncthreads();
+  uint32_t res = s_warp[warp] + x - v;
+  total = s_warp[32];
+  __syncthreads();
+  return res;
+}
+
+// ------------------------------------------------------------- line scan (k_line_scan) -
+// Newlines per 64 KB tile, the first '>' and the number of '>' bytes.
+__global__ void __launch_bounds__(256) k_line_scan(const uint8_t* __restrict__ buf,
+                                                   unsigned long long F, uint32_t* tile_nl,
+                                                   Scalars* sc) {
+  const unsigned long long t0 = (unsigned long long)blockIdx.x * kTileBytes;
+  const unsigned long long t1 = min(t0 + (unsigned long long)kTileBytes, F);
+  uint32_t nl = 0, gt = 0;
+  unsigned long long first = ~0ull;
+  for (unsigned long long p = t0 + 16ull * threadIdx.x; p < t1; p += 16ull * blockDim.x) {
+    uint32_t w[4];
+    if (p + 16 <= F) {
+      uint4 v = __ldg(reinterpret_cast<const uint4*>(buf + p));
+      w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+    } else {
+      for (int i = 0; i < 4; i++) {
+        uint32_t x = 0;
+        for (int b = 0; b < 4; b++) {
+          unsigned long long q = p + 4 * i + b;
+          if (q < F) x |= (uint32_t)buf[q] << (8 * b);
+        }
+        w[i] = x;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      nl += __popc(__vcmpeq4(w[i], 0x0A0A0A0Au)) >> 3;
+      uint32_t g = __vcmpeq4(w[i], 0x3E3E3E3Eu);
+      // a zero byte past F never compares equal to '>'
+      gt += __popc(g) >> 3;
+      if (g && first == ~0ull) first = p + 4 * i + (__ffs(g) - 1) / 8;
+    }
+  }
+  __shared__ uint32_t s_nl[8], s_gt[8];
+  __shared__ unsigned long long s_first[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    nl += __shfl_down_sync(FULLMASK, nl, o);
+    gt += __shfl_down_sync(FULLMASK, gt, o);
+    unsigned long long f2 = __shfl_down_sync(FULLMASK, first, o);
+    first = min(first, f2);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { s_nl[warp] = nl; s_gt[warp] = gt; s_first[warp] = first; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t a = 0, b = 0;
+    unsigned long long f = ~0ull;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) { a += s_nl[i]; b += s_gt[i]; f = min(f, s_first[i]); }
+    tile_nl[blockIdx.x] = a;
+    if (b) atomicAdd(&sc->n_reads, (unsigned long long)b);
+    if (f != ~0ull) atomicMin(&sc->s0, f);
+  }
+}
+
+// One CTA: exclusive prefix of tile newline counts (in place, plus the grand total at
+// [ntiles]) and the number of newlines before the first '>'.
+__global__ void __launch_bounds__(1024) k_tile_prefix(const uint8_t* __restrict__ buf,
+                                                      unsigned long long F, uint32_t* tile_nl,
+                                                      int ntiles, Scalars* sc) {
+  __shared__ uint32_t s_warp[33];
+  uint32_t carry = 0;
+  for (int base = 0; base < ntiles; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    uint32_t v = i < ntiles ? tile_nl[i] : 0;
+    uint32_t tot;
+    uint32_t ex = block_exclusive_sum(v, s_warp, tot);
+    if (i < ntiles) tile_nl[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) tile_nl[ntiles] = carry;
+  __syncthreads();
+  // newlines in [tile_start(s0), s0)
+  const unsigned long long s0 = sc->s0;
+  uint32_t cnt = 0;
+  if (s0 < F) {
+    const unsigned long long ts = (s0 / kTileBytes) * kTileBytes;
+    for (unsigned long long p = ts + threadIdx.x; p < s0; p += blockDim.x) cnt += (buf[p] == '\n');
+  }
+  uint32_t tot;
+  block_exclusive_sum(cnt, s_warp, tot);
+  if (threadIdx.x == 0) {
+    sc->nl_before_s0 = s0 < F ? tile_nl[s0 / kTileBytes] + tot : carry;
+  }
+}
+
+// --------------------------------------------------------- k-mer window extraction --
+// 16 input bytes -> 2-bit codes (byte 0 in the top bits), the bit-2 plane of the
+// codes, newline flags and N flags.
+__device__ __forceinline__ uint32_t pack4_codes(uint32_t w) {
+  return (((w >> 1) & 0x03030303u) * 0x40100401u) >> 24;
+}
+__device__ __forceinline__ uint32_t pack4_nbits(uint32_t w) {
+  return (((w >> 3) & 0x01010101u) * 0x40100401u) >> 24;
+}
+__device__ __forceinline__ uint32_t flags4(uint32_t eq) {
+  return ((eq & 0x01010101u) * 0x01020408u) >> 24;
+}
+
+struct UnitBits {
+  uint32_t codes;  // base j at bits 2(15-j)+1..2(15-j)
+  uint32_t nbits;  // code bit 2 of base j at bit 2(15-j)
+  uint32_t nl;     // bit j: byte j is '\n'
+  uint32_t nn;     // bit j: byte j is 'N' or 'n'
+};
+
+__device__ __forceinline__ UnitBits decode_unit(const uint32_t w[4]) {
+  UnitBits u;
+  u.codes = (pack4_codes(w[0]) << 24) | (pack4_codes(w[1]) << 16) | (pack4_codes(w[2]) << 8) |
+            pack4_codes(w[3]);
+  u.nbits = (pack4_nbits(w[0]) << 24) | (pack4_nbits(w[1]) << 16) | (pack4_nbits(w[2]) << 8) |
+            pack4_nbits(w[3]);
+  u.nl = flags4(__vcmpeq4(w[0], 0x0A0A0A0Au)) | (flags4(__vcmpeq4(w[1], 0x0A0A0A0Au)) << 4) |
+         (flags4(__vcmpeq4(w[2], 0x0A0A0A0Au)) << 8) | (flags4(__vcmpeq4(w[3], 0x0A0A0A0Au)) << 12);
+  u.nn = flags4(__vcmpeq4(w[0] | 0x20202020u, 0x6E6E6E6Eu)) |
+         (flags4(__vcmpeq4(w[1] | 0x20202020u, 0x6E6E6E6Eu)) << 4) |
+         (flags4(__vcmpeq4(w[2] | 0x20202020u, 0x6E6E6E6Eu)) << 8) |
+         (flags4(__vcmpeq4(w[3] | 0x20202020u, 0x6E6E6E6Eu)) << 12);
+  return u;
+}
+
+__device__ __forceinline__ void load_unit(const uint8_t* __restrict__ buf, unsigned long long F,
+                                          unsigned long long p, uint32_t w[4]) {
+  if (p + 16 <= F) {
+    uint4 v = __ldg(reinterpret_cast<const uint4*>(buf + p));
+    w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      uint32_t x = 0;
+      for (int b = 0; b < 4; b++) {
+        unsigned long long q = p + 4 * i + b;
+        if (q < F) x |= (uint32_t)buf[q] << (8 * b);
+      }
+      w[i] = x;
+    }
+  }
+}
+
+// Rolling state: packed codes (newest base in bits 0-1 of r0) and a history of
+// "window breakers" (newline, or N under the drop policy), newest at bit 0 of h0.
+struct Roll {
+  uint64_t r0, r1, r2;
+  uint64_t h0, h1;
+};
+
+__device__ __forceinline__ void roll_push(Roll& s, const UnitBits& u, bool drop_n) {
+  s.r2 = (s.r2 << 32) | (s.r1 >> 32);
+  s.r1 = (s.r1 << 32) | (s.r0 >> 32);
+  // an 'N' (code 7) ORs its bit 2 into the previous base's low bit (kmer_shift)
+  s.r0 = (s.r0 << 32) | (uint64_t)u.codes | ((uint64_t)u.nbits << 2);
+  uint32_t brk = u.nl | (drop_n ? u.nn : 0u);
+  uint32_t rev = __brev(brk) >> 16;  // byte j -> age 15-j
+  s.h1 = (s.h1 << 16) | (s.h0 >> 48);
+  s.h0 = (s.h0 << 16) | (uint64_t)rev;
+}
+
+template <typename KeyT>
+__device__ __forceinline__ KeyT window_key(const Roll& s, int sh, const KeyT kmask);
+
+template <>
+__device__ __forceinline__ uint64_t window_key<uint64_t>(const Roll& s, int sh, const uint64_t kmask) {
+  uint64_t x = sh ? ((s.r0 >> sh) | (s.r1 << (64 - sh))) : s.r0;
+  return x & kmask;
+}
+
+template <>
+__device__ __forceinline__ u128 window_key<u128>(const Roll& s, int sh, const u128 kmask) {
+  uint64_t lo = sh ? ((s.r0 >> sh) | (s.r1 << (64 - sh))) : s.r0;
+  uint64_t hi = sh ? ((s.r1 >> sh) | (s.r2 << (64 - sh))) : s.r1;
+  return (((u128)hi << 64) | lo) & kmask;
+}
+
+// window of ages [a, a+k) holds no breaker
+__device__ __forceinline__ bool window_clear(const Roll& s, int a, int k) {
+  uint64_t lo = a ? ((s.h0 >> a) | (s.h1 << (64 - a))) : s.h0;
+  uint64_t m = k >= 64 ? ~0ull : ((1ull << k) - 1ull);
+  return (lo & m) == 0;
+}
+
+// Reference record-start rule: a sequence line ending at `pos` (a newline) must be
+// followed by '>' when its line start p satisfies p <= F - m.
+__device__ void check_record_start(const uint8_t* __restrict__ buf, unsigned long long F, int m,
+                                   unsigned long long pos, uint8_t next, uint32_t* err) {
+  if (pos + 1 >= F || next == '>') return;
+  long long lim = (long long)F - (long long)m;
+  if (lim < 0) return;
+  bool counts = true;
+  if ((long long)pos > lim) {
+    // line start <= lim  <=>  no newline in [lim, pos)
+    for (long long q = lim; q < (long long)pos; q++)
+      if (buf[q] == '\n') { counts = false; break; }
+  }
+  if (counts) atomicOr(err, ERR_FORMAT);
+}
+
+template <typename KeyT, bool SCATTER>
+__global__ void __launch_bounds__(kExtractThreads, 1)
+k_extract(CountArgs a, KeyT* __restrict__ keys_out) {
+  extern __shared__ uint32_t s_bins[];
+  __shared__ uint32_t s_wpar[kExtractThreads / 32];
+  __shared__ uint32_t s_red[kExtractThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int NW = kExtractThreads / 32;
+  const int B = 1 << a.bbits;
+  const int k = a.k;
+  const int shift = 2 * k - a.bbits;
+  const KeyT kmask = KeyOps<KeyT>::mask(2 * k);
+  const bool drop_n = a.drop_n != 0;
+  const uint8_t* __restrict__ buf = a.fasta;
+  const unsigned long long F = a.F;
+  const unsigned long long s0 = a.sc->s0;
+  const int c = blockIdx.x;
+
+  if (!SCATTER) {
+    for (int i = tid; i < B; i += kExtractThreads) s_bins[i] = 0;
+  } else {
+    for (int i = tid; i < B; i += kExtractThreads) s_bins[i] = a.bstart[i] + a.counts[(size_t)c * B + i];
+  }
+  __syncthreads();
+
+  const unsigned long long c0 = (unsigned long long)c * a.chunk;
+  const unsigned long long c1 = min(c0 + a.chunk, F);
+  uint32_t local = 0;
+  const int warm_units = (k - 1 + 15) / 16;
+  if (c0 < c1 && s0 < F) {
+    uint32_t carry = (a.tile_nl[c0 / kTileBytes] ^ a.sc->nl_before_s0) & 1u;
+    for (unsigned long long base = c0; base < c1; base += (unsigned long long)kExtractThreads * kSegBytes) {
+      const unsigned long long seg = base + (unsigned long long)tid * kSegBytes;
+      const bool active = seg < c1;
+      uint32_t w[4][4];
+      uint32_t nlc = 0;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        unsigned long long p = seg + 16ull * u;
+        if (active && p < c1) {
+          load_unit(buf, F, p, w[u]);
+#pragma unroll
+          for (int i = 0; i < 4; i++) nlc += __popc(__vcmpeq4(w[u][i], 0x0A0A0A0Au)) >> 3;
+        } else {
+          w[u][0] = w[u][1] = w[u][2] = w[u][3] = 0;
+        }
+      }
+      // parity of the line count at the segment start (block XOR-scan)
+      const unsigned bal = __ballot_sync(FULLMASK, nlc & 1u);
+      if (lane == 0) s_wpar[warp] = __popc(bal) & 1u;
+      __syncthreads();
+      uint32_t wp = 0, tot = 0;
+#pragma unroll
+      for (int i = 0; i < NW; i++) {
+        uint32_t x = s_wpar[i];
+        tot ^= x;
+        if (i < warp) wp ^= x;
+      }
+      __syncthreads();
+      uint32_t pin = carry ^ wp ^ (__popc(bal & lanemask_lt()) & 1u);
+      carry ^= tot;
+      if (!active) continue;
+
+      Roll s;
+      s.r0 = s.r1 = s.r2 = 0;
+      s.h0 = s.h1 = 0;
+      for (int u = warm_units; u >= 1; u--) {
+        long long p = (long long)seg - 16ll * u;
+        if (p < 0) continue;
+        uint32_t ww[4];
+        load_unit(buf, F, (unsigned long long)p, ww);
+        roll_push(s, decode_unit(ww), drop_n);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const unsigned long long p = seg + 16ull * u;
+        if (p >= c1) break;
+        const UnitBits ub = decode_unit(w[u]);
+        roll_push(s, ub, drop_n);
+        // line parity per byte: exclusive prefix XOR of the newline bits
+        uint32_t x = ub.nl;
+        x ^= x << 1; x ^= x << 2; x ^= x << 4; x ^= x << 8;
+        uint32_t ex = (x << 1) & 0xffffu;
+        uint32_t odd = (pin ? ~ex : ex) & 0xffffu;
+        pin ^= __popc(ub.nl) & 1u;
+        uint32_t in = 0xffffu;
+        if (p + 16 > F) in &= (1u << (uint32_t)(F - p)) - 1u;
+        if (p < s0) in &= s0 - p >= 16 ? 0u : ~((1u << (uint32_t)(s0 - p)) - 1u);
+        if (!SCATTER) {
+          uint32_t ends = ub.nl & odd & in;  // newlines that end sequence lines
+          while (ends) {
+            int q = __ffs(ends) - 1;
+            ends &= ends - 1;
+            uint8_t next;
+            if (q < 15) next = (uint8_t)(w[u][(q + 1) >> 2] >> (8 * ((q + 1) & 3)));
+            else next = p + 16 < F ? buf[p + 16] : (uint8_t)'>';
+            check_record_start(buf, F, a.lmer_m, p + q, next, &a.sc->err);
+          }
+        }
+        uint32_t v = odd & in & ~ub.nl;
+        if (!v) continue;
+        // all 16 windows of this unit span ages [0, k+15)
+        const bool all_clear =
+            k + 15 <= 64 ? window_clear(s, 0, k + 15)
+                         : (s.h0 == 0 && (s.h1 & ((1ull << (k + 15 - 64)) - 1ull)) == 0);
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          if (!((v >> j) & 1u)) continue;
+          const int age = 15 - j;
+          if (!all_clear && !window_clear(s, age, k)) continue;
+          const KeyT key = window_key<KeyT>(s, 2 * age, kmask);
+          const uint32_t beta = (uint32_t)(key >> shift);
+          if (SCATTER) {
+            uint32_t pos = atomicAdd(&s_bins[beta], 1u);
+            if (pos < a.n_keys) keys_out[pos] = key;
+            else atomicOr(&a.sc->err, ERR_BOUNDS);
+          } else {
+            atomicAdd(&s_bins[beta], 1u);
+            local++;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (!SCATTER) {
+    for (int i = tid; i < B; i += kExtractThreads) a.counts[(size_t)c * B + i] = s_bins[i];
+    uint32_t x = local;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULLMASK, x, o);
+    if (lane == 0) s_red[warp] = x;
+    __syncthreads();
+    if (tid == 0) {
+      unsigned long long tsum = 0;
+      for (int i = 0; i < NW; i++) tsum += s_red[i];
+      if (tsum) atomicAdd(&a.sc->n_windows, tsum);
+    }
+  }
+}
+
+// counts[c][b] -> exclusive prefix over chunks (in place); totals into bstart[b].
+__global__ void __launch_bounds__(256) k_col_prefix(uint32_t* counts, int grid, int B, uint32_t* totals) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  uint32_t run = 0;
+  for (int c = 0; c < grid; c++) {
+    size_t i = (size_t)c * B + b;
+    uint32_t v = counts[i];
+    counts[i] = run;
+    run += v;
+  }
+  totals[b] = run;
+}
+
+__global__ void __launch_bounds__(1024) k_bucket_prefix(uint32_t* bstart, int B) {
+  __shared__ uint32_t s_warp[33];
+  uint32_t carry = 0;
+  for (int base = 0; base < B; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    uint32_t v = i < B ? bstart[i] : 0;
+    uint32_t tot;
+    uint32_t ex = block_exclusive_sum(v, s_warp, tot);
+    if (i < B) bstart[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) bstart[B] = carry;
+}
+
+// ------------------------------------------------------------- per-bucket table ------
+template <typename KeyT>
+struct BucketCfg;
+template <>
+struct BucketCfg<uint64_t> {
+  static constexpr int H = 8192;
+};
+template <>
+struct BucketCfg<u128> {
+  static constexpr int H = 4096;
+};
+
+template <typename KeyT>
+struct BucketSmem {
+  static constexpr int H = BucketCfg<KeyT>::H;
+  static constexpr int NW = kBucketThreads / 32;
+  static constexpr size_t off_key = 0;
+  static constexpr size_t off_cnt = off_key + sizeof(KeyT) * H;
+  static constexpr size_t off_wc = off_cnt + sizeof(uint32_t) * H;
+  static constexpr size_t off_hist = off_wc + sizeof(uint16_t) * NW * 256;
+  static constexpr size_t bytes = off_hist + sizeof(uint32_t) * kHistSmem;
+};
+
+template <typename KeyT>
+__device__ __forceinline__ bool hash_insert(KeyT* skey, uint32_t* scnt, uint32_t hmask, KeyT r,
+                                            uint32_t c) {
+  const KeyT EMPTY = ~(KeyT)0;
+  uint32_t h = (uint32_t)(KeyOps<KeyT>::hash(r) >> 40) & hmask;
+  for (uint32_t probe = 0; probe <= hmask; probe++) {
+    KeyT cur = *(volatile KeyT*)&skey[h];
+    if (cur == r) {
+      atomicAdd(&scnt[h], c);
+      return true;
+    }
+    if (cur == EMPTY) {
+      KeyT old = KeyOps<KeyT>::cas(&skey[h], EMPTY, r);
+      if (old == EMPTY || old == r) {
+        atomicAdd(&scnt[h], c);
+        return true;
+      }
+    }
+    h = (h + 1) & hmask;
+  }
+  return false;
+}
+
+template <typename KeyT>
+__global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a) {
+  using SM = BucketSmem<KeyT>;
+  constexpr int H = SM::H;
+  constexpr int NW = SM::NW;
+  constexpr int HALF = H / 2;
+  constexpr int RMAX = (HALF + kBucketThreads - 1) / kBucketThreads;  // radix rounds per warp
+  extern __shared__ __align__(16) unsigned char smem[];
+  KeyT* skey = reinterpret_cast<KeyT*>(smem + SM::off_key);
+  uint32_t* scnt = reinterpret_cast<uint32_t*>(smem + SM::off_cnt);
+  uint16_t* wc = reinterpret_cast<uint16_t*>(smem + SM::off_wc);
+  uint32_t* shist = reinterpret_cast<uint32_t*>(smem + SM::off_hist);
+  __shared__ uint32_t s_warp[33];
+  __shared__ uint32_t s_beta, s_ovf, s_T, s_d[3];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int B = 1 << a.bbits;
+  const int rem = 2 * a.k - a.bbits;  // remainder bits below the bucket id
+  const KeyT rmask = KeyOps<KeyT>::mask(rem);
+  const KeyT EMPTY = ~(KeyT)0;
+  const KeyT* __restrict__ keys = reinterpret_cast<const KeyT*>(a.keys);
+  KeyT* __restrict__ tkeys = reinterpret_cast<KeyT*>(a.tkeys);
+  const int hbins = a.t < kHistSmem ? a.t : kHistSmem;
+  for (int i = tid; i < hbins; i += kBucketThreads) shist[i] = 0;
+
+  while (true) {
+    __syncthreads();
+    if (tid == 0) s_beta = atomicAdd(&a.sc->ticket_bucket, 1u);
+    __syncthreads();
+    const uint32_t beta = s_beta;
+    if (beta >= (uint32_t)B) break;
+    const uint32_t base = a.bstart[beta];
+    const uint32_t n = a.bstart[beta + 1] - base;
+    int slog = 0;
+    while (slog < rem && (n >> slog) > (uint32_t)HALF) slog++;
+    bool haveT = false;
+    uint32_t T = 0;
+    if (n == 0) {  // empty bucket: nothing to aggregate
+      if (tid == 0) {
+        st_release(&a.flags[beta], kLbAgg);
+        unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
+        st_release(&a.flags[beta], kLbIncl | ex);
+        const uint32_t T0 = (uint32_t)ex;
+        a.tb[beta] = T0;
+        a.tsub[3 * beta] = a.tsub[3 * beta + 1] = a.tsub[3 * beta + 2] = T0;
+        if (beta == (uint32_t)B - 1) {
+          a.tb[B] = T0;
+          a.sc->n_unique = ex;
+        }
+      }
+      continue;
+    }
+    const int slog_max = rem < 20 ? rem : 20;
+    while (true) {  // attempts with more sub-passes after an overflow
+      const uint32_t nsub = 1u << slog;
+      // on-chip table sized to the bucket when it is counted in one pass
+      uint32_t Heff = (uint32_t)H;
+      if (slog == 0) {
+        Heff = 1024;
+        while (Heff < 2 * n && Heff < (uint32_t)H) Heff <<= 1;
+      }
+      const uint32_t hmask = Heff - 1;
+      uint32_t acc = 0;
+      bool ovf = false;
+      if (tid < 3) s_d[tid] = 0;
+      for (uint32_t j = 0; j < nsub; j++) {
+        for (uint32_t i = tid; i < Heff; i += kBucketThreads) {
+          skey[i] = EMPTY;
+          scnt[i] = 0;
+        }
+        if (tid == 0) s_ovf = 0;
+        __syncthreads();
+        // --- hash aggregation of this sub-range (warp-aggregated inserts)
+        for (uint32_t i0 = (uint32_t)warp * 32; i0 < n; i0 += NW * 32) {
+          const uint32_t i = i0 + lane;
+          const bool valid = i < n;
+          KeyT r = valid ? (keys[base + i] & rmask) : (KeyT)0;
+          bool mine = valid && (slog == 0 || (uint32_t)(KeyOps<KeyT>::shr(r, rem - slog) & (nsub - 1)) == j);
+          const unsigned m = __ballot_sync(FULLMASK, mine);
+          if (mine) {
+            const unsigned peers = KeyOps<KeyT>::match(m, r);
+            if (lane == __ffs(peers) - 1) {
+              if (!hash_insert<KeyT>(skey, scnt, hmask, r, (uint32_t)__popc(peers))) s_ovf = 1;
+            }
+          }
+        }
+        __syncthreads();
+        if (s_ovf) { ovf = true; break; }
+        // --- compaction of occupied slots into [0, u)
+        constexpr int SPT = H / kBucketThreads;
+        const uint32_t spt = Heff / kBucketThreads;  // >= 2 since Heff >= 1024
+        KeyT rk[SPT];
+        uint32_t rc[SPT];
+        uint32_t occ = 0;
+#pragma unroll
+        for (int q = 0; q < SPT; q++) {
+          rk[q] = EMPTY;
+          rc[q] = 0;
+          if ((uint32_t)q < spt) {
+            rk[q] = skey[tid * spt + q];
+            rc[q] = scnt[tid * spt + q];
+            occ += rk[q] != EMPTY;
+          }
+        }
+        uint32_t u;
+        uint32_t off = block_exclusive_sum(occ, s_warp, u);
+#pragma unroll
+        for (int q = 0; q < SPT; q++) {
+          if (rk[q] != EMPTY) {
+            skey[off] = rk[q];
+            scnt[off] = rc[q];
+            off++;
+          }
+        }
+        if (u > Heff / 2) { ovf = true; __syncthreads(); break; }
+        if (!haveT) {
+          if (tid == 0) {
+            if (slog == 0) st_release(&a.flags[beta], kLbAgg | (unsigned long long)u);
+            unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
+            s_T = (uint32_t)ex;
+            if (slog == 0) st_release(&a.flags[beta], kLbIncl | (ex + u));
+          }
+          __syncthreads();
+          T = s_T;
+          haveT = true;
+        }
+        __syncthreads();
+        // --- stable LSD radix sort of the u distinct remainders, 8-bit digits
+        const int sort_bits = rem - slog;
+        const int npass = (sort_bits + 7) / 8;
+        KeyT* sk = skey;
+        uint32_t* sc = scnt;
+        KeyT* dk = skey + Heff / 2;
+        uint32_t* dc = scnt + Heff / 2;
+        const uint32_t E = (u + NW - 1) / NW;
+        const uint32_t e0 = (uint32_t)warp * E;
+        const uint32_t e1 = min(e0 + E, u);
+        for (int pass = 0; pass < npass; pass++) {
+          const int sh = 8 * pass;
+          for (int i = lane; i < 256; i += 32) wc[warp * 256 + i] = 0;
+          __syncwarp();
+          uint32_t dig[RMAX], offs[RMAX];
+#pragma unroll
+          for (int rr = 0; rr < RMAX; rr++) {
+            const uint32_t idx = e0 + rr * 32 + lane;
+            const bool v = idx < e1;
+            const uint32_t d = v ? (uint32_t)(KeyOps<KeyT>::shr(sk[idx], sh) & 0xff) : 0u;
+            const unsigned vm = __ballot_sync(FULLMASK, v);
+            uint32_t bse = 0;
+            unsigned peers = 0;
+            if (v) {
+              peers = __match_any_sync(vm, d);
+              if (lane == __ffs(peers) - 1) {
+                bse = wc[warp * 256 + d];
+                wc[warp * 256 + d] = (uint16_t)(bse + __popc(peers));
+              }
+            }
+            __syncwarp();
+            const int leader = v ? __ffs(peers) - 1 : lane;
+            bse = __shfl_sync(FULLMASK, bse, leader);
+            dig[rr] = d;
+            offs[rr] = bse + __popc(peers & lanemask_lt());
+          }
+          __syncthreads();
+          // exclusive scan over (digit, warp) in digit-major order
+          {
+            constexpr int PER = (256 * NW) / kBucketThreads;
+            uint32_t vals[PER];
+            uint32_t sum = 0;
+#pragma unroll
+            for (int q = 0; q < PER; q++) {
+              const int e = tid * PER + q;  // e = d * NW + w
+              const int d = e / NW, w = e % NW;
+              vals[q] = wc[w * 256 + d];
+              sum += vals[q];
+            }
+            uint32_t tot;
+            uint32_t ex = block_exclusive_sum(sum, s_warp, tot);
+#pragma unroll
+            for (int q = 0; q < PER; q++) {
+              const int e = tid * PER + q;
+              const int d = e / NW, w = e % NW;
+              wc[w * 256 + d] = (uint16_t)ex;
+              ex += vals[q];
+            }
+          }
+          __syncthreads();
+#pragma unroll
+          for (int rr = 0; rr < RMAX; rr++) {
+            const uint32_t idx = e0 + rr * 32 + lane;
+            if (idx < e1) {
+              const uint32_t pos = wc[warp * 256 + dig[rr]] + offs[rr];
+              dk[pos] = sk[idx];
+              dc[pos] = sc[idx];
+            }
+          }
+          __syncthreads();
+          KeyT* tk = sk; sk = dk; dk = tk;
+          uint32_t* tc = sc; sc = dc; dc = tc;
+        }
+        // --- write this sub-range of the table
+        const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
+        uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
+        for (uint32_t i0 = 0; i0 < u; i0 += kBucketThreads) {
+          const uint32_t i = i0 + tid;
+          const bool v = i < u;
+          uint32_t d2 = 3;
+          if (v) {
+            const KeyT r = sk[i];
+            const uint32_t cnt = sc[i];
+            const unsigned long long row = (unsigned long long)T + acc + i;
+            if (row < a.cap) {
+              tkeys[row] = hi_bits | r;
+              a.tcounts[row] = cnt;
+            } else {
+              atomicOr(&a.sc->err, ERR_BOUNDS);
+            }
+            if (cnt < (uint32_t)a.t) {
+              if (cnt < (uint32_t)kHistSmem) atomicAdd(&shist[cnt], 1u);
+              else atomicAdd(&a.hist[cnt], 1ull);
+            }
+            d2 = (uint32_t)(KeyOps<KeyT>::shr(r, rem - 2) & 3);
+          }
+          dl0 += __popc(__ballot_sync(FULLMASK, v && d2 == 0));
+          dl1 += __popc(__ballot_sync(FULLMASK, v && d2 == 1));
+          dl2 += __popc(__ballot_sync(FULLMASK, v && d2 == 2));
+        }
+        if (lane == 0) {
+          if (dl0) atomicAdd(&s_d[0], dl0);
+          if (dl1) atomicAdd(&s_d[1], dl1);
+          if (dl2) atomicAdd(&s_d[2], dl2);
+        }
+        acc += u;
+        __syncthreads();
+      }
+      if (!ovf) {
+        if (tid == 0) {
+          if (slog > 0) st_release(&a.flags[beta], kLbIncl | ((unsigned long long)T + acc));
+          a.tb[beta] = T;
+          a.tsub[3 * beta + 0] = T + s_d[0];
+          a.tsub[3 * beta + 1] = T + s_d[0] + s_d[1];
+          a.tsub[3 * beta + 2] = T + s_d[0] + s_d[1] + s_d[2];
+          if (beta == (uint32_t)B - 1) {
+            a.tb[B] = T + acc;
+            a.sc->n_unique = (unsigned long long)T + acc;
+          }
+        }
+        break;
+      }
+      slog++;
+      if (slog > slog_max) {
+        // cannot split further: report and unblock successors
+        if (tid == 0) {
+          atomicOr(&a.sc->err, ERR_BUCKET);
+          if (!haveT) {
+            unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
+            T = (uint32_t)ex;
+          }
+          st_release(&a.flags[beta], kLbIncl | (unsigned long long)T);
+          a.tb[beta] = T;
+          a.tsub[3 * beta] = a.tsub[3 * beta + 1] = a.tsub[3 * beta + 2] = T;
+          if (beta == (uint32_t)B - 1) { a.tb[B] = T; a.sc->n_unique = T; }
+        }
+        break;
+      }
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < hbins; i += kBucketThreads)
+    if (shist[i]) atomicAdd(&a.hist[i], (unsigned long long)shist[i]);
+}
+
+// ------------------------------------------------------ histogram (other t) / cutoff --
+__global__ void __launch_bounds__(256) k_histogram(const uint32_t* __restrict__ tcounts,
+                                                   unsigned long long u, int t,
+                                                   unsigned long long* hist) {
+  __shared__ uint32_t sh[kHistSmem];
+  const int hb = t < kHistSmem ? t : kHistSmem;
+  for (int i = threadIdx.x; i < hb; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < u;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    uint32_t c = tcounts[i];
+    if (c < (uint32_t)t) {
+      if (c < (uint32_t)kHistSmem) atomicAdd(&sh[c], 1u);
+      else atomicAdd(&hist[c], 1ull);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < hb; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
+}
+
+// cutoff = first minimum of hist[1..t) (t == 1 -> 1); kept = U - sum(hist[1..cutoff))
+__global__ void __launch_bounds__(1024) k_cutoff(const unsigned long long* __restrict__ hist, int t,
+                                                 Scalars* sc) {
+  __shared__ unsigned long long s_v[32];
+  __shared__ int s_i[32];
+  unsigned long long best = ~0ull;
+  int bi = 0x7fffffff;
+  for (int c = 1 + threadIdx.x; c < t; c += blockDim.x) {
+    unsigned long long v = hist[c];
+    if (v < best || (v == best && c < bi)) { best = v; bi = c; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long v2 = __shfl_down_sync(FULLMASK, best, o);
+    int i2 = __shfl_down_sync(FULLMASK, bi, o);
+    if (v2 < best || (v2 == best && i2 < bi)) { best = v2; bi = i2; }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { s_v[warp] = best; s_i[warp] = bi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+      if (s_v[w] < best || (s_v[w] == best && s_i[w] < bi)) { best = s_v[w]; bi = s_i[w]; }
+    const int cut = t > 1 ? bi : 1;
+    unsigned long long below = 0;
+    for (int c = 1; c < cut && c < t; c++) below += hist[c];
+    sc->cutoff = (uint32_t)cut;
+    sc->n_kept = sc->n_unique - below;
+  }
+}
+
+// ----------------------------------------------------------------- macro-nodes -------
+template <typename KeyT>
+struct MnSmem {
+  static constexpr size_t off_key = 0;
+  static constexpr size_t off_cnt = off_key + sizeof(KeyT) * kMnCap;
+  static constexpr size_t off_tag = off_cnt + sizeof(uint32_t) * kMnCap;
+  static constexpr size_t off_ord = off_tag + sizeof(uint8_t) * kMnCap;
+  static constexpr size_t off_nid = off_ord + sizeof(uint16_t) * kMnCap;
+  static constexpr size_t bytes = off_nid + sizeof(uint16_t) * kMnCap;
+};
+
+template <typename KeyT>
+__device__ __forceinline__ uint32_t lower_bound_s(const KeyT* k, uint32_t lo, uint32_t hi, KeyT x) {
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (k[mid] < x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+template <typename KeyT>
+__device__ __forceinline__ uint32_t upper_bound_s(const KeyT* k, uint32_t lo, uint32_t hi, KeyT x) {
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (!(x < k[mid])) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+template <typename KeyT>
+__global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
+  using SM = MnSmem<KeyT>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  KeyT* ikey = reinterpret_cast<KeyT*>(smem + SM::off_key);
+  uint32_t* icnt = reinterpret_cast<uint32_t*>(smem + SM::off_cnt);
+  uint8_t* itag = reinterpret_cast<uint8_t*>(smem + SM::off_tag);
+  uint16_t* ord = reinterpret_cast<uint16_t*>(smem + SM::off_ord);
+  uint16_t* nid = reinterpret_cast<uint16_t*>(smem + SM::off_nid);
+  __shared__ uint32_t s_warp[33];
+  __shared__ uint32_t s_beta, s_off[6], s_NO;
+  __shared__ uint32_t s_ovf;
+
+  const int tid = threadIdx.x;
+  const int B = 1 << a.bbits;
+  const int k = a.k;
+  const int nb = 2 * (k - 1);
+  const KeyT succ_mask = KeyOps<KeyT>::mask(nb);
+  const uint32_t cut = a.sc->cutoff;
+  const KeyT* __restrict__ tkeys = reinterpret_cast<const KeyT*>(a.tkeys);
+  KeyT* __restrict__ nkeys = reinterpret_cast<KeyT*>(a.nkeys);
+
+  while (true) {
+    __syncthreads();
+    if (tid == 0) s_beta = atomicAdd(&a.sc->ticket_mn, 1u);
+    __syncthreads();
+    const uint32_t beta = s_beta;
+    if (beta >= (uint32_t)B) break;
+    if (tid == 0) { s_ovf = 0; s_off[0] = 0; }
+    __syncthreads();
+    // gather the five sorted streams, keeping counts >= cutoff
+    uint32_t len = 0;
+    for (int st = 0; st < 5; st++) {
+      uint32_t lo, hi;
+      if (st == 0) {
+        lo = a.tb[beta];
+        hi = a.tb[beta + 1];
+      } else {
+        const uint32_t f = st - 1;
+        const uint32_t bp = (f << (a.bbits - 2)) | (beta >> 2);
+        const uint32_t d = beta & 3;
+        lo = d == 0 ? a.tb[bp] : a.tsub[3 * bp + d - 1];
+        hi = d == 3 ? a.tb[bp + 1] : a.tsub[3 * bp + d];
+      }
+      for (uint32_t i0 = lo; i0 < hi; i0 += kMnThreads) {
+        const uint32_t i = i0 + tid;
+        const bool v = i < hi;
+        uint32_t c = v ? a.tcounts[i] : 0;
+        const bool keep = v && c >= cut;
+        uint32_t tot;
+        uint32_t pos = block_exclusive_sum(keep ? 1u : 0u, s_warp, tot);
+        if (keep) {
+          const uint32_t o = len + pos;
+          if (o < (uint32_t)kMnCap) {
+            const KeyT x = tkeys[i];
+            if (st == 0) {
+              ikey[o] = x >> 2;
+              itag[o] = (uint8_t)((uint32_t)(x & 3));
+            } else {
+              ikey[o] = x & succ_mask;
+              itag[o] = (uint8_t)(4 + (st - 1));
+            }
+            icnt[o] = c;
+          }
+        }
+        len += tot;
+      }
+      if (tid == 0) s_off[st + 1] = len;
+    }
+    __syncthreads();
+    const uint32_t m = len;
+    if (m > (uint32_t)kMnCap) {
+      if (tid == 0) atomicOr(&a.sc->err, ERR_MN_CAPACITY);
+    }
+    const uint32_t mm = m > (uint32_t)kMnCap ? 0u : m;
+    // merge rank of every item across the five streams
+    for (uint32_t i = tid; i < mm; i += kMnThreads) {
+      int st = 0;
+      while (i >= s_off[st + 1]) st++;
+      const KeyT x = ikey[i];
+      uint32_t rank = i - s_off[st];
+      for (int b = 0; b < 5; b++) {
+        if (b == st) continue;
+        const uint32_t lo = s_off[b], hi = s_off[b + 1];
+        rank += (b < st ? upper_bound_s(ikey, lo, hi, x) : lower_bound_s(ikey, lo, hi, x)) - lo;
+      }
+      ord[rank] = (uint16_t)i;
+    }
+    __syncthreads();
+    // node boundaries and node index per merged position
+    uint32_t nodes = 0;
+    for (uint32_t r0 = 0; r0 < mm; r0 += kMnThreads) {
+      const uint32_t r = r0 + tid;
+      uint32_t flag = 0;
+      if (r < mm) flag = (r == 0) || !(ikey[ord[r - 1]] == ikey[ord[r]]);
+      uint32_t tot;
+      uint32_t ex = block_exclusive_sum(flag, s_warp, tot);
+      if (r < mm) nid[r] = (uint16_t)(nodes + ex + flag - 1);
+      nodes += tot;
+    }
+    if (tid == 0) {
+      st_release(&a.flags[beta], kLbAgg | (unsigned long long)nodes);
+      unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
+      st_release(&a.flags[beta], kLbIncl | (ex + nodes));
+      s_NO = (uint32_t)ex;
+      if (beta == (uint32_t)B - 1) a.sc->n_nodes = ex + nodes;
+    }
+    __syncthreads();
+    const unsigned long long NO = s_NO;
+    if (NO + nodes > a.cap) {
+      if (tid == 0) atomicOr(&a.sc->err, ERR_MN_CAPACITY);
+      continue;
+    }
+    for (uint32_t r = tid; r < mm; r += kMnThreads) {
+      if (r == 0 || nid[r] != nid[r - 1]) {
+        const unsigned long long q = NO + nid[r];
+        nkeys[q] = ikey[ord[r]];
+        reinterpret_cast<uint4*>(a.nsuf)[q] = make_uint4(0, 0, 0, 0);
+        reinterpret_cast<uint4*>(a.npre)[q] = make_uint4(0, 0, 0, 0);
+      }
+    }
+    __syncthreads();
+    for (uint32_t r = tid; r < mm; r += kMnThreads) {
+      const uint32_t i = ord[r];
+      const unsigned long long q = NO + nid[r];
+      const uint32_t tg = itag[i];
+      if (tg < 4) a.nsuf[4 * q + tg] = icnt[i];
+      else a.npre[4 * q + (tg - 4)] = icnt[i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- packed KmerPairs --
+template <typename KeyT>
+__global__ void k_pack_pairs(const KeyT* __restrict__ k, const uint32_t* __restrict__ c,
+                             unsigned long long u, uint32_t* __restrict__ out) {
+  constexpr int WORDS = (sizeof(KeyT) + 4) / 4;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < u;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const KeyT x = k[i];
+    uint32_t* o = out + i * WORDS;
+#pragma unroll
+    for (int w = 0; w < WORDS - 1; w++) o[w] = (uint32_t)(x >> (32 * w));
+    o[WORDS - 1] = c[i];
+  }
+}
+
+// =================================================================== launchers =====
+static int g_sms = 0;
+static int sm_count() {
+  if (!g_sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms <= 0) g_sms = 1;
+  }
+  return g_sms;
+}
+
+size_t bucket_smem_bytes(int wide) {
+  return wide ? BucketSmem<u128>::bytes : BucketSmem<uint64_t>::bytes;
+}
+size_t mn_smem_bytes(int wide) { return wide ? MnSmem<u128>::bytes : MnSmem<uint64_t>::bytes; }
+int bucket_ctas_per_sm(int) { return 2; }
+int mn_ctas_per_sm(int wide) { return wide ? 2 : 3; }
+
+cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st) {
+  const int ntiles = (int)((a.F + kTileBytes - 1) / kTileBytes);
+  if (ntiles > 0) k_line_scan<<<ntiles, 256, 0, st>>>(a.fasta, a.F, a.tile_nl, a.sc);
+  k_tile_prefix<<<1, 1024, 0, st>>>(a.fasta, a.F, a.tile_nl, ntiles, a.sc);
+  return cudaGetLastError();
+}
+
+template <typename KeyT, bool SCATTER>
+static cudaError_t launch_extract_t(const CountArgs& a, KeyT* out, cudaStream_t st) {
+  const size_t smem = sizeof(uint32_t) << a.bbits;
+  cudaError_t e = cudaFuncSetAttribute(k_extract<KeyT, SCATTER>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_extract<KeyT, SCATTER><<<a.grid, kExtractThreads, smem, st>>>(a, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_count(const CountArgs& a, int wide, cudaStream_t st) {
+  return wide ? launch_extract_t<u128, false>(a, nullptr, st)
+              : launch_extract_t<uint64_t, false>(a, nullptr, st);
+}
+
+cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st) {
+  const int B = 1 << a.bbits;
+  k_col_prefix<<<(B + 255) / 256, 256, 0, st>>>(a.counts, a.grid, B, a.bstart);
+  k_bucket_prefix<<<1, 1024, 0, st>>>(a.bstart, B);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const CountArgs& a, void* keys_out, int wide, cudaStream_t st) {
+  return wide ? launch_extract_t<u128, true>(a, reinterpret_cast<u128*>(keys_out), st)
+              : launch_extract_t<uint64_t, true>(a, reinterpret_cast<uint64_t*>(keys_out), st);
+}
+
+template <typename KeyT>
+static cudaError_t launch_bucket_t(const BucketArgs& a, int grid, cudaStream_t st) {
+  const size_t smem = BucketSmem<KeyT>::bytes;
+  cudaError_t e = cudaFuncSetAttribute(k_bucket_table<KeyT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (grid <= 0) grid = sm_count() * bucket_ctas_per_sm(sizeof(KeyT) == 16);
+  k_bucket_table<KeyT><<<grid, kBucketThreads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_table(const BucketArgs& a, int wide, int grid, cudaStream_t st) {
+  return wide ? launch_bucket_t<u128>(a, grid, st) : launch_bucket_t<uint64_t>(a, grid, st);
+}
+
+cudaError_t launch_histogram(const uint32_t* tcounts, unsigned long long u, int t,
+                             unsigned long long* hist, cudaStream_t st) {
+  int grid = (int)((u + 255) / 256);
+  if (grid > sm_count() * 8) grid = sm_count() * 8;
+  if (grid < 1) grid = 1;
+  k_histogram<<<grid, 256, 0, st>>>(tcounts, u, t, hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cutoff(const unsigned long long* hist, int t, Scalars* sc, cudaStream_t st) {
+  k_cutoff<<<1, 1024, 0, st>>>(hist, t, sc);
+  return cudaGetLastError();
+}
+
+template <typename KeyT>
+static cudaError_t launch_mn_t(const MnArgs& a, int grid, cudaStream_t st) {
+  const size_t smem = MnSmem<KeyT>::bytes;
+  cudaError_t e = cudaFuncSetAttribute(k_macro_nodes<KeyT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (grid <= 0) grid = sm_count() * mn_ctas_per_sm(sizeof(KeyT) == 16);
+  k_macro_nodes<KeyT><<<grid, kMnThreads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_macro_nodes(const MnArgs& a, int wide, int grid, cudaStream_t st) {
+  return wide ? launch_mn_t<u128>(a, grid, st) : launch_mn_t<uint64_t>(a, grid, st);
+}
+
+cudaError_t launch_pack_pairs(const void* tkeys, const uint32_t* tcounts, unsigned long long u,
+                              int wide, void* out, cudaStream_t st) {
+  if (u == 0) return cudaSuccess;
+  int grid = (int)((u + 255) / 256);
+  if (grid > sm_count() * 16) grid = sm_count() * 16;
+  if (wide)
+    k_pack_pairs<u128><<<grid, 256, 0, st>>>(reinterpret_cast<const u128*>(tkeys), tcounts, u,
+                                             reinterpret_cast<uint32_t*>(out));
+  else
+    k_pack_pairs<uint64_t><<<grid, 256, 0, st>>>(reinterpret_cast<const uint64_t*>(tkeys), tcounts,
+                                                 u, reinterpret_cast<uint32_t*>(out));
+  return cudaGetLastError();
+}
+
+}  // namespace pk

@@ -116,6 +116,77 @@ def sample_reads(rng, genome: np.ndarray, n_reads: int, read_len, err: float,
     return out
 
 
+def _header_block(first_index: int, n: int):
+    """Concatenated b">r<i>\n" headers and their lengths, built without a Python loop."""
+    ids = np.arange(first_index, first_index + n, dtype=np.int64)
+    nd = np.ones(n, dtype=np.int64)
+    x = ids.copy()
+    while True:
+        x //= 10
+        more = x > 0
+        if not more.any():
+            break
+        nd += more
+    hl = nd + 3  # '>' 'r' digits '\n'
+    off = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(hl, out=off[1:])
+    hb = np.empty(int(off[-1]), dtype=np.uint8)
+    hb[off[:-1]] = ord(">")
+    hb[off[:-1] + 1] = ord("r")
+    hb[off[1:] - 1] = ord("\n")
+    v = ids.copy()
+    for d in range(int(nd.max())):
+        has = nd > d
+        pos = off[:-1] + 2 + nd - 1 - d
+        hb[pos[has]] = (48 + v[has] % 10).astype(np.uint8)
+        v //= 10
+    return hb, hl
+
+
+def matrix_to_fasta(mat: np.ndarray, first_index: int = 0) -> bytes:
+    """FASTA for equal-length reads given as an (n, L) uint8 ASCII matrix."""
+    n, L = mat.shape
+    if n == 0:
+        return b""
+    hb, hl = _header_block(first_index, n)
+    rec = hl + L + 1
+    off = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(rec, out=off[1:])
+    buf = np.empty(int(off[-1]), dtype=np.uint8)
+    hoff = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(hl, out=hoff[1:])
+    hpos = np.repeat(off[:-1] - hoff[:-1], hl) + np.arange(hb.size)
+    buf[hpos] = hb
+    spos = (off[:-1] + hl)[:, None] + np.arange(L)[None, :]
+    buf[spos] = mat
+    buf[off[1:] - 1] = ord("\n")
+    return buf.tobytes()
+
+
+def sample_read_matrix(rng, genome: np.ndarray, n_reads: int, read_len: int, err: float,
+                       random_strand: bool = True, n_rate: float = 0.0) -> np.ndarray:
+    """Equal-length reads as an (n, L) ASCII matrix."""
+    out = np.empty((n_reads, read_len), dtype=np.uint8)
+    chunk = 1 << 18
+    for c0 in range(0, n_reads, chunk):
+        c1 = min(n_reads, c0 + chunk)
+        m = c1 - c0
+        starts = rng.integers(0, genome.size - read_len + 1, size=m)
+        codes = genome[starts[:, None] + np.arange(read_len)[None, :]]
+        if err > 0:
+            e = rng.random(codes.shape) < err
+            codes = np.where(e, (codes + rng.integers(1, 4, size=codes.shape)) & 3, codes)
+        if random_strand:
+            rev = rng.random(m) < 0.5
+            codes = np.where(rev[:, None], 3 - codes[:, ::-1], codes)
+        asc = _ACGT[codes]
+        if n_rate > 0:
+            nm = rng.random(asc.shape) < n_rate
+            asc = np.where(nm, np.uint8(_N), asc)
+        out[c0:c1] = asc
+    return out
+
+
 def reads_to_fasta(reads: Sequence[np.ndarray], first_index: int = 0) -> bytes:
     """One ``>r<i>`` header line and one sequence line per read."""
     n = len(reads)
@@ -200,8 +271,8 @@ def config1(scale: float = 1.0) -> ReadSet:
     glen = int(1_000_000 * scale)
     genome = random_genome(g, glen, 0.5)
     n = int(round(30 * glen / 100))
-    reads = sample_reads(_rng(2001), genome, n, 100, 0.01)
-    return ReadSet("plain-1Mbp-30x-k32", reads_to_fasta(reads), 32, 30, 100, n, glen)
+    mat = sample_read_matrix(_rng(2001), genome, n, 100, 0.01)
+    return ReadSet("plain-1Mbp-30x-k32", matrix_to_fasta(mat), 32, 30, 100, n, glen)
 
 
 def config2(scale: float = 1.0) -> ReadSet:
@@ -213,8 +284,8 @@ def config2(scale: float = 1.0) -> ReadSet:
     unit = min(5000, max(200, glen // 200))
     frac = plant_repeat_families(g, genome, 20, unit, 3, 6, 0.5)
     n = int(round(80 * glen / 100))
-    reads = sample_reads(_rng(2002), genome, n, 100, 0.005)
-    return ReadSet("bacterial-4.6Mbp-80x-k32", reads_to_fasta(reads), 32, 80, 100, n, glen,
+    mat = sample_read_matrix(_rng(2002), genome, n, 100, 0.005)
+    return ReadSet("bacterial-4.6Mbp-80x-k32", matrix_to_fasta(mat), 32, 80, 100, n, glen,
                    repeat_fraction=frac)
 
 
@@ -226,8 +297,8 @@ def config3(scale: float = 1.0) -> ReadSet:
     genome = random_genome(g, glen, 0.45)
     frac = plant_tandem_and_interspersed(g, genome, 0.10, 2, 500, 0.45)
     n = int(round(40 * glen / 150))
-    reads = sample_reads(_rng(2003), genome, n, 150, 0.003, n_rate=0.0005)
-    return ReadSet("longk-50Mbp-40x-k63", reads_to_fasta(reads), 63, 40, 150, n, glen,
+    mat = sample_read_matrix(_rng(2003), genome, n, 150, 0.003, n_rate=0.0005)
+    return ReadSet("longk-50Mbp-40x-k63", matrix_to_fasta(mat), 63, 40, 150, n, glen,
                    drop_n=True, repeat_fraction=frac)
 
 
@@ -255,8 +326,8 @@ def config5_job(index: int, scale: float = 1.0) -> ReadSet:
     k = int(g.choice([31, 32, 63]))
     genome = random_genome(g, glen, 0.5)
     n = max(1, int(round(cov * glen / 100)))
-    reads = sample_reads(g, genome, n, 100, 0.005)
-    return ReadSet(f"serve-job-{index}", reads_to_fasta(reads), k, cov, 100, n, glen)
+    mat = sample_read_matrix(g, genome, n, 100, 0.005)
+    return ReadSet(f"serve-job-{index}", matrix_to_fasta(mat), k, cov, 100, n, glen)
 
 
 def small_case(seed: int, genome_len: int = 2000, n_reads: int = 300, read_len=100,

@@ -1,0 +1,57 @@
+"""C-ABI library checks that need no GPU: it loads, exports every function the
+public headers declare, and fails loudly (no CPU fallback) without a device."""
+import ctypes
+
+import pytest
+
+import pakman_plus_gb300 as pk
+from pakman_plus_gb300 import build as pkbuild
+from pakman_plus_gb300 import capi
+
+
+@pytest.fixture(scope="module")
+def lib():
+    pkbuild.build()
+    return capi.lib()
+
+
+def test_every_declared_function_is_exported(lib):
+    names = capi.header_functions()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(capi._SIGS), set(names) ^ set(capi._SIGS)
+
+
+def test_params_layout_matches_c(lib):
+    p = capi.default_params()
+    assert ctypes.sizeof(capi.PkParams) == 64
+    assert ctypes.sizeof(capi.PkSummary) == 48
+    assert (p.k, p.lmer_length, p.num_buckets, p.batch_kmers) == (32, 8, 21, 100_000_000)
+
+
+def test_status_strings(lib):
+    assert capi.status_string(capi.PK_OK) == "ok"
+    assert "'>'" in capi.status_string(capi.PK_ERR_FORMAT)
+    assert capi.status_string(99) == "unknown status"
+
+
+def test_null_arguments_are_rejected(lib):
+    assert lib.pk_job_sync(None) == capi.PK_ERR_INVALID
+    assert lib.pk_count(None, None, 0, None) == capi.PK_ERR_INVALID
+    assert lib.pk_cutoff(None, 21, None, None, None) == capi.PK_ERR_INVALID
+    assert lib.pk_ctx_create(0, 0, None) == capi.PK_ERR_INVALID
+
+
+def test_no_cpu_fallback_without_device(lib):
+    n = ctypes.c_int()
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(pk.PakmanError) as e:
+        pk.Context(0)
+    assert e.value.status == capi.PK_ERR_NO_DEVICE
