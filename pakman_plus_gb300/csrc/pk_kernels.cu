@@ -242,7 +242,7 @@ __device__ __forceinline__ uint32_t flags4(uint32_t eq) {
 
 struct UnitBits {
   uint32_t codes;  // base j at bits 2(15-j)+1..2(15-j)
-  uint32_t nbits;  // code bit 2 of base j at bit 2(15-j)
+  uint32_t nbits;  // code bit 2 of byte j at bit 2(15-j)
   uint32_t nl;     // bit j: byte j is '\n'
   uint32_t nn;     // bit j: byte j is 'N' or 'n'
 };
@@ -280,38 +280,50 @@ __device__ __forceinline__ void load_unit(const uint8_t* __restrict__ buf, unsig
   }
 }
 
-// Rolling state: packed codes (newest base in bits 0-1 of r0) and a history of
-// "window breakers" (newline, or N under the drop policy), newest at bit 0 of h0.
+// Rolling state: packed 2-bit codes (newest base in bits 0-1 of r0), the bit-2 plane
+// of the codes at each byte's own low-bit position (n*), and a history of "window
+// breakers" (newline, or N under the drop policy), newest at bit 0 of h0.
 struct Roll {
   uint64_t r0, r1, r2;
+  uint64_t n0, n1, n2;
   uint64_t h0, h1;
 };
 
 __device__ __forceinline__ void roll_push(Roll& s, const UnitBits& u, bool drop_n) {
   s.r2 = (s.r2 << 32) | (s.r1 >> 32);
   s.r1 = (s.r1 << 32) | (s.r0 >> 32);
-  // an 'N' (code 7) ORs its bit 2 into the previous base's low bit (kmer_shift)
-  s.r0 = (s.r0 << 32) | (uint64_t)u.codes | ((uint64_t)u.nbits << 2);
+  s.r0 = (s.r0 << 32) | (uint64_t)u.codes;
+  s.n2 = (s.n2 << 32) | (s.n1 >> 32);
+  s.n1 = (s.n1 << 32) | (s.n0 >> 32);
+  s.n0 = (s.n0 << 32) | (uint64_t)u.nbits;
   uint32_t brk = u.nl | (drop_n ? u.nn : 0u);
   uint32_t rev = __brev(brk) >> 16;  // byte j -> age 15-j
   s.h1 = (s.h1 << 16) | (s.h0 >> 48);
   s.h0 = (s.h0 << 16) | (uint64_t)rev;
 }
 
+// The k-mer whose newest byte has age sh/2: kmer_shift ORs a byte's code bit 2 into
+// the previous base's low bit, so only bytes inside the window (age >= sh/2)
+// contribute their bit-2 plane, shifted up by one base.
 template <typename KeyT>
 __device__ __forceinline__ KeyT window_key(const Roll& s, int sh, const KeyT kmask);
 
 template <>
 __device__ __forceinline__ uint64_t window_key<uint64_t>(const Roll& s, int sh, const uint64_t kmask) {
   uint64_t x = sh ? ((s.r0 >> sh) | (s.r1 << (64 - sh))) : s.r0;
-  return x & kmask;
+  uint64_t n = sh ? ((s.n0 >> sh) | (s.n1 << (64 - sh))) : s.n0;
+  return (x | (n << 2)) & kmask;
 }
 
 template <>
 __device__ __forceinline__ u128 window_key<u128>(const Roll& s, int sh, const u128 kmask) {
   uint64_t lo = sh ? ((s.r0 >> sh) | (s.r1 << (64 - sh))) : s.r0;
   uint64_t hi = sh ? ((s.r1 >> sh) | (s.r2 << (64 - sh))) : s.r1;
-  return (((u128)hi << 64) | lo) & kmask;
+  uint64_t nlo = sh ? ((s.n0 >> sh) | (s.n1 << (64 - sh))) : s.n0;
+  uint64_t nhi = sh ? ((s.n1 >> sh) | (s.n2 << (64 - sh))) : s.n1;
+  const u128 x = ((u128)hi << 64) | lo;
+  const u128 n = ((u128)nhi << 64) | nlo;
+  return (x | (n << 2)) & kmask;
 }
 
 // window of ages [a, a+k) holds no breaker
@@ -402,6 +414,7 @@ k_extract(CountArgs a, KeyT* __restrict__ keys_out) {
 
       Roll s;
       s.r0 = s.r1 = s.r2 = 0;
+      s.n0 = s.n1 = s.n2 = 0;
       s.h0 = s.h1 = 0;
       for (int u = warm_units; u >= 1; u--) {
         long long p = (long long)seg - 16ll * u;
