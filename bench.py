@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-windows", type=int, default=60_000_000)
+    ap.add_argument("--bucket-bits", type=int, default=0, help="partition digits (0 = automatic)")
     return ap.parse_args()
 
 
@@ -226,7 +227,8 @@ def main():
     stream = torch.cuda.Stream(device=local)
     job = pk.Job(ctx, stream=stream.cuda_stream)
     params = pk.default_params(k=rs.k, num_buckets=rs.t, coverage=rs.coverage, read_length=rs.read_len,
-                               drop_n=int(rs.drop_n), batch_kmers=rs.batch)
+                               drop_n=int(rs.drop_n), batch_kmers=rs.batch,
+                               bucket_bits=args.bucket_bits)
     job.enable_timing(True)
     torch.cuda.synchronize()
     for _ in range(args.warmup):

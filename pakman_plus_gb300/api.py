@@ -192,10 +192,16 @@ class Job:
 
     # -- histogram cutoff
     def cutoff(self, num_buckets: int) -> Tuple[int, np.ndarray, int]:
+        """(cutoff, histogram, kept rows).  Raises EmptyAfterCutoff (carrying the same
+        three values as attributes) when no row reaches the cutoff."""
         cut, kept = c_uint32(), c_uint64()
         hist = np.zeros(num_buckets, np.uint64)
-        check(capi.lib().pk_cutoff(self._h, num_buckets, byref(cut), hist.ctypes.data, byref(kept)),
-              "pk_cutoff")
+        try:
+            check(capi.lib().pk_cutoff(self._h, num_buckets, byref(cut), hist.ctypes.data,
+                                       byref(kept)), "pk_cutoff")
+        except EmptyAfterCutoff as e:
+            e.cutoff, e.hist, e.kept = cut.value, hist, kept.value
+            raise
         return cut.value, hist, kept.value
 
     # -- macro-nodes

@@ -18,6 +18,8 @@
 
 using namespace pk;
 
+static const int kMaxPartitionBits = 13;
+
 // ------------------------------------------------------------------ errors ------
 static thread_local std::string t_last_error;
 
@@ -83,8 +85,9 @@ struct pk_job {
   uint64_t mn_cap = 0;
   Scalars* d_sc = nullptr;
   Scalars* h_sc = nullptr;  // pinned mirror
-  DevBuf fasta, tile_nl, counts, bstart, keys, tkeys, tcounts, tb, tsub, flags_b, flags_m, hist,
-      hist2, nkeys, nsuf, npre, packed;
+  DevBuf fasta, tile_nl, counts, bstart, keys, tkeys, tcounts, tu, tsub, flags_m, hist, hist2,
+      nkeys, nsuf, npre, packed, doff, dkeys, dcounts;
+  bool dense_valid = false;
   bool timing = false;
   cudaEvent_t ev0[ST_COUNT_] = {}, ev1[ST_COUNT_] = {};
   bool ev_rec[ST_COUNT_] = {};
@@ -133,9 +136,11 @@ static void job_free(pk_job* j, DevBuf& b) {
 
 static void job_free_all(pk_job* j) {
   DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->keys,  &j->tkeys,
-                   &j->tcounts, &j->tb,    &j->tsub,    &j->flags_b, &j->flags_m, &j->hist,
-                   &j->hist2,  &j->nkeys,  &j->nsuf,    &j->npre,    &j->packed};
+                   &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
+                   &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
+                   &j->dcounts};
   for (DevBuf* b : all) job_free(j, *b);
+  j->dense_valid = false;
 }
 
 // per-stage CUDA events on the job's stream (begin/end pairs, so host-side gaps
@@ -298,8 +303,9 @@ pk_status pk_job_sync(pk_job* j) {
 pk_status pk_job_memory(pk_job* j, uint64_t* bytes) {
   if (!j || !bytes) return fail(PK_ERR_INVALID, "null argument");
   DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->keys,  &j->tkeys,
-                   &j->tcounts, &j->tb,    &j->tsub,    &j->flags_b, &j->flags_m, &j->hist,
-                   &j->hist2,  &j->nkeys,  &j->nsuf,    &j->npre,    &j->packed};
+                   &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
+                   &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
+                   &j->dcounts};
   uint64_t s = 0;
   for (DevBuf* b : all) s += b->bytes;
   *bytes = s;
@@ -346,16 +352,16 @@ static pk_status check_params(const pk_params* p) {
   return PK_OK;
 }
 
+// Partition digits: the leading key bits that pick a bucket.  Two limits meet here:
+// the scatter keeps one partially filled 32-byte sector per (CTA, bucket) in L2, so
+// 2^bits buckets x one CTA per SM must stay well inside the 126 MB L2 (<= 2^13); and a
+// bucket's distinct keys should fit the on-chip table of the per-bucket kernel.
 static int auto_bucket_bits(uint64_t F, int k, int wide) {
-  // leading-key-bit partition sized so an average bucket fills about half of the
-  // on-chip hash table of the per-bucket kernel
-  const double per_bucket = wide ? 2048.0 : 4096.0;
-  const double est = 0.7 * (double)F;  // k-mer windows per input byte for ~100 bp reads
+  const double per_bucket = wide ? 6000.0 : 12000.0;  // keys per bucket aimed at
+  const double est = 0.7 * (double)F;                 // k-mer windows per byte, ~100 bp reads
   int b = 2;
-  while (b < 15 && est / (double)(1u << b) > per_bucket) b++;
-  int cap = 2 * k - 2;
-  if (cap > 15) cap = 15;
-  return std::max(2, std::min(b, cap));
+  while (b < kMaxPartitionBits && est / (double)(1u << b) > per_bucket) b++;
+  return std::max(2, std::min(b, 2 * k - 2));
 }
 
 // Stages 1-5: device FASTA -> sorted (k-mer, count) table, resident.
@@ -424,15 +430,13 @@ static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk
   a.n_keys = N;
   PK_TRY(job_alloc(j, j->tkeys, (size_t)W * N));
   PK_TRY(job_alloc(j, j->tcounts, sizeof(uint32_t) * N));
-  PK_TRY(job_alloc(j, j->tb, sizeof(uint32_t) * (B + 1)));
+  PK_TRY(job_alloc(j, j->tu, sizeof(uint32_t) * (size_t)B));
   PK_TRY(job_alloc(j, j->tsub, sizeof(uint32_t) * 3 * (size_t)B));
-  PK_TRY(job_alloc(j, j->flags_b, sizeof(unsigned long long) * B));
   const int t = p->num_buckets;
   PK_TRY(job_alloc(j, j->hist, sizeof(unsigned long long) * (size_t)t));
-  PK_CUDA(cudaMemsetAsync(j->flags_b.p, 0, sizeof(unsigned long long) * B, j->stream));
   PK_CUDA(cudaMemsetAsync(j->hist.p, 0, sizeof(unsigned long long) * (size_t)t, j->stream));
-  PK_CUDA(cudaMemsetAsync(j->tb.p, 0, sizeof(uint32_t) * (B + 1), j->stream));
   j->t_hist = t;
+  j->dense_valid = false;
 
   mark_begin(j, ST_SCATTER);
   PK_CUDA(launch_scatter(a, j->keys.p, j->wide, j->stream));
@@ -443,9 +447,8 @@ static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk
   b.bstart = (const uint32_t*)j->bstart.p;
   b.tkeys = j->tkeys.p;
   b.tcounts = (uint32_t*)j->tcounts.p;
-  b.tb = (uint32_t*)j->tb.p;
+  b.tu = (uint32_t*)j->tu.p;
   b.tsub = (uint32_t*)j->tsub.p;
-  b.flags = (unsigned long long*)j->flags_b.p;
   b.hist = (unsigned long long*)j->hist.p;
   b.t = t;
   b.k = k;
@@ -504,14 +507,32 @@ pk_status pk_table_info(pk_job* j, uint64_t* u, uint64_t* w, uint64_t* r) {
   return PK_OK;
 }
 
+// Dense (contiguous, ascending) copy of the resident sparse table, built on demand.
+static pk_status materialize_dense(pk_job* j) {
+  if (j->dense_valid) return PK_OK;
+  const uint64_t u = j->h_sc->n_unique;
+  const int B = 1 << j->bbits;
+  const size_t W = j->wide ? 16 : 8;
+  PK_TRY(job_alloc(j, j->doff, sizeof(uint32_t) * (B + 1)));
+  PK_TRY(job_alloc(j, j->dkeys, W * (u ? u : 1)));
+  PK_TRY(job_alloc(j, j->dcounts, 4 * (u ? u : 1)));
+  PK_CUDA(launch_row_offsets((const uint32_t*)j->tu.p, (uint32_t*)j->doff.p, B, j->stream));
+  PK_CUDA(launch_compact_rows(j->tkeys.p, (const uint32_t*)j->tcounts.p, (const uint32_t*)j->bstart.p,
+                              (const uint32_t*)j->tu.p, (const uint32_t*)j->doff.p, B, j->wide,
+                              j->dkeys.p, (uint32_t*)j->dcounts.p, nullptr, j->stream));
+  j->dense_valid = true;
+  return PK_OK;
+}
+
 pk_status pk_copy_table(pk_job* j, void* keys, uint32_t* counts, uint64_t cap) {
   uint64_t u = 0;
   PK_TRY(pk_table_info(j, &u, nullptr, nullptr));
   if (cap < u) return fail(PK_ERR_INVALID, "capacity smaller than the table");
   const size_t W = j->wide ? 16 : 8;
-  if (u && keys) PK_CUDA(cudaMemcpyAsync(keys, j->tkeys.p, W * u, cudaMemcpyDeviceToHost, j->stream));
+  PK_TRY(materialize_dense(j));
+  if (u && keys) PK_CUDA(cudaMemcpyAsync(keys, j->dkeys.p, W * u, cudaMemcpyDeviceToHost, j->stream));
   if (u && counts)
-    PK_CUDA(cudaMemcpyAsync(counts, j->tcounts.p, 4 * u, cudaMemcpyDeviceToHost, j->stream));
+    PK_CUDA(cudaMemcpyAsync(counts, j->dcounts.p, 4 * u, cudaMemcpyDeviceToHost, j->stream));
   PK_CUDA(cudaStreamSynchronize(j->stream));
   return PK_OK;
 }
@@ -522,8 +543,13 @@ pk_status pk_copy_table_packed(pk_job* j, void* pairs, uint64_t cap) {
   if (cap < u) return fail(PK_ERR_INVALID, "capacity smaller than the table");
   if (!u) return PK_OK;
   const size_t rec = j->wide ? 20 : 12;
+  const int B = 1 << j->bbits;
+  PK_TRY(job_alloc(j, j->doff, sizeof(uint32_t) * (B + 1)));
   PK_TRY(job_alloc(j, j->packed, rec * u));
-  PK_CUDA(launch_pack_pairs(j->tkeys.p, (const uint32_t*)j->tcounts.p, u, j->wide, j->packed.p, j->stream));
+  PK_CUDA(launch_row_offsets((const uint32_t*)j->tu.p, (uint32_t*)j->doff.p, B, j->stream));
+  PK_CUDA(launch_compact_rows(j->tkeys.p, (const uint32_t*)j->tcounts.p, (const uint32_t*)j->bstart.p,
+                              (const uint32_t*)j->tu.p, (const uint32_t*)j->doff.p, B, j->wide, nullptr,
+                              nullptr, j->packed.p, j->stream));
   PK_CUDA(cudaMemcpyAsync(pairs, j->packed.p, rec * u, cudaMemcpyDeviceToHost, j->stream));
   PK_CUDA(cudaStreamSynchronize(j->stream));
   job_free(j, j->packed);
@@ -533,8 +559,12 @@ pk_status pk_copy_table_packed(pk_job* j, void* pairs, uint64_t cap) {
 pk_status pk_table_device(pk_job* j, const void** k, const uint32_t** c) {
   if (!j) return fail(PK_ERR_INVALID, "job is null");
   if (j->stage < 1) return fail(PK_ERR_STATE, "no table: call pk_count first");
-  if (k) *k = j->tkeys.p;
-  if (c) *c = (const uint32_t*)j->tcounts.p;
+  PK_TRY(set_device(j->ctx));
+  PK_TRY(sync_scalars(j));
+  PK_TRY(materialize_dense(j));
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  if (k) *k = j->dkeys.p;
+  if (c) *c = (const uint32_t*)j->dcounts.p;
   return PK_OK;
 }
 
@@ -546,7 +576,8 @@ static pk_status cutoff_enqueue(pk_job* j, int t) {
     PK_TRY(sync_scalars(j));
     PK_TRY(job_alloc(j, j->hist2, sizeof(unsigned long long) * (size_t)t));
     PK_CUDA(cudaMemsetAsync(j->hist2.p, 0, sizeof(unsigned long long) * (size_t)t, j->stream));
-    PK_CUDA(launch_histogram((const uint32_t*)j->tcounts.p, j->h_sc->n_unique, t,
+    PK_TRY(materialize_dense(j));
+    PK_CUDA(launch_histogram((const uint32_t*)j->dcounts.p, j->h_sc->n_unique, t,
                              (unsigned long long*)j->hist2.p, j->stream));
     hist = (const unsigned long long*)j->hist2.p;
   }
@@ -591,7 +622,8 @@ static pk_status mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) 
   MnArgs m{};
   m.tkeys = j->tkeys.p;
   m.tcounts = (const uint32_t*)j->tcounts.p;
-  m.tb = (const uint32_t*)j->tb.p;
+  m.bstart = (const uint32_t*)j->bstart.p;
+  m.tu = (const uint32_t*)j->tu.p;
   m.tsub = (const uint32_t*)j->tsub.p;
   m.flags = (unsigned long long*)j->flags_m.p;
   m.nkeys = j->nkeys.p;

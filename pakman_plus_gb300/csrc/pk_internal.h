@@ -55,14 +55,15 @@ struct CountArgs {
   Scalars* sc;
 };
 
+// The table is kept "sparse": the u rows of bucket b sit at [bstart[b], bstart[b] + u),
+// inside the bucket's own key range, ascending.
 struct BucketArgs {
   const void* keys;          // bucketed keys (uint64 or u128), N entries
   const uint32_t* bstart;    // 2^bbits + 1
-  void* tkeys;               // table keys out
-  uint32_t* tcounts;         // table counts out
-  uint32_t* tb;              // 2^bbits + 1 table bucket starts out
-  uint32_t* tsub;            // 3 * 2^bbits: table index where next-2-bit digit 1,2,3 starts
-  unsigned long long* flags; // 2^bbits look-back words (zeroed)
+  void* tkeys;               // table keys out (N capacity)
+  uint32_t* tcounts;         // table counts out (N capacity)
+  uint32_t* tu;              // 2^bbits: rows per bucket
+  uint32_t* tsub;            // 3 * 2^bbits: rows of the bucket whose next 2 key bits are < 1, 2, 3
   unsigned long long* hist;  // t bins (zeroed)
   int t;
   int k;
@@ -74,7 +75,8 @@ struct BucketArgs {
 struct MnArgs {
   const void* tkeys;
   const uint32_t* tcounts;
-  const uint32_t* tb;
+  const uint32_t* bstart;
+  const uint32_t* tu;
   const uint32_t* tsub;
   unsigned long long* flags; // 2^bbits look-back words (zeroed)
   void* nkeys;               // node keys out (capacity cap)
@@ -96,8 +98,12 @@ cudaError_t launch_histogram(const uint32_t* tcounts, unsigned long long u, int 
                              unsigned long long* hist, cudaStream_t st);
 cudaError_t launch_cutoff(const unsigned long long* hist, int t, Scalars* sc, cudaStream_t st);
 cudaError_t launch_macro_nodes(const MnArgs& a, int wide, int grid, cudaStream_t st);
-cudaError_t launch_pack_pairs(const void* tkeys, const uint32_t* tcounts, unsigned long long u,
-                              int wide, void* out, cudaStream_t st);
+// Dense copy of the sparse table (doff: exclusive prefix of tu, computed by
+// launch_row_offsets).  packed != null writes KmerPairs records instead of arrays.
+cudaError_t launch_row_offsets(const uint32_t* tu, uint32_t* doff, int B, cudaStream_t st);
+cudaError_t launch_compact_rows(const void* tkeys, const uint32_t* tcounts, const uint32_t* bstart,
+                                const uint32_t* tu, const uint32_t* doff, int B, int wide,
+                                void* dkeys, uint32_t* dcounts, void* packed, cudaStream_t st);
 
 size_t bucket_smem_bytes(int wide);
 size_t mn_smem_bytes(int wide);

@@ -563,6 +563,12 @@ __device__ __forceinline__ bool hash_insert(KeyT* skey, uint32_t* scnt, uint32_t
   return false;
 }
 
+// Per bucket: aggregate the bucket's keys into (remainder, count) in an on-chip
+// hash table, radix-sort the distinct remainders and write them as table rows at
+// the bucket's own key range [bstart, bstart + u) ("sparse" table: no inter-bucket
+// dependency).  When the distinct keys of a bucket exceed the on-chip capacity the
+// bucket is counted in 2^slog sub-passes, each taking the keys whose next slog
+// remainder bits equal the sub-pass index (so sub-passes come out in key order).
 template <typename KeyT>
 __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a) {
   using SM = BucketSmem<KeyT>;
@@ -576,7 +582,8 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   uint16_t* wc = reinterpret_cast<uint16_t*>(smem + SM::off_wc);
   uint32_t* shist = reinterpret_cast<uint32_t*>(smem + SM::off_hist);
   __shared__ uint32_t s_warp[33];
-  __shared__ uint32_t s_beta, s_ovf, s_T, s_d[3];
+  __shared__ uint32_t s_beta, s_ovf, s_d[3];
+  __shared__ float s_ratio;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int B = 1 << a.bbits;
@@ -587,6 +594,8 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   KeyT* __restrict__ tkeys = reinterpret_cast<KeyT*>(a.tkeys);
   const int hbins = a.t < kHistSmem ? a.t : kHistSmem;
   for (int i = tid; i < hbins; i += kBucketThreads) shist[i] = 0;
+  if (tid == 0) s_ratio = 0.5f;  // running distinct/keys ratio of this CTA's buckets
+  const int slog_max = rem < 20 ? rem : 20;
 
   while (true) {
     __syncthreads();
@@ -596,36 +605,26 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
     if (beta >= (uint32_t)B) break;
     const uint32_t base = a.bstart[beta];
     const uint32_t n = a.bstart[beta + 1] - base;
-    int slog = 0;
-    while (slog < rem && (n >> slog) > (uint32_t)HALF) slog++;
-    bool haveT = false;
-    uint32_t T = 0;
-    if (n == 0) {  // empty bucket: nothing to aggregate
+    if (n == 0) {
       if (tid == 0) {
-        st_release(&a.flags[beta], kLbAgg);
-        unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
-        st_release(&a.flags[beta], kLbIncl | ex);
-        const uint32_t T0 = (uint32_t)ex;
-        a.tb[beta] = T0;
-        a.tsub[3 * beta] = a.tsub[3 * beta + 1] = a.tsub[3 * beta + 2] = T0;
-        if (beta == (uint32_t)B - 1) {
-          a.tb[B] = T0;
-          a.sc->n_unique = ex;
-        }
+        a.tu[beta] = 0;
+        a.tsub[3 * beta] = a.tsub[3 * beta + 1] = a.tsub[3 * beta + 2] = 0;
       }
       continue;
     }
-    const int slog_max = rem < 20 ? rem : 20;
-    while (true) {  // attempts with more sub-passes after an overflow
+    // sub-passes expected from the distinct/keys ratio seen so far
+    int slog = 0;
+    while (slog < slog_max && (float)(n >> slog) * s_ratio * 1.2f > (float)HALF) slog++;
+    uint32_t acc = 0;
+    while (true) {  // attempts; an overflow doubles the sub-pass count
       const uint32_t nsub = 1u << slog;
-      // on-chip table sized to the bucket when it is counted in one pass
       uint32_t Heff = (uint32_t)H;
       if (slog == 0) {
         Heff = 1024;
         while (Heff < 2 * n && Heff < (uint32_t)H) Heff <<= 1;
       }
       const uint32_t hmask = Heff - 1;
-      uint32_t acc = 0;
+      acc = 0;
       bool ovf = false;
       if (tid < 3) s_d[tid] = 0;
       for (uint32_t j = 0; j < nsub; j++) {
@@ -669,6 +668,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
         }
         uint32_t u;
         uint32_t off = block_exclusive_sum(occ, s_warp, u);
+        if (u > Heff / 2) { ovf = true; break; }  // the sort needs a second half
 #pragma unroll
         for (int q = 0; q < SPT; q++) {
           if (rk[q] != EMPTY) {
@@ -676,18 +676,6 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
             scnt[off] = rc[q];
             off++;
           }
-        }
-        if (u > Heff / 2) { ovf = true; __syncthreads(); break; }
-        if (!haveT) {
-          if (tid == 0) {
-            if (slog == 0) st_release(&a.flags[beta], kLbAgg | (unsigned long long)u);
-            unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
-            s_T = (uint32_t)ex;
-            if (slog == 0) st_release(&a.flags[beta], kLbIncl | (ex + u));
-          }
-          __syncthreads();
-          T = s_T;
-          haveT = true;
         }
         __syncthreads();
         // --- stable LSD radix sort of the u distinct remainders, 8-bit digits
@@ -763,7 +751,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
           KeyT* tk = sk; sk = dk; dk = tk;
           uint32_t* tc = sc; sc = dc; dc = tc;
         }
-        // --- write this sub-range of the table
+        // --- write this sub-range of the bucket's rows
         const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
         uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
         for (uint32_t i0 = 0; i0 < u; i0 += kBucketThreads) {
@@ -773,16 +761,12 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
           if (v) {
             const KeyT r = sk[i];
             const uint32_t cnt = sc[i];
-            const unsigned long long row = (unsigned long long)T + acc + i;
+            const unsigned long long row = (unsigned long long)base + acc + i;
             if (row < a.cap) {
               tkeys[row] = hi_bits | r;
               a.tcounts[row] = cnt;
             } else {
               atomicOr(&a.sc->err, ERR_BOUNDS);
-            }
-            if (cnt < (uint32_t)a.t) {
-              if (cnt < (uint32_t)kHistSmem) atomicAdd(&shist[cnt], 1u);
-              else atomicAdd(&a.hist[cnt], 1ull);
             }
             d2 = (uint32_t)(KeyOps<KeyT>::shr(r, rem - 2) & 3);
           }
@@ -798,42 +782,64 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
         acc += u;
         __syncthreads();
       }
-      if (!ovf) {
-        if (tid == 0) {
-          if (slog > 0) st_release(&a.flags[beta], kLbIncl | ((unsigned long long)T + acc));
-          a.tb[beta] = T;
-          a.tsub[3 * beta + 0] = T + s_d[0];
-          a.tsub[3 * beta + 1] = T + s_d[0] + s_d[1];
-          a.tsub[3 * beta + 2] = T + s_d[0] + s_d[1] + s_d[2];
-          if (beta == (uint32_t)B - 1) {
-            a.tb[B] = T + acc;
-            a.sc->n_unique = (unsigned long long)T + acc;
-          }
-        }
-        break;
-      }
-      slog++;
-      if (slog > slog_max) {
-        // cannot split further: report and unblock successors
-        if (tid == 0) {
-          atomicOr(&a.sc->err, ERR_BUCKET);
-          if (!haveT) {
-            unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
-            T = (uint32_t)ex;
-          }
-          st_release(&a.flags[beta], kLbIncl | (unsigned long long)T);
-          a.tb[beta] = T;
-          a.tsub[3 * beta] = a.tsub[3 * beta + 1] = a.tsub[3 * beta + 2] = T;
-          if (beta == (uint32_t)B - 1) { a.tb[B] = T; a.sc->n_unique = T; }
-        }
-        break;
-      }
+      if (!ovf) break;
       __syncthreads();
+      if (++slog > slog_max) {
+        if (tid == 0) atomicOr(&a.sc->err, ERR_BUCKET);
+        acc = 0;
+        break;
+      }
+    }
+    // the histogram is added only once the bucket's rows are final
+    for (uint32_t i = tid; i < acc; i += kBucketThreads) {
+      const uint32_t cnt = a.tcounts[base + i];
+      if (cnt < (uint32_t)a.t) {
+        if (cnt < (uint32_t)kHistSmem) atomicAdd(&shist[cnt], 1u);
+        else atomicAdd(&a.hist[cnt], 1ull);
+      }
+    }
+    if (tid == 0) {
+      a.tu[beta] = acc;
+      a.tsub[3 * beta + 0] = s_d[0];
+      a.tsub[3 * beta + 1] = s_d[0] + s_d[1];
+      a.tsub[3 * beta + 2] = s_d[0] + s_d[1] + s_d[2];
+      atomicAdd(&a.sc->n_unique, (unsigned long long)acc);
+      s_ratio = 0.5f * s_ratio + 0.5f * ((float)acc / (float)n);
     }
   }
   __syncthreads();
   for (int i = tid; i < hbins; i += kBucketThreads)
     if (shist[i]) atomicAdd(&a.hist[i], (unsigned long long)shist[i]);
+}
+
+// Dense copy of the sparse table: rows of bucket b move to doff[b] (exclusive prefix
+// of tu).  mode 0: keys + counts arrays; mode 1: packed KmerPairs records.
+template <typename KeyT>
+__global__ void __launch_bounds__(256) k_compact_rows(const KeyT* __restrict__ skeys,
+                                                      const uint32_t* __restrict__ scounts,
+                                                      const uint32_t* __restrict__ bstart,
+                                                      const uint32_t* __restrict__ tu,
+                                                      const uint32_t* __restrict__ doff, int B,
+                                                      KeyT* __restrict__ dkeys,
+                                                      uint32_t* __restrict__ dcounts,
+                                                      uint32_t* __restrict__ packed, int mode) {
+  constexpr int WORDS = (sizeof(KeyT) + 4) / 4;
+  for (int b = blockIdx.x; b < B; b += gridDim.x) {
+    const uint32_t src = bstart[b], dst = doff[b], u = tu[b];
+    for (uint32_t i = threadIdx.x; i < u; i += blockDim.x) {
+      const KeyT x = skeys[src + i];
+      const uint32_t c = scounts[src + i];
+      if (mode == 0) {
+        dkeys[dst + i] = x;
+        dcounts[dst + i] = c;
+      } else {
+        uint32_t* o = packed + (size_t)(dst + i) * WORDS;
+#pragma unroll
+        for (int w = 0; w < WORDS - 1; w++) o[w] = (uint32_t)(x >> (32 * w));
+        o[WORDS - 1] = c;
+      }
+    }
+  }
 }
 
 // ------------------------------------------------------ histogram (other t) / cutoff --
@@ -915,6 +921,31 @@ __device__ __forceinline__ uint32_t upper_bound_s(const KeyT* k, uint32_t lo, ui
   return lo;
 }
 
+// Node key of table row `row` as seen from stream `st`: the prefix (k-1)-mer x >> 2
+// for the suffix-side stream (st == 0), the suffix (k-1)-mer for the others.
+template <typename KeyT>
+__device__ __forceinline__ KeyT node_key(const KeyT* __restrict__ tkeys, uint32_t row, int st,
+                                         KeyT succ_mask) {
+  const KeyT x = tkeys[row];
+  return st == 0 ? (x >> 2) : (x & succ_mask);
+}
+
+// first row in [lo, hi) whose node key is > piv
+template <typename KeyT>
+__device__ uint32_t upper_bound_rows(const KeyT* __restrict__ tkeys, uint32_t lo, uint32_t hi, int st,
+                                     KeyT succ_mask, KeyT piv) {
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (!(piv < node_key(tkeys, mid, st, succ_mask))) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// Per (k-1)-mer bucket: the suffix-side stream (table bucket beta, node = x >> 2,
+// extension = last base) and four prefix-side streams (table buckets whose remaining
+// bits continue with beta, node = x & SUCC_MASK, extension = first base f) are each
+// sorted by node key; merged they give the bucket's macro-nodes in key order.  A
+// bucket is processed in segments of at most kMnCap rows split at node-key pivots.
 template <typename KeyT>
 __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
   using SM = MnSmem<KeyT>;
@@ -925,17 +956,19 @@ __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
   uint16_t* ord = reinterpret_cast<uint16_t*>(smem + SM::off_ord);
   uint16_t* nid = reinterpret_cast<uint16_t*>(smem + SM::off_nid);
   __shared__ uint32_t s_warp[33];
-  __shared__ uint32_t s_beta, s_off[6], s_NO;
-  __shared__ uint32_t s_ovf;
+  __shared__ uint32_t s_beta, s_off[6], s_cur[5], s_end[5], s_segend[5], s_more, s_last;
+  __shared__ unsigned long long s_NO;
 
   const int tid = threadIdx.x;
   const int B = 1 << a.bbits;
   const int k = a.k;
   const int nb = 2 * (k - 1);
   const KeyT succ_mask = KeyOps<KeyT>::mask(nb);
+  const KeyT KINF = ~(KeyT)0;  // above every (k-1)-mer key
   const uint32_t cut = a.sc->cutoff;
   const KeyT* __restrict__ tkeys = reinterpret_cast<const KeyT*>(a.tkeys);
   KeyT* __restrict__ nkeys = reinterpret_cast<KeyT*>(a.nkeys);
+  constexpr uint32_t PER = (kMnCap - 16) / 5;  // rows per stream per segment before ties
 
   while (true) {
     __syncthreads();
@@ -943,122 +976,144 @@ __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
     __syncthreads();
     const uint32_t beta = s_beta;
     if (beta >= (uint32_t)B) break;
-    if (tid == 0) { s_ovf = 0; s_off[0] = 0; }
-    __syncthreads();
-    // gather the five sorted streams, keeping counts >= cutoff
-    uint32_t len = 0;
-    for (int st = 0; st < 5; st++) {
-      uint32_t lo, hi;
-      if (st == 0) {
-        lo = a.tb[beta];
-        hi = a.tb[beta + 1];
-      } else {
-        const uint32_t f = st - 1;
-        const uint32_t bp = (f << (a.bbits - 2)) | (beta >> 2);
+    if (tid == 0) {
+      s_cur[0] = a.bstart[beta];
+      s_end[0] = a.bstart[beta] + a.tu[beta];
+      for (int f = 0; f < 4; f++) {
+        const uint32_t bp = ((uint32_t)f << (a.bbits - 2)) | (beta >> 2);
         const uint32_t d = beta & 3;
-        lo = d == 0 ? a.tb[bp] : a.tsub[3 * bp + d - 1];
-        hi = d == 3 ? a.tb[bp + 1] : a.tsub[3 * bp + d];
+        const uint32_t b0 = a.bstart[bp];
+        s_cur[f + 1] = b0 + (d == 0 ? 0u : a.tsub[3 * bp + d - 1]);
+        s_end[f + 1] = b0 + (d == 3 ? a.tu[bp] : a.tsub[3 * bp + d]);
       }
-      for (uint32_t i0 = lo; i0 < hi; i0 += kMnThreads) {
-        const uint32_t i = i0 + tid;
-        const bool v = i < hi;
-        uint32_t c = v ? a.tcounts[i] : 0;
-        const bool keep = v && c >= cut;
-        uint32_t tot;
-        uint32_t pos = block_exclusive_sum(keep ? 1u : 0u, s_warp, tot);
-        if (keep) {
-          const uint32_t o = len + pos;
-          if (o < (uint32_t)kMnCap) {
-            const KeyT x = tkeys[i];
-            if (st == 0) {
-              ikey[o] = x >> 2;
-              itag[o] = (uint8_t)((uint32_t)(x & 3));
-            } else {
-              ikey[o] = x & succ_mask;
-              itag[o] = (uint8_t)(4 + (st - 1));
+    }
+    __syncthreads();
+    bool first = true;
+    bool multi = false;
+    unsigned long long NO = 0, done_nodes = 0;
+    while (true) {
+      // ---- choose this segment's rows
+      if (tid == 0) {
+        uint32_t left = 0;
+        for (int st = 0; st < 5; st++) left += s_end[st] - s_cur[st];
+        s_more = left > 0;
+        KeyT piv = KINF;
+        for (int st = 0; st < 5; st++)
+          if (s_end[st] - s_cur[st] > PER) {
+            KeyT kk = node_key(tkeys, s_cur[st] + PER - 1, st, succ_mask);
+            if (kk < piv) piv = kk;
+          }
+        s_last = 1;
+        for (int st = 0; st < 5; st++) {
+          s_segend[st] = piv == KINF ? s_end[st]
+                                     : upper_bound_rows(tkeys, s_cur[st], s_end[st], st, succ_mask, piv);
+          if (s_segend[st] != s_end[st]) s_last = 0;
+        }
+      }
+      __syncthreads();
+      if (!s_more && !first) break;
+      const bool last = s_last != 0;
+      if (first && !last) multi = true;
+      // ---- gather the segment's kept rows (count >= cutoff) into five sorted runs
+      uint32_t len = 0;
+      if (tid == 0) s_off[0] = 0;
+      for (int st = 0; st < 5; st++) {
+        const uint32_t lo = s_cur[st], hi = s_segend[st];
+        for (uint32_t i0 = lo; i0 < hi; i0 += kMnThreads) {
+          const uint32_t i = i0 + tid;
+          const bool v = i < hi;
+          const uint32_t c = v ? a.tcounts[i] : 0;
+          const bool keep = v && c >= cut;
+          uint32_t tot;
+          const uint32_t pos = block_exclusive_sum(keep ? 1u : 0u, s_warp, tot);
+          if (keep) {
+            const uint32_t o = len + pos;
+            if (o < (uint32_t)kMnCap) {
+              const KeyT x = tkeys[i];
+              ikey[o] = st == 0 ? (x >> 2) : (x & succ_mask);
+              itag[o] = (uint8_t)(st == 0 ? (uint32_t)(x & 3) : (uint32_t)(3 + st));
+              icnt[o] = c;
             }
-            icnt[o] = c;
+          }
+          len += tot;
+        }
+        if (tid == 0) s_off[st + 1] = len;
+      }
+      __syncthreads();
+      if (len > (uint32_t)kMnCap) {  // cannot happen with PER-sized segments
+        if (tid == 0) atomicOr(&a.sc->err, ERR_MN_CAPACITY);
+        len = 0;
+      }
+      const uint32_t mm = len;
+      // ---- merge rank of every item across the five runs
+      for (uint32_t i = tid; i < mm; i += kMnThreads) {
+        int st = 0;
+        while (i >= s_off[st + 1]) st++;
+        const KeyT x = ikey[i];
+        uint32_t rank = i - s_off[st];
+        for (int b = 0; b < 5; b++) {
+          if (b == st) continue;
+          const uint32_t lo = s_off[b], hi = s_off[b + 1];
+          rank += (b < st ? upper_bound_s(ikey, lo, hi, x) : lower_bound_s(ikey, lo, hi, x)) - lo;
+        }
+        ord[rank] = (uint16_t)i;
+      }
+      __syncthreads();
+      // ---- node boundaries and node index per merged position
+      uint32_t nodes = 0;
+      for (uint32_t r0 = 0; r0 < mm; r0 += kMnThreads) {
+        const uint32_t r = r0 + tid;
+        uint32_t flag = 0;
+        if (r < mm) flag = (r == 0) || !(ikey[ord[r - 1]] == ikey[ord[r]]);
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_sum(flag, s_warp, tot);
+        if (r < mm) nid[r] = (uint16_t)(nodes + ex + flag - 1);
+        nodes += tot;
+      }
+      // ---- node offset: decoupled look-back over node buckets
+      if (first) {
+        if (tid == 0) {
+          if (!multi) st_release(&a.flags[beta], kLbAgg | (unsigned long long)nodes);
+          const unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
+          if (!multi) st_release(&a.flags[beta], kLbIncl | (ex + nodes));
+          s_NO = ex;
+        }
+        __syncthreads();
+        NO = s_NO;
+      }
+      const unsigned long long q0 = NO + done_nodes;
+      if (q0 + nodes <= a.cap) {
+        for (uint32_t r = tid; r < mm; r += kMnThreads) {
+          if (r == 0 || nid[r] != nid[r - 1]) {
+            const unsigned long long q = q0 + nid[r];
+            nkeys[q] = ikey[ord[r]];
+            reinterpret_cast<uint4*>(a.nsuf)[q] = make_uint4(0, 0, 0, 0);
+            reinterpret_cast<uint4*>(a.npre)[q] = make_uint4(0, 0, 0, 0);
           }
         }
-        len += tot;
+        __syncthreads();
+        for (uint32_t r = tid; r < mm; r += kMnThreads) {
+          const uint32_t i = ord[r];
+          const unsigned long long q = q0 + nid[r];
+          const uint32_t tg = itag[i];
+          if (tg < 4) a.nsuf[4 * q + tg] = icnt[i];
+          else a.npre[4 * q + (tg - 4)] = icnt[i];
+        }
+      } else if (tid == 0) {
+        atomicOr(&a.sc->err, ERR_MN_CAPACITY);
       }
-      if (tid == 0) s_off[st + 1] = len;
-    }
-    __syncthreads();
-    const uint32_t m = len;
-    if (m > (uint32_t)kMnCap) {
-      if (tid == 0) atomicOr(&a.sc->err, ERR_MN_CAPACITY);
-    }
-    const uint32_t mm = m > (uint32_t)kMnCap ? 0u : m;
-    // merge rank of every item across the five streams
-    for (uint32_t i = tid; i < mm; i += kMnThreads) {
-      int st = 0;
-      while (i >= s_off[st + 1]) st++;
-      const KeyT x = ikey[i];
-      uint32_t rank = i - s_off[st];
-      for (int b = 0; b < 5; b++) {
-        if (b == st) continue;
-        const uint32_t lo = s_off[b], hi = s_off[b + 1];
-        rank += (b < st ? upper_bound_s(ikey, lo, hi, x) : lower_bound_s(ikey, lo, hi, x)) - lo;
-      }
-      ord[rank] = (uint16_t)i;
-    }
-    __syncthreads();
-    // node boundaries and node index per merged position
-    uint32_t nodes = 0;
-    for (uint32_t r0 = 0; r0 < mm; r0 += kMnThreads) {
-      const uint32_t r = r0 + tid;
-      uint32_t flag = 0;
-      if (r < mm) flag = (r == 0) || !(ikey[ord[r - 1]] == ikey[ord[r]]);
-      uint32_t tot;
-      uint32_t ex = block_exclusive_sum(flag, s_warp, tot);
-      if (r < mm) nid[r] = (uint16_t)(nodes + ex + flag - 1);
-      nodes += tot;
+      done_nodes += nodes;
+      first = false;
+      __syncthreads();
+      if (tid == 0)
+        for (int st = 0; st < 5; st++) s_cur[st] = s_segend[st];
+      __syncthreads();
+      if (last) break;
     }
     if (tid == 0) {
-      st_release(&a.flags[beta], kLbAgg | (unsigned long long)nodes);
-      unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
-      st_release(&a.flags[beta], kLbIncl | (ex + nodes));
-      s_NO = (uint32_t)ex;
-      if (beta == (uint32_t)B - 1) a.sc->n_nodes = ex + nodes;
+      if (multi) st_release(&a.flags[beta], kLbIncl | (NO + done_nodes));
+      if (beta == (uint32_t)B - 1) a.sc->n_nodes = NO + done_nodes;
     }
-    __syncthreads();
-    const unsigned long long NO = s_NO;
-    if (NO + nodes > a.cap) {
-      if (tid == 0) atomicOr(&a.sc->err, ERR_MN_CAPACITY);
-      continue;
-    }
-    for (uint32_t r = tid; r < mm; r += kMnThreads) {
-      if (r == 0 || nid[r] != nid[r - 1]) {
-        const unsigned long long q = NO + nid[r];
-        nkeys[q] = ikey[ord[r]];
-        reinterpret_cast<uint4*>(a.nsuf)[q] = make_uint4(0, 0, 0, 0);
-        reinterpret_cast<uint4*>(a.npre)[q] = make_uint4(0, 0, 0, 0);
-      }
-    }
-    __syncthreads();
-    for (uint32_t r = tid; r < mm; r += kMnThreads) {
-      const uint32_t i = ord[r];
-      const unsigned long long q = NO + nid[r];
-      const uint32_t tg = itag[i];
-      if (tg < 4) a.nsuf[4 * q + tg] = icnt[i];
-      else a.npre[4 * q + (tg - 4)] = icnt[i];
-    }
-  }
-}
-
-// ---------------------------------------------------------------- packed KmerPairs --
-template <typename KeyT>
-__global__ void k_pack_pairs(const KeyT* __restrict__ k, const uint32_t* __restrict__ c,
-                             unsigned long long u, uint32_t* __restrict__ out) {
-  constexpr int WORDS = (sizeof(KeyT) + 4) / 4;
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < u;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
-    const KeyT x = k[i];
-    uint32_t* o = out + i * WORDS;
-#pragma unroll
-    for (int w = 0; w < WORDS - 1; w++) o[w] = (uint32_t)(x >> (32 * w));
-    o[WORDS - 1] = c[i];
   }
 }
 
@@ -1159,17 +1214,41 @@ cudaError_t launch_macro_nodes(const MnArgs& a, int wide, int grid, cudaStream_t
   return wide ? launch_mn_t<u128>(a, grid, st) : launch_mn_t<uint64_t>(a, grid, st);
 }
 
-cudaError_t launch_pack_pairs(const void* tkeys, const uint32_t* tcounts, unsigned long long u,
-                              int wide, void* out, cudaStream_t st) {
-  if (u == 0) return cudaSuccess;
-  int grid = (int)((u + 255) / 256);
-  if (grid > sm_count() * 16) grid = sm_count() * 16;
+__global__ void __launch_bounds__(1024) k_copy_prefix(const uint32_t* __restrict__ in,
+                                                      uint32_t* __restrict__ out, int B) {
+  __shared__ uint32_t s_warp[33];
+  uint32_t carry = 0;
+  for (int base = 0; base < B; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    uint32_t v = i < B ? in[i] : 0;
+    uint32_t tot;
+    uint32_t ex = block_exclusive_sum(v, s_warp, tot);
+    if (i < B) out[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) out[B] = carry;
+}
+
+cudaError_t launch_row_offsets(const uint32_t* tu, uint32_t* doff, int B, cudaStream_t st) {
+  k_copy_prefix<<<1, 1024, 0, st>>>(tu, doff, B);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compact_rows(const void* tkeys, const uint32_t* tcounts, const uint32_t* bstart,
+                                const uint32_t* tu, const uint32_t* doff, int B, int wide,
+                                void* dkeys, uint32_t* dcounts, void* packed, cudaStream_t st) {
+  int grid = B < sm_count() * 16 ? B : sm_count() * 16;
+  if (grid < 1) grid = 1;
+  const int mode = packed ? 1 : 0;
   if (wide)
-    k_pack_pairs<u128><<<grid, 256, 0, st>>>(reinterpret_cast<const u128*>(tkeys), tcounts, u,
-                                             reinterpret_cast<uint32_t*>(out));
+    k_compact_rows<u128><<<grid, 256, 0, st>>>(reinterpret_cast<const u128*>(tkeys), tcounts, bstart,
+                                               tu, doff, B, reinterpret_cast<u128*>(dkeys), dcounts,
+                                               reinterpret_cast<uint32_t*>(packed), mode);
   else
-    k_pack_pairs<uint64_t><<<grid, 256, 0, st>>>(reinterpret_cast<const uint64_t*>(tkeys), tcounts,
-                                                 u, reinterpret_cast<uint32_t*>(out));
+    k_compact_rows<uint64_t><<<grid, 256, 0, st>>>(reinterpret_cast<const uint64_t*>(tkeys), tcounts,
+                                                   bstart, tu, doff, B,
+                                                   reinterpret_cast<uint64_t*>(dkeys), dcounts,
+                                                   reinterpret_cast<uint32_t*>(packed), mode);
   return cudaGetLastError();
 }
 

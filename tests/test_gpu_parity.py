@@ -124,8 +124,13 @@ def test_cutoff_with_other_t_and_explicit_min_count():
         job.count(g.fasta, p)
         for t in (2, 7, 40):
             hist, cut = po.cutoff(tab.counts, t)
-            c2, h2, kept = job.cutoff(t)
-            assert c2 == cut and np.array_equal(h2, hist)
+            kept_ref = int((tab.counts >= cut).sum())
+            try:
+                c2, h2, kept = job.cutoff(t)
+            except pk.EmptyAfterCutoff as e:
+                assert kept_ref == 0
+                c2, h2, kept = e.cutoff, e.hist, e.kept
+            assert c2 == cut and np.array_equal(h2, hist) and kept == kept_ref
         # "freq > threshold" of the PaK-Graph builder = min_count threshold+1
         m = job.build_macro_nodes(3)
         mn = job.macro_nodes()
