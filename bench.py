@@ -30,8 +30,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "k-mers/sec count+macro-node on 1 GB300 (% HBM roofline); served p50/p99 latency"
 UNIT = "k-mers/s"
-KERNELS_PER_STEP = 9  # line scan, tile prefix, bucket count, column prefix, bucket prefix,
-#                       scatter, bucket table, cutoff, macro-nodes
+KERNELS_PER_STEP = 10  # line scan, tile prefix, bucket count, column prefix, bucket prefix,
+#                        scatter, bucket table, cutoff, kept filter, macro-nodes
 
 
 def parse():
@@ -120,7 +120,8 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def stage_bytes(stage: str, F: int, N: int, U: int, M: int, W: int, t: int, B: int, G: int) -> int:
+def stage_bytes(stage: str, F: int, N: int, U: int, V: int, M: int, W: int, t: int, B: int,
+                G: int) -> int:
     """Algorithmic bytes one launch of a stage must move (read + write)."""
     return {
         "line_scan": F,
@@ -129,7 +130,8 @@ def stage_bytes(stage: str, F: int, N: int, U: int, M: int, W: int, t: int, B: i
         "scatter": F + N * W,
         "bucket_table": N * W + U * (W + 4),
         "cutoff": 8 * t,
-        "macro_nodes": 2 * U * (W + 4) + M * (W + 32),
+        "kept_filter": U * (W + 4) + V * (W + 4),
+        "macro_nodes": 2 * V * (W + 4) + M * (W + 32),
     }.get(stage, 0)
 
 
@@ -299,7 +301,7 @@ def main():
         avg = {k: v / args.steps for k, v in stage_acc.items()}
         kern = {k: v for k, v in avg.items() if k != "h2d" and v > 0}
         dom = max(kern, key=kern.get)
-        dom_bytes = stage_bytes(dom, F, N, U, M, W, rs.t, B, G)
+        dom_bytes = stage_bytes(dom, F, N, U, V, M, W, rs.t, B, G)
         achieved = dom_bytes / (kern[dom] / 1000.0) / 1e9
         traffic = None
         tp = os.path.join(ROOT, "profiles", "traffic.json")

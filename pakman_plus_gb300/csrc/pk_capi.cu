@@ -64,11 +64,13 @@ enum Stage {
   ST_SCATTER,
   ST_TABLE,
   ST_CUTOFF,
+  ST_FILTER,
   ST_MN,
   ST_COUNT_
 };
-static const char* kStageNames[ST_COUNT_] = {"h2d",     "line_scan", "bucket_count", "bucket_offsets",
-                                             "scatter", "bucket_table", "cutoff", "macro_nodes"};
+static const char* kStageNames[ST_COUNT_] = {"h2d",          "line_scan", "bucket_count",
+                                             "bucket_offsets", "scatter", "bucket_table",
+                                             "cutoff",       "kept_filter", "macro_nodes"};
 
 struct pk_job {
   pk_ctx* ctx = nullptr;
@@ -86,7 +88,7 @@ struct pk_job {
   Scalars* d_sc = nullptr;
   Scalars* h_sc = nullptr;  // pinned mirror
   DevBuf fasta, tile_nl, counts, bstart, keys, tkeys, tcounts, tu, tsub, flags_m, hist, hist2,
-      nkeys, nsuf, npre, packed, doff, dkeys, dcounts;
+      nkeys, nsuf, npre, packed, doff, dkeys, dcounts, flags_f, kkeys, kcounts, kstart, kcount, ksub;
   bool dense_valid = false;
   bool timing = false;
   cudaEvent_t ev0[ST_COUNT_] = {}, ev1[ST_COUNT_] = {};
@@ -138,7 +140,8 @@ static void job_free_all(pk_job* j) {
   DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->keys,  &j->tkeys,
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
-                   &j->dcounts};
+                   &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
+                   &j->ksub};
   for (DevBuf* b : all) job_free(j, *b);
   j->dense_valid = false;
 }
@@ -305,7 +308,8 @@ pk_status pk_job_memory(pk_job* j, uint64_t* bytes) {
   DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->keys,  &j->tkeys,
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
-                   &j->dcounts};
+                   &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
+                   &j->ksub};
   uint64_t s = 0;
   for (DevBuf* b : all) s += b->bytes;
   *bytes = s;
@@ -608,23 +612,51 @@ pk_status pk_cutoff(pk_job* j, int32_t t, uint32_t* cutoff, uint64_t* hist, uint
 static pk_status mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
   const int B = 1 << j->bbits;
   const size_t W = j->wide ? 16 : 8;
+  const uint64_t kcap = kept_bound ? kept_bound : 1;
   uint64_t cap = 2 * kept_bound;
   if (cap == 0) cap = 1;
+  PK_TRY(job_alloc(j, j->kkeys, W * kcap));
+  PK_TRY(job_alloc(j, j->kcounts, 4 * kcap));
+  PK_TRY(job_alloc(j, j->kstart, sizeof(uint32_t) * B));
+  PK_TRY(job_alloc(j, j->kcount, sizeof(uint32_t) * B));
+  PK_TRY(job_alloc(j, j->ksub, sizeof(uint32_t) * 3 * (size_t)B));
+  PK_TRY(job_alloc(j, j->flags_f, sizeof(unsigned long long) * B));
   PK_TRY(job_alloc(j, j->nkeys, W * cap));
   PK_TRY(job_alloc(j, j->nsuf, 16 * cap));
   PK_TRY(job_alloc(j, j->npre, 16 * cap));
   PK_TRY(job_alloc(j, j->flags_m, sizeof(unsigned long long) * B));
+  PK_CUDA(cudaMemsetAsync(j->flags_f.p, 0, sizeof(unsigned long long) * B, j->stream));
   PK_CUDA(cudaMemsetAsync(j->flags_m.p, 0, sizeof(unsigned long long) * B, j->stream));
   PK_CUDA(cudaMemsetAsync(&j->d_sc->ticket_mn, 0, sizeof(uint32_t), j->stream));
+  PK_CUDA(cudaMemsetAsync(&j->d_sc->ticket_filter, 0, sizeof(uint32_t), j->stream));
   PK_CUDA(cudaMemsetAsync(&j->d_sc->n_nodes, 0, sizeof(unsigned long long), j->stream));
+  PK_CUDA(cudaMemsetAsync(&j->d_sc->n_kept_rows, 0, sizeof(unsigned long long), j->stream));
   if (min_count) PK_CUDA(cudaMemcpyAsync(&j->d_sc->cutoff, &min_count, sizeof(uint32_t), cudaMemcpyHostToDevice, j->stream));
   j->mn_cap = cap;
+  FilterArgs f{};
+  f.tkeys = j->tkeys.p;
+  f.tcounts = (const uint32_t*)j->tcounts.p;
+  f.bstart = (const uint32_t*)j->bstart.p;
+  f.tu = (const uint32_t*)j->tu.p;
+  f.flags = (unsigned long long*)j->flags_f.p;
+  f.kkeys = j->kkeys.p;
+  f.kcounts = (uint32_t*)j->kcounts.p;
+  f.kstart = (uint32_t*)j->kstart.p;
+  f.kcount = (uint32_t*)j->kcount.p;
+  f.ksub = (uint32_t*)j->ksub.p;
+  f.cap = kcap;
+  f.k = j->params.k;
+  f.bbits = j->bbits;
+  f.sc = j->d_sc;
+  mark_begin(j, ST_FILTER);
+  PK_CUDA(launch_filter_kept(f, j->wide, 0, j->stream));
+  mark_end(j, ST_FILTER);
   MnArgs m{};
-  m.tkeys = j->tkeys.p;
-  m.tcounts = (const uint32_t*)j->tcounts.p;
-  m.bstart = (const uint32_t*)j->bstart.p;
-  m.tu = (const uint32_t*)j->tu.p;
-  m.tsub = (const uint32_t*)j->tsub.p;
+  m.kkeys = j->kkeys.p;
+  m.kcounts = (const uint32_t*)j->kcounts.p;
+  m.kstart = (const uint32_t*)j->kstart.p;
+  m.kcount = (const uint32_t*)j->kcount.p;
+  m.ksub = (const uint32_t*)j->ksub.p;
   m.flags = (unsigned long long*)j->flags_m.p;
   m.nkeys = j->nkeys.p;
   m.nsuf = (uint32_t*)j->nsuf.p;

@@ -23,6 +23,8 @@ constexpr int kBucketThreads = 512;
 constexpr int kMnThreads = 512;
 constexpr int kMnCap = 4096;        // items (k-mer records) per macro-node segment on chip
 constexpr int kHistSmem = 1024;     // count-histogram bins kept in shared memory
+constexpr int kBucketStack = 256;   // pending sub-ranges of one bucket (binary-trie split)
+constexpr int kMaxBucketAttempts = 1 << 16;  // sub-range attempts per bucket before giving up
 
 struct Scalars {                    // device-side scalars of one job
   unsigned long long s0;            // index of the first '>' (F if none)
@@ -33,10 +35,11 @@ struct Scalars {                    // device-side scalars of one job
   uint32_t ticket_bucket;           // work tickets
   uint32_t ticket_mn;
   uint32_t cutoff;                  // histogram cutoff
-  uint32_t pad;
+  uint32_t ticket_filter;
   unsigned long long n_unique;      // U
   unsigned long long n_kept;        // V
   unsigned long long n_nodes;       // M
+  unsigned long long n_kept_rows;   // V as counted by the filter
 };
 
 struct CountArgs {
@@ -72,12 +75,30 @@ struct BucketArgs {
   Scalars* sc;
 };
 
-struct MnArgs {
+// Kept rows (count >= cutoff), dense and ascending, with per-bucket extents.
+struct FilterArgs {
   const void* tkeys;
   const uint32_t* tcounts;
   const uint32_t* bstart;
   const uint32_t* tu;
-  const uint32_t* tsub;
+  unsigned long long* flags; // 2^bbits look-back words (zeroed)
+  void* kkeys;               // kept keys out
+  uint32_t* kcounts;         // kept counts out
+  uint32_t* kstart;          // 2^bbits
+  uint32_t* kcount;          // 2^bbits
+  uint32_t* ksub;            // 3 * 2^bbits
+  unsigned long long cap;    // kept-row capacity
+  int k;
+  int bbits;
+  Scalars* sc;
+};
+
+struct MnArgs {
+  const void* kkeys;
+  const uint32_t* kcounts;
+  const uint32_t* kstart;
+  const uint32_t* kcount;
+  const uint32_t* ksub;
   unsigned long long* flags; // 2^bbits look-back words (zeroed)
   void* nkeys;               // node keys out (capacity cap)
   uint32_t* nsuf;            // 4 * cap
@@ -97,6 +118,7 @@ cudaError_t launch_bucket_table(const BucketArgs& a, int wide, int grid, cudaStr
 cudaError_t launch_histogram(const uint32_t* tcounts, unsigned long long u, int t,
                              unsigned long long* hist, cudaStream_t st);
 cudaError_t launch_cutoff(const unsigned long long* hist, int t, Scalars* sc, cudaStream_t st);
+cudaError_t launch_filter_kept(const FilterArgs& a, int wide, int grid, cudaStream_t st);
 cudaError_t launch_macro_nodes(const MnArgs& a, int wide, int grid, cudaStream_t st);
 // Dense copy of the sparse table (doff: exclusive prefix of tu, computed by
 // launch_row_offsets).  packed != null writes KmerPairs records instead of arrays.

@@ -43,6 +43,7 @@ struct KeyOps<uint64_t> {
   __device__ __forceinline__ static unsigned match(unsigned m, uint64_t x) {
     return __match_any_sync(m, (unsigned long long)x);
   }
+  __device__ __forceinline__ static int top_bit(uint64_t x) { return 63 - __clzll((long long)x); }
   __device__ __forceinline__ static uint64_t cas(uint64_t* p, uint64_t cmp, uint64_t val) {
     return atomicCAS(reinterpret_cast<unsigned long long*>(p), (unsigned long long)cmp,
                      (unsigned long long)val);
@@ -65,6 +66,10 @@ struct KeyOps<u128> {
   __device__ __forceinline__ static unsigned match(unsigned m, u128 x) {
     return __match_any_sync(m, (unsigned long long)x) &
            __match_any_sync(m, (unsigned long long)(x >> 64));
+  }
+  __device__ __forceinline__ static int top_bit(u128 x) {
+    const uint64_t hi = (uint64_t)(x >> 64);
+    return hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)(uint64_t)x);
   }
   __device__ __forceinline__ static u128 cas(u128* p, u128 cmp, u128 val) { return atomicCAS(p, cmp, val); }
 };
@@ -140,6 +145,30 @@ __device__ __forceinline__ uint32_t block_exclusive_sum(uint32_t v, uint32_t* s_
   total = s_warp[32];
   __syncthreads();
   return res;
+}
+
+// Block-wide OR and AND of a key (result in x_or/x_and of every thread).
+template <typename KeyT>
+__device__ void block_or_and(KeyT& x_or, KeyT& x_and, KeyT* s_red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint64_t olo = (uint64_t)x_or, ohi = (uint64_t)(x_or >> 32 >> 32);
+  uint64_t alo = (uint64_t)x_and, ahi = (uint64_t)(x_and >> 32 >> 32);
+  for (int o = 16; o > 0; o >>= 1) {
+    olo |= __shfl_xor_sync(FULLMASK, olo, o);
+    ohi |= __shfl_xor_sync(FULLMASK, ohi, o);
+    alo &= __shfl_xor_sync(FULLMASK, alo, o);
+    ahi &= __shfl_xor_sync(FULLMASK, ahi, o);
+  }
+  if (lane == 0) {
+    s_red[warp] = (KeyT)olo | ((KeyT)ohi << 32 << 32);
+    s_red[nw + warp] = (KeyT)alo | ((KeyT)ahi << 32 << 32);
+  }
+  __syncthreads();
+  KeyT ro = 0, ra = ~(KeyT)0;
+  for (int w = 0; w < nw; w++) { ro |= s_red[w]; ra &= s_red[nw + w]; }
+  x_or = ro;
+  x_and = ra;
+  __syncthreads();
 }
 
 // ------------------------------------------------------------- line scan (k_line_scan) -
@@ -582,7 +611,11 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   uint16_t* wc = reinterpret_cast<uint16_t*>(smem + SM::off_wc);
   uint32_t* shist = reinterpret_cast<uint32_t*>(smem + SM::off_hist);
   __shared__ uint32_t s_warp[33];
-  __shared__ uint32_t s_beta, s_ovf, s_d[3];
+  __shared__ uint32_t s_beta, s_ovf, s_d[3], s_fail;
+  __shared__ int s_sp;
+  __shared__ KeyT s_stk_v[kBucketStack];
+  __shared__ int s_stk_l[kBucketStack];
+  __shared__ KeyT s_red_k[2 * (kBucketThreads / 32)];
   __shared__ float s_ratio;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -595,7 +628,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   const int hbins = a.t < kHistSmem ? a.t : kHistSmem;
   for (int i = tid; i < hbins; i += kBucketThreads) shist[i] = 0;
   if (tid == 0) s_ratio = 0.5f;  // running distinct/keys ratio of this CTA's buckets
-  const int slog_max = rem < 20 ? rem : 20;
+  const int slog_max = rem < 7 ? rem : 7;  // initial split guess (<= 128 sub-ranges)
 
   while (true) {
     __syncthreads();
@@ -605,6 +638,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
     if (beta >= (uint32_t)B) break;
     const uint32_t base = a.bstart[beta];
     const uint32_t n = a.bstart[beta + 1] - base;
+    if (tid == 0) s_fail = 0;
     if (n == 0) {
       if (tid == 0) {
         a.tu[beta] = 0;
@@ -612,184 +646,223 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       }
       continue;
     }
-    // sub-passes expected from the distinct/keys ratio seen so far
+    // Sub-ranges of the bucket are counted one at a time, in key order.  A sub-range
+    // is the set of remainders whose top `plen` bits equal `pv`.  The first split
+    // guesses from the distinct/keys ratio seen so far; a sub-range whose distinct
+    // keys overflow the on-chip table is split at the first bit where its keys differ
+    // (a binary trie), so any skew terminates.
     int slog = 0;
     while (slog < slog_max && (float)(n >> slog) * s_ratio * 1.2f > (float)HALF) slog++;
+    if (tid == 0) {
+      s_sp = 0;
+      for (int j = (1 << slog) - 1; j >= 0; j--) {
+        s_stk_v[s_sp] = (KeyT)j;
+        s_stk_l[s_sp] = slog;
+        s_sp++;
+      }
+      s_d[0] = s_d[1] = s_d[2] = 0;
+    }
     uint32_t acc = 0;
-    while (true) {  // attempts; an overflow doubles the sub-pass count
-      const uint32_t nsub = 1u << slog;
+    int attempts = 0;
+    bool failed = false;
+    __syncthreads();
+    while (s_sp > 0) {
+      const KeyT pv = s_stk_v[s_sp - 1];
+      const int plen = s_stk_l[s_sp - 1];
+      __syncthreads();
+      if (tid == 0) s_sp--;
+      if (++attempts > kMaxBucketAttempts) { failed = true; break; }
       uint32_t Heff = (uint32_t)H;
-      if (slog == 0) {
+      if (plen == 0) {
         Heff = 1024;
         while (Heff < 2 * n && Heff < (uint32_t)H) Heff <<= 1;
       }
       const uint32_t hmask = Heff - 1;
-      acc = 0;
-      bool ovf = false;
-      if (tid < 3) s_d[tid] = 0;
-      for (uint32_t j = 0; j < nsub; j++) {
-        for (uint32_t i = tid; i < Heff; i += kBucketThreads) {
-          skey[i] = EMPTY;
-          scnt[i] = 0;
-        }
-        if (tid == 0) s_ovf = 0;
-        __syncthreads();
-        // --- hash aggregation of this sub-range (warp-aggregated inserts)
-        for (uint32_t i0 = (uint32_t)warp * 32; i0 < n; i0 += NW * 32) {
-          const uint32_t i = i0 + lane;
-          const bool valid = i < n;
-          KeyT r = valid ? (keys[base + i] & rmask) : (KeyT)0;
-          bool mine = valid && (slog == 0 || (uint32_t)(KeyOps<KeyT>::shr(r, rem - slog) & (nsub - 1)) == j);
-          const unsigned m = __ballot_sync(FULLMASK, mine);
-          if (mine) {
-            const unsigned peers = KeyOps<KeyT>::match(m, r);
-            if (lane == __ffs(peers) - 1) {
-              if (!hash_insert<KeyT>(skey, scnt, hmask, r, (uint32_t)__popc(peers))) s_ovf = 1;
-            }
-          }
-        }
-        __syncthreads();
-        if (s_ovf) { ovf = true; break; }
-        // --- compaction of occupied slots into [0, u)
-        constexpr int SPT = H / kBucketThreads;
-        const uint32_t spt = Heff / kBucketThreads;  // >= 2 since Heff >= 1024
-        KeyT rk[SPT];
-        uint32_t rc[SPT];
-        uint32_t occ = 0;
-#pragma unroll
-        for (int q = 0; q < SPT; q++) {
-          rk[q] = EMPTY;
-          rc[q] = 0;
-          if ((uint32_t)q < spt) {
-            rk[q] = skey[tid * spt + q];
-            rc[q] = scnt[tid * spt + q];
-            occ += rk[q] != EMPTY;
-          }
-        }
-        uint32_t u;
-        uint32_t off = block_exclusive_sum(occ, s_warp, u);
-        if (u > Heff / 2) { ovf = true; break; }  // the sort needs a second half
-#pragma unroll
-        for (int q = 0; q < SPT; q++) {
-          if (rk[q] != EMPTY) {
-            skey[off] = rk[q];
-            scnt[off] = rc[q];
-            off++;
-          }
-        }
-        __syncthreads();
-        // --- stable LSD radix sort of the u distinct remainders, 8-bit digits
-        const int sort_bits = rem - slog;
-        const int npass = (sort_bits + 7) / 8;
-        KeyT* sk = skey;
-        uint32_t* sc = scnt;
-        KeyT* dk = skey + Heff / 2;
-        uint32_t* dc = scnt + Heff / 2;
-        const uint32_t E = (u + NW - 1) / NW;
-        const uint32_t e0 = (uint32_t)warp * E;
-        const uint32_t e1 = min(e0 + E, u);
-        for (int pass = 0; pass < npass; pass++) {
-          const int sh = 8 * pass;
-          for (int i = lane; i < 256; i += 32) wc[warp * 256 + i] = 0;
-          __syncwarp();
-          uint32_t dig[RMAX], offs[RMAX];
-#pragma unroll
-          for (int rr = 0; rr < RMAX; rr++) {
-            const uint32_t idx = e0 + rr * 32 + lane;
-            const bool v = idx < e1;
-            const uint32_t d = v ? (uint32_t)(KeyOps<KeyT>::shr(sk[idx], sh) & 0xff) : 0u;
-            const unsigned vm = __ballot_sync(FULLMASK, v);
-            uint32_t bse = 0;
-            unsigned peers = 0;
-            if (v) {
-              peers = __match_any_sync(vm, d);
-              if (lane == __ffs(peers) - 1) {
-                bse = wc[warp * 256 + d];
-                wc[warp * 256 + d] = (uint16_t)(bse + __popc(peers));
-              }
-            }
-            __syncwarp();
-            const int leader = v ? __ffs(peers) - 1 : lane;
-            bse = __shfl_sync(FULLMASK, bse, leader);
-            dig[rr] = d;
-            offs[rr] = bse + __popc(peers & lanemask_lt());
-          }
-          __syncthreads();
-          // exclusive scan over (digit, warp) in digit-major order
-          {
-            constexpr int PER = (256 * NW) / kBucketThreads;
-            uint32_t vals[PER];
-            uint32_t sum = 0;
-#pragma unroll
-            for (int q = 0; q < PER; q++) {
-              const int e = tid * PER + q;  // e = d * NW + w
-              const int d = e / NW, w = e % NW;
-              vals[q] = wc[w * 256 + d];
-              sum += vals[q];
-            }
-            uint32_t tot;
-            uint32_t ex = block_exclusive_sum(sum, s_warp, tot);
-#pragma unroll
-            for (int q = 0; q < PER; q++) {
-              const int e = tid * PER + q;
-              const int d = e / NW, w = e % NW;
-              wc[w * 256 + d] = (uint16_t)ex;
-              ex += vals[q];
-            }
-          }
-          __syncthreads();
-#pragma unroll
-          for (int rr = 0; rr < RMAX; rr++) {
-            const uint32_t idx = e0 + rr * 32 + lane;
-            if (idx < e1) {
-              const uint32_t pos = wc[warp * 256 + dig[rr]] + offs[rr];
-              dk[pos] = sk[idx];
-              dc[pos] = sc[idx];
-            }
-          }
-          __syncthreads();
-          KeyT* tk = sk; sk = dk; dk = tk;
-          uint32_t* tc = sc; sc = dc; dc = tc;
-        }
-        // --- write this sub-range of the bucket's rows
-        const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
-        uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
-        for (uint32_t i0 = 0; i0 < u; i0 += kBucketThreads) {
-          const uint32_t i = i0 + tid;
-          const bool v = i < u;
-          uint32_t d2 = 3;
-          if (v) {
-            const KeyT r = sk[i];
-            const uint32_t cnt = sc[i];
-            const unsigned long long row = (unsigned long long)base + acc + i;
-            if (row < a.cap) {
-              tkeys[row] = hi_bits | r;
-              a.tcounts[row] = cnt;
-            } else {
-              atomicOr(&a.sc->err, ERR_BOUNDS);
-            }
-            d2 = (uint32_t)(KeyOps<KeyT>::shr(r, rem - 2) & 3);
-          }
-          dl0 += __popc(__ballot_sync(FULLMASK, v && d2 == 0));
-          dl1 += __popc(__ballot_sync(FULLMASK, v && d2 == 1));
-          dl2 += __popc(__ballot_sync(FULLMASK, v && d2 == 2));
-        }
-        if (lane == 0) {
-          if (dl0) atomicAdd(&s_d[0], dl0);
-          if (dl1) atomicAdd(&s_d[1], dl1);
-          if (dl2) atomicAdd(&s_d[2], dl2);
-        }
-        acc += u;
-        __syncthreads();
+      for (uint32_t i = tid; i < Heff; i += kBucketThreads) {
+        skey[i] = EMPTY;
+        scnt[i] = 0;
       }
-      if (!ovf) break;
+      if (tid == 0) s_ovf = 0;
       __syncthreads();
-      if (++slog > slog_max) {
-        if (tid == 0) atomicOr(&a.sc->err, ERR_BUCKET);
-        acc = 0;
-        break;
+      // --- hash aggregation of this sub-range (warp-aggregated inserts); OR/AND of
+      //     the sub-range's remainders locate its first differing bit if it overflows
+      KeyT kor = 0, kand = ~(KeyT)0;
+      const int psh = rem - plen;
+      for (uint32_t i0 = (uint32_t)warp * 32; i0 < n; i0 += NW * 32) {
+        const uint32_t i = i0 + lane;
+        const bool valid = i < n;
+        KeyT r = valid ? (keys[base + i] & rmask) : (KeyT)0;
+        const bool mine = valid && (plen == 0 || KeyOps<KeyT>::shr(r, psh) == pv);
+        if (mine) { kor |= r; kand &= r; }
+        const unsigned m = __ballot_sync(FULLMASK, mine);
+        if (mine) {
+          const unsigned peers = KeyOps<KeyT>::match(m, r);
+          if (lane == __ffs(peers) - 1) {
+            if (!hash_insert<KeyT>(skey, scnt, hmask, r, (uint32_t)__popc(peers))) s_ovf = 1;
+          }
+        }
       }
+      __syncthreads();
+      bool ovf = s_ovf != 0;
+      // --- compaction of occupied slots into [0, u)
+      constexpr int SPT = H / kBucketThreads;
+      const uint32_t spt = Heff / kBucketThreads;  // >= 2 since Heff >= 1024
+      KeyT rk[SPT];
+      uint32_t rc[SPT];
+      uint32_t occ = 0;
+#pragma unroll
+      for (int q = 0; q < SPT; q++) {
+        rk[q] = EMPTY;
+        rc[q] = 0;
+        if (!ovf && (uint32_t)q < spt) {
+          rk[q] = skey[tid * spt + q];
+          rc[q] = scnt[tid * spt + q];
+          occ += rk[q] != EMPTY;
+        }
+      }
+      uint32_t u;
+      uint32_t off = block_exclusive_sum(occ, s_warp, u);
+      if (u > Heff / 2) ovf = true;  // the sort needs a second half
+      if (ovf) {
+        // split at the highest bit (below the prefix) where the sub-range's keys differ
+        block_or_and<KeyT>(kor, kand, s_red_k);
+        if (tid == 0) {
+          const KeyT diff = (kor ^ kand) & KeyOps<KeyT>::mask(psh);
+          if (diff == 0 || s_sp + 2 > kBucketStack) {
+            s_fail = 1;
+          } else {
+            const int bit = KeyOps<KeyT>::top_bit(diff);  // bit index from the bottom
+            const int clen = rem - bit;                   // child prefix length
+            const KeyT cp = KeyOps<KeyT>::shr(kand, bit + 1) << 1;  // common bits, then 0
+            s_stk_v[s_sp] = cp | (KeyT)1;
+            s_stk_l[s_sp] = clen;
+            s_stk_v[s_sp + 1] = cp;
+            s_stk_l[s_sp + 1] = clen;
+            s_sp += 2;
+          }
+        }
+        __syncthreads();
+        if (s_fail) { failed = true; break; }
+        continue;
+      }
+#pragma unroll
+      for (int q = 0; q < SPT; q++) {
+        if (rk[q] != EMPTY) {
+          skey[off] = rk[q];
+          scnt[off] = rc[q];
+          off++;
+        }
+      }
+      __syncthreads();
+      // --- stable LSD radix sort of the u distinct remainders, 8-bit digits
+      const int sort_bits = psh;
+      const int npass = (sort_bits + 7) / 8;
+      KeyT* sk = skey;
+      uint32_t* sc = scnt;
+      KeyT* dk = skey + Heff / 2;
+      uint32_t* dc = scnt + Heff / 2;
+      const uint32_t E = (u + NW - 1) / NW;
+      const uint32_t e0 = (uint32_t)warp * E;
+      const uint32_t e1 = min(e0 + E, u);
+      for (int pass = 0; pass < npass; pass++) {
+        const int sh = 8 * pass;
+        for (int i = lane; i < 256; i += 32) wc[warp * 256 + i] = 0;
+        __syncwarp();
+        uint32_t dig[RMAX], offs[RMAX];
+#pragma unroll
+        for (int rr = 0; rr < RMAX; rr++) {
+          const uint32_t idx = e0 + rr * 32 + lane;
+          const bool v = idx < e1;
+          const uint32_t d = v ? (uint32_t)(KeyOps<KeyT>::shr(sk[idx], sh) & 0xff) : 0u;
+          const unsigned vm = __ballot_sync(FULLMASK, v);
+          uint32_t bse = 0;
+          unsigned peers = 0;
+          if (v) {
+            peers = __match_any_sync(vm, d);
+            if (lane == __ffs(peers) - 1) {
+              bse = wc[warp * 256 + d];
+              wc[warp * 256 + d] = (uint16_t)(bse + __popc(peers));
+            }
+          }
+          __syncwarp();
+          const int leader = v ? __ffs(peers) - 1 : lane;
+          bse = __shfl_sync(FULLMASK, bse, leader);
+          dig[rr] = d;
+          offs[rr] = bse + __popc(peers & lanemask_lt());
+        }
+        __syncthreads();
+        // exclusive scan over (digit, warp) in digit-major order
+        {
+          constexpr int PER = (256 * NW) / kBucketThreads;
+          uint32_t vals[PER];
+          uint32_t sum = 0;
+#pragma unroll
+          for (int q = 0; q < PER; q++) {
+            const int e = tid * PER + q;  // e = d * NW + w
+            const int d = e / NW, w = e % NW;
+            vals[q] = wc[w * 256 + d];
+            sum += vals[q];
+          }
+          uint32_t tot;
+          uint32_t ex = block_exclusive_sum(sum, s_warp, tot);
+#pragma unroll
+          for (int q = 0; q < PER; q++) {
+            const int e = tid * PER + q;
+            const int d = e / NW, w = e % NW;
+            wc[w * 256 + d] = (uint16_t)ex;
+            ex += vals[q];
+          }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int rr = 0; rr < RMAX; rr++) {
+          const uint32_t idx = e0 + rr * 32 + lane;
+          if (idx < e1) {
+            const uint32_t pos = wc[warp * 256 + dig[rr]] + offs[rr];
+            dk[pos] = sk[idx];
+            dc[pos] = sc[idx];
+          }
+        }
+        __syncthreads();
+        KeyT* tk = sk; sk = dk; dk = tk;
+        uint32_t* tc = sc; sc = dc; dc = tc;
+      }
+      // --- write this sub-range of the bucket's rows
+      const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
+      uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
+      for (uint32_t i0 = 0; i0 < u; i0 += kBucketThreads) {
+        const uint32_t i = i0 + tid;
+        const bool v = i < u;
+        uint32_t d2 = 3;
+        if (v) {
+          const KeyT r = sk[i];
+          const uint32_t cnt = sc[i];
+          const unsigned long long row = (unsigned long long)base + acc + i;
+          if (row < a.cap) {
+            tkeys[row] = hi_bits | r;
+            a.tcounts[row] = cnt;
+          } else {
+            atomicOr(&a.sc->err, ERR_BOUNDS);
+          }
+          d2 = (uint32_t)(KeyOps<KeyT>::shr(r, rem - 2) & 3);
+        }
+        dl0 += __popc(__ballot_sync(FULLMASK, v && d2 == 0));
+        dl1 += __popc(__ballot_sync(FULLMASK, v && d2 == 1));
+        dl2 += __popc(__ballot_sync(FULLMASK, v && d2 == 2));
+      }
+      if (lane == 0) {
+        if (dl0) atomicAdd(&s_d[0], dl0);
+        if (dl1) atomicAdd(&s_d[1], dl1);
+        if (dl2) atomicAdd(&s_d[2], dl2);
+      }
+      acc += u;
+      __syncthreads();
     }
+    if (failed) {
+      if (tid == 0) atomicOr(&a.sc->err, ERR_BUCKET);
+      acc = 0;
+    }
+    __syncthreads();
     // the histogram is added only once the bucket's rows are final
     for (uint32_t i = tid; i < acc; i += kBucketThreads) {
       const uint32_t cnt = a.tcounts[base + i];
@@ -921,31 +994,116 @@ __device__ __forceinline__ uint32_t upper_bound_s(const KeyT* k, uint32_t lo, ui
   return lo;
 }
 
-// Node key of table row `row` as seen from stream `st`: the prefix (k-1)-mer x >> 2
-// for the suffix-side stream (st == 0), the suffix (k-1)-mer for the others.
+// Kept rows (count >= cutoff) of every table bucket, written densely in key order --
+// the k-mers construct_kmer_histogram hands to macro-node construction.  Per bucket:
+// kstart (first kept row), kcount, and ksub (kept rows whose next two key bits are
+// < 1, 2, 3).  Warps scan 32-row steps with ballots; bucket offsets come from a
+// decoupled look-back (every bucket publishes its aggregate before waiting).
 template <typename KeyT>
-__device__ __forceinline__ KeyT node_key(const KeyT* __restrict__ tkeys, uint32_t row, int st,
+__global__ void __launch_bounds__(kMnThreads) k_filter_kept(FilterArgs a) {
+  __shared__ uint32_t s_warp[33];
+  __shared__ uint32_t s_beta, s_K, s_d[3];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = kMnThreads / 32;
+  const int B = 1 << a.bbits;
+  const int rem = 2 * a.k - a.bbits;
+  const uint32_t cut = a.sc->cutoff;
+  const KeyT* __restrict__ tkeys = reinterpret_cast<const KeyT*>(a.tkeys);
+  KeyT* __restrict__ kkeys = reinterpret_cast<KeyT*>(a.kkeys);
+  while (true) {
+    __syncthreads();
+    if (tid == 0) s_beta = atomicAdd(&a.sc->ticket_filter, 1u);
+    if (tid < 3) s_d[tid] = 0;
+    __syncthreads();
+    const uint32_t beta = s_beta;
+    if (beta >= (uint32_t)B) break;
+    const uint32_t r0 = a.bstart[beta], u = a.tu[beta];
+    const uint32_t per = ((u + NW - 1) / NW + 31) & ~31u;  // rows per warp, whole steps
+    const uint32_t w0 = min(u, warp * per), w1 = min(u, w0 + per);
+    uint32_t mine = 0;
+    for (uint32_t i0 = w0; i0 < w1; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      const bool keep = i < w1 && a.tcounts[r0 + i] >= cut;
+      mine += __popc(__ballot_sync(FULLMASK, keep));
+    }
+    uint32_t v;
+    const uint32_t wex = block_exclusive_sum(lane == 0 ? mine : 0u, s_warp, v);
+    const uint32_t wbase = __shfl_sync(FULLMASK, wex, 0);
+    if (tid == 0) {
+      st_release(&a.flags[beta], kLbAgg | (unsigned long long)v);
+      const unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
+      st_release(&a.flags[beta], kLbIncl | (ex + v));
+      s_K = (uint32_t)ex;
+      if (beta == (uint32_t)B - 1) a.sc->n_kept_rows = ex + v;
+    }
+    __syncthreads();
+    const uint32_t K = s_K;
+    uint32_t pos = K + wbase;
+    uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
+    for (uint32_t i0 = w0; i0 < w1; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      const uint32_t c = i < w1 ? a.tcounts[r0 + i] : 0;
+      const bool keep = i < w1 && c >= cut;
+      const unsigned bal = __ballot_sync(FULLMASK, keep);
+      uint32_t d2 = 3;
+      if (keep) {
+        const KeyT x = tkeys[r0 + i];
+        const uint32_t o = pos + __popc(bal & lanemask_lt());
+        if (o < a.cap) {
+          kkeys[o] = x;
+          a.kcounts[o] = c;
+        } else {
+          atomicOr(&a.sc->err, ERR_BOUNDS);
+        }
+        d2 = (uint32_t)(KeyOps<KeyT>::shr(x, rem - 2) & 3);
+      }
+      dl0 += __popc(__ballot_sync(FULLMASK, keep && d2 == 0));
+      dl1 += __popc(__ballot_sync(FULLMASK, keep && d2 == 1));
+      dl2 += __popc(__ballot_sync(FULLMASK, keep && d2 == 2));
+      pos += __popc(bal);
+    }
+    if (lane == 0) {
+      if (dl0) atomicAdd(&s_d[0], dl0);
+      if (dl1) atomicAdd(&s_d[1], dl1);
+      if (dl2) atomicAdd(&s_d[2], dl2);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      a.kstart[beta] = K;
+      a.kcount[beta] = v;
+      a.ksub[3 * beta + 0] = s_d[0];
+      a.ksub[3 * beta + 1] = s_d[0] + s_d[1];
+      a.ksub[3 * beta + 2] = s_d[0] + s_d[1] + s_d[2];
+    }
+  }
+}
+
+// Node key of kept row `row` as seen from stream `st`: the prefix (k-1)-mer x >> 2 for
+// the suffix-side stream (st == 0), the suffix (k-1)-mer for the others.
+template <typename KeyT>
+__device__ __forceinline__ KeyT node_key(const KeyT* __restrict__ kk, uint32_t row, int st,
                                          KeyT succ_mask) {
-  const KeyT x = tkeys[row];
+  const KeyT x = kk[row];
   return st == 0 ? (x >> 2) : (x & succ_mask);
 }
 
 // first row in [lo, hi) whose node key is > piv
 template <typename KeyT>
-__device__ uint32_t upper_bound_rows(const KeyT* __restrict__ tkeys, uint32_t lo, uint32_t hi, int st,
+__device__ uint32_t upper_bound_rows(const KeyT* __restrict__ kk, uint32_t lo, uint32_t hi, int st,
                                      KeyT succ_mask, KeyT piv) {
   while (lo < hi) {
     uint32_t mid = (lo + hi) >> 1;
-    if (!(piv < node_key(tkeys, mid, st, succ_mask))) lo = mid + 1; else hi = mid;
+    if (!(piv < node_key(kk, mid, st, succ_mask))) lo = mid + 1; else hi = mid;
   }
   return lo;
 }
 
-// Per (k-1)-mer bucket: the suffix-side stream (table bucket beta, node = x >> 2,
-// extension = last base) and four prefix-side streams (table buckets whose remaining
-// bits continue with beta, node = x & SUCC_MASK, extension = first base f) are each
-// sorted by node key; merged they give the bucket's macro-nodes in key order.  A
-// bucket is processed in segments of at most kMnCap rows split at node-key pivots.
+// Per (k-1)-mer bucket: the suffix-side stream (kept rows of table bucket beta, node =
+// x >> 2, extension = last base) and four prefix-side streams (kept rows of the table
+// buckets whose remaining bits continue with beta, node = x & SUCC_MASK, extension =
+// first base f) are each sorted by node key; merged they give the bucket's
+// macro-nodes in key order.  A bucket larger than kMnCap rows is processed in
+// segments split at node-key pivots.
 template <typename KeyT>
 __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
   using SM = MnSmem<KeyT>;
@@ -956,7 +1114,7 @@ __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
   uint16_t* ord = reinterpret_cast<uint16_t*>(smem + SM::off_ord);
   uint16_t* nid = reinterpret_cast<uint16_t*>(smem + SM::off_nid);
   __shared__ uint32_t s_warp[33];
-  __shared__ uint32_t s_beta, s_off[6], s_cur[5], s_end[5], s_segend[5], s_more, s_last;
+  __shared__ uint32_t s_beta, s_off[6], s_cur[5], s_end[5], s_segend[5], s_last;
   __shared__ unsigned long long s_NO;
 
   const int tid = threadIdx.x;
@@ -965,10 +1123,9 @@ __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
   const int nb = 2 * (k - 1);
   const KeyT succ_mask = KeyOps<KeyT>::mask(nb);
   const KeyT KINF = ~(KeyT)0;  // above every (k-1)-mer key
-  const uint32_t cut = a.sc->cutoff;
-  const KeyT* __restrict__ tkeys = reinterpret_cast<const KeyT*>(a.tkeys);
+  const KeyT* __restrict__ kk = reinterpret_cast<const KeyT*>(a.kkeys);
   KeyT* __restrict__ nkeys = reinterpret_cast<KeyT*>(a.nkeys);
-  constexpr uint32_t PER = (kMnCap - 16) / 5;  // rows per stream per segment before ties
+  constexpr uint32_t CAP = kMnCap - 16;  // rows per segment before ties
 
   while (true) {
     __syncthreads();
@@ -977,14 +1134,14 @@ __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
     const uint32_t beta = s_beta;
     if (beta >= (uint32_t)B) break;
     if (tid == 0) {
-      s_cur[0] = a.bstart[beta];
-      s_end[0] = a.bstart[beta] + a.tu[beta];
+      s_cur[0] = a.kstart[beta];
+      s_end[0] = a.kstart[beta] + a.kcount[beta];
       for (int f = 0; f < 4; f++) {
         const uint32_t bp = ((uint32_t)f << (a.bbits - 2)) | (beta >> 2);
         const uint32_t d = beta & 3;
-        const uint32_t b0 = a.bstart[bp];
-        s_cur[f + 1] = b0 + (d == 0 ? 0u : a.tsub[3 * bp + d - 1]);
-        s_end[f + 1] = b0 + (d == 3 ? a.tu[bp] : a.tsub[3 * bp + d]);
+        const uint32_t b0 = a.kstart[bp];
+        s_cur[f + 1] = b0 + (d == 0 ? 0u : a.ksub[3 * bp + d - 1]);
+        s_end[f + 1] = b0 + (d == 3 ? a.kcount[bp] : a.ksub[3 * bp + d]);
       }
     }
     __syncthreads();
@@ -992,59 +1149,53 @@ __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
     bool multi = false;
     unsigned long long NO = 0, done_nodes = 0;
     while (true) {
-      // ---- choose this segment's rows
+      // ---- choose this segment's rows: everything left, or rows up to a pivot key
       if (tid == 0) {
-        uint32_t left = 0;
-        for (int st = 0; st < 5; st++) left += s_end[st] - s_cur[st];
-        s_more = left > 0;
+        uint32_t total = 0;
+        for (int st = 0; st < 5; st++) total += s_end[st] - s_cur[st];
         KeyT piv = KINF;
-        for (int st = 0; st < 5; st++)
-          if (s_end[st] - s_cur[st] > PER) {
-            KeyT kk = node_key(tkeys, s_cur[st] + PER - 1, st, succ_mask);
-            if (kk < piv) piv = kk;
+        if (total > CAP) {
+          const float frac = 0.9f * (float)CAP / (float)total;
+          for (int st = 0; st < 5; st++) {
+            const uint32_t take = (uint32_t)((float)(s_end[st] - s_cur[st]) * frac);
+            if (take >= 1) {
+              const KeyT kx = node_key(kk, s_cur[st] + take - 1, st, succ_mask);
+              if (kx < piv) piv = kx;
+            }
           }
+        }
         s_last = 1;
         for (int st = 0; st < 5; st++) {
           s_segend[st] = piv == KINF ? s_end[st]
-                                     : upper_bound_rows(tkeys, s_cur[st], s_end[st], st, succ_mask, piv);
+                                     : upper_bound_rows(kk, s_cur[st], s_end[st], st, succ_mask, piv);
           if (s_segend[st] != s_end[st]) s_last = 0;
         }
+        uint32_t o = 0;
+        for (int st = 0; st < 5; st++) {
+          s_off[st] = o;
+          o += s_segend[st] - s_cur[st];
+        }
+        s_off[5] = o;
       }
       __syncthreads();
-      if (!s_more && !first) break;
       const bool last = s_last != 0;
       if (first && !last) multi = true;
-      // ---- gather the segment's kept rows (count >= cutoff) into five sorted runs
-      uint32_t len = 0;
-      if (tid == 0) s_off[0] = 0;
-      for (int st = 0; st < 5; st++) {
-        const uint32_t lo = s_cur[st], hi = s_segend[st];
-        for (uint32_t i0 = lo; i0 < hi; i0 += kMnThreads) {
-          const uint32_t i = i0 + tid;
-          const bool v = i < hi;
-          const uint32_t c = v ? a.tcounts[i] : 0;
-          const bool keep = v && c >= cut;
-          uint32_t tot;
-          const uint32_t pos = block_exclusive_sum(keep ? 1u : 0u, s_warp, tot);
-          if (keep) {
-            const uint32_t o = len + pos;
-            if (o < (uint32_t)kMnCap) {
-              const KeyT x = tkeys[i];
-              ikey[o] = st == 0 ? (x >> 2) : (x & succ_mask);
-              itag[o] = (uint8_t)(st == 0 ? (uint32_t)(x & 3) : (uint32_t)(3 + st));
-              icnt[o] = c;
-            }
-          }
-          len += tot;
-        }
-        if (tid == 0) s_off[st + 1] = len;
+      uint32_t mm = s_off[5];
+      if (mm > (uint32_t)kMnCap) {  // cannot happen with CAP-sized segments
+        if (tid == 0) atomicOr(&a.sc->err, ERR_MN_CAPACITY);
+        mm = 0;
+      }
+      // ---- gather the five sorted runs
+      for (uint32_t i = tid; i < mm; i += kMnThreads) {
+        int st = 0;
+        while (i >= s_off[st + 1]) st++;
+        const uint32_t row = s_cur[st] + (i - s_off[st]);
+        const KeyT x = kk[row];
+        ikey[i] = st == 0 ? (x >> 2) : (x & succ_mask);
+        itag[i] = (uint8_t)(st == 0 ? (uint32_t)(x & 3) : (uint32_t)(3 + st));
+        icnt[i] = a.kcounts[row];
       }
       __syncthreads();
-      if (len > (uint32_t)kMnCap) {  // cannot happen with PER-sized segments
-        if (tid == 0) atomicOr(&a.sc->err, ERR_MN_CAPACITY);
-        len = 0;
-      }
-      const uint32_t mm = len;
       // ---- merge rank of every item across the five runs
       for (uint32_t i = tid; i < mm; i += kMnThreads) {
         int st = 0;
@@ -1197,6 +1348,17 @@ cudaError_t launch_histogram(const uint32_t* tcounts, unsigned long long u, int 
 cudaError_t launch_cutoff(const unsigned long long* hist, int t, Scalars* sc, cudaStream_t st) {
   k_cutoff<<<1, 1024, 0, st>>>(hist, t, sc);
   return cudaGetLastError();
+}
+
+template <typename KeyT>
+static cudaError_t launch_filter_t(const FilterArgs& a, int grid, cudaStream_t st) {
+  if (grid <= 0) grid = sm_count() * 4;
+  k_filter_kept<KeyT><<<grid, kMnThreads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_filter_kept(const FilterArgs& a, int wide, int grid, cudaStream_t st) {
+  return wide ? launch_filter_t<u128>(a, grid, st) : launch_filter_t<uint64_t>(a, grid, st);
 }
 
 template <typename KeyT>
