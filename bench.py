@@ -30,8 +30,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "k-mers/sec count+macro-node on 1 GB300 (% HBM roofline); served p50/p99 latency"
 UNIT = "k-mers/s"
-KERNELS_PER_STEP = 10  # line scan, tile prefix, bucket count, column prefix, bucket prefix,
-#                        scatter, bucket table, cutoff, kept filter, macro-nodes
+KERNELS_PER_STEP = 12  # line scan, tile prefix, bucket count, column prefix, bucket prefix,
+#                        coarse offsets, coarse scatter, fine scatter, bucket table, cutoff,
+#                        kept filter, macro-nodes
 
 
 def parse():
@@ -127,7 +128,8 @@ def stage_bytes(stage: str, F: int, N: int, U: int, V: int, M: int, W: int, t: i
         "line_scan": F,
         "bucket_count": F + 4 * G * B,
         "bucket_offsets": 3 * 4 * G * B,
-        "scatter": F + N * W,
+        "scatter_coarse": F + N * W,
+        "scatter_fine": 2 * N * W,
         "bucket_table": N * W + U * (W + 4),
         "cutoff": 8 * t,
         "kept_filter": U * (W + 4) + V * (W + 4),

@@ -18,7 +18,7 @@
 
 using namespace pk;
 
-static const int kMaxPartitionBits = 13;
+static const int kMaxPartitionBits = 15;
 
 // ------------------------------------------------------------------ errors ------
 static thread_local std::string t_last_error;
@@ -62,15 +62,17 @@ enum Stage {
   ST_BUCKET_COUNT,
   ST_OFFSETS,
   ST_SCATTER,
+  ST_SCATTER_FINE,
   ST_TABLE,
   ST_CUTOFF,
   ST_FILTER,
   ST_MN,
   ST_COUNT_
 };
-static const char* kStageNames[ST_COUNT_] = {"h2d",          "line_scan", "bucket_count",
-                                             "bucket_offsets", "scatter", "bucket_table",
-                                             "cutoff",       "kept_filter", "macro_nodes"};
+static const char* kStageNames[ST_COUNT_] = {"h2d",          "line_scan",      "bucket_count",
+                                             "bucket_offsets", "scatter_coarse", "scatter_fine",
+                                             "bucket_table", "cutoff",         "kept_filter",
+                                             "macro_nodes"};
 
 struct pk_job {
   pk_ctx* ctx = nullptr;
@@ -88,7 +90,8 @@ struct pk_job {
   Scalars* d_sc = nullptr;
   Scalars* h_sc = nullptr;  // pinned mirror
   DevBuf fasta, tile_nl, counts, bstart, keys, tkeys, tcounts, tu, tsub, flags_m, hist, hist2,
-      nkeys, nsuf, npre, packed, doff, dkeys, dcounts, flags_f, kkeys, kcounts, kstart, kcount, ksub;
+      nkeys, nsuf, npre, packed, doff, dkeys, dcounts, flags_f, kkeys, kcounts, kstart, kcount, ksub,
+      coff, cstart, slice_start, fcur;
   bool dense_valid = false;
   bool timing = false;
   cudaEvent_t ev0[ST_COUNT_] = {}, ev1[ST_COUNT_] = {};
@@ -141,7 +144,7 @@ static void job_free_all(pk_job* j) {
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
-                   &j->ksub};
+                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur};
   for (DevBuf* b : all) job_free(j, *b);
   j->dense_valid = false;
 }
@@ -309,7 +312,7 @@ pk_status pk_job_memory(pk_job* j, uint64_t* bytes) {
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
-                   &j->ksub};
+                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur};
   uint64_t s = 0;
   for (DevBuf* b : all) s += b->bytes;
   *bytes = s;
@@ -356,13 +359,13 @@ static pk_status check_params(const pk_params* p) {
   return PK_OK;
 }
 
-// Partition digits: the leading key bits that pick a bucket.  Two limits meet here:
-// the scatter keeps one partially filled 32-byte sector per (CTA, bucket) in L2, so
-// 2^bits buckets x one CTA per SM must stay well inside the 126 MB L2 (<= 2^13); and a
-// bucket's distinct keys should fit the on-chip table of the per-bucket kernel.
+// Partition digits: the leading key bits that pick a bucket, sized so an average
+// bucket holds a few thousand keys (the per-bucket kernel counts a bucket on chip).
+// The keys reach their buckets in two passes (kCoarseBits coarse regions, then fine
+// buckets inside each region), so the digit count is not tied to L2 capacity.
 static int auto_bucket_bits(uint64_t F, int k, int wide) {
-  const double per_bucket = wide ? 6000.0 : 12000.0;  // keys per bucket aimed at
-  const double est = 0.7 * (double)F;                 // k-mer windows per byte, ~100 bp reads
+  const double per_bucket = wide ? 3000.0 : 5000.0;  // keys per bucket aimed at
+  const double est = 0.7 * (double)F;                // k-mer windows per byte, ~100 bp reads
   int b = 2;
   while (b < kMaxPartitionBits && est / (double)(1u << b) > per_bucket) b++;
   return std::max(2, std::min(b, 2 * k - 2));
@@ -404,6 +407,7 @@ static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk
   a.lmer_m = std::min(k, p->lmer_length);
   a.drop_n = p->drop_n ? 1 : 0;
   a.bbits = j->bbits;
+  a.cbits = std::min(j->bbits, kCoarseBits);
   a.grid = grid;
   a.chunk = chunk;
   a.tile_nl = (uint32_t*)j->tile_nl.p;
@@ -442,9 +446,30 @@ static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk
   j->t_hist = t;
   j->dense_valid = false;
 
+  // two-pass partition: coarse regions (pass 1), then fine buckets (pass 2).  The
+  // coarse copy lives in the table buffer, which is written only after pass 2.
+  const int Cn = 1 << a.cbits;
+  PK_TRY(job_alloc(j, j->coff, sizeof(uint32_t) * (size_t)grid * Cn));
+  PK_TRY(job_alloc(j, j->cstart, sizeof(uint32_t) * (Cn + 1)));
+  PK_TRY(job_alloc(j, j->slice_start, sizeof(uint32_t) * (Cn + 1)));
+  PK_TRY(job_alloc(j, j->fcur, sizeof(uint32_t) * (size_t)B));
+  const bool two_pass = a.cbits < a.bbits;
   mark_begin(j, ST_SCATTER);
-  PK_CUDA(launch_scatter(a, j->keys.p, j->wide, j->stream));
+  PK_CUDA(launch_coarse_offsets(a, (uint32_t*)j->coff.p, (uint32_t*)j->cstart.p,
+                                (uint32_t*)j->slice_start.p, j->wide, j->stream));
+  PK_CUDA(launch_scatter_coarse(a, (const uint32_t*)j->coff.p, two_pass ? j->tkeys.p : j->keys.p,
+                                j->wide, j->stream));
   mark_end(j, ST_SCATTER);
+  mark_begin(j, ST_SCATTER_FINE);
+  if (two_pass) {
+    PK_CUDA(cudaMemcpyAsync(j->fcur.p, j->bstart.p, sizeof(uint32_t) * (size_t)B, cudaMemcpyDeviceToDevice,
+                            j->stream));
+    PK_CUDA(cudaMemsetAsync(&j->d_sc->ticket_fine, 0, sizeof(uint32_t), j->stream));
+    PK_CUDA(launch_scatter_fine(j->tkeys.p, (const uint32_t*)j->cstart.p, (const uint32_t*)j->slice_start.p,
+                                (uint32_t*)j->fcur.p, j->keys.p, k, a.bbits, a.cbits, j->wide,
+                                &j->d_sc->ticket_fine, N, &j->d_sc->err, j->stream));
+  }
+  mark_end(j, ST_SCATTER_FINE);
   mark_begin(j, ST_TABLE);
   BucketArgs b{};
   b.keys = j->keys.p;

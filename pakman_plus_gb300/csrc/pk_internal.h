@@ -25,6 +25,10 @@ constexpr int kMnCap = 4096;        // items (k-mer records) per macro-node segm
 constexpr int kHistSmem = 1024;     // count-histogram bins kept in shared memory
 constexpr int kBucketStack = 256;   // pending sub-ranges of one bucket (binary-trie split)
 constexpr int kMaxBucketAttempts = 1 << 16;  // sub-range attempts per bucket before giving up
+constexpr int kCoarseBits = 7;      // pass-1 partition digits (coarse regions)
+constexpr int kOvfSlots = 256;      // slots past the order-preserving table (no wrap-around)
+constexpr int kProbeMax = 64;       // longest probe of the order-preserving table
+constexpr int kClusterMax = 64;     // longest cluster sorted in place
 
 struct Scalars {                    // device-side scalars of one job
   unsigned long long s0;            // index of the first '>' (F if none)
@@ -36,6 +40,8 @@ struct Scalars {                    // device-side scalars of one job
   uint32_t ticket_mn;
   uint32_t cutoff;                  // histogram cutoff
   uint32_t ticket_filter;
+  uint32_t ticket_fine;
+  uint32_t pad2;
   unsigned long long n_unique;      // U
   unsigned long long n_kept;        // V
   unsigned long long n_nodes;       // M
@@ -49,6 +55,7 @@ struct CountArgs {
   int lmer_m;        // min(k, LMER_LENGTH): record-start checks follow the l-mer pass
   int drop_n;
   int bbits;         // bucket bits (top bits of the 2k-bit key)
+  int cbits;         // coarse bits of the pass-1 partition (<= bbits, <= kCoarseBits)
   int grid;          // extraction CTAs (chunks)
   unsigned long long chunk;  // bytes per chunk (multiple of kTileBytes)
   uint32_t* tile_nl;         // ceil(F / kTileBytes) + 1, exclusive newline prefix
@@ -114,6 +121,14 @@ cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st);
 cudaError_t launch_bucket_count(const CountArgs& a, int wide, cudaStream_t st);
 cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st);
 cudaError_t launch_scatter(const CountArgs& a, void* keys_out, int wide, cudaStream_t st);
+// Two-pass partition: coarse regions (pass 1) then fine buckets inside each region.
+cudaError_t launch_coarse_offsets(const CountArgs& a, uint32_t* coff, uint32_t* cstart,
+                                  uint32_t* slice_start, int wide, cudaStream_t st);
+cudaError_t launch_scatter_coarse(const CountArgs& a, const uint32_t* coff, void* out, int wide,
+                                  cudaStream_t st);
+cudaError_t launch_scatter_fine(const void* in, const uint32_t* cstart, const uint32_t* slice_start,
+                                uint32_t* fcur, void* out, int k, int bbits, int cbits, int wide,
+                                uint32_t* ticket, unsigned long long cap, uint32_t* err, cudaStream_t st);
 cudaError_t launch_bucket_table(const BucketArgs& a, int wide, int grid, cudaStream_t st);
 cudaError_t launch_histogram(const uint32_t* tcounts, unsigned long long u, int t,
                              unsigned long long* hist, cudaStream_t st);

@@ -518,6 +518,292 @@ k_extract(CountArgs a, KeyT* __restrict__ keys_out) {
   }
 }
 
+// ----------------------------------------------------- two-pass partition of keys ---
+// Pass 1 (k_scatter_coarse): roll the k-mers of a chunk again and append each key to a
+// shared-memory ring of its coarse bucket (leading kCoarseBits bits); full 128-byte
+// lines are flushed by warps to the chunk's segment of the coarse region, so global
+// stores are whole lines instead of scattered 8/16-byte writes.
+template <typename KeyT>
+struct CoarseCfg {
+  static constexpr int C = 1 << kCoarseBits;               // coarse buckets
+  static constexpr int R = sizeof(KeyT) == 8 ? 128 : 64;    // ring slots per bucket
+  static constexpr int FU = 128 / (int)sizeof(KeyT);        // keys per 128-byte line
+  static constexpr int BP = sizeof(KeyT) == 8 ? 16 : 8;     // window positions per batch
+  static constexpr size_t smem = sizeof(KeyT) * C * R;
+};
+
+template <typename KeyT>
+__device__ __forceinline__ void guarded_store(KeyT* __restrict__ out, uint32_t idx, KeyT v,
+                                              unsigned long long cap, uint32_t* err) {
+  if (idx < cap) out[idx] = v;
+  else atomicOr(err, ERR_BOUNDS);
+}
+
+template <typename KeyT>
+__device__ __forceinline__ void coarse_flush(KeyT* ring, uint32_t* w, uint32_t* f, const uint32_t* g,
+                                             KeyT* __restrict__ out, bool final_flush,
+                                             unsigned long long cap, uint32_t* err) {
+  using CF = CoarseCfg<KeyT>;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = kExtractThreads / 32;
+  for (int b = warp; b < CF::C; b += NW) {
+    const uint32_t W = w[b];
+    uint32_t Fv = f[b];
+    KeyT* rb = ring + b * CF::R;
+    const uint32_t gb = g[b];
+    if (W - Fv > (uint32_t)CF::R) {
+      // the ring overflowed this batch: keys past Fv+R went straight to global memory
+      for (uint32_t x = lane; x < (uint32_t)CF::R; x += 32)
+        guarded_store(out, gb + Fv + x, rb[(Fv + x) & (CF::R - 1)], cap, err);
+      Fv = W;
+    } else {
+      while (W - Fv >= 32) {
+        guarded_store(out, gb + Fv + lane, rb[(Fv + lane) & (CF::R - 1)], cap, err);
+        Fv += 32;
+      }
+      if (W - Fv >= (uint32_t)CF::FU) {
+        if (lane < CF::FU) guarded_store(out, gb + Fv + lane, rb[(Fv + lane) & (CF::R - 1)], cap, err);
+        Fv += CF::FU;
+      }
+      if (final_flush && W > Fv) {
+        if ((uint32_t)lane < W - Fv) guarded_store(out, gb + Fv + lane, rb[(Fv + lane) & (CF::R - 1)], cap, err);
+        Fv = W;
+      }
+    }
+    __syncwarp();
+    if (lane == 0) f[b] = Fv;
+  }
+}
+
+template <typename KeyT>
+__global__ void __launch_bounds__(kExtractThreads, 1)
+k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restrict__ out) {
+  using CF = CoarseCfg<KeyT>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  KeyT* ring = reinterpret_cast<KeyT*>(smem_raw);
+  __shared__ uint32_t s_w[CF::C], s_f[CF::C], s_g[CF::C];
+  __shared__ uint32_t s_wpar[kExtractThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int NW = kExtractThreads / 32;
+  const int k = a.k;
+  const int cshift = 2 * k - a.cbits;  // coarse bucket = leading cbits bits
+  const KeyT kmask = KeyOps<KeyT>::mask(2 * k);
+  const bool drop_n = a.drop_n != 0;
+  const uint8_t* __restrict__ buf = a.fasta;
+  const unsigned long long F = a.F;
+  const unsigned long long s0 = a.sc->s0;
+  const int c = blockIdx.x;
+  const int Cn = 1 << a.cbits;
+  for (int i = tid; i < CF::C; i += kExtractThreads) {
+    s_w[i] = 0;
+    s_f[i] = 0;
+    s_g[i] = i < Cn ? coff[(size_t)c * Cn + i] : 0;
+  }
+  __syncthreads();
+  const unsigned long long c0 = (unsigned long long)c * a.chunk;
+  const unsigned long long c1 = min(c0 + a.chunk, F);
+  const int warm_units = (k - 1 + 15) / 16;
+  if (c0 < c1 && s0 < F) {
+    uint32_t carry = (a.tile_nl[c0 / kTileBytes] ^ a.sc->nl_before_s0) & 1u;
+    for (unsigned long long base = c0; base < c1; base += (unsigned long long)kExtractThreads * kSegBytes) {
+      const unsigned long long seg = base + (unsigned long long)tid * kSegBytes;
+      const bool active = seg < c1;
+      uint32_t w[4][4];
+      uint32_t nlc = 0;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        unsigned long long p = seg + 16ull * u;
+        if (active && p < c1) {
+          load_unit(buf, F, p, w[u]);
+#pragma unroll
+          for (int i = 0; i < 4; i++) nlc += __popc(__vcmpeq4(w[u][i], 0x0A0A0A0Au)) >> 3;
+        } else {
+          w[u][0] = w[u][1] = w[u][2] = w[u][3] = 0;
+        }
+      }
+      const unsigned bal = __ballot_sync(FULLMASK, nlc & 1u);
+      if (lane == 0) s_wpar[warp] = __popc(bal) & 1u;
+      __syncthreads();
+      uint32_t wp = 0, tot = 0;
+#pragma unroll
+      for (int i = 0; i < NW; i++) {
+        uint32_t x = s_wpar[i];
+        tot ^= x;
+        if (i < warp) wp ^= x;
+      }
+      __syncthreads();
+      uint32_t pin = carry ^ wp ^ (__popc(bal & lanemask_lt()) & 1u);
+      carry ^= tot;
+
+      Roll s;
+      s.r0 = s.r1 = s.r2 = 0;
+      s.n0 = s.n1 = s.n2 = 0;
+      s.h0 = s.h1 = 0;
+      if (active) {
+        for (int u = warm_units; u >= 1; u--) {
+          long long p = (long long)seg - 16ll * u;
+          if (p < 0) continue;
+          uint32_t ww[4];
+          load_unit(buf, F, (unsigned long long)p, ww);
+          roll_push(s, decode_unit(ww), drop_n);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const unsigned long long p = seg + 16ull * u;
+        const bool live = active && p < c1;
+        uint32_t v = 0;
+        bool all_clear = false;
+        if (live) {
+          const UnitBits ub = decode_unit(w[u]);
+          roll_push(s, ub, drop_n);
+          uint32_t x = ub.nl;
+          x ^= x << 1; x ^= x << 2; x ^= x << 4; x ^= x << 8;
+          const uint32_t ex = (x << 1) & 0xffffu;
+          const uint32_t odd = (pin ? ~ex : ex) & 0xffffu;
+          pin ^= __popc(ub.nl) & 1u;
+          uint32_t in = 0xffffu;
+          if (p + 16 > F) in &= (1u << (uint32_t)(F - p)) - 1u;
+          if (p < s0) in &= s0 - p >= 16 ? 0u : ~((1u << (uint32_t)(s0 - p)) - 1u);
+          v = odd & in & ~ub.nl;
+          all_clear = k + 15 <= 64 ? window_clear(s, 0, k + 15)
+                                   : (s.h0 == 0 && (s.h1 & ((1ull << (k + 15 - 64)) - 1ull)) == 0);
+        }
+#pragma unroll
+        for (int half = 0; half < 16 / CF::BP; half++) {
+#pragma unroll
+          for (int jj = 0; jj < CF::BP; jj++) {
+            const int j = half * CF::BP + jj;
+            if (!((v >> j) & 1u)) continue;
+            const int age = 15 - j;
+            if (!all_clear && !window_clear(s, age, k)) continue;
+            const KeyT key = window_key<KeyT>(s, 2 * age, kmask);
+            const uint32_t b = (uint32_t)(key >> cshift);
+            const uint32_t pos = atomicAdd(&s_w[b], 1u);
+            if (pos - s_f[b] < (uint32_t)CF::R) ring[b * CF::R + (pos & (CF::R - 1))] = key;
+            else guarded_store(out, s_g[b] + pos, key, a.n_keys, &a.sc->err);
+          }
+          __syncthreads();
+          coarse_flush<KeyT>(ring, s_w, s_f, s_g, out, false, a.n_keys, &a.sc->err);
+          __syncthreads();
+        }
+      }
+    }
+  }
+  __syncthreads();
+  coarse_flush<KeyT>(ring, s_w, s_f, s_g, out, true, a.n_keys, &a.sc->err);
+}
+
+// Coarse offsets: coff[c][g] = start of chunk c's segment in coarse region g (the
+// coarse region is the union of its fine buckets' regions); cstart[g] = region start;
+// slice_start[g] = first pass-2 slice of region g.
+__global__ void __launch_bounds__(256) k_coarse_offsets(const uint32_t* __restrict__ counts,
+                                                        const uint32_t* __restrict__ bstart, int grid,
+                                                        int bbits, int cbits, uint32_t* coff,
+                                                        uint32_t* cstart, uint32_t* slice_start,
+                                                        int slice_keys) {
+  __shared__ uint32_t s_c[1 << kCoarseBits];
+  const int c = blockIdx.x;
+  const int B = 1 << bbits, Cn = 1 << cbits, fb = bbits - cbits;
+  for (int i = threadIdx.x; i < Cn; i += blockDim.x) s_c[i] = 0;
+  __syncthreads();
+  for (int b = threadIdx.x; b < B; b += blockDim.x) atomicAdd(&s_c[b >> fb], counts[(size_t)c * B + b]);
+  __syncthreads();
+  for (int g = threadIdx.x; g < Cn; g += blockDim.x) coff[(size_t)c * Cn + g] = bstart[g << fb] + s_c[g];
+  if (c == 0 && threadIdx.x == 0) {
+    uint32_t acc = 0;
+    for (int g = 0; g < Cn; g++) {
+      cstart[g] = bstart[g << fb];
+      slice_start[g] = acc;
+      const uint32_t n = bstart[(g + 1) << fb] - bstart[g << fb];
+      acc += (n + slice_keys - 1) / slice_keys;
+    }
+    cstart[Cn] = bstart[B];
+    slice_start[Cn] = acc;
+  }
+}
+
+// Pass 2 (k_scatter_fine): a slice of a coarse region (in chunk order) is counting-
+// sorted in shared memory by fine bucket; each fine run is written at a position
+// reserved with one atomic per (slice, fine bucket), so runs land contiguously.
+template <typename KeyT>
+struct FineCfg {
+  static constexpr int S = sizeof(KeyT) == 8 ? 4096 : 2048;  // keys per slice
+  static constexpr int FBMAX = 1 << (15 - kCoarseBits);     // fine buckets per coarse
+  static constexpr size_t smem = 2 * sizeof(KeyT) * S + sizeof(uint16_t) * S;
+};
+
+template <typename KeyT>
+__global__ void __launch_bounds__(512) k_scatter_fine(const KeyT* __restrict__ in,
+                                                     const uint32_t* __restrict__ cstart,
+                                                     const uint32_t* __restrict__ slice_start,
+                                                     uint32_t* fcur, KeyT* __restrict__ out,
+                                                     int k, int bbits, int cbits, uint32_t* ticket,
+                                                     unsigned long long cap, uint32_t* err) {
+  using FC = FineCfg<KeyT>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  KeyT* A = reinterpret_cast<KeyT*>(smem_raw);
+  KeyT* Bk = A + FC::S;
+  uint16_t* bin = reinterpret_cast<uint16_t*>(Bk + FC::S);
+  __shared__ uint32_t s_hist[FC::FBMAX], s_loff[FC::FBMAX], s_goff[FC::FBMAX], s_fill[FC::FBMAX];
+  __shared__ uint32_t s_warp[33];
+  __shared__ uint32_t s_slice, s_g;
+  const int tid = threadIdx.x;
+  const int Cn = 1 << cbits, fb = bbits - cbits, FB = 1 << fb;
+  const int fshift = 2 * k - bbits;
+  const uint32_t nslices = slice_start[Cn];
+  while (true) {
+    __syncthreads();
+    if (tid == 0) {
+      s_slice = atomicAdd(ticket, 1u);
+      if (s_slice < nslices) {
+        int lo = 0, hi = Cn - 1;  // last g with slice_start[g] <= slice
+        while (lo < hi) {
+          int mid = (lo + hi + 1) >> 1;
+          if (slice_start[mid] <= s_slice) lo = mid; else hi = mid - 1;
+        }
+        s_g = lo;
+      }
+    }
+    for (int i = tid; i < FB; i += blockDim.x) { s_hist[i] = 0; s_fill[i] = 0; }
+    __syncthreads();
+    const uint32_t sl = s_slice;
+    if (sl >= nslices) break;
+    const uint32_t g = s_g;
+    const uint32_t r0 = cstart[g] + (sl - slice_start[g]) * FC::S;
+    const uint32_t r1 = min(r0 + (uint32_t)FC::S, cstart[g + 1]);
+    const uint32_t m = r1 - r0;
+    for (uint32_t i = tid; i < m; i += blockDim.x) {
+      const KeyT x = in[r0 + i];
+      const uint32_t f = (uint32_t)(x >> fshift) & (uint32_t)(FB - 1);
+      A[i] = x;
+      bin[i] = (uint16_t)f;
+      atomicAdd(&s_hist[f], 1u);
+    }
+    __syncthreads();
+    // local offsets and reserved global positions per fine bucket
+    uint32_t hv = tid < FB ? s_hist[tid] : 0;
+    uint32_t tot;
+    uint32_t ex = block_exclusive_sum(hv, s_warp, tot);
+    if (tid < FB) {
+      s_loff[tid] = ex;
+      s_goff[tid] = hv ? atomicAdd(&fcur[(g << fb) + tid], hv) : 0u;
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < m; i += blockDim.x) {
+      const uint32_t f = bin[i];
+      const uint32_t p = s_loff[f] + atomicAdd(&s_fill[f], 1u);
+      Bk[p] = A[i];
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < m; i += blockDim.x) {
+      const KeyT x = Bk[i];
+      const uint32_t f = (uint32_t)(x >> fshift) & (uint32_t)(FB - 1);
+      guarded_store(out, s_goff[f] + (i - s_loff[f]), x, cap, err);
+    }
+  }
+}
+
 // counts[c][b] -> exclusive prefix over chunks (in place); totals into bstart[b].
 __global__ void __launch_bounds__(256) k_col_prefix(uint32_t* counts, int grid, int B, uint32_t* totals) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -590,6 +876,42 @@ __device__ __forceinline__ bool hash_insert(KeyT* skey, uint32_t* scnt, uint32_t
     h = (h + 1) & hmask;
   }
   return false;
+}
+
+// Rows [base+acc, base+acc+u) of a bucket from the sorted on-chip run (sk, sc), plus the
+// per-bucket counts of rows by the next two key bits (s_d).
+template <typename KeyT>
+__device__ void write_bucket_rows(const KeyT* sk, const uint32_t* sc, uint32_t u, const BucketArgs& a,
+                                  uint32_t beta, int rem, uint32_t base, uint32_t acc,
+                                  KeyT* __restrict__ tkeys, uint32_t* s_d) {
+  const int tid = threadIdx.x, lane = tid & 31;
+  const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
+  uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
+  for (uint32_t i0 = 0; i0 < u; i0 += kBucketThreads) {
+    const uint32_t i = i0 + tid;
+    const bool v = i < u;
+    uint32_t d2 = 3;
+    if (v) {
+      const KeyT r = sk[i];
+      const uint32_t cnt = sc[i];
+      const unsigned long long row = (unsigned long long)base + acc + i;
+      if (row < a.cap) {
+        tkeys[row] = hi_bits | r;
+        a.tcounts[row] = cnt;
+      } else {
+        atomicOr(&a.sc->err, ERR_BOUNDS);
+      }
+      d2 = (uint32_t)(KeyOps<KeyT>::shr(r, rem - 2) & 3);
+    }
+    dl0 += __popc(__ballot_sync(FULLMASK, v && d2 == 0));
+    dl1 += __popc(__ballot_sync(FULLMASK, v && d2 == 1));
+    dl2 += __popc(__ballot_sync(FULLMASK, v && d2 == 2));
+  }
+  if (lane == 0) {
+    if (dl0) atomicAdd(&s_d[0], dl0);
+    if (dl1) atomicAdd(&s_d[1], dl1);
+    if (dl2) atomicAdd(&s_d[2], dl2);
+  }
 }
 
 // Per bucket: aggregate the bucket's keys into (remainder, count) in an on-chip
@@ -672,6 +994,106 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       __syncthreads();
       if (tid == 0) s_sp--;
       if (++attempts > kMaxBucketAttempts) { failed = true; break; }
+      const int psh = rem - plen;
+      // ---- fast path: order-preserving placement.  The home slot is the top bits of
+      // the remainder below the prefix, so (without wrap-around) every cluster of
+      // occupied slots holds keys whose homes lie inside it: sorting each cluster
+      // sorts the table.  Skewed sub-ranges (long probes or clusters) take the
+      // hashed path below.
+      {
+        const float uest = fmaxf(64.f, (float)n * s_ratio);
+        uint32_t M = 1024;
+        while ((float)M < 3.f * uest && M < (uint32_t)(H - kOvfSlots)) M <<= 1;
+        if (M > (uint32_t)(H - kOvfSlots)) M = H - kOvfSlots;
+        const uint32_t T = M + kOvfSlots;
+        for (uint32_t i = tid; i < T; i += kBucketThreads) {
+          skey[i] = EMPTY;
+          scnt[i] = 0;
+        }
+        if (tid == 0) s_ovf = 0;
+        __syncthreads();
+        const KeyT lmask = KeyOps<KeyT>::mask(psh);
+        for (uint32_t i = tid; i < n; i += kBucketThreads) {
+          const KeyT r = keys[base + i] & rmask;
+          if (plen != 0 && !(KeyOps<KeyT>::shr(r, psh) == pv)) continue;
+          const KeyT rl = r & lmask;
+          const uint32_t t32 = psh > 32 ? (uint32_t)KeyOps<KeyT>::shr(rl, psh - 32)
+                                        : (uint32_t)KeyOps<KeyT>::low32(rl) << (32 - psh);
+          const uint32_t home = (uint32_t)(((unsigned long long)t32 * M) >> 32);
+          uint32_t q = home;
+          bool placed = false;
+          while (q < T && q - home < (uint32_t)kProbeMax) {
+            const KeyT cur = *(volatile KeyT*)&skey[q];
+            if (cur == r) { atomicAdd(&scnt[q], 1u); placed = true; break; }
+            if (cur == EMPTY) {
+              const KeyT old = KeyOps<KeyT>::cas(&skey[q], EMPTY, r);
+              if (old == EMPTY || old == r) { atomicAdd(&scnt[q], 1u); placed = true; break; }
+            }
+            q++;
+          }
+          if (!placed) s_ovf = 1;
+        }
+        __syncthreads();
+        if (!s_ovf) {
+          // sort every cluster (a maximal run of occupied slots) by insertion
+          const uint32_t spt2 = (T + kBucketThreads - 1) / kBucketThreads;
+          for (uint32_t q0 = tid * spt2; q0 < min(T, (tid + 1) * spt2); q0++) {
+            if (skey[q0] == EMPTY || (q0 > 0 && skey[q0 - 1] != EMPTY)) continue;
+            uint32_t e = q0 + 1;
+            while (e < T && skey[e] != EMPTY) e++;
+            if (e - q0 > (uint32_t)kClusterMax) { s_ovf = 1; continue; }
+            for (uint32_t x = q0 + 1; x < e; x++) {
+              const KeyT kx = skey[x];
+              const uint32_t cx = scnt[x];
+              uint32_t y = x;
+              while (y > q0 && kx < skey[y - 1]) {
+                skey[y] = skey[y - 1];
+                scnt[y] = scnt[y - 1];
+                y--;
+              }
+              skey[y] = kx;
+              scnt[y] = cx;
+            }
+          }
+          __syncthreads();
+        }
+        if (!s_ovf) {
+          // order-preserving compaction into [0, u)
+          constexpr int SPT = H / kBucketThreads;
+          const uint32_t spt = (T + kBucketThreads - 1) / kBucketThreads;
+          KeyT rk[SPT];
+          uint32_t rc[SPT];
+          uint32_t occ = 0;
+#pragma unroll
+          for (int qq = 0; qq < SPT; qq++) {
+            rk[qq] = EMPTY;
+            rc[qq] = 0;
+            const uint32_t slot = tid * spt + qq;
+            if ((uint32_t)qq < spt && slot < T) {
+              rk[qq] = skey[slot];
+              rc[qq] = scnt[slot];
+              occ += rk[qq] != EMPTY;
+            }
+          }
+          uint32_t u;
+          uint32_t off = block_exclusive_sum(occ, s_warp, u);
+#pragma unroll
+          for (int qq = 0; qq < SPT; qq++) {
+            if (rk[qq] != EMPTY) {
+              skey[off] = rk[qq];
+              scnt[off] = rc[qq];
+              off++;
+            }
+          }
+          __syncthreads();
+          write_bucket_rows<KeyT>(skey, scnt, u, a, beta, rem, base, acc, tkeys, s_d);
+          acc += u;
+          __syncthreads();
+          continue;
+        }
+        __syncthreads();
+      }
+      // ---- hashed path (skewed sub-ranges)
       uint32_t Heff = (uint32_t)H;
       if (plen == 0) {
         Heff = 1024;
@@ -687,7 +1109,6 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       // --- hash aggregation of this sub-range (warp-aggregated inserts); OR/AND of
       //     the sub-range's remainders locate its first differing bit if it overflows
       KeyT kor = 0, kand = ~(KeyT)0;
-      const int psh = rem - plen;
       for (uint32_t i0 = (uint32_t)warp * 32; i0 < n; i0 += NW * 32) {
         const uint32_t i = i0 + lane;
         const bool valid = i < n;
@@ -827,34 +1248,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
         KeyT* tk = sk; sk = dk; dk = tk;
         uint32_t* tc = sc; sc = dc; dc = tc;
       }
-      // --- write this sub-range of the bucket's rows
-      const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
-      uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
-      for (uint32_t i0 = 0; i0 < u; i0 += kBucketThreads) {
-        const uint32_t i = i0 + tid;
-        const bool v = i < u;
-        uint32_t d2 = 3;
-        if (v) {
-          const KeyT r = sk[i];
-          const uint32_t cnt = sc[i];
-          const unsigned long long row = (unsigned long long)base + acc + i;
-          if (row < a.cap) {
-            tkeys[row] = hi_bits | r;
-            a.tcounts[row] = cnt;
-          } else {
-            atomicOr(&a.sc->err, ERR_BOUNDS);
-          }
-          d2 = (uint32_t)(KeyOps<KeyT>::shr(r, rem - 2) & 3);
-        }
-        dl0 += __popc(__ballot_sync(FULLMASK, v && d2 == 0));
-        dl1 += __popc(__ballot_sync(FULLMASK, v && d2 == 1));
-        dl2 += __popc(__ballot_sync(FULLMASK, v && d2 == 2));
-      }
-      if (lane == 0) {
-        if (dl0) atomicAdd(&s_d[0], dl0);
-        if (dl1) atomicAdd(&s_d[1], dl1);
-        if (dl2) atomicAdd(&s_d[2], dl2);
-      }
+      write_bucket_rows<KeyT>(sk, sc, u, a, beta, rem, base, acc, tkeys, s_d);
       acc += u;
       __syncthreads();
     }
@@ -1307,6 +1701,53 @@ static cudaError_t launch_extract_t(const CountArgs& a, KeyT* out, cudaStream_t 
 cudaError_t launch_bucket_count(const CountArgs& a, int wide, cudaStream_t st) {
   return wide ? launch_extract_t<u128, false>(a, nullptr, st)
               : launch_extract_t<uint64_t, false>(a, nullptr, st);
+}
+
+template <typename KeyT>
+static cudaError_t launch_coarse_t(const CountArgs& a, const uint32_t* coff, KeyT* out, cudaStream_t st) {
+  const size_t smem = CoarseCfg<KeyT>::smem;
+  cudaError_t e = cudaFuncSetAttribute(k_scatter_coarse<KeyT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_scatter_coarse<KeyT><<<a.grid, kExtractThreads, smem, st>>>(a, coff, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_coarse(const CountArgs& a, const uint32_t* coff, void* out, int wide,
+                                  cudaStream_t st) {
+  return wide ? launch_coarse_t<u128>(a, coff, reinterpret_cast<u128*>(out), st)
+              : launch_coarse_t<uint64_t>(a, coff, reinterpret_cast<uint64_t*>(out), st);
+}
+
+cudaError_t launch_coarse_offsets(const CountArgs& a, uint32_t* coff, uint32_t* cstart,
+                                  uint32_t* slice_start, int wide, cudaStream_t st) {
+  const int sk = wide ? FineCfg<u128>::S : FineCfg<uint64_t>::S;
+  k_coarse_offsets<<<a.grid, 256, 0, st>>>(a.counts, a.bstart, a.grid, a.bbits, a.cbits, coff, cstart,
+                                           slice_start, sk);
+  return cudaGetLastError();
+}
+
+template <typename KeyT>
+static cudaError_t launch_fine_t(const KeyT* in, const uint32_t* cstart, const uint32_t* slice_start,
+                                 uint32_t* fcur, KeyT* out, int k, int bbits, int cbits, uint32_t* ticket,
+                                 unsigned long long cap, uint32_t* err, cudaStream_t st) {
+  const size_t smem = FineCfg<KeyT>::smem;
+  cudaError_t e = cudaFuncSetAttribute(k_scatter_fine<KeyT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_scatter_fine<KeyT><<<sm_count() * 3, 512, smem, st>>>(in, cstart, slice_start, fcur, out, k, bbits,
+                                                         cbits, ticket, cap, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_fine(const void* in, const uint32_t* cstart, const uint32_t* slice_start,
+                                uint32_t* fcur, void* out, int k, int bbits, int cbits, int wide,
+                                uint32_t* ticket, unsigned long long cap, uint32_t* err, cudaStream_t st) {
+  return wide ? launch_fine_t<u128>(reinterpret_cast<const u128*>(in), cstart, slice_start, fcur,
+                                    reinterpret_cast<u128*>(out), k, bbits, cbits, ticket, cap, err, st)
+              : launch_fine_t<uint64_t>(reinterpret_cast<const uint64_t*>(in), cstart, slice_start, fcur,
+                                        reinterpret_cast<uint64_t*>(out), k, bbits, cbits, ticket, cap, err,
+                                        st);
 }
 
 cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st) {
