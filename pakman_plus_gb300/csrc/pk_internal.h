@@ -20,15 +20,14 @@ constexpr int kTileBytes = 65536;   // line-scan tile; chunk boundaries are mult
 constexpr int kExtractThreads = 512;
 constexpr int kSegBytes = 64;       // bytes per thread per extraction step
 constexpr int kBucketThreads = 512;
-constexpr int kMnThreads = 512;
-constexpr int kMnCap = 4096;        // items (k-mer records) per macro-node segment on chip
+constexpr int kMnThreads = 128;
+constexpr int kMnCap = 2048;        // items (k-mer records) per macro-node segment on chip
 constexpr int kHistSmem = 1024;     // count-histogram bins kept in shared memory
 constexpr int kBucketStack = 256;   // pending sub-ranges of one bucket (binary-trie split)
 constexpr int kMaxBucketAttempts = 1 << 16;  // sub-range attempts per bucket before giving up
 constexpr int kCoarseBits = 7;      // pass-1 partition digits (coarse regions)
-constexpr int kOvfSlots = 256;      // slots past the order-preserving table (no wrap-around)
-constexpr int kProbeMax = 64;       // longest probe of the order-preserving table
-constexpr int kClusterMax = 64;     // longest cluster sorted in place
+constexpr int kSortBinBits = 10;    // top remainder bits of the per-bucket counting sort
+constexpr int kBinMax = 128;        // largest bin sorted by ranking (else radix sort)
 
 struct Scalars {                    // device-side scalars of one job
   unsigned long long s0;            // index of the first '>' (F if none)

@@ -773,12 +773,24 @@ __global__ void __launch_bounds__(512) k_scatter_fine(const KeyT* __restrict__ i
     const uint32_t r0 = cstart[g] + (sl - slice_start[g]) * FC::S;
     const uint32_t r1 = min(r0 + (uint32_t)FC::S, cstart[g + 1]);
     const uint32_t m = r1 - r0;
-    for (uint32_t i = tid; i < m; i += blockDim.x) {
-      const KeyT x = in[r0 + i];
-      const uint32_t f = (uint32_t)(x >> fshift) & (uint32_t)(FB - 1);
-      A[i] = x;
-      bin[i] = (uint16_t)f;
-      atomicAdd(&s_hist[f], 1u);
+    {
+      constexpr int PT = FC::S / 512;  // keys per thread, all loads issued first
+      KeyT xs[PT];
+#pragma unroll
+      for (int q = 0; q < PT; q++) {
+        const uint32_t i = q * 512 + tid;
+        xs[q] = i < m ? in[r0 + i] : (KeyT)0;
+      }
+#pragma unroll
+      for (int q = 0; q < PT; q++) {
+        const uint32_t i = q * 512 + tid;
+        if (i < m) {
+          const uint32_t f = (uint32_t)(xs[q] >> fshift) & (uint32_t)(FB - 1);
+          A[i] = xs[q];
+          bin[i] = (uint16_t)f;
+          atomicAdd(&s_hist[f], 1u);
+        }
+      }
     }
     __syncthreads();
     // local offsets and reserved global positions per fine bucket
@@ -995,109 +1007,13 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       if (tid == 0) s_sp--;
       if (++attempts > kMaxBucketAttempts) { failed = true; break; }
       const int psh = rem - plen;
-      // ---- fast path: order-preserving placement.  The home slot is the top bits of
-      // the remainder below the prefix, so (without wrap-around) every cluster of
-      // occupied slots holds keys whose homes lie inside it: sorting each cluster
-      // sorts the table.  Skewed sub-ranges (long probes or clusters) take the
-      // hashed path below.
+      // table sized for the distinct keys expected (2.5x), at least 1024 slots; an
+      // overflow splits the sub-range
+      uint32_t Heff = 1024;
       {
-        const float uest = fmaxf(64.f, (float)n * s_ratio);
-        uint32_t M = 1024;
-        while ((float)M < 3.f * uest && M < (uint32_t)(H - kOvfSlots)) M <<= 1;
-        if (M > (uint32_t)(H - kOvfSlots)) M = H - kOvfSlots;
-        const uint32_t T = M + kOvfSlots;
-        for (uint32_t i = tid; i < T; i += kBucketThreads) {
-          skey[i] = EMPTY;
-          scnt[i] = 0;
-        }
-        if (tid == 0) s_ovf = 0;
-        __syncthreads();
-        const KeyT lmask = KeyOps<KeyT>::mask(psh);
-        for (uint32_t i = tid; i < n; i += kBucketThreads) {
-          const KeyT r = keys[base + i] & rmask;
-          if (plen != 0 && !(KeyOps<KeyT>::shr(r, psh) == pv)) continue;
-          const KeyT rl = r & lmask;
-          const uint32_t t32 = psh > 32 ? (uint32_t)KeyOps<KeyT>::shr(rl, psh - 32)
-                                        : (uint32_t)KeyOps<KeyT>::low32(rl) << (32 - psh);
-          const uint32_t home = (uint32_t)(((unsigned long long)t32 * M) >> 32);
-          uint32_t q = home;
-          bool placed = false;
-          while (q < T && q - home < (uint32_t)kProbeMax) {
-            const KeyT cur = *(volatile KeyT*)&skey[q];
-            if (cur == r) { atomicAdd(&scnt[q], 1u); placed = true; break; }
-            if (cur == EMPTY) {
-              const KeyT old = KeyOps<KeyT>::cas(&skey[q], EMPTY, r);
-              if (old == EMPTY || old == r) { atomicAdd(&scnt[q], 1u); placed = true; break; }
-            }
-            q++;
-          }
-          if (!placed) s_ovf = 1;
-        }
-        __syncthreads();
-        if (!s_ovf) {
-          // sort every cluster (a maximal run of occupied slots) by insertion
-          const uint32_t spt2 = (T + kBucketThreads - 1) / kBucketThreads;
-          for (uint32_t q0 = tid * spt2; q0 < min(T, (tid + 1) * spt2); q0++) {
-            if (skey[q0] == EMPTY || (q0 > 0 && skey[q0 - 1] != EMPTY)) continue;
-            uint32_t e = q0 + 1;
-            while (e < T && skey[e] != EMPTY) e++;
-            if (e - q0 > (uint32_t)kClusterMax) { s_ovf = 1; continue; }
-            for (uint32_t x = q0 + 1; x < e; x++) {
-              const KeyT kx = skey[x];
-              const uint32_t cx = scnt[x];
-              uint32_t y = x;
-              while (y > q0 && kx < skey[y - 1]) {
-                skey[y] = skey[y - 1];
-                scnt[y] = scnt[y - 1];
-                y--;
-              }
-              skey[y] = kx;
-              scnt[y] = cx;
-            }
-          }
-          __syncthreads();
-        }
-        if (!s_ovf) {
-          // order-preserving compaction into [0, u)
-          constexpr int SPT = H / kBucketThreads;
-          const uint32_t spt = (T + kBucketThreads - 1) / kBucketThreads;
-          KeyT rk[SPT];
-          uint32_t rc[SPT];
-          uint32_t occ = 0;
-#pragma unroll
-          for (int qq = 0; qq < SPT; qq++) {
-            rk[qq] = EMPTY;
-            rc[qq] = 0;
-            const uint32_t slot = tid * spt + qq;
-            if ((uint32_t)qq < spt && slot < T) {
-              rk[qq] = skey[slot];
-              rc[qq] = scnt[slot];
-              occ += rk[qq] != EMPTY;
-            }
-          }
-          uint32_t u;
-          uint32_t off = block_exclusive_sum(occ, s_warp, u);
-#pragma unroll
-          for (int qq = 0; qq < SPT; qq++) {
-            if (rk[qq] != EMPTY) {
-              skey[off] = rk[qq];
-              scnt[off] = rc[qq];
-              off++;
-            }
-          }
-          __syncthreads();
-          write_bucket_rows<KeyT>(skey, scnt, u, a, beta, rem, base, acc, tkeys, s_d);
-          acc += u;
-          __syncthreads();
-          continue;
-        }
-        __syncthreads();
-      }
-      // ---- hashed path (skewed sub-ranges)
-      uint32_t Heff = (uint32_t)H;
-      if (plen == 0) {
-        Heff = 1024;
-        while (Heff < 2 * n && Heff < (uint32_t)H) Heff <<= 1;
+        const float uest = (float)n * s_ratio * 2.5f;
+        while ((float)Heff < uest && Heff < (uint32_t)H) Heff <<= 1;
+        if (plen > 0) Heff = H;
       }
       const uint32_t hmask = Heff - 1;
       for (uint32_t i = tid; i < Heff; i += kBucketThreads) {
@@ -1109,18 +1025,22 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       // --- hash aggregation of this sub-range (warp-aggregated inserts); OR/AND of
       //     the sub-range's remainders locate its first differing bit if it overflows
       KeyT kor = 0, kand = ~(KeyT)0;
-      for (uint32_t i0 = (uint32_t)warp * 32; i0 < n; i0 += NW * 32) {
-        const uint32_t i = i0 + lane;
-        const bool valid = i < n;
-        KeyT r = valid ? (keys[base + i] & rmask) : (KeyT)0;
-        const bool mine = valid && (plen == 0 || KeyOps<KeyT>::shr(r, psh) == pv);
-        if (mine) { kor |= r; kand &= r; }
-        const unsigned m = __ballot_sync(FULLMASK, mine);
-        if (mine) {
-          const unsigned peers = KeyOps<KeyT>::match(m, r);
-          if (lane == __ffs(peers) - 1) {
-            if (!hash_insert<KeyT>(skey, scnt, hmask, r, (uint32_t)__popc(peers))) s_ovf = 1;
-          }
+      constexpr int PF = 4;  // keys loaded per thread before inserting (latency hiding)
+      for (uint32_t i0 = 0; i0 < n; i0 += PF * kBucketThreads) {
+        KeyT rr[PF];
+#pragma unroll
+        for (int q = 0; q < PF; q++) {
+          const uint32_t i = i0 + q * kBucketThreads + tid;
+          rr[q] = i < n ? (keys[base + i] & rmask) : EMPTY;
+        }
+#pragma unroll
+        for (int q = 0; q < PF; q++) {
+          const KeyT r = rr[q];
+          if (r == EMPTY) continue;
+          if (plen != 0 && !(KeyOps<KeyT>::shr(r, psh) == pv)) continue;
+          kor |= r;
+          kand &= r;
+          if (!hash_insert<KeyT>(skey, scnt, hmask, r, 1u)) s_ovf = 1;
         }
       }
       __syncthreads();
@@ -1175,78 +1095,143 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
         }
       }
       __syncthreads();
-      // --- stable LSD radix sort of the u distinct remainders, 8-bit digits
-      const int sort_bits = psh;
-      const int npass = (sort_bits + 7) / 8;
+      // --- sort the u distinct remainders: counting sort by their top bits below the
+      //     prefix, then each element's rank among its bin (bins hold one error
+      //     family of a k-mer, a few dozen keys); a bin above kBinMax falls back to
+      //     a stable LSD radix sort
       KeyT* sk = skey;
       uint32_t* sc = scnt;
-      KeyT* dk = skey + Heff / 2;
-      uint32_t* dc = scnt + Heff / 2;
-      const uint32_t E = (u + NW - 1) / NW;
-      const uint32_t e0 = (uint32_t)warp * E;
-      const uint32_t e1 = min(e0 + E, u);
-      for (int pass = 0; pass < npass; pass++) {
-        const int sh = 8 * pass;
-        for (int i = lane; i < 256; i += 32) wc[warp * 256 + i] = 0;
-        __syncwarp();
-        uint32_t dig[RMAX], offs[RMAX];
+      {
+        const int dbits = psh < kSortBinBits ? psh : kSortBinBits;
+        const uint32_t nbins = 1u << dbits;
+        const int dsh = psh - dbits;
+        uint32_t* bh = reinterpret_cast<uint32_t*>(wc);  // [nbins] counts -> offsets
+        uint32_t* bf = bh + (1u << kSortBinBits);        // [nbins] fill
+        for (uint32_t i = tid; i < nbins; i += kBucketThreads) { bh[i] = 0; bf[i] = 0; }
+        if (tid == 0) s_ovf = 0;
+        __syncthreads();
+        for (uint32_t i = tid; i < u; i += kBucketThreads)
+          atomicAdd(&bh[(uint32_t)KeyOps<KeyT>::shr(skey[i], dsh) & (nbins - 1)], 1u);
+        __syncthreads();
+        constexpr int BPT = (1 << kSortBinBits) / kBucketThreads;
+        uint32_t hv[BPT], hs = 0, hm = 0;
 #pragma unroll
-        for (int rr = 0; rr < RMAX; rr++) {
-          const uint32_t idx = e0 + rr * 32 + lane;
-          const bool v = idx < e1;
-          const uint32_t d = v ? (uint32_t)(KeyOps<KeyT>::shr(sk[idx], sh) & 0xff) : 0u;
-          const unsigned vm = __ballot_sync(FULLMASK, v);
-          uint32_t bse = 0;
-          unsigned peers = 0;
-          if (v) {
-            peers = __match_any_sync(vm, d);
-            if (lane == __ffs(peers) - 1) {
-              bse = wc[warp * 256 + d];
-              wc[warp * 256 + d] = (uint16_t)(bse + __popc(peers));
+        for (int q = 0; q < BPT; q++) {
+          const uint32_t bi = tid * BPT + q;
+          hv[q] = bi < nbins ? bh[bi] : 0u;
+          hs += hv[q];
+          hm = max(hm, hv[q]);
+        }
+        uint32_t tot;
+        uint32_t ex = block_exclusive_sum(hs, s_warp, tot);
+#pragma unroll
+        for (int q = 0; q < BPT; q++) {
+          const uint32_t bi = tid * BPT + q;
+          if (bi < nbins) bh[bi] = ex;
+          ex += hv[q];
+        }
+        if (hm > (uint32_t)kBinMax) s_ovf = 1;
+        __syncthreads();
+        KeyT* bk = skey + Heff / 2;
+        uint32_t* bc = scnt + Heff / 2;
+        for (uint32_t i = tid; i < u; i += kBucketThreads) {
+          const KeyT x = skey[i];
+          const uint32_t bi = (uint32_t)KeyOps<KeyT>::shr(x, dsh) & (nbins - 1);
+          const uint32_t pos = bh[bi] + atomicAdd(&bf[bi], 1u);
+          bk[pos] = x;
+          bc[pos] = scnt[i];
+        }
+        __syncthreads();
+        if (!s_ovf) {
+          for (uint32_t i = tid; i < u; i += kBucketThreads) {
+            const KeyT x = bk[i];
+            const uint32_t bi = (uint32_t)KeyOps<KeyT>::shr(x, dsh) & (nbins - 1);
+            const uint32_t b0 = bh[bi], b1 = b0 + bf[bi];
+            uint32_t rank = 0;
+            for (uint32_t j = b0; j < b1; j++) rank += bk[j] < x;
+            skey[b0 + rank] = x;
+            scnt[b0 + rank] = bc[i];
+          }
+          __syncthreads();
+        } else {
+          // stable LSD radix sort of the binned run (bins already in order)
+          sk = bk;
+          sc = bc;
+          KeyT* dk = skey;
+          uint32_t* dc = scnt;
+          const int npass = (psh + 7) / 8;
+          const uint32_t E = (u + NW - 1) / NW;
+          const uint32_t e0 = (uint32_t)warp * E;
+          const uint32_t e1 = min(e0 + E, u);
+          const uint32_t rounds = (E + 31) / 32;
+          for (int pass = 0; pass < npass; pass++) {
+            const int sh = 8 * pass;
+            __syncthreads();
+            for (int i = lane; i < 256; i += 32) wc[warp * 256 + i] = 0;
+            __syncwarp();
+            uint32_t dig[RMAX], offs[RMAX];
+#pragma unroll
+            for (int rr = 0; rr < RMAX; rr++) {
+              dig[rr] = 0;
+              offs[rr] = 0;
+              if ((uint32_t)rr >= rounds) continue;
+              const uint32_t idx = e0 + rr * 32 + lane;
+              const bool v = idx < e1;
+              const uint32_t d = v ? (uint32_t)(KeyOps<KeyT>::shr(sk[idx], sh) & 0xff) : 0u;
+              const unsigned vm = __ballot_sync(FULLMASK, v);
+              uint32_t bse = 0;
+              unsigned peers = 0;
+              if (v) {
+                peers = __match_any_sync(vm, d);
+                if (lane == __ffs(peers) - 1) {
+                  bse = wc[warp * 256 + d];
+                  wc[warp * 256 + d] = (uint16_t)(bse + __popc(peers));
+                }
+              }
+              __syncwarp();
+              const int leader = v ? __ffs(peers) - 1 : lane;
+              bse = __shfl_sync(FULLMASK, bse, leader);
+              dig[rr] = d;
+              offs[rr] = bse + __popc(peers & lanemask_lt());
             }
-          }
-          __syncwarp();
-          const int leader = v ? __ffs(peers) - 1 : lane;
-          bse = __shfl_sync(FULLMASK, bse, leader);
-          dig[rr] = d;
-          offs[rr] = bse + __popc(peers & lanemask_lt());
-        }
-        __syncthreads();
-        // exclusive scan over (digit, warp) in digit-major order
-        {
-          constexpr int PER = (256 * NW) / kBucketThreads;
-          uint32_t vals[PER];
-          uint32_t sum = 0;
+            __syncthreads();
+            {
+              constexpr int PER = (256 * NW) / kBucketThreads;
+              uint32_t vals[PER];
+              uint32_t sum = 0;
 #pragma unroll
-          for (int q = 0; q < PER; q++) {
-            const int e = tid * PER + q;  // e = d * NW + w
-            const int d = e / NW, w = e % NW;
-            vals[q] = wc[w * 256 + d];
-            sum += vals[q];
-          }
-          uint32_t tot;
-          uint32_t ex = block_exclusive_sum(sum, s_warp, tot);
+              for (int q = 0; q < PER; q++) {
+                const int e = tid * PER + q;  // e = d * NW + w
+                const int d = e / NW, w = e % NW;
+                vals[q] = wc[w * 256 + d];
+                sum += vals[q];
+              }
+              uint32_t tot2;
+              uint32_t ex2 = block_exclusive_sum(sum, s_warp, tot2);
 #pragma unroll
-          for (int q = 0; q < PER; q++) {
-            const int e = tid * PER + q;
-            const int d = e / NW, w = e % NW;
-            wc[w * 256 + d] = (uint16_t)ex;
-            ex += vals[q];
-          }
-        }
-        __syncthreads();
+              for (int q = 0; q < PER; q++) {
+                const int e = tid * PER + q;
+                const int d = e / NW, w = e % NW;
+                wc[w * 256 + d] = (uint16_t)ex2;
+                ex2 += vals[q];
+              }
+            }
+            __syncthreads();
 #pragma unroll
-        for (int rr = 0; rr < RMAX; rr++) {
-          const uint32_t idx = e0 + rr * 32 + lane;
-          if (idx < e1) {
-            const uint32_t pos = wc[warp * 256 + dig[rr]] + offs[rr];
-            dk[pos] = sk[idx];
-            dc[pos] = sc[idx];
+            for (int rr = 0; rr < RMAX; rr++) {
+              if ((uint32_t)rr >= rounds) continue;
+              const uint32_t idx = e0 + rr * 32 + lane;
+              if (idx < e1) {
+                const uint32_t pos = wc[warp * 256 + dig[rr]] + offs[rr];
+                dk[pos] = sk[idx];
+                dc[pos] = sc[idx];
+              }
+            }
+            __syncthreads();
+            KeyT* tk = sk; sk = dk; dk = tk;
+            uint32_t* tc = sc; sc = dc; dc = tc;
           }
         }
-        __syncthreads();
-        KeyT* tk = sk; sk = dk; dk = tk;
-        uint32_t* tc = sc; sc = dc; dc = tc;
       }
       write_bucket_rows<KeyT>(sk, sc, u, a, beta, rem, base, acc, tkeys, s_d);
       acc += u;
@@ -1394,50 +1379,39 @@ __device__ __forceinline__ uint32_t upper_bound_s(const KeyT* k, uint32_t lo, ui
 // < 1, 2, 3).  Warps scan 32-row steps with ballots; bucket offsets come from a
 // decoupled look-back (every bucket publishes its aggregate before waiting).
 template <typename KeyT>
-__global__ void __launch_bounds__(kMnThreads) k_filter_kept(FilterArgs a) {
-  __shared__ uint32_t s_warp[33];
-  __shared__ uint32_t s_beta, s_K, s_d[3];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  constexpr int NW = kMnThreads / 32;
+__global__ void __launch_bounds__(256) k_filter_kept(FilterArgs a) {
+  // one warp per table bucket: no block-wide barriers
+  const int lane = threadIdx.x & 31;
   const int B = 1 << a.bbits;
   const int rem = 2 * a.k - a.bbits;
   const uint32_t cut = a.sc->cutoff;
   const KeyT* __restrict__ tkeys = reinterpret_cast<const KeyT*>(a.tkeys);
   KeyT* __restrict__ kkeys = reinterpret_cast<KeyT*>(a.kkeys);
   while (true) {
-    __syncthreads();
-    if (tid == 0) s_beta = atomicAdd(&a.sc->ticket_filter, 1u);
-    if (tid < 3) s_d[tid] = 0;
-    __syncthreads();
-    const uint32_t beta = s_beta;
+    uint32_t beta = 0;
+    if (lane == 0) beta = atomicAdd(&a.sc->ticket_filter, 1u);
+    beta = __shfl_sync(FULLMASK, beta, 0);
     if (beta >= (uint32_t)B) break;
     const uint32_t r0 = a.bstart[beta], u = a.tu[beta];
-    const uint32_t per = ((u + NW - 1) / NW + 31) & ~31u;  // rows per warp, whole steps
-    const uint32_t w0 = min(u, warp * per), w1 = min(u, w0 + per);
-    uint32_t mine = 0;
-    for (uint32_t i0 = w0; i0 < w1; i0 += 32) {
+    uint32_t v = 0;
+    for (uint32_t i0 = 0; i0 < u; i0 += 32) {
       const uint32_t i = i0 + lane;
-      const bool keep = i < w1 && a.tcounts[r0 + i] >= cut;
-      mine += __popc(__ballot_sync(FULLMASK, keep));
+      v += __popc(__ballot_sync(FULLMASK, i < u && a.tcounts[r0 + i] >= cut));
     }
-    uint32_t v;
-    const uint32_t wex = block_exclusive_sum(lane == 0 ? mine : 0u, s_warp, v);
-    const uint32_t wbase = __shfl_sync(FULLMASK, wex, 0);
-    if (tid == 0) {
+    unsigned long long K = 0;
+    if (lane == 0) {
       st_release(&a.flags[beta], kLbAgg | (unsigned long long)v);
-      const unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
-      st_release(&a.flags[beta], kLbIncl | (ex + v));
-      s_K = (uint32_t)ex;
-      if (beta == (uint32_t)B - 1) a.sc->n_kept_rows = ex + v;
+      K = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
+      st_release(&a.flags[beta], kLbIncl | (K + v));
+      if (beta == (uint32_t)B - 1) a.sc->n_kept_rows = K + v;
     }
-    __syncthreads();
-    const uint32_t K = s_K;
-    uint32_t pos = K + wbase;
+    K = __shfl_sync(FULLMASK, K, 0);
+    uint32_t pos = (uint32_t)K;
     uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
-    for (uint32_t i0 = w0; i0 < w1; i0 += 32) {
+    for (uint32_t i0 = 0; i0 < u; i0 += 32) {
       const uint32_t i = i0 + lane;
-      const uint32_t c = i < w1 ? a.tcounts[r0 + i] : 0;
-      const bool keep = i < w1 && c >= cut;
+      const uint32_t c = i < u ? a.tcounts[r0 + i] : 0;
+      const bool keep = i < u && c >= cut;
       const unsigned bal = __ballot_sync(FULLMASK, keep);
       uint32_t d2 = 3;
       if (keep) {
@@ -1457,17 +1431,11 @@ __global__ void __launch_bounds__(kMnThreads) k_filter_kept(FilterArgs a) {
       pos += __popc(bal);
     }
     if (lane == 0) {
-      if (dl0) atomicAdd(&s_d[0], dl0);
-      if (dl1) atomicAdd(&s_d[1], dl1);
-      if (dl2) atomicAdd(&s_d[2], dl2);
-    }
-    __syncthreads();
-    if (tid == 0) {
-      a.kstart[beta] = K;
+      a.kstart[beta] = (uint32_t)K;
       a.kcount[beta] = v;
-      a.ksub[3 * beta + 0] = s_d[0];
-      a.ksub[3 * beta + 1] = s_d[0] + s_d[1];
-      a.ksub[3 * beta + 2] = s_d[0] + s_d[1] + s_d[2];
+      a.ksub[3 * beta + 0] = dl0;
+      a.ksub[3 * beta + 1] = dl0 + dl1;
+      a.ksub[3 * beta + 2] = dl0 + dl1 + dl2;
     }
   }
 }
@@ -1679,7 +1647,7 @@ size_t bucket_smem_bytes(int wide) {
 }
 size_t mn_smem_bytes(int wide) { return wide ? MnSmem<u128>::bytes : MnSmem<uint64_t>::bytes; }
 int bucket_ctas_per_sm(int) { return 2; }
-int mn_ctas_per_sm(int wide) { return wide ? 2 : 3; }
+int mn_ctas_per_sm(int wide) { return wide ? 4 : 6; }
 
 cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st) {
   const int ntiles = (int)((a.F + kTileBytes - 1) / kTileBytes);
@@ -1793,8 +1761,8 @@ cudaError_t launch_cutoff(const unsigned long long* hist, int t, Scalars* sc, cu
 
 template <typename KeyT>
 static cudaError_t launch_filter_t(const FilterArgs& a, int grid, cudaStream_t st) {
-  if (grid <= 0) grid = sm_count() * 4;
-  k_filter_kept<KeyT><<<grid, kMnThreads, 0, st>>>(a);
+  if (grid <= 0) grid = sm_count() * 8;
+  k_filter_kept<KeyT><<<grid, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
 
