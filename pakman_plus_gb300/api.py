@@ -210,16 +210,23 @@ class Job:
         check(capi.lib().pk_build_macro_nodes(self._h, min_count, byref(m)), "pk_build_macro_nodes")
         return m.value
 
-    def macro_nodes(self, coverage: Optional[int] = None) -> MacroNodeTable:
+    def macro_nodes(self, coverage: Optional[int] = None, out=None) -> MacroNodeTable:
+        """Copy the macro-node table to the host.  `out` = (keys, suffix, prefix) arrays
+        to fill (e.g. in pinned memory), each with room for at least n_nodes rows."""
         s = self.summary()
         m = s.n_nodes
-        keys = np.empty(m, key_dtype(self.params.k))
-        suf = np.empty((m, 4), np.uint32)
-        pre = np.empty((m, 4), np.uint32)
+        if out is None:
+            keys = np.empty(m, key_dtype(self.params.k))
+            suf = np.empty((m, 4), np.uint32)
+            pre = np.empty((m, 4), np.uint32)
+            cap = m
+        else:
+            keys, suf, pre = out
+            cap = min(keys.shape[0], suf.shape[0], pre.shape[0])
         check(capi.lib().pk_copy_macro_nodes(self._h, keys.ctypes.data, suf.ctypes.data,
-                                             pre.ctypes.data, m), "pk_copy_macro_nodes")
+                                             pre.ctypes.data, cap), "pk_copy_macro_nodes")
         cov = coverage if coverage is not None else self.params.coverage
-        return MacroNodeTable(keys, suf, pre, cov, self.params.k)
+        return MacroNodeTable(keys[:m], suf[:m], pre[:m], cov, self.params.k)
 
     # -- whole path
     def run(self, fasta, params: capi.PkParams) -> Summary:

@@ -276,7 +276,7 @@ struct UnitBits {
   uint32_t nn;     // bit j: byte j is 'N' or 'n'
 };
 
-__device__ __forceinline__ UnitBits decode_unit(const uint32_t w[4]) {
+__device__ __forceinline__ UnitBits decode_unit(const uint32_t w[4], bool want_n = true) {
   UnitBits u;
   u.codes = (pack4_codes(w[0]) << 24) | (pack4_codes(w[1]) << 16) | (pack4_codes(w[2]) << 8) |
             pack4_codes(w[3]);
@@ -284,10 +284,12 @@ __device__ __forceinline__ UnitBits decode_unit(const uint32_t w[4]) {
             pack4_nbits(w[3]);
   u.nl = flags4(__vcmpeq4(w[0], 0x0A0A0A0Au)) | (flags4(__vcmpeq4(w[1], 0x0A0A0A0Au)) << 4) |
          (flags4(__vcmpeq4(w[2], 0x0A0A0A0Au)) << 8) | (flags4(__vcmpeq4(w[3], 0x0A0A0A0Au)) << 12);
-  u.nn = flags4(__vcmpeq4(w[0] | 0x20202020u, 0x6E6E6E6Eu)) |
-         (flags4(__vcmpeq4(w[1] | 0x20202020u, 0x6E6E6E6Eu)) << 4) |
-         (flags4(__vcmpeq4(w[2] | 0x20202020u, 0x6E6E6E6Eu)) << 8) |
-         (flags4(__vcmpeq4(w[3] | 0x20202020u, 0x6E6E6E6Eu)) << 12);
+  u.nn = 0;
+  if (want_n)
+    u.nn = flags4(__vcmpeq4(w[0] | 0x20202020u, 0x6E6E6E6Eu)) |
+           (flags4(__vcmpeq4(w[1] | 0x20202020u, 0x6E6E6E6Eu)) << 4) |
+           (flags4(__vcmpeq4(w[2] | 0x20202020u, 0x6E6E6E6Eu)) << 8) |
+           (flags4(__vcmpeq4(w[3] | 0x20202020u, 0x6E6E6E6Eu)) << 12);
   return u;
 }
 
@@ -450,13 +452,13 @@ k_extract(CountArgs a, KeyT* __restrict__ keys_out) {
         if (p < 0) continue;
         uint32_t ww[4];
         load_unit(buf, F, (unsigned long long)p, ww);
-        roll_push(s, decode_unit(ww), drop_n);
+        roll_push(s, decode_unit(ww, drop_n), drop_n);
       }
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         const unsigned long long p = seg + 16ull * u;
         if (p >= c1) break;
-        const UnitBits ub = decode_unit(w[u]);
+        const UnitBits ub = decode_unit(w[u], drop_n);
         roll_push(s, ub, drop_n);
         // line parity per byte: exclusive prefix XOR of the newline bits
         uint32_t x = ub.nl;
@@ -645,7 +647,7 @@ k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restric
           if (p < 0) continue;
           uint32_t ww[4];
           load_unit(buf, F, (unsigned long long)p, ww);
-          roll_push(s, decode_unit(ww), drop_n);
+          roll_push(s, decode_unit(ww, drop_n), drop_n);
         }
       }
 #pragma unroll
@@ -655,7 +657,7 @@ k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restric
         uint32_t v = 0;
         bool all_clear = false;
         if (live) {
-          const UnitBits ub = decode_unit(w[u]);
+          const UnitBits ub = decode_unit(w[u], drop_n);
           roll_push(s, ub, drop_n);
           uint32_t x = ub.nl;
           x ^= x << 1; x ^= x << 2; x ^= x << 4; x ^= x << 8;
