@@ -144,6 +144,31 @@ pk_status pk_job_enable_timing(pk_job* job, int on);
 pk_status pk_job_stage_times(pk_job* job, float* ms, int capacity, int* n_stages);
 const char* pk_stage_name(int stage);
 
+/* ---- histogram cutoff that allocates nothing ---------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory at
+ * call time (an application whose own allocator owns every device allocation, a
+ * latency-critical loop where an allocation may block, a process whose device-memory
+ * budget is already committed): the histogram of counts < num_buckets, the first-
+ * minimum cutoff over [1, num_buckets) and the number of rows >= cutoff -- the same
+ * results as pk_cutoff -- over a count column already in device memory (for example the
+ * counts from pk_table_device).
+ *   d_counts  device array of n_rows row counts (read only)
+ *   d_cutoff  device output, 1 uint32 (required)
+ *   d_hist    device output, num_buckets uint64, or NULL
+ *   d_kept    device output, 1 uint64, or NULL
+ *   stream    cudaStream_t to run on (NULL = the legacy default stream)
+ * Scratch is one static device array of PK_NOALLOC_MAX_BUCKETS uint64 bins that every
+ * GPU loading this library holds until the process exits; num_buckets above that
+ * maximum returns PK_ERR_INVALID.  The function calls no cudaMalloc, cudaFree or other
+ * allocating routine.  Its first call on a device, made with that device current, looks
+ * up the scratch array's device address; make that first call before any stream
+ * capture.  All calls share the one array and each call clears it first: calls whose
+ * work overlaps on the GPU race and give wrong results.  Returns once the work is
+ * enqueued on `stream`. */
+#define PK_NOALLOC_MAX_BUCKETS 4096
+pk_status pk_cutoff_noalloc(const uint32_t* d_counts, uint64_t n_rows, int32_t num_buckets,
+                            uint32_t* d_cutoff, uint64_t* d_hist, uint64_t* d_kept, void* stream);
+
 /* Pinned host memory for fast transfers (cudaHostAlloc). */
 pk_status pk_host_alloc(uint64_t bytes, void** out);
 void pk_host_free(void* p);

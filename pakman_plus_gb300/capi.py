@@ -102,6 +102,8 @@ _SIGS = {
     "pk_job_enable_timing": (c_int, [c_void_p, c_int]),
     "pk_job_stage_times": (c_int, [c_void_p, POINTER(c_float), c_int, POINTER(c_int)]),
     "pk_stage_name": (c_char_p, [c_int]),
+    "pk_cutoff_noalloc": (c_int, [c_void_p, c_uint64, c_int32, c_void_p, c_void_p, c_void_p,
+                                  c_void_p]),
     "pk_host_alloc": (c_int, [c_uint64, POINTER(c_void_p)]),
     "pk_host_free": (None, [c_void_p]),
 }

@@ -28,6 +28,8 @@ static pk_status fail(pk_status s, const std::string& msg) {
   return s;
 }
 
+pk_status pk::set_error(pk_status s, const std::string& msg) { return fail(s, msg); }
+
 #define PK_CUDA(call)                                                                     \
   do {                                                                                    \
     cudaError_t e_ = (call);                                                              \

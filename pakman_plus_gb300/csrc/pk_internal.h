@@ -4,7 +4,14 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
+#include "../../include/pakman_gb300.h"
+
 namespace pk {
+
+// Records the calling thread's last-error text (pk_last_error) and returns s.
+pk_status set_error(pk_status s, const std::string& msg);
 
 // Device error word bits (pk_job error flag).
 enum : uint32_t {
