@@ -366,7 +366,10 @@ static pk_status check_params(const pk_params* p) {
 // The keys reach their buckets in two passes (kCoarseBits coarse regions, then fine
 // buckets inside each region), so the digit count is not tied to L2 capacity.
 static int auto_bucket_bits(uint64_t F, int k, int wide) {
-  const double per_bucket = wide ? 3000.0 : 5000.0;  // keys per bucket aimed at
+  // keys per bucket aimed at: large enough to amortise the per-bucket work of the
+  // table and macro-node kernels, small enough that a bucket's distinct keys usually
+  // fit one on-chip hash table (8192 64-bit or 4096 128-bit slots at load <= 1/2)
+  const double per_bucket = wide ? 3000.0 : 16000.0;
   const double est = 0.7 * (double)F;                // k-mer windows per byte, ~100 bp reads
   int b = 2;
   while (b < kMaxPartitionBits && est / (double)(1u << b) > per_bucket) b++;

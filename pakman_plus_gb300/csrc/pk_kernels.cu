@@ -725,28 +725,30 @@ __global__ void __launch_bounds__(256) k_coarse_offsets(const uint32_t* __restri
   }
 }
 
-// Pass 2 (k_scatter_fine): a slice of a coarse region (in chunk order) is counting-
-// sorted in shared memory by fine bucket; each fine run is written at a position
-// reserved with one atomic per (slice, fine bucket), so runs land contiguously.
+// Pass 2 (k_scatter_fine): a slice of a coarse region (in chunk order) is counted by
+// fine bucket in shared memory; one atomic per (slice, fine bucket) reserves a run in
+// the bucket's region and every key goes to its run at a shared-memory-atomic rank.
+// Keys stay in registers, so the CTA needs only three small tables and many CTAs fit
+// an SM to hide the load latency.
 template <typename KeyT>
 struct FineCfg {
-  static constexpr int S = sizeof(KeyT) == 8 ? 4096 : 2048;  // keys per slice
+  static constexpr int T = 512;                             // threads
+  static constexpr int PT = sizeof(KeyT) == 8 ? 16 : 8;      // keys per thread
+  static constexpr int S = T * PT;                          // keys per slice (64 KB)
   static constexpr int FBMAX = 1 << (15 - kCoarseBits);     // fine buckets per coarse
-  static constexpr size_t smem = 2 * sizeof(KeyT) * S + sizeof(uint16_t) * S;
+  static constexpr size_t smem = sizeof(KeyT) * S;
 };
 
 template <typename KeyT>
-__global__ void __launch_bounds__(512) k_scatter_fine(const KeyT* __restrict__ in,
-                                                     const uint32_t* __restrict__ cstart,
-                                                     const uint32_t* __restrict__ slice_start,
-                                                     uint32_t* fcur, KeyT* __restrict__ out,
-                                                     int k, int bbits, int cbits, uint32_t* ticket,
-                                                     unsigned long long cap, uint32_t* err) {
+__global__ void __launch_bounds__(512, 2) k_scatter_fine(const KeyT* __restrict__ in,
+                                                        const uint32_t* __restrict__ cstart,
+                                                        const uint32_t* __restrict__ slice_start,
+                                                        uint32_t* fcur, KeyT* __restrict__ out,
+                                                        int k, int bbits, int cbits, uint32_t* ticket,
+                                                        unsigned long long cap, uint32_t* err) {
   using FC = FineCfg<KeyT>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  KeyT* A = reinterpret_cast<KeyT*>(smem_raw);
-  KeyT* Bk = A + FC::S;
-  uint16_t* bin = reinterpret_cast<uint16_t*>(Bk + FC::S);
+  KeyT* stage = reinterpret_cast<KeyT*>(smem_raw);  // the slice grouped by fine bucket
   __shared__ uint32_t s_hist[FC::FBMAX], s_loff[FC::FBMAX], s_goff[FC::FBMAX], s_fill[FC::FBMAX];
   __shared__ uint32_t s_warp[33];
   __shared__ uint32_t s_slice, s_g;
@@ -767,7 +769,7 @@ __global__ void __launch_bounds__(512) k_scatter_fine(const KeyT* __restrict__ i
         s_g = lo;
       }
     }
-    for (int i = tid; i < FB; i += blockDim.x) { s_hist[i] = 0; s_fill[i] = 0; }
+    for (int i = tid; i < FB; i += FC::T) { s_hist[i] = 0; s_fill[i] = 0; }
     __syncthreads();
     const uint32_t sl = s_slice;
     if (sl >= nslices) break;
@@ -775,43 +777,40 @@ __global__ void __launch_bounds__(512) k_scatter_fine(const KeyT* __restrict__ i
     const uint32_t r0 = cstart[g] + (sl - slice_start[g]) * FC::S;
     const uint32_t r1 = min(r0 + (uint32_t)FC::S, cstart[g + 1]);
     const uint32_t m = r1 - r0;
+    KeyT xs[FC::PT];
+    uint32_t fs[FC::PT];
+#pragma unroll
+    for (int q = 0; q < FC::PT; q++) {
+      const uint32_t i = q * FC::T + tid;
+      xs[q] = i < m ? in[r0 + i] : (KeyT)0;
+    }
+#pragma unroll
+    for (int q = 0; q < FC::PT; q++) {
+      const uint32_t i = q * FC::T + tid;
+      fs[q] = (uint32_t)(xs[q] >> fshift) & (uint32_t)(FB - 1);
+      if (i < m) atomicAdd(&s_hist[fs[q]], 1u);
+    }
+    __syncthreads();
     {
-      constexpr int PT = FC::S / 512;  // keys per thread, all loads issued first
-      KeyT xs[PT];
-#pragma unroll
-      for (int q = 0; q < PT; q++) {
-        const uint32_t i = q * 512 + tid;
-        xs[q] = i < m ? in[r0 + i] : (KeyT)0;
-      }
-#pragma unroll
-      for (int q = 0; q < PT; q++) {
-        const uint32_t i = q * 512 + tid;
-        if (i < m) {
-          const uint32_t f = (uint32_t)(xs[q] >> fshift) & (uint32_t)(FB - 1);
-          A[i] = xs[q];
-          bin[i] = (uint16_t)f;
-          atomicAdd(&s_hist[f], 1u);
-        }
+      // FB <= FC::T: one fine bucket per thread
+      const uint32_t hv = tid < FB ? s_hist[tid] : 0u;
+      uint32_t tot;
+      const uint32_t ex = block_exclusive_sum(hv, s_warp, tot);
+      if (tid < FB) {
+        s_loff[tid] = ex;
+        s_goff[tid] = hv ? atomicAdd(&fcur[(g << fb) + tid], hv) : 0u;
       }
     }
     __syncthreads();
-    // local offsets and reserved global positions per fine bucket
-    uint32_t hv = tid < FB ? s_hist[tid] : 0;
-    uint32_t tot;
-    uint32_t ex = block_exclusive_sum(hv, s_warp, tot);
-    if (tid < FB) {
-      s_loff[tid] = ex;
-      s_goff[tid] = hv ? atomicAdd(&fcur[(g << fb) + tid], hv) : 0u;
+#pragma unroll
+    for (int q = 0; q < FC::PT; q++) {
+      const uint32_t i = q * FC::T + tid;
+      if (i < m) stage[s_loff[fs[q]] + atomicAdd(&s_fill[fs[q]], 1u)] = xs[q];
     }
     __syncthreads();
-    for (uint32_t i = tid; i < m; i += blockDim.x) {
-      const uint32_t f = bin[i];
-      const uint32_t p = s_loff[f] + atomicAdd(&s_fill[f], 1u);
-      Bk[p] = A[i];
-    }
-    __syncthreads();
-    for (uint32_t i = tid; i < m; i += blockDim.x) {
-      const KeyT x = Bk[i];
+    // runs of one fine bucket are contiguous in `stage` and in `out`: coalesced stores
+    for (uint32_t i = tid; i < m; i += FC::T) {
+      const KeyT x = stage[i];
       const uint32_t f = (uint32_t)(x >> fshift) & (uint32_t)(FB - 1);
       guarded_store(out, s_goff[f] + (i - s_loff[f]), x, cap, err);
     }
@@ -897,7 +896,7 @@ __device__ __forceinline__ bool hash_insert(KeyT* skey, uint32_t* scnt, uint32_t
 template <typename KeyT>
 __device__ void write_bucket_rows(const KeyT* sk, const uint32_t* sc, uint32_t u, const BucketArgs& a,
                                   uint32_t beta, int rem, uint32_t base, uint32_t acc,
-                                  KeyT* __restrict__ tkeys, uint32_t* s_d) {
+                                  KeyT* __restrict__ tkeys, uint32_t* s_d, uint32_t* shist) {
   const int tid = threadIdx.x, lane = tid & 31;
   const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
   uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
@@ -914,6 +913,10 @@ __device__ void write_bucket_rows(const KeyT* sk, const uint32_t* sc, uint32_t u
         a.tcounts[row] = cnt;
       } else {
         atomicOr(&a.sc->err, ERR_BOUNDS);
+      }
+      if (cnt < (uint32_t)a.t) {
+        if (cnt < (uint32_t)kHistSmem) atomicAdd(&shist[cnt], 1u);
+        else atomicAdd(&a.hist[cnt], 1ull);
       }
       d2 = (uint32_t)(KeyOps<KeyT>::shr(r, rem - 2) & 3);
     }
@@ -947,7 +950,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   uint16_t* wc = reinterpret_cast<uint16_t*>(smem + SM::off_wc);
   uint32_t* shist = reinterpret_cast<uint32_t*>(smem + SM::off_hist);
   __shared__ uint32_t s_warp[33];
-  __shared__ uint32_t s_beta, s_ovf, s_d[3], s_fail;
+  __shared__ uint32_t s_beta, s_ovf, s_d[3], s_fail, s_nb[2];
   __shared__ int s_sp;
   __shared__ KeyT s_stk_v[kBucketStack];
   __shared__ int s_stk_l[kBucketStack];
@@ -966,14 +969,28 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   if (tid == 0) s_ratio = 0.5f;  // running distinct/keys ratio of this CTA's buckets
   const int slog_max = rem < 7 ? rem : 7;  // initial split guess (<= 128 sub-ranges)
 
+  // the next bucket's ticket and extent are fetched while the current one is counted
+  uint32_t next_beta = 0, next_base = 0, next_end = 0;
+  if (tid == 0) {
+    next_beta = atomicAdd(&a.sc->ticket_bucket, 1u);
+    if (next_beta < (uint32_t)B) { next_base = a.bstart[next_beta]; next_end = a.bstart[next_beta + 1]; }
+  }
   while (true) {
     __syncthreads();
-    if (tid == 0) s_beta = atomicAdd(&a.sc->ticket_bucket, 1u);
+    if (tid == 0) {
+      s_beta = next_beta;
+      s_nb[0] = next_base;
+      s_nb[1] = next_end;
+      if (next_beta < (uint32_t)B) {
+        next_beta = atomicAdd(&a.sc->ticket_bucket, 1u);
+        if (next_beta < (uint32_t)B) { next_base = a.bstart[next_beta]; next_end = a.bstart[next_beta + 1]; }
+      }
+    }
     __syncthreads();
     const uint32_t beta = s_beta;
     if (beta >= (uint32_t)B) break;
-    const uint32_t base = a.bstart[beta];
-    const uint32_t n = a.bstart[beta + 1] - base;
+    const uint32_t base = s_nb[0];
+    const uint32_t n = s_nb[1] - base;
     if (tid == 0) s_fail = 0;
     if (n == 0) {
       if (tid == 0) {
@@ -1024,10 +1041,8 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       }
       if (tid == 0) s_ovf = 0;
       __syncthreads();
-      // --- hash aggregation of this sub-range (warp-aggregated inserts); OR/AND of
-      //     the sub-range's remainders locate its first differing bit if it overflows
-      KeyT kor = 0, kand = ~(KeyT)0;
-      constexpr int PF = 4;  // keys loaded per thread before inserting (latency hiding)
+      // --- hash aggregation of this sub-range
+      constexpr int PF = 4;  // keys loaded per thread before inserting
       for (uint32_t i0 = 0; i0 < n; i0 += PF * kBucketThreads) {
         KeyT rr[PF];
 #pragma unroll
@@ -1038,18 +1053,17 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
 #pragma unroll
         for (int q = 0; q < PF; q++) {
           const KeyT r = rr[q];
-          if (r == EMPTY) continue;
-          if (plen != 0 && !(KeyOps<KeyT>::shr(r, psh) == pv)) continue;
-          kor |= r;
-          kand &= r;
-          if (!hash_insert<KeyT>(skey, scnt, hmask, r, 1u)) s_ovf = 1;
+          const bool v = r != EMPTY && (plen == 0 || KeyOps<KeyT>::shr(r, psh) == pv);
+          if (v && !hash_insert<KeyT>(skey, scnt, hmask, r, 1u)) s_ovf = 1;
         }
       }
       __syncthreads();
       bool ovf = s_ovf != 0;
       // --- compaction of occupied slots into [0, u)
+      // order is irrelevant here (the run is sorted next), so slots are read with a
+      // stride of one block: conflict-free shared-memory access
       constexpr int SPT = H / kBucketThreads;
-      const uint32_t spt = Heff / kBucketThreads;  // >= 2 since Heff >= 1024
+      const uint32_t spt = Heff / kBucketThreads;
       KeyT rk[SPT];
       uint32_t rc[SPT];
       uint32_t occ = 0;
@@ -1058,8 +1072,8 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
         rk[q] = EMPTY;
         rc[q] = 0;
         if (!ovf && (uint32_t)q < spt) {
-          rk[q] = skey[tid * spt + q];
-          rc[q] = scnt[tid * spt + q];
+          rk[q] = skey[q * kBucketThreads + tid];
+          rc[q] = scnt[q * kBucketThreads + tid];
           occ += rk[q] != EMPTY;
         }
       }
@@ -1067,7 +1081,17 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       uint32_t off = block_exclusive_sum(occ, s_warp, u);
       if (u > Heff / 2) ovf = true;  // the sort needs a second half
       if (ovf) {
-        // split at the highest bit (below the prefix) where the sub-range's keys differ
+        // split at the highest bit (below the prefix) where the sub-range's keys
+        // differ: OR and AND of the sub-range's remainders (overflow is rare, so they
+        // are gathered here rather than during the inserts)
+        KeyT kor = 0, kand = ~(KeyT)0;
+        for (uint32_t i = tid; i < n; i += kBucketThreads) {
+          const KeyT r = keys[base + i] & rmask;
+          if (plen == 0 || KeyOps<KeyT>::shr(r, psh) == pv) {
+            kor |= r;
+            kand &= r;
+          }
+        }
         block_or_and<KeyT>(kor, kand, s_red_k);
         if (tid == 0) {
           const KeyT diff = (kor ^ kand) & KeyOps<KeyT>::mask(psh);
@@ -1235,7 +1259,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
           }
         }
       }
-      write_bucket_rows<KeyT>(sk, sc, u, a, beta, rem, base, acc, tkeys, s_d);
+      write_bucket_rows<KeyT>(sk, sc, u, a, beta, rem, base, acc, tkeys, s_d, shist);
       acc += u;
       __syncthreads();
     }
@@ -1244,14 +1268,6 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       acc = 0;
     }
     __syncthreads();
-    // the histogram is added only once the bucket's rows are final
-    for (uint32_t i = tid; i < acc; i += kBucketThreads) {
-      const uint32_t cnt = a.tcounts[base + i];
-      if (cnt < (uint32_t)a.t) {
-        if (cnt < (uint32_t)kHistSmem) atomicAdd(&shist[cnt], 1u);
-        else atomicAdd(&a.hist[cnt], 1ull);
-      }
-    }
     if (tid == 0) {
       a.tu[beta] = acc;
       a.tsub[3 * beta + 0] = s_d[0];
@@ -1478,7 +1494,7 @@ __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
   uint16_t* ord = reinterpret_cast<uint16_t*>(smem + SM::off_ord);
   uint16_t* nid = reinterpret_cast<uint16_t*>(smem + SM::off_nid);
   __shared__ uint32_t s_warp[33];
-  __shared__ uint32_t s_beta, s_off[6], s_cur[5], s_end[5], s_segend[5], s_last;
+  __shared__ uint32_t s_beta, s_off[6], s_cur[5], s_end[5], s_segend[5], s_beg[5], s_last;
   __shared__ unsigned long long s_NO;
 
   const int tid = threadIdx.x;
@@ -1508,127 +1524,143 @@ __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
         s_end[f + 1] = b0 + (d == 3 ? a.kcount[bp] : a.ksub[3 * bp + d]);
       }
     }
+    if (tid == 0)
+      for (int st = 0; st < 5; st++) s_beg[st] = s_cur[st];
     __syncthreads();
-    bool first = true;
-    bool multi = false;
-    unsigned long long NO = 0, done_nodes = 0;
-    while (true) {
-      // ---- choose this segment's rows: everything left, or rows up to a pivot key
-      if (tid == 0) {
-        uint32_t total = 0;
-        for (int st = 0; st < 5; st++) total += s_end[st] - s_cur[st];
-        KeyT piv = KINF;
-        if (total > CAP) {
-          const float frac = 0.9f * (float)CAP / (float)total;
-          for (int st = 0; st < 5; st++) {
-            const uint32_t take = (uint32_t)((float)(s_end[st] - s_cur[st]) * frac);
-            if (take >= 1) {
-              const KeyT kx = node_key(kk, s_cur[st] + take - 1, st, succ_mask);
-              if (kx < piv) piv = kx;
+    // A bucket that fits one segment is merged, counted and written in one pass.  A
+    // larger one is first merged to count its nodes (so its aggregate is published
+    // before any wait and later buckets do not queue behind it), then merged again
+    // and written.
+    bool counting = false;
+    unsigned long long NO = 0, total = 0;
+    for (int pass = 0; pass < 2; pass++) {
+      bool first = true;
+      unsigned long long done_nodes = 0;
+      while (true) {
+        // ---- choose this segment's rows: everything left, or rows up to a pivot key
+        if (tid == 0) {
+          uint32_t rows = 0;
+          for (int st = 0; st < 5; st++) rows += s_end[st] - s_cur[st];
+          KeyT piv = KINF;
+          if (rows > CAP) {
+            const float frac = 0.9f * (float)CAP / (float)rows;
+            for (int st = 0; st < 5; st++) {
+              const uint32_t take = (uint32_t)((float)(s_end[st] - s_cur[st]) * frac);
+              if (take >= 1) {
+                const KeyT kx = node_key(kk, s_cur[st] + take - 1, st, succ_mask);
+                if (kx < piv) piv = kx;
+              }
             }
           }
-        }
-        s_last = 1;
-        for (int st = 0; st < 5; st++) {
-          s_segend[st] = piv == KINF ? s_end[st]
-                                     : upper_bound_rows(kk, s_cur[st], s_end[st], st, succ_mask, piv);
-          if (s_segend[st] != s_end[st]) s_last = 0;
-        }
-        uint32_t o = 0;
-        for (int st = 0; st < 5; st++) {
-          s_off[st] = o;
-          o += s_segend[st] - s_cur[st];
-        }
-        s_off[5] = o;
-      }
-      __syncthreads();
-      const bool last = s_last != 0;
-      if (first && !last) multi = true;
-      uint32_t mm = s_off[5];
-      if (mm > (uint32_t)kMnCap) {  // cannot happen with CAP-sized segments
-        if (tid == 0) atomicOr(&a.sc->err, ERR_MN_CAPACITY);
-        mm = 0;
-      }
-      // ---- gather the five sorted runs
-      for (uint32_t i = tid; i < mm; i += kMnThreads) {
-        int st = 0;
-        while (i >= s_off[st + 1]) st++;
-        const uint32_t row = s_cur[st] + (i - s_off[st]);
-        const KeyT x = kk[row];
-        ikey[i] = st == 0 ? (x >> 2) : (x & succ_mask);
-        itag[i] = (uint8_t)(st == 0 ? (uint32_t)(x & 3) : (uint32_t)(3 + st));
-        icnt[i] = a.kcounts[row];
-      }
-      __syncthreads();
-      // ---- merge rank of every item across the five runs
-      for (uint32_t i = tid; i < mm; i += kMnThreads) {
-        int st = 0;
-        while (i >= s_off[st + 1]) st++;
-        const KeyT x = ikey[i];
-        uint32_t rank = i - s_off[st];
-        for (int b = 0; b < 5; b++) {
-          if (b == st) continue;
-          const uint32_t lo = s_off[b], hi = s_off[b + 1];
-          rank += (b < st ? upper_bound_s(ikey, lo, hi, x) : lower_bound_s(ikey, lo, hi, x)) - lo;
-        }
-        ord[rank] = (uint16_t)i;
-      }
-      __syncthreads();
-      // ---- node boundaries and node index per merged position
-      uint32_t nodes = 0;
-      for (uint32_t r0 = 0; r0 < mm; r0 += kMnThreads) {
-        const uint32_t r = r0 + tid;
-        uint32_t flag = 0;
-        if (r < mm) flag = (r == 0) || !(ikey[ord[r - 1]] == ikey[ord[r]]);
-        uint32_t tot;
-        const uint32_t ex = block_exclusive_sum(flag, s_warp, tot);
-        if (r < mm) nid[r] = (uint16_t)(nodes + ex + flag - 1);
-        nodes += tot;
-      }
-      // ---- node offset: decoupled look-back over node buckets
-      if (first) {
-        if (tid == 0) {
-          if (!multi) st_release(&a.flags[beta], kLbAgg | (unsigned long long)nodes);
-          const unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
-          if (!multi) st_release(&a.flags[beta], kLbIncl | (ex + nodes));
-          s_NO = ex;
+          s_last = 1;
+          for (int st = 0; st < 5; st++) {
+            s_segend[st] = piv == KINF ? s_end[st]
+                                       : upper_bound_rows(kk, s_cur[st], s_end[st], st, succ_mask, piv);
+            if (s_segend[st] != s_end[st]) s_last = 0;
+          }
+          uint32_t o = 0;
+          for (int st = 0; st < 5; st++) {
+            s_off[st] = o;
+            o += s_segend[st] - s_cur[st];
+          }
+          s_off[5] = o;
         }
         __syncthreads();
-        NO = s_NO;
-      }
-      const unsigned long long q0 = NO + done_nodes;
-      if (q0 + nodes <= a.cap) {
-        for (uint32_t r = tid; r < mm; r += kMnThreads) {
-          if (r == 0 || nid[r] != nid[r - 1]) {
-            const unsigned long long q = q0 + nid[r];
-            nkeys[q] = ikey[ord[r]];
-            reinterpret_cast<uint4*>(a.nsuf)[q] = make_uint4(0, 0, 0, 0);
-            reinterpret_cast<uint4*>(a.npre)[q] = make_uint4(0, 0, 0, 0);
+        const bool last = s_last != 0;
+        if (pass == 0 && first && !last) counting = true;
+        uint32_t mm = s_off[5];
+        if (mm > (uint32_t)kMnCap) {  // cannot happen with CAP-sized segments
+          if (tid == 0) atomicOr(&a.sc->err, ERR_MN_CAPACITY);
+          mm = 0;
+        }
+        // ---- gather the five sorted runs
+        for (uint32_t i = tid; i < mm; i += kMnThreads) {
+          int st = 0;
+          while (i >= s_off[st + 1]) st++;
+          const uint32_t row = s_cur[st] + (i - s_off[st]);
+          const KeyT x = kk[row];
+          ikey[i] = st == 0 ? (x >> 2) : (x & succ_mask);
+          itag[i] = (uint8_t)(st == 0 ? (uint32_t)(x & 3) : (uint32_t)(3 + st));
+          icnt[i] = a.kcounts[row];
+        }
+        __syncthreads();
+        // ---- merge rank of every item across the five runs
+        for (uint32_t i = tid; i < mm; i += kMnThreads) {
+          int st = 0;
+          while (i >= s_off[st + 1]) st++;
+          const KeyT x = ikey[i];
+          uint32_t rank = i - s_off[st];
+          for (int b = 0; b < 5; b++) {
+            if (b == st) continue;
+            const uint32_t lo = s_off[b], hi = s_off[b + 1];
+            rank += (b < st ? upper_bound_s(ikey, lo, hi, x) : lower_bound_s(ikey, lo, hi, x)) - lo;
+          }
+          ord[rank] = (uint16_t)i;
+        }
+        __syncthreads();
+        // ---- node boundaries and node index per merged position
+        uint32_t nodes = 0;
+        for (uint32_t r0 = 0; r0 < mm; r0 += kMnThreads) {
+          const uint32_t r = r0 + tid;
+          uint32_t flag = 0;
+          if (r < mm) flag = (r == 0) || !(ikey[ord[r - 1]] == ikey[ord[r]]);
+          uint32_t tot;
+          const uint32_t ex = block_exclusive_sum(flag, s_warp, tot);
+          if (r < mm) nid[r] = (uint16_t)(nodes + ex + flag - 1);
+          nodes += tot;
+        }
+        if (!counting) {
+          // ---- node offset: decoupled look-back over node buckets
+          if (first) {
+            if (tid == 0) {
+              const unsigned long long mine = pass == 0 ? nodes : total;
+              st_release(&a.flags[beta], kLbAgg | mine);
+              const unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
+              st_release(&a.flags[beta], kLbIncl | (ex + mine));
+              s_NO = ex;
+            }
+            __syncthreads();
+            NO = s_NO;
+          }
+          const unsigned long long q0 = NO + done_nodes;
+          if (q0 + nodes <= a.cap) {
+            for (uint32_t r = tid; r < mm; r += kMnThreads) {
+              if (r == 0 || nid[r] != nid[r - 1]) {
+                const unsigned long long q = q0 + nid[r];
+                nkeys[q] = ikey[ord[r]];
+                reinterpret_cast<uint4*>(a.nsuf)[q] = make_uint4(0, 0, 0, 0);
+                reinterpret_cast<uint4*>(a.npre)[q] = make_uint4(0, 0, 0, 0);
+              }
+            }
+            __syncthreads();
+            for (uint32_t r = tid; r < mm; r += kMnThreads) {
+              const uint32_t i = ord[r];
+              const unsigned long long q = q0 + nid[r];
+              const uint32_t tg = itag[i];
+              if (tg < 4) a.nsuf[4 * q + tg] = icnt[i];
+              else a.npre[4 * q + (tg - 4)] = icnt[i];
+            }
+          } else if (tid == 0) {
+            atomicOr(&a.sc->err, ERR_MN_CAPACITY);
           }
         }
+        done_nodes += nodes;
+        first = false;
         __syncthreads();
-        for (uint32_t r = tid; r < mm; r += kMnThreads) {
-          const uint32_t i = ord[r];
-          const unsigned long long q = q0 + nid[r];
-          const uint32_t tg = itag[i];
-          if (tg < 4) a.nsuf[4 * q + tg] = icnt[i];
-          else a.npre[4 * q + (tg - 4)] = icnt[i];
-        }
-      } else if (tid == 0) {
-        atomicOr(&a.sc->err, ERR_MN_CAPACITY);
+        if (tid == 0)
+          for (int st = 0; st < 5; st++) s_cur[st] = s_segend[st];
+        __syncthreads();
+        if (last) break;
       }
-      done_nodes += nodes;
-      first = false;
-      __syncthreads();
+      total = done_nodes;
+      if (!counting) break;
+      // counted: rewind and write
+      counting = false;
       if (tid == 0)
-        for (int st = 0; st < 5; st++) s_cur[st] = s_segend[st];
+        for (int st = 0; st < 5; st++) s_cur[st] = s_beg[st];
       __syncthreads();
-      if (last) break;
     }
-    if (tid == 0) {
-      if (multi) st_release(&a.flags[beta], kLbIncl | (NO + done_nodes));
-      if (beta == (uint32_t)B - 1) a.sc->n_nodes = NO + done_nodes;
-    }
+    if (tid == 0 && beta == (uint32_t)B - 1) a.sc->n_nodes = NO + total;
   }
 }
 
@@ -1702,11 +1734,11 @@ static cudaError_t launch_fine_t(const KeyT* in, const uint32_t* cstart, const u
                                  uint32_t* fcur, KeyT* out, int k, int bbits, int cbits, uint32_t* ticket,
                                  unsigned long long cap, uint32_t* err, cudaStream_t st) {
   const size_t smem = FineCfg<KeyT>::smem;
-  cudaError_t e = cudaFuncSetAttribute(k_scatter_fine<KeyT>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_scatter_fine<KeyT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
   if (e != cudaSuccess) return e;
-  k_scatter_fine<KeyT><<<sm_count() * 3, 512, smem, st>>>(in, cstart, slice_start, fcur, out, k, bbits,
-                                                         cbits, ticket, cap, err);
+  k_scatter_fine<KeyT><<<sm_count() * 2, FineCfg<KeyT>::T, smem, st>>>(in, cstart, slice_start, fcur, out,
+                                                                        k, bbits, cbits, ticket, cap, err);
   return cudaGetLastError();
 }
 
