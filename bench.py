@@ -43,9 +43,12 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["bacterial", "plain", "longk"], default="bacterial")
     ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--e2e-workers", type=int, default=2,
+                    help="jobs in flight in the end-to-end (serving API) measurement")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-windows", type=int, default=60_000_000)
+    ap.add_argument("--cpu-sample-windows", type=int, default=0,
+                    help="windows in the CPU baseline's sample (0: the whole read set)")
     ap.add_argument("--bucket-bits", type=int, default=0, help="partition digits (0 = automatic)")
     return ap.parse_args()
 
@@ -142,20 +145,32 @@ def pipeline_bytes(F, N, U, V, M, W):
     return F + 2 * N * W + 2 * U * (W + 4) + 4 * U + 4 * V * (W + 4) + M * (W + 32)
 
 
-def cpu_baseline(rs, sample_windows: int):
-    """Oracle port (single thread) on the first reads of the same workload."""
-    from oracle import pk_oracle as po
-    lines = rs.fasta.split(b"\n")
+def _cpu_sample(rs, sample_windows: int):
+    """The first reads of the workload holding about `sample_windows` windows (0: all)."""
+    if sample_windows <= 0:
+        return rs.fasta, rs.n_reads
     per_read = max(1, rs.read_len - rs.k + 1)
     reads = min(rs.n_reads, max(1, sample_windows // per_read))
-    sample = b"\n".join(lines[: 2 * reads]) + b"\n"
+    if reads >= rs.n_reads:
+        return rs.fasta, rs.n_reads
+    lines = rs.fasta.split(b"\n")
+    return b"\n".join(lines[: 2 * reads]) + b"\n", reads
+
+
+def cpu_baseline(rs, sample_windows: int):
+    """The oracle's multi-threaded restatement of the reference's owner-partitioned
+    counting (all host cores) plus cutoff and macro-nodes, on the same read set."""
+    from oracle import pk_oracle as po
+    sample, reads = _cpu_sample(rs, sample_windows)
+    threads = os.cpu_count() or 1
+    po.lib()
     t0 = time.perf_counter()
-    pipe = po.run(sample, rs.k, rs.t, rs.drop_n)
+    pipe = po.run(sample, rs.k, rs.t, rs.drop_n, threads=threads)
     dt = time.perf_counter() - t0
     n = pipe.table.n_windows
-    return {"value": n / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"first {reads} reads ({n} k-mer windows) of the same read set, "
-                      f"count + cutoff + macro-nodes, {dt:.2f} s"}
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reads} reads ({n} k-mer windows) of the same read set, count + cutoff + "
+                      f"macro-nodes, {dt:.2f} s on {threads} threads"}
 
 
 def run_reference_arm(args, rank, world):
@@ -163,16 +178,14 @@ def run_reference_arm(args, rank, world):
         return 0
     rs = workload(args.workload, args.scale)
     from oracle import pk_oracle as po
-    per_read = max(1, rs.read_len - rs.k + 1)
-    reads = min(rs.n_reads, max(1, args.cpu_sample_windows // per_read))
-    lines = rs.fasta.split(b"\n")
-    sample = b"\n".join(lines[: 2 * reads]) + b"\n"
+    sample, reads = _cpu_sample(rs, args.cpu_sample_windows)
     exe = po.build_reference(rs.k) if os.path.isdir(po.REFERENCE_TREE) else None
     if exe is None:
         exe_path = os.path.join(po.REF_OUT, f"pakman_ref_k{rs.k}")
         exe = exe_path if os.path.exists(exe_path) and os.access(exe_path, os.X_OK) else None
     kind = "reference" if exe else "port"
     threads = os.cpu_count() or 1
+    po.lib()
     times, n_windows = [], 0
     for step in range(args.warmup + args.steps):
         if kind == "reference":
@@ -182,14 +195,14 @@ def run_reference_arm(args, rank, world):
             n_windows = int(r.table_counts.sum())
         else:
             t0 = time.perf_counter()
-            pipe = po.run(sample, rs.k, rs.t, rs.drop_n)
+            pipe = po.run(sample, rs.k, rs.t, rs.drop_n, threads=threads)
             dt = time.perf_counter() - t0
             n_windows = pipe.table.n_windows
         if step >= args.warmup:
             times.append(dt)
     ms = 1000.0 * sum(times) / len(times)
     value = n_windows / (ms / 1000.0)
-    cores = threads if kind == "reference" else 1
+    cores = threads
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64" if rs.k <= 32 else "u128",
@@ -268,38 +281,62 @@ def main():
         ms_step = float(t.item())
     value = s.n_windows * world / (ms_step / 1000.0)
 
-    # end to end through the C ABI: pinned host FASTA in, macro-node table out
-    e2e = None
-    e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 10))
+    # end to end through the public API: pinned host FASTA in, macro-node table out,
+    # every step; requests go through the serving front end (pk_submit / pk_wait) with
+    # `e2e_workers` jobs in flight, so one job's copies overlap another's kernels
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(4, min(args.steps, 12))
+    depth = max(1, args.e2e_workers)
     pinned = torch.empty(F, dtype=torch.uint8, pin_memory=True)
     pinned.copy_(host)
     pin_np = pinned.numpy()
     W = 8 if rs.k <= 32 else 16
     cap = max(1, 2 * s.n_kept)
-    out_keys = torch.empty(cap * W, dtype=torch.uint8, pin_memory=True).numpy().view(
-        np.uint64 if W == 8 else pk.KEY128)
-    out_suf = torch.empty(cap * 16, dtype=torch.uint8, pin_memory=True).numpy().view(np.uint32).reshape(cap, 4)
-    out_pre = torch.empty(cap * 16, dtype=torch.uint8, pin_memory=True).numpy().view(np.uint32).reshape(cap, 4)
-    pinned_out = (out_keys, out_suf, out_pre)
+
+    def pinned_out():
+        keys = torch.empty(cap * W, dtype=torch.uint8, pin_memory=True).numpy().view(
+            np.uint64 if W == 8 else pk.KEY128)
+        suf = torch.empty(cap * 16, dtype=torch.uint8, pin_memory=True).numpy().view(np.uint32).reshape(cap, 4)
+        pre = torch.empty(cap * 16, dtype=torch.uint8, pin_memory=True).numpy().view(np.uint32).reshape(cap, 4)
+        return keys, suf, pre
+
+    outs = [pinned_out() for _ in range(depth)]
+    # one job, one request at a time (no overlap), for reference
     job.run(pin_np, params)
-    job.macro_nodes(out=pinned_out)
+    job.macro_nodes(out=outs[0])
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        job.run(pin_np, params)
+        job.macro_nodes(out=outs[0])
+    serial_ms = 1000.0 * (time.perf_counter() - t0) / 2
+    job.reset()
+    srv = pk.Server(ctx, workers=depth)
+    for tk in [srv.submit(pin_np, params, out=outs[i]) for i in range(depth)]:  # warm-up
+        srv.wait(tk)
+        srv.release(tk)
     if dist:
         dist.barrier()
+    tickets = []
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        se = job.run(pin_np, params)
-        mn = job.macro_nodes(out=pinned_out)
+    for i in range(e2e_steps):
+        if i >= depth:
+            srv.wait(tickets[i - depth])
+        tickets.append(srv.submit(pin_np, params, out=outs[i % depth]))
+    infos = [srv.wait(tk) for tk in tickets[-depth:]]
     t1 = time.perf_counter()
+    lat = sorted((srv.poll(tk).end_ns - srv.poll(tk).start_ns) / 1e6 for tk in tickets)
+    se = infos[-1].summary
+    srv.close()
     e2e_ms = 1000.0 * (t1 - t0) / e2e_steps
     if dist:
         t = torch.tensor([e2e_ms], device=f"cuda:{local}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
     e2e = {"value": se.n_windows * world / (e2e_ms / 1000.0), "unit": UNIT,
-           "h2d_bytes_per_step": F, "d2h_bytes_per_step": int(mn.keys.nbytes + mn.suffix_counts.nbytes
-                                                                + mn.prefix_counts.nbytes + 48),
-           "ms_per_step": e2e_ms, "steps": e2e_steps}
+           "h2d_bytes_per_step": F, "d2h_bytes_per_step": int(se.n_nodes * (W + 32) + 48),
+           "ms_per_step": e2e_ms, "steps": e2e_steps,
+           "mode": f"pk_submit/pk_wait, {depth} jobs in flight, pinned host buffers",
+           "job_ms_p50": lat[len(lat) // 2], "serial_ms_per_step": serial_ms}
 
     if rank == 0:
         peak, peak_kind = peaks()

@@ -176,6 +176,70 @@ void pk_host_free(void* p);
 /* Library version string. */
 const char* pk_version(void);
 
+/* ---- Serving: many independent count -> cutoff -> macro-node jobs on one GPU ----
+ *
+ * The submit / poll interface of the serving design (there is no reference
+ * counterpart: the reference runs one read set per MPI job).  A server owns
+ * `workers` job slots on one context, each with its own CUDA stream, so one job's
+ * host<->device copies and host synchronisations overlap other jobs' kernels.
+ * Admission: a request starts only when the estimate of its device footprint fits
+ * the context's free HBM budget (requests wait in FIFO order; the head of the queue
+ * is never overtaken); a job that still runs out of device memory is put back at the
+ * head of the queue and retried when another job has finished.  Results are
+ * bit-identical to a job run alone. */
+typedef struct pk_server pk_server;
+
+typedef struct pk_request {
+  const char* fasta;          /* host FASTA (pinned memory copies fastest); must stay
+                                 valid until the request has completed */
+  uint64_t fasta_bytes;
+  pk_params params;
+  /* Macro-node output, filled on completion.  Either caller buffers with room for
+   * mn_capacity rows (keys: 8 or 16 bytes per row, suffix / prefix: 4 uint32 per
+   * row; more nodes than that gives PK_ERR_LIMIT with n_nodes in the summary), or
+   * all three NULL: the server keeps the table in pinned host memory, read with
+   * pk_result_get(). */
+  void* mn_keys;
+  uint32_t* mn_suffix;
+  uint32_t* mn_prefix;
+  uint64_t mn_capacity;
+} pk_request;
+
+typedef struct pk_request_info {
+  pk_status status;           /* the job's own status (PK_OK, PK_ERR_FORMAT, ...) */
+  int32_t done;               /* 1 once the job has finished (ok or failed) */
+  pk_summary summary;
+  uint64_t submit_ns;         /* CLOCK_MONOTONIC timestamps */
+  uint64_t start_ns;
+  uint64_t end_ns;
+  uint32_t attempts;          /* > 1 when the job was re-queued after running out of HBM */
+  uint32_t reserved;
+} pk_request_info;
+
+typedef struct pk_server_stats {
+  uint64_t submitted, completed, failed, queued, running;
+  uint64_t admitted_bytes;       /* sum of the running jobs' footprint estimates */
+  uint64_t peak_admitted_bytes;
+  uint64_t requeued;             /* jobs re-queued after running out of HBM */
+} pk_server_stats;
+
+pk_status pk_server_create(pk_ctx* ctx, int32_t workers, pk_server** out);
+/* Waits for running jobs, drops queued ones, frees every result. */
+void pk_server_destroy(pk_server* s);
+pk_status pk_submit(pk_server* s, const pk_request* req, uint64_t* ticket);
+/* Non-blocking: fills *info (info->done == 0 while queued or running). */
+pk_status pk_poll(pk_server* s, uint64_t ticket, pk_request_info* info);
+/* Blocks until the job is done or timeout_ms (< 0: no limit) passes; PK_ERR_BUSY on timeout. */
+pk_status pk_wait(pk_server* s, uint64_t ticket, int64_t timeout_ms, pk_request_info* info);
+/* Server-kept macro-node table of a finished request (valid until pk_result_release). */
+pk_status pk_result_get(pk_server* s, uint64_t ticket, const void** keys, const uint32_t** suffix,
+                        const uint32_t** prefix, uint64_t* n_nodes);
+/* Forgets a finished request and frees what the server kept for it. */
+pk_status pk_result_release(pk_server* s, uint64_t ticket);
+pk_status pk_server_get_stats(pk_server* s, pk_server_stats* out);
+/* Device footprint the admission control assumes for a request (bytes). */
+uint64_t pk_request_footprint(const pk_request* req);
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,6 +41,7 @@
  *    u32 counts per side indexed by ext, 0 meaning absent.
  *  - visit value (:75-79) = ceil(count / coverage), exact in integers.
  */
+#include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -217,6 +218,225 @@ int pko_count(const uint8_t* buf, size_t n, int k, int drop_n, pko_key** keys_ou
   *keys_out = keys;
   *counts_out = cnts;
   *n_unique = u;
+  return PKO_OK;
+}
+
+/*
+ * Multi-threaded counting with the reference's distributed structure on threads
+ * instead of MPI ranks: each thread walks a contiguous run of whole records
+ * (DivideReads, src/input_reading.cpp:69-243), its k-mers are routed to an owner
+ * by key range (the exchange of transfer_kmers, src/kmer_counting.cpp:254-352),
+ * and each owner sorts and run-length aggregates what it received
+ * (SortAndAggregate, :169-250).  Owners hold disjoint, ordered key ranges, so their
+ * tables concatenate into the same sorted unique table as pko_count.  Valid input
+ * only: record boundaries are found by "\n>"; a malformed record is reported by
+ * the serial pko_count.
+ */
+typedef struct {
+  const uint8_t* buf;
+  size_t begin, end;
+  int k, drop_n, wide, pbits, nparts;
+  collect_t c;
+  size_t reads;
+  size_t* part_n;    /* [nparts] keys per owner range */
+  void* routed;      /* keys grouped by owner range */
+  size_t* part_off;  /* [nparts + 1] */
+  int rc;
+} mt_walker;
+
+typedef struct {
+  mt_walker* w;
+  int nthreads, nparts, wide;
+  int next_part; /* shared work counter */
+  pthread_mutex_t mu;
+  pko_key** out_keys;   /* [nparts] */
+  uint32_t** out_cnts;  /* [nparts] */
+  size_t* out_u;        /* [nparts] */
+  size_t* out_n;        /* [nparts] */
+  int rc;
+} mt_job;
+
+static inline int part_of(u128 key, int k, int pbits) {
+  return (int)(key >> (2 * k - pbits));
+}
+
+static void* mt_walk(void* arg) {
+  mt_walker* w = (mt_walker*)arg;
+  memset(&w->c, 0, sizeof(w->c));
+  w->c.wide = w->wide;
+  w->rc = walk_kmers(w->buf + w->begin, w->end - w->begin, w->k, w->drop_n, collect_emit, &w->c,
+                     &w->reads);
+  if (w->c.oom) w->rc = PKO_ENOMEM;
+  if (w->rc != PKO_OK) return NULL;
+  /* route to owner ranges (counting pass, then a stable scatter) */
+  w->part_n = (size_t*)calloc((size_t)w->nparts, sizeof(size_t));
+  w->part_off = (size_t*)calloc((size_t)w->nparts + 1, sizeof(size_t));
+  const size_t esz = w->wide ? sizeof(rec_t) : sizeof(uint64_t);
+  w->routed = malloc((w->c.n ? w->c.n : 1) * esz);
+  if (!w->part_n || !w->part_off || !w->routed) { w->rc = PKO_ENOMEM; return NULL; }
+  for (size_t i = 0; i < w->c.n; i++) {
+    u128 key = w->wide ? w->c.k128[i].key : (u128)w->c.k64[i];
+    w->part_n[part_of(key, w->k, w->pbits)]++;
+  }
+  size_t acc = 0;
+  for (int p = 0; p < w->nparts; p++) { w->part_off[p] = acc; acc += w->part_n[p]; }
+  w->part_off[w->nparts] = acc;
+  size_t* fill = (size_t*)calloc((size_t)w->nparts, sizeof(size_t));
+  if (!fill) { w->rc = PKO_ENOMEM; return NULL; }
+  for (size_t i = 0; i < w->c.n; i++) {
+    u128 key = w->wide ? w->c.k128[i].key : (u128)w->c.k64[i];
+    int p = part_of(key, w->k, w->pbits);
+    size_t d = w->part_off[p] + fill[p]++;
+    if (w->wide) ((rec_t*)w->routed)[d] = w->c.k128[i];
+    else ((uint64_t*)w->routed)[d] = w->c.k64[i];
+  }
+  free(fill);
+  free(w->c.k64);
+  free(w->c.k128);
+  w->c.k64 = NULL;
+  w->c.k128 = NULL;
+  return NULL;
+}
+
+static void* mt_owner(void* arg) {
+  mt_job* J = (mt_job*)arg;
+  const size_t esz = J->wide ? sizeof(rec_t) : sizeof(uint64_t);
+  while (1) {
+    pthread_mutex_lock(&J->mu);
+    int p = J->next_part++;
+    pthread_mutex_unlock(&J->mu);
+    if (p >= J->nparts) break;
+    size_t n = 0;
+    for (int t = 0; t < J->nthreads; t++) n += J->w[t].part_n[p];
+    unsigned char* a = (unsigned char*)malloc((n ? n : 1) * esz);
+    pko_key* keys = (pko_key*)malloc((n ? n : 1) * sizeof(pko_key));
+    uint32_t* cnts = (uint32_t*)malloc((n ? n : 1) * sizeof(uint32_t));
+    if (!a || !keys || !cnts) {
+      free(a); free(keys); free(cnts);
+      J->rc = PKO_ENOMEM;
+      continue;
+    }
+    size_t o = 0;
+    for (int t = 0; t < J->nthreads; t++) {
+      memcpy(a + o * esz, (unsigned char*)J->w[t].routed + J->w[t].part_off[p] * esz, J->w[t].part_n[p] * esz);
+      o += J->w[t].part_n[p];
+    }
+    int k = J->w[0].k;
+    int rc = J->wide ? radix_sort_recs((rec_t*)a, n, 2 * k) : radix_sort_u64((uint64_t*)a, n, 2 * k);
+    if (rc != PKO_OK) J->rc = rc;
+    size_t u = 0;
+    for (size_t i = 0; i < n;) {
+      u128 key = J->wide ? ((rec_t*)a)[i].key : (u128)((uint64_t*)a)[i];
+      size_t j = i + 1;
+      while (j < n && (J->wide ? ((rec_t*)a)[j].key : (u128)((uint64_t*)a)[j]) == key) j++;
+      keys[u].lo = (uint64_t)key;
+      keys[u].hi = (uint64_t)(key >> 64);
+      cnts[u] = (uint32_t)(j - i);
+      u++;
+      i = j;
+    }
+    free(a);
+    J->out_keys[p] = keys;
+    J->out_cnts[p] = cnts;
+    J->out_u[p] = u;
+    J->out_n[p] = n;
+  }
+  return NULL;
+}
+
+int pko_count_mt(const uint8_t* buf, size_t n, int k, int drop_n, int threads, pko_key** keys_out,
+                 uint32_t** counts_out, size_t* n_unique, size_t* n_windows, size_t* n_reads) {
+  if (k < 2 || k > 64 || threads < 1) return PKO_EARG;
+  if (threads > 256) threads = 256;
+  int pbits = 0;
+  while ((1 << pbits) < 8 * threads && pbits < 2 * k && pbits < 16) pbits++;
+  const int nparts = 1 << pbits;
+  size_t first = 0;
+  while (first < n && buf[first] != '>') first++;
+  /* chunk starts: whole records ("\n>") */
+  size_t* st = (size_t*)malloc(((size_t)threads + 1) * sizeof(size_t));
+  mt_walker* w = (mt_walker*)calloc((size_t)threads, sizeof(mt_walker));
+  pthread_t* th = (pthread_t*)malloc((size_t)threads * sizeof(pthread_t));
+  if (!st || !w || !th) { free(st); free(w); free(th); return PKO_ENOMEM; }
+  st[0] = first;
+  for (int t = 1; t < threads; t++) {
+    size_t p = first + (n - first) / (size_t)threads * (size_t)t;
+    if (p < st[t - 1]) p = st[t - 1];
+    while (p < n && !(buf[p] == '>' && p > 0 && buf[p - 1] == '\n')) p++;
+    st[t] = p;
+  }
+  st[threads] = n;
+  for (int t = 0; t < threads; t++) {
+    w[t].buf = buf;
+    w[t].begin = st[t];
+    w[t].end = st[t + 1];
+    w[t].k = k;
+    w[t].drop_n = drop_n;
+    w[t].wide = k > 32;
+    w[t].pbits = pbits;
+    w[t].nparts = nparts;
+    pthread_create(&th[t], NULL, mt_walk, &w[t]);
+  }
+  int rc = PKO_OK;
+  size_t reads = 0;
+  for (int t = 0; t < threads; t++) {
+    pthread_join(th[t], NULL);
+    if (w[t].rc != PKO_OK) rc = w[t].rc;
+    reads += w[t].reads;
+  }
+  mt_job J;
+  memset(&J, 0, sizeof(J));
+  J.w = w;
+  J.nthreads = threads;
+  J.nparts = nparts;
+  J.wide = k > 32;
+  pthread_mutex_init(&J.mu, NULL);
+  J.out_keys = (pko_key**)calloc((size_t)nparts, sizeof(pko_key*));
+  J.out_cnts = (uint32_t**)calloc((size_t)nparts, sizeof(uint32_t*));
+  J.out_u = (size_t*)calloc((size_t)nparts, sizeof(size_t));
+  J.out_n = (size_t*)calloc((size_t)nparts, sizeof(size_t));
+  if (!J.out_keys || !J.out_cnts || !J.out_u || !J.out_n) rc = PKO_ENOMEM;
+  if (rc == PKO_OK) {
+    for (int t = 0; t < threads; t++) pthread_create(&th[t], NULL, mt_owner, &J);
+    for (int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+    rc = J.rc;
+  }
+  size_t u = 0, nw = 0;
+  if (rc == PKO_OK)
+    for (int p = 0; p < nparts; p++) { u += J.out_u[p]; nw += J.out_n[p]; }
+  pko_key* keys = NULL;
+  uint32_t* cnts = NULL;
+  if (rc == PKO_OK) {
+    keys = (pko_key*)malloc((u ? u : 1) * sizeof(pko_key));
+    cnts = (uint32_t*)malloc((u ? u : 1) * sizeof(uint32_t));
+    if (!keys || !cnts) rc = PKO_ENOMEM;
+  }
+  size_t o = 0;
+  for (int p = 0; p < nparts; p++) {
+    if (rc == PKO_OK && J.out_u[p]) {
+      memcpy(keys + o, J.out_keys[p], J.out_u[p] * sizeof(pko_key));
+      memcpy(cnts + o, J.out_cnts[p], J.out_u[p] * sizeof(uint32_t));
+      o += J.out_u[p];
+    }
+    if (J.out_keys) free(J.out_keys[p]);
+    if (J.out_cnts) free(J.out_cnts[p]);
+  }
+  for (int t = 0; t < threads; t++) {
+    free(w[t].part_n);
+    free(w[t].part_off);
+    free(w[t].routed);
+    free(w[t].c.k64);
+    free(w[t].c.k128);
+  }
+  free(J.out_keys); free(J.out_cnts); free(J.out_u); free(J.out_n);
+  pthread_mutex_destroy(&J.mu);
+  free(st); free(w); free(th);
+  if (rc != PKO_OK) { free(keys); free(cnts); return rc; }
+  *keys_out = keys;
+  *counts_out = cnts;
+  *n_unique = u;
+  *n_windows = nw;
+  if (n_reads) *n_reads = reads;
   return PKO_OK;
 }
 

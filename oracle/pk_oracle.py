@@ -43,7 +43,7 @@ def build(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
         tmp = LIB + ".tmp"
-        subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-shared", "-fPIC", "-o", tmp, src])
+        subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-pthread", "-shared", "-fPIC", "-o", tmp, src])
         os.replace(tmp, LIB)
     return LIB
 
@@ -72,6 +72,9 @@ def lib():
         L.pko_count.argtypes = [vp, sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp),
                                 ctypes.POINTER(vp), ctypes.POINTER(sz), ctypes.POINTER(sz),
                                 ctypes.POINTER(sz)]
+        L.pko_count_mt.argtypes = [vp, sz, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp),
+                                   ctypes.POINTER(vp), ctypes.POINTER(sz), ctypes.POINTER(sz),
+                                   ctypes.POINTER(sz)]
         L.pko_count_windows.argtypes = [vp, sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(sz),
                                         ctypes.POINTER(sz)]
         L.pko_cutoff.argtypes = [vp, sz, ctypes.c_int, vp, ctypes.POINTER(ctypes.c_int)]
@@ -93,7 +96,7 @@ def _take(ptr: int, count: int, dtype) -> np.ndarray:
         return np.empty(0, dtype=dtype)
     nbytes = count * np.dtype(dtype).itemsize
     buf = (ctypes.c_char * nbytes).from_address(ptr)
-    out = np.frombuffer(bytes(buf), dtype=dtype).copy()
+    out = np.frombuffer(buf, dtype=dtype).copy()
     L.pko_free(ptr)
     return out
 
@@ -117,13 +120,19 @@ class MacroNodes:
     n_kept: int
 
 
-def count(fasta: bytes, k: int, drop_n: bool = False) -> Table:
+def count(fasta: bytes, k: int, drop_n: bool = False, threads: int = 1) -> Table:
+    """Sorted unique (k-mer, count) table.  threads > 1 uses the owner-partitioned
+    multi-threaded restatement (valid input only; same table)."""
     L = lib()
-    buf = ctypes.create_string_buffer(fasta, len(fasta))
+    arr = np.frombuffer(fasta, dtype=np.uint8)
     kp, cp = ctypes.c_void_p(), ctypes.c_void_p()
     u, w, r = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
-    rc = L.pko_count(ctypes.addressof(buf), len(fasta), k, int(drop_n), ctypes.byref(kp),
-                     ctypes.byref(cp), ctypes.byref(u), ctypes.byref(w), ctypes.byref(r))
+    if threads > 1:
+        rc = L.pko_count_mt(arr.ctypes.data, arr.size, k, int(drop_n), int(threads), ctypes.byref(kp),
+                            ctypes.byref(cp), ctypes.byref(u), ctypes.byref(w), ctypes.byref(r))
+    else:
+        rc = L.pko_count(arr.ctypes.data, arr.size, k, int(drop_n), ctypes.byref(kp),
+                         ctypes.byref(cp), ctypes.byref(u), ctypes.byref(w), ctypes.byref(r))
     if rc != PKO_OK:
         raise OracleError(rc, "pko_count")
     keys = _take(kp.value, u.value, KEY_DTYPE)
@@ -180,9 +189,9 @@ class Pipeline:
     mn: Optional[MacroNodes]
 
 
-def run(fasta: bytes, k: int, t: int = 21, drop_n: bool = False) -> Pipeline:
+def run(fasta: bytes, k: int, t: int = 21, drop_n: bool = False, threads: int = 1) -> Pipeline:
     """Whole path: table, histogram/cutoff, macro-nodes (None if nothing is kept)."""
-    tab = count(fasta, k, drop_n)
+    tab = count(fasta, k, drop_n, threads)
     hist, cut = cutoff(tab.counts, t)
     try:
         mn = macro_nodes(tab, k, cut)

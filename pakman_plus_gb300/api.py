@@ -343,3 +343,125 @@ class PakmanSession:
 
     def close(self):
         self.job.close()
+
+
+@dataclass
+class RequestInfo:
+    """State of one served request (times are CLOCK_MONOTONIC nanoseconds)."""
+    ticket: int
+    status: int
+    done: bool
+    summary: Summary
+    submit_ns: int
+    start_ns: int
+    end_ns: int
+    attempts: int
+
+    @property
+    def latency_ms(self) -> float:
+        return (self.end_ns - self.submit_ns) / 1e6
+
+    @property
+    def queue_ms(self) -> float:
+        return (self.start_ns - self.submit_ns) / 1e6
+
+
+class Server:
+    """Serving front end over ``pk_submit`` / ``pk_poll``: independent read sets run
+    by ``workers`` job slots with continuous batching and HBM-budget admission (the
+    context's budget).  Each request's result equals that of the same read set run
+    alone in a :class:`Job`."""
+
+    def __init__(self, ctx: Context, workers: int = 2):
+        self.ctx = ctx
+        h = c_void_p()
+        check(capi.lib().pk_server_create(ctx.handle, workers, byref(h)), "pk_server_create")
+        self._h = h
+        self._live: Dict[int, tuple] = {}  # ticket -> (input buffer, out arrays, params)
+
+    def submit(self, fasta, params: capi.PkParams, out=None) -> int:
+        """Queue one read set.  `fasta` stays referenced until :meth:`release`.  `out` =
+        (keys, suffix, prefix) host arrays receiving the macro-node table (pinned memory
+        copies fastest); without it the server keeps the table for :meth:`result`."""
+        buf = _as_bytes_ptr(fasta)
+        r = capi.PkRequest()
+        r.fasta = buf[0]
+        r.fasta_bytes = buf[1]
+        r.params = params
+        if out is not None:
+            keys, suf, pre = out
+            r.mn_keys = keys.ctypes.data
+            r.mn_suffix = suf.ctypes.data
+            r.mn_prefix = pre.ctypes.data
+            r.mn_capacity = min(keys.shape[0], suf.shape[0], pre.shape[0])
+        t = c_uint64()
+        check(capi.lib().pk_submit(self._h, byref(r), byref(t)), "pk_submit")
+        self._live[t.value] = (fasta, buf, out, params)
+        return t.value
+
+    @staticmethod
+    def _info(ticket: int, i: capi.PkRequestInfo) -> RequestInfo:
+        return RequestInfo(ticket, i.status, bool(i.done), Summary.from_c(i.summary), i.submit_ns,
+                           i.start_ns, i.end_ns, i.attempts)
+
+    def poll(self, ticket: int) -> RequestInfo:
+        i = capi.PkRequestInfo()
+        check(capi.lib().pk_poll(self._h, ticket, byref(i)), "pk_poll")
+        return self._info(ticket, i)
+
+    def wait(self, ticket: int, timeout: Optional[float] = None) -> RequestInfo:
+        """Block until the request is done; raises the job's error if it failed."""
+        i = capi.PkRequestInfo()
+        ms = -1 if timeout is None else int(timeout * 1000)
+        check(capi.lib().pk_wait(self._h, ticket, ms, byref(i)), "pk_wait")
+        check(i.status, "request")
+        return self._info(ticket, i)
+
+    def result(self, ticket: int, coverage: Optional[int] = None) -> MacroNodeTable:
+        """The macro-node table of a finished request (copied out of the server)."""
+        info = self.wait(ticket)
+        fasta, buf, out, params = self._live[ticket]
+        m = info.summary.n_nodes
+        cov = coverage if coverage is not None else params.coverage
+        if out is not None:
+            keys, suf, pre = out
+            return MacroNodeTable(keys[:m], suf[:m], pre[:m], cov, params.k)
+        kp, sp, pp, n = c_void_p(), c_void_p(), c_void_p(), c_uint64()
+        check(capi.lib().pk_result_get(self._h, ticket, byref(kp), byref(sp), byref(pp), byref(n)),
+              "pk_result_get")
+        W = 8 if params.k <= 32 else 16
+        keys = np.frombuffer((ctypes.c_char * (W * m)).from_address(kp.value), np.uint8).copy() \
+            if m else np.empty(0, np.uint8)
+        suf = np.frombuffer((ctypes.c_char * (16 * m)).from_address(sp.value), np.uint32).copy() \
+            if m else np.empty(0, np.uint32)
+        pre = np.frombuffer((ctypes.c_char * (16 * m)).from_address(pp.value), np.uint32).copy() \
+            if m else np.empty(0, np.uint32)
+        return MacroNodeTable(keys.view(key_dtype(params.k)), suf.reshape(m, 4), pre.reshape(m, 4), cov,
+                              params.k)
+
+    def release(self, ticket: int):
+        check(capi.lib().pk_result_release(self._h, ticket), "pk_result_release")
+        self._live.pop(ticket, None)
+
+    def stats(self) -> Dict[str, int]:
+        s = capi.PkServerStats()
+        check(capi.lib().pk_server_get_stats(self._h, byref(s)), "pk_server_get_stats")
+        return {n: getattr(s, n) for n, _ in capi.PkServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.lib().pk_server_destroy(self._h)
+            self._h = None
+            self._live.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -20,7 +20,7 @@ ROOT = os.path.dirname(HERE)
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpakman_gb300.so")
-SOURCES = ["pk_kernels.cu", "pk_capi.cu", "pk_noalloc.cu"]
+SOURCES = ["pk_kernels.cu", "pk_capi.cu", "pk_noalloc.cu", "pk_server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

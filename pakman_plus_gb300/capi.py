@@ -40,6 +40,23 @@ class PkSummary(ctypes.Structure):
                 ("key_bytes", c_int32)]
 
 
+class PkRequest(ctypes.Structure):
+    _fields_ = [("fasta", c_void_p), ("fasta_bytes", c_uint64), ("params", PkParams),
+                ("mn_keys", c_void_p), ("mn_suffix", c_void_p), ("mn_prefix", c_void_p),
+                ("mn_capacity", c_uint64)]
+
+
+class PkRequestInfo(ctypes.Structure):
+    _fields_ = [("status", c_int), ("done", c_int32), ("summary", PkSummary),
+                ("submit_ns", c_uint64), ("start_ns", c_uint64), ("end_ns", c_uint64),
+                ("attempts", c_uint32), ("reserved", c_uint32)]
+
+
+class PkServerStats(ctypes.Structure):
+    _fields_ = [(n, c_uint64) for n in ("submitted", "completed", "failed", "queued", "running",
+                                        "admitted_bytes", "peak_admitted_bytes", "requeued")]
+
+
 class PakmanError(RuntimeError):
     """A failed C-ABI call; `status` is the pk_status code."""
 
@@ -104,6 +121,16 @@ _SIGS = {
     "pk_stage_name": (c_char_p, [c_int]),
     "pk_cutoff_noalloc": (c_int, [c_void_p, c_uint64, c_int32, c_void_p, c_void_p, c_void_p,
                                   c_void_p]),
+    "pk_server_create": (c_int, [c_void_p, c_int32, POINTER(c_void_p)]),
+    "pk_server_destroy": (None, [c_void_p]),
+    "pk_submit": (c_int, [c_void_p, POINTER(PkRequest), POINTER(c_uint64)]),
+    "pk_poll": (c_int, [c_void_p, c_uint64, POINTER(PkRequestInfo)]),
+    "pk_wait": (c_int, [c_void_p, c_uint64, ctypes.c_int64, POINTER(PkRequestInfo)]),
+    "pk_result_get": (c_int, [c_void_p, c_uint64, POINTER(c_void_p), POINTER(c_void_p),
+                              POINTER(c_void_p), POINTER(c_uint64)]),
+    "pk_result_release": (c_int, [c_void_p, c_uint64]),
+    "pk_server_get_stats": (c_int, [c_void_p, POINTER(PkServerStats)]),
+    "pk_request_footprint": (c_uint64, [POINTER(PkRequest)]),
     "pk_host_alloc": (c_int, [c_uint64, POINTER(c_void_p)]),
     "pk_host_free": (None, [c_void_p]),
 }

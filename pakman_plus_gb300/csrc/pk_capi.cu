@@ -370,7 +370,7 @@ static int auto_bucket_bits(uint64_t F, int k, int wide) {
   // table and macro-node kernels, small enough that a bucket's distinct keys usually
   // fit one on-chip hash table (8192 64-bit or 4096 128-bit slots at load <= 1/2)
   const double per_bucket = wide ? 3000.0 : 16000.0;
-  const double est = 0.7 * (double)F;                // k-mer windows per byte, ~100 bp reads
+  const double est = 0.62 * (double)F;               // k-mer windows per byte, 100 bp reads, k=32
   int b = 2;
   while (b < kMaxPartitionBits && est / (double)(1u << b) > per_bucket) b++;
   return std::max(2, std::min(b, 2 * k - 2));

@@ -55,3 +55,23 @@ def test_no_cpu_fallback_without_device(lib):
     with pytest.raises(pk.PakmanError) as e:
         pk.Context(0)
     assert e.value.status == capi.PK_ERR_NO_DEVICE
+
+
+def test_serving_structs_and_footprint(lib):
+    # pk_request: pointer, size, 64-byte params, three pointers, capacity
+    assert ctypes.sizeof(capi.PkRequest) == 8 + 8 + 64 + 8 * 3 + 8
+    assert ctypes.sizeof(capi.PkRequestInfo) == 8 + 48 + 8 * 3 + 8
+    assert ctypes.sizeof(capi.PkServerStats) == 64
+    r = capi.PkRequest()
+    r.params = capi.default_params(k=32)
+    r.fasta_bytes = 1 << 20
+    small = lib.pk_request_footprint(ctypes.byref(r))
+    r.fasta_bytes = 1 << 24
+    big = lib.pk_request_footprint(ctypes.byref(r))
+    r.params = capi.default_params(k=63)
+    wide = lib.pk_request_footprint(ctypes.byref(r))
+    assert small < big < wide
+    assert big >= (1 << 24) * (1 + 2 * 8 + 4)  # FASTA + two key arrays + counts at N = F
+    assert lib.pk_request_footprint(None) == 0
+    assert lib.pk_server_create(None, 2, None) == capi.PK_ERR_INVALID
+    assert lib.pk_submit(None, None, None) == capi.PK_ERR_INVALID

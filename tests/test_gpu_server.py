@@ -1,0 +1,108 @@
+"""Serving path (pk_submit / pk_poll): each request's result equals the same read
+set run alone, in any mix of sizes and k, with failures isolated to their request and
+admission held within the context's HBM budget."""
+import numpy as np
+import pytest
+
+import pakman_plus_gb300 as pk
+from gpu_helpers import assert_mn_equal, ctx, run_gpu
+from pakman_plus_gb300 import build as pkbuild
+from pakman_plus_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _mix():
+    cases = []
+    for i, (k, glen, nreads, t) in enumerate([(32, 20000, 6000, 21), (31, 5000, 1500, 12),
+                                              (63, 12000, 4000, 10), (32, 60000, 20000, 30),
+                                              (17, 3000, 900, 8), (63, 3000, 800, 5)]):
+        lens = np.random.default_rng(9000 + i).integers(90, 152, nreads)
+        rs = synth.small_case(9100 + i, genome_len=glen, n_reads=nreads, read_len=lens, err=0.005,
+                              k=k, coverage=20)
+        cases.append((rs.fasta, k, t, 20))
+    return cases
+
+
+def _params(k, t, cov):
+    return pk.default_params(k=k, num_buckets=t, coverage=cov)
+
+
+def test_requests_match_jobs_run_alone():
+    cases = _mix()
+    alone = [run_gpu(f, k, t, cov) for f, k, t, cov in cases]
+    with pk.Server(ctx(), workers=3) as srv:
+        tickets = [srv.submit(f, _params(k, t, cov)) for f, k, t, cov in cases]
+        for tk, (s, _, _, _, mn, err) in zip(tickets, alone):
+            assert err is None
+            info = srv.wait(tk)
+            assert info.done and info.status == 0
+            assert info.summary.n_windows == s.n_windows
+            assert info.summary.n_unique == s.n_unique
+            assert info.summary.cutoff == s.cutoff
+            assert info.summary.n_nodes == s.n_nodes
+            got = srv.result(tk)
+            ref = pk.to_key128(mn.keys)
+            assert_mn_equal(got, ref, mn.suffix_counts, mn.prefix_counts)
+            assert info.submit_ns <= info.start_ns <= info.end_ns
+            srv.release(tk)
+        st = srv.stats()
+        assert st["completed"] == len(cases) and st["failed"] == 0
+
+
+def test_caller_buffers_and_capacity_limit():
+    f, k, t, cov = _mix()[0]
+    s, _, _, _, mn, _ = run_gpu(f, k, t, cov)
+    m = s.n_nodes
+    keys = np.zeros(m + 5, np.uint64)
+    suf = np.zeros((m + 5, 4), np.uint32)
+    pre = np.zeros((m + 5, 4), np.uint32)
+    small = (np.zeros(m - 1, np.uint64), np.zeros((m - 1, 4), np.uint32), np.zeros((m - 1, 4), np.uint32))
+    with pk.Server(ctx(), workers=2) as srv:
+        a = srv.submit(f, _params(k, t, cov), out=(keys, suf, pre))
+        b = srv.submit(f, _params(k, t, cov), out=small)
+        got = srv.result(a)
+        assert_mn_equal(got, pk.to_key128(mn.keys), mn.suffix_counts, mn.prefix_counts)
+        with pytest.raises(pk.PakmanError) as e:
+            srv.wait(b)
+        assert e.value.status == pk.capi.PK_ERR_LIMIT
+        assert srv.poll(b).summary.n_nodes == m
+
+
+def test_failed_request_does_not_disturb_others():
+    cases = _mix()[:3]
+    # a record that does not start with '>' (the reference asserts)
+    bad = cases[0][0].replace(b"\n>r150\n", b"\nxr150\n", 1)
+    assert bad != cases[0][0]
+    with pk.Server(ctx(), workers=2) as srv:
+        t_ok = [srv.submit(f, _params(k, t, cov)) for f, k, t, cov in cases]
+        t_bad = srv.submit(bad, _params(32, 21, 20))
+        with pytest.raises(pk.FormatError):
+            srv.wait(t_bad)
+        for tk, (f, k, t, cov) in zip(t_ok, cases):
+            s = run_gpu(f, k, t, cov)[0]
+            assert srv.wait(tk).summary.n_nodes == s.n_nodes
+        st = srv.stats()
+        assert st["failed"] == 1 and st["completed"] == 3
+
+
+def test_admission_stays_within_budget():
+    pkbuild.build()
+    cases = _mix()
+    fp = []
+    for f, k, t, cov in cases:
+        r = pk.capi.PkRequest()
+        r.fasta_bytes = len(f)
+        r.params = _params(k, t, cov)
+        fp.append(pk.capi.lib().pk_request_footprint(r))
+    budget = max(fp) + min(fp)  # the largest job plus the smallest fit together, no more
+    with pk.Context(0, hbm_budget=budget) as c, pk.Server(c, workers=4) as srv:
+        tickets = [srv.submit(f, _params(k, t, cov)) for f, k, t, cov in cases]
+        for tk, (f, k, t, cov) in zip(tickets, cases):
+            s = run_gpu(f, k, t, cov)[0]
+            assert srv.wait(tk).summary.n_nodes == s.n_nodes
+        st = srv.stats()
+        assert st["peak_admitted_bytes"] <= budget
+        assert st["completed"] == len(cases)
+        used, _ = c.memory()
+        assert used == 0

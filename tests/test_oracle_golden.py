@@ -45,3 +45,16 @@ def test_window_count_matches_table_sum():
     w, reads = po.count_windows(g.fasta, g.k)
     assert w == g.n_windows
     assert reads == g.fasta.count(b">")
+
+
+@pytest.mark.parametrize("k", [11, 32, 63])
+def test_threaded_port_equals_serial_oracle(k):
+    """The multi-threaded restatement (CPU baseline) builds the same table."""
+    from pakman_plus_gb300 import synth
+    lens = np.random.default_rng(k).integers(40, 151, 4000)
+    rs = synth.small_case(500 + k, genome_len=8000, n_reads=4000, read_len=lens, err=0.01, k=k)
+    a = po.count(rs.fasta, k)
+    for threads in (2, 5, 16):
+        b = po.count(rs.fasta, k, threads=threads)
+        assert np.array_equal(a.keys, b.keys) and np.array_equal(a.counts, b.counts)
+        assert (a.n_windows, a.n_reads) == (b.n_windows, b.n_reads)
