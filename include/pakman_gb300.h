@@ -106,6 +106,13 @@ pk_status pk_job_memory(pk_job* job, uint64_t* bytes);
 pk_status pk_count(pk_job* job, const char* fasta, uint64_t n, const pk_params* p);
 pk_status pk_count_device(pk_job* job, const void* d_fasta, uint64_t n, const pk_params* p);
 pk_status pk_table_info(pk_job* job, uint64_t* n_unique, uint64_t* n_windows, uint64_t* n_reads);
+/* Load an existing frequency table instead of counting (the input of the PaK-Graph
+ * builder, Pakman_Subgraph::build_graph, src/pakman_graph.hpp:592-673, whose table
+ * comes from elsewhere).  Rows ascending and unique, keys below 4^k in the layout of
+ * pk_copy_table, counts >= 1.  Afterwards pk_cutoff / pk_build_macro_nodes run as
+ * after pk_count (n_windows = sum of counts, n_reads = 0). */
+pk_status pk_table_load(pk_job* job, const void* keys, const uint32_t* counts, uint64_t n_rows,
+                        const pk_params* params);
 /* Table rows ascending by k-mer: keys as uint64 (k <= 32) or {uint64 lo, hi}
  * (k > 32), counts as uint32.  capacity = rows the buffers hold. */
 pk_status pk_copy_table(pk_job* job, void* keys, uint32_t* counts, uint64_t capacity);

@@ -167,6 +167,16 @@ class Job:
         self.params = params
         check(capi.lib().pk_count_device(self._h, c_void_p(ptr), n, byref(params)), "pk_count_device")
 
+    def load_table(self, keys: np.ndarray, counts: np.ndarray, params: capi.PkParams):
+        """Use an existing ascending, unique (k-mer, count) table instead of counting."""
+        self.params = params
+        if keys.dtype != key_dtype(params.k):
+            keys = keys.astype(key_dtype(params.k)) if params.k <= 32 else to_key128(keys)
+        keys = np.ascontiguousarray(keys)
+        counts = np.ascontiguousarray(counts, dtype=np.uint32)
+        check(capi.lib().pk_table_load(self._h, keys.ctypes.data, counts.ctypes.data, counts.size,
+                                       byref(params)), "pk_table_load")
+
     def table_info(self) -> Tuple[int, int, int]:
         u, w, r = c_uint64(), c_uint64(), c_uint64()
         check(capi.lib().pk_table_info(self._h, byref(u), byref(w), byref(r)), "pk_table_info")

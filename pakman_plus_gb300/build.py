@@ -20,6 +20,9 @@ ROOT = os.path.dirname(HERE)
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpakman_gb300.so")
+HOST = os.path.join(HERE, "host")
+BIN = os.path.join(HERE, "bin")
+PKMER = os.path.join(BIN, "pkmer")
 SOURCES = ["pk_kernels.cu", "pk_capi.cu", "pk_noalloc.cu", "pk_server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -55,8 +58,32 @@ def _compile(src: str) -> str:
     return obj
 
 
+def cxx() -> str:
+    for cand in (os.environ.get("CXX"), shutil.which("g++")):
+        if cand:
+            return cand
+    raise RuntimeError("g++ not found")
+
+
+def build_pkmer(force: bool = False) -> str:
+    """The pkmer command-line driver, linked against the in-tree library."""
+    src = os.path.join(HOST, "pkmer.cpp")
+    if (not force and os.path.exists(PKMER) and os.path.getmtime(PKMER) >= os.path.getmtime(src)
+            and os.path.getmtime(PKMER) >= os.path.getmtime(LIB)):
+        return PKMER
+    os.makedirs(BIN, exist_ok=True)
+    cmd = [cxx(), "-O2", "-std=c++17", "-I", INCLUDE, src, "-o", PKMER + ".tmp", "-L", HERE,
+           "-lpakman_gb300", "-Wl,-rpath,$ORIGIN/.."]
+    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(f"g++ failed on pkmer.cpp:\n{p.stdout}")
+    os.replace(PKMER + ".tmp", PKMER)
+    return PKMER
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     if not force and up_to_date():
+        build_pkmer()
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     with cf.ThreadPoolExecutor(len(SOURCES)) as ex:
@@ -67,8 +94,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if p.returncode != 0:
         raise RuntimeError(f"link failed:\n{p.stdout}")
     os.replace(tmp, LIB)
+    build_pkmer(force=True)
     if verbose:
-        print(f"built {LIB}")
+        print(f"built {LIB} and {PKMER}")
     return LIB
 
 

@@ -103,6 +103,7 @@ _SIGS = {
     "pk_job_memory": (c_int, [c_void_p, POINTER(c_uint64)]),
     "pk_count": (c_int, [c_void_p, c_void_p, c_uint64, POINTER(PkParams)]),
     "pk_count_device": (c_int, [c_void_p, c_void_p, c_uint64, POINTER(PkParams)]),
+    "pk_table_load": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64, POINTER(PkParams)]),
     "pk_table_info": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64)]),
     "pk_copy_table": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64]),
     "pk_copy_table_packed": (c_int, [c_void_p, c_void_p, c_uint64]),

@@ -518,6 +518,70 @@ pk_status pk_count(pk_job* j, const char* fasta, uint64_t n, const pk_params* p)
   return count_impl(j, j->fasta.p, n, p);
 }
 
+// An existing (k-mer, count) table in place of counting: host rows ascending and
+// unique, k-mers below 4^k.  The rows are laid out as the counting stages leave them
+// (every bucket's rows contiguous), so cutoff and macro-nodes run unchanged.
+pk_status pk_table_load(pk_job* j, const void* keys, const uint32_t* counts, uint64_t n, const pk_params* p) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  PK_TRY(check_params(p));
+  if (n && (!keys || !counts)) return fail(PK_ERR_INVALID, "keys and counts must not be null");
+  if (n >= 0xffffffffull) return fail(PK_ERR_LIMIT, "tables of 2^32-1 rows or more are not supported");
+  const int k = p->k;
+  const bool wide = k > 32;
+  const uint64_t* kw = (const uint64_t*)keys;
+  unsigned long long total = 0;
+  for (uint64_t i = 0; i < n; i++) {
+    const unsigned __int128 x = wide ? ((unsigned __int128)kw[2 * i + 1] << 64) | kw[2 * i]
+                                     : (unsigned __int128)kw[i];
+    if (k < 64 && (x >> (2 * k)) != 0) return fail(PK_ERR_INVALID, "row " + std::to_string(i) + " is not a k-mer");
+    if (i) {
+      const unsigned __int128 y = wide ? ((unsigned __int128)kw[2 * i - 1] << 64) | kw[2 * i - 2]
+                                       : (unsigned __int128)kw[i - 1];
+      if (!(y < x)) return fail(PK_ERR_INVALID, "rows must be ascending and unique (row " + std::to_string(i) + ")");
+    }
+    if (counts[i] == 0) return fail(PK_ERR_INVALID, "row " + std::to_string(i) + " has count 0");
+    total += counts[i];
+  }
+  PK_TRY(set_device(j->ctx));
+  for (int i = 0; i < ST_COUNT_; i++) j->ev_rec[i] = false;
+  j->params = *p;
+  j->wide = wide;
+  j->F = 0;
+  j->N = n;
+  j->stage = 0;
+  int bb = p->bucket_bits;
+  if (!bb) {  // about 4000 rows per bucket
+    bb = 2;
+    while (bb < kMaxPartitionBits && (double)n / (double)(1u << bb) > 4000.0) bb++;
+  }
+  j->bbits = std::max(2, std::min(bb, std::min(kMaxPartitionBits, 2 * k - 2)));
+  const int B = 1 << j->bbits;
+  const size_t W = wide ? 16 : 8;
+  PK_TRY(job_alloc(j, j->tkeys, W * (n ? n : 1)));
+  PK_TRY(job_alloc(j, j->tcounts, 4 * (n ? n : 1)));
+  PK_TRY(job_alloc(j, j->bstart, sizeof(uint32_t) * (B + 1)));
+  PK_TRY(job_alloc(j, j->tu, sizeof(uint32_t) * (size_t)B));
+  PK_TRY(job_alloc(j, j->tsub, sizeof(uint32_t) * 3 * (size_t)B));
+  if (n) {
+    PK_CUDA(cudaMemcpyAsync(j->tkeys.p, keys, W * n, cudaMemcpyHostToDevice, j->stream));
+    PK_CUDA(cudaMemcpyAsync(j->tcounts.p, counts, 4 * n, cudaMemcpyHostToDevice, j->stream));
+  }
+  PK_CUDA(cudaMemsetAsync(j->tsub.p, 0, sizeof(uint32_t) * 3 * (size_t)B, j->stream));
+  PK_CUDA(launch_table_bounds(j->tkeys.p, n, j->bbits, k, (uint32_t*)j->bstart.p, (uint32_t*)j->tu.p,
+                              wide, j->stream));
+  Scalars init{};
+  memset(&init, 0, sizeof(init));
+  init.n_unique = n;
+  init.n_windows = total;
+  *j->h_sc = init;
+  PK_CUDA(cudaMemcpyAsync(j->d_sc, j->h_sc, sizeof(Scalars), cudaMemcpyHostToDevice, j->stream));
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  j->t_hist = 0;  // no histogram was fused into a counting pass
+  j->dense_valid = false;
+  j->stage = 1;
+  return PK_OK;
+}
+
 static pk_status sync_scalars(pk_job* j) {
   PK_CUDA(cudaMemcpyAsync(j->h_sc, j->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost, j->stream));
   PK_CUDA(cudaStreamSynchronize(j->stream));

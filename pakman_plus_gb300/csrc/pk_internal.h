@@ -136,6 +136,9 @@ cudaError_t launch_scatter_fine(const void* in, const uint32_t* cstart, const ui
                                 uint32_t* fcur, void* out, int k, int bbits, int cbits, int wide,
                                 uint32_t* ticket, unsigned long long cap, uint32_t* err, cudaStream_t st);
 cudaError_t launch_bucket_table(const BucketArgs& a, int wide, int grid, cudaStream_t st);
+// bstart / tu of a dense ascending table (pk_table_load)
+cudaError_t launch_table_bounds(const void* keys, unsigned long long n, int bbits, int k, uint32_t* bstart,
+                                uint32_t* tu, int wide, cudaStream_t st);
 cudaError_t launch_histogram(const uint32_t* tcounts, unsigned long long u, int t,
                              unsigned long long* hist, cudaStream_t st);
 cudaError_t launch_cutoff(const unsigned long long* hist, int t, Scalars* sc, cudaStream_t st);

@@ -1664,6 +1664,33 @@ __global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
   }
 }
 
+// ------------------------------------------------------- loaded (external) tables --
+// Bucket extents of a dense ascending table: bstart[b] = first row whose key's top
+// `bbits` bits are >= b, tu[b] = rows of bucket b (the sparse layout with no gaps).
+template <typename KeyT>
+__global__ void __launch_bounds__(256) k_table_bounds(const KeyT* __restrict__ keys, unsigned long long n,
+                                                      int bbits, int rem, uint32_t* bstart) {
+  const int B = 1 << bbits;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b > B) return;
+  unsigned long long lo = 0, hi = n;
+  if (b == B) {
+    lo = n;
+  } else {
+    const KeyT x = KeyOps<KeyT>::shl((KeyT)(uint32_t)b, rem);
+    while (lo < hi) {
+      const unsigned long long mid = (lo + hi) >> 1;
+      if (keys[mid] < x) lo = mid + 1; else hi = mid;
+    }
+  }
+  bstart[b] = (uint32_t)lo;
+}
+
+__global__ void __launch_bounds__(256) k_table_sizes(const uint32_t* bstart, int B, uint32_t* tu) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < B) tu[b] = bstart[b + 1] - bstart[b];
+}
+
 // =================================================================== launchers =====
 static int g_sms = 0;
 static int sm_count() {
@@ -1857,4 +1884,21 @@ cudaError_t launch_compact_rows(const void* tkeys, const uint32_t* tcounts, cons
   return cudaGetLastError();
 }
 
+}  // namespace pk
+
+namespace pk {
+cudaError_t launch_table_bounds(const void* keys, unsigned long long n, int bbits, int k, uint32_t* bstart,
+                                uint32_t* tu, int wide, cudaStream_t st) {
+  const int B = 1 << bbits;
+  const int rem = 2 * k - bbits;
+  const int grid = (B + 1 + 255) / 256;
+  if (wide) {
+    k_table_bounds<u128><<<grid, 256, 0, st>>>((const u128*)keys, n, bbits, rem, bstart);
+    k_table_sizes<<<(B + 255) / 256, 256, 0, st>>>(bstart, B, tu);
+  } else {
+    k_table_bounds<uint64_t><<<grid, 256, 0, st>>>((const uint64_t*)keys, n, bbits, rem, bstart);
+    k_table_sizes<<<(B + 255) / 256, 256, 0, st>>>(bstart, B, tu);
+  }
+  return cudaGetLastError();
+}
 }  // namespace pk
