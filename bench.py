@@ -50,6 +50,13 @@ def parse():
     ap.add_argument("--cpu-sample-windows", type=int, default=0,
                     help="windows in the CPU baseline's sample (0: the whole read set)")
     ap.add_argument("--bucket-bits", type=int, default=0, help="partition digits (0 = automatic)")
+    ap.add_argument("--serve", action="store_true",
+                    help="serving benchmark: Poisson stream of jobs through pk_submit, p50/p99 latency")
+    ap.add_argument("--serve-jobs", type=int, default=5000)
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="mean arrivals per second")
+    ap.add_argument("--serve-pool", type=int, default=32, help="distinct generated read sets")
+    ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--serve-budget-gb", type=float, default=160.0)
     return ap.parse_args()
 
 
@@ -216,6 +223,125 @@ def run_reference_arm(args, rank, world):
     return 0
 
 
+def run_serve(args, rank, world):
+    """Serving workload: jobs (genome log-uniform 10 kb-20 Mbp, 100 bp reads at 30-80x,
+    k in {31, 32, 63}) arrive as a Poisson stream and go through pk_submit/pk_wait
+    with HBM-budget admission; the same stream is then served one job at a time (the
+    plain one-job-per-launch path).  A pool of generated read sets stands in for the
+    stream's inputs (job i uses pool entry i mod P with that entry's k)."""
+    if rank != 0:
+        return 0
+    import threading
+
+    import numpy as np
+    import torch
+
+    import pakman_plus_gb300 as pk
+    from pakman_plus_gb300 import build as pkbuild
+    from pakman_plus_gb300 import synth
+
+    pkbuild.build()
+    torch.cuda.set_device(0)
+    t_gen = time.perf_counter()
+    pool, pinned, params, pool_bytes = [], [], [], 0
+    for i in range(args.serve_pool):  # generated and pinned one at a time
+        rs = synth.config5_job(i)
+        pool.append(rs)
+        buf = torch.empty(len(rs.fasta), dtype=torch.uint8, pin_memory=True)
+        buf.numpy()[:] = np.frombuffer(rs.fasta, np.uint8)
+        pinned.append(buf)
+        pool_bytes += len(rs.fasta)
+        params.append(pk.default_params(k=rs.k, num_buckets=21, coverage=rs.coverage, read_length=100))
+        rs.fasta = b""  # the pinned copy is the input from here on
+    t_gen = time.perf_counter() - t_gen
+    budget = int(args.serve_budget_gb * 1e9)
+    ctx = pk.Context(0, hbm_budget=budget)
+    # each pool entry alone, once: reference summaries and warm-up
+    # (a job whose k-mers all fall below the cutoff ends with PK_ERR_EMPTY, as the
+    # reference aborts; that outcome must then be the same in the stream)
+    alone = []
+    with pk.Job(ctx) as job:
+        for e, rs in enumerate(pool):
+            t0 = time.perf_counter()
+            status = 0
+            try:
+                job.run(pinned[e].numpy(), params[e])
+                job.macro_nodes()
+            except pk.EmptyAfterCutoff as ex:
+                status = ex.status
+            alone.append((job.summary(), time.perf_counter() - t0, status))
+            job.reset()
+    rng = np.random.Generator(np.random.PCG64(5_000_001))
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, args.serve_jobs))
+    entries = [i % len(pool) for i in range(args.serve_jobs)]
+
+    def serve(workers):
+        srv = pk.Server(ctx, workers=workers)
+        tickets = [None] * args.serve_jobs
+        ready = threading.Semaphore(0)
+
+        def producer():
+            t0 = time.perf_counter()
+            for i, e in enumerate(entries):
+                dt = t0 + arrivals[i] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                tickets[i] = srv.submit(pinned[e].numpy(), params[e])
+                ready.release()
+
+        th = threading.Thread(target=producer, daemon=True)
+        th.start()
+        lat, first_submit, last_end, windows, mismatches = [], None, 0, 0, 0
+        for i, e in enumerate(entries):
+            ready.acquire()
+            try:
+                srv.wait(tickets[i])
+            except pk.PakmanError:
+                pass  # compared with the job run alone below
+            info = srv.poll(tickets[i])
+            srv.release(tickets[i])
+            ref, _, ref_status = alone[e]
+            s = info.summary
+            if info.status != ref_status or (s.n_windows, s.n_unique, s.n_kept, s.cutoff) != (
+                    ref.n_windows, ref.n_unique, ref.n_kept, ref.cutoff) or (
+                    ref_status == 0 and s.n_nodes != ref.n_nodes):
+                mismatches += 1
+            lat.append(info.latency_ms)
+            first_submit = info.submit_ns if first_submit is None else min(first_submit, info.submit_ns)
+            last_end = max(last_end, info.end_ns)
+            windows += s.n_windows
+        th.join()
+        st = srv.stats()
+        srv.close()
+        lat = np.array(lat)
+        span = (last_end - first_submit) / 1e9
+        return {"workers": workers, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                "max_ms": float(lat.max()), "kmers_per_s": windows / span, "span_s": span,
+                "peak_admitted_gb": st["peak_admitted_bytes"] / 1e9, "requeued": st["requeued"],
+                "results_differing_from_alone": mismatches}
+
+    served = serve(args.serve_workers)
+    plain = serve(1)
+    total_windows = sum(alone[e][0].n_windows for e in entries)
+    offered = total_windows / arrivals[-1]
+    line = {"metric": "served p50/p99 latency of count + macro-node jobs", "impl": "serve",
+            "value": served["p99_ms"], "unit": "ms (p99)", "higher_is_better": False,
+            "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": "serving: Poisson arrivals, genome log-uniform 10 kb-20 Mbp, 100 bp reads "
+                                   "at 30-80x, 0.5% errors, k in {31,32,63}",
+                       "jobs": args.serve_jobs, "rate_per_s": args.serve_rate, "pool_read_sets": len(pool),
+                       "pool_fasta_gb": pool_bytes / 1e9, "pool_gen_s": t_gen,
+                       "hbm_budget_gb": args.serve_budget_gb,
+                       "offered_kmers_per_s": offered,
+                       "alone_ms_by_entry": [round(a[1] * 1000, 2) for a in alone],
+                       "entries_empty_after_cutoff": sum(1 for a in alone if a[2] != 0)},
+            "served": served, "plain_one_job_at_a_time": plain}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -223,6 +349,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
+    if args.serve:
+        return run_serve(args, rank, world)
 
     import numpy as np
     import torch

@@ -64,7 +64,7 @@ typedef struct pk_params {
   int32_t drop_n;       /* 0: reference behaviour (an 'N' is code 7 OR-ed into the
                            window); 1: windows containing 'N'/'n' are skipped */
   uint64_t batch_kmers; /* -b: MAX_KMER_COUNT; the table is the same for any value */
-  int32_t bucket_bits;  /* partition digits (leading key bits); 0 = automatic */
+  int32_t bucket_bits;  /* partition digits (leading key bits), 2..18; 0 = automatic */
   int32_t reserved[7];
 } pk_params;
 

@@ -18,7 +18,7 @@
 
 using namespace pk;
 
-static const int kMaxPartitionBits = 15;
+static const int kMaxPartitionBits = kMaxPartBits;
 
 // ------------------------------------------------------------------ errors ------
 static thread_local std::string t_last_error;
@@ -91,7 +91,7 @@ struct pk_job {
   uint64_t mn_cap = 0;
   Scalars* d_sc = nullptr;
   Scalars* h_sc = nullptr;  // pinned mirror
-  DevBuf fasta, tile_nl, counts, bstart, keys, tkeys, tcounts, tu, tsub, flags_m, hist, hist2,
+  DevBuf fasta, tile_nl, counts, bstart, hstart, keys, tkeys, tcounts, tu, tsub, flags_m, hist, hist2,
       nkeys, nsuf, npre, packed, doff, dkeys, dcounts, flags_f, kkeys, kcounts, kstart, kcount, ksub,
       coff, cstart, slice_start, fcur;
   bool dense_valid = false;
@@ -142,7 +142,7 @@ static void job_free(pk_job* j, DevBuf& b) {
 }
 
 static void job_free_all(pk_job* j) {
-  DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->keys,  &j->tkeys,
+  DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->hstart, &j->keys,  &j->tkeys,
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
@@ -310,7 +310,7 @@ pk_status pk_job_sync(pk_job* j) {
 
 pk_status pk_job_memory(pk_job* j, uint64_t* bytes) {
   if (!j || !bytes) return fail(PK_ERR_INVALID, "null argument");
-  DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->keys,  &j->tkeys,
+  DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->hstart, &j->keys,  &j->tkeys,
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
@@ -357,7 +357,8 @@ static pk_status check_params(const pk_params* p) {
   if (p->k < 2 || p->k > 64) return fail(PK_ERR_INVALID, "k must be in 2..64");
   if (p->lmer_length < 1 || p->lmer_length > 32) return fail(PK_ERR_INVALID, "lmer_length must be in 1..32");
   if (p->num_buckets < 1) return fail(PK_ERR_INVALID, "num_buckets (-t) must be >= 1");
-  if (p->bucket_bits < 0 || p->bucket_bits > 15) return fail(PK_ERR_INVALID, "bucket_bits must be in 0..15");
+  if (p->bucket_bits < 0 || p->bucket_bits > kMaxPartitionBits)
+    return fail(PK_ERR_INVALID, "bucket_bits must be in 0.." + std::to_string(kMaxPartitionBits));
   return PK_OK;
 }
 
@@ -384,10 +385,14 @@ static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk
   j->F = n;
   j->stage = 0;
   const int W = j->wide ? 16 : 8;
-  const int bb = p->bucket_bits ? std::min(p->bucket_bits, std::min(15, 2 * k - 2))
+  const int bb = p->bucket_bits ? std::min(p->bucket_bits, std::min(kMaxPartitionBits, 2 * k - 2))
                                 : auto_bucket_bits(n, k, j->wide);
   j->bbits = std::max(2, bb);
   const int B = 1 << j->bbits;
+  // the counting pass histograms at most kHistBits digits; deeper partitions get their
+  // fine bucket sizes from a count over the coarse regions (k_fine_count)
+  const int hb = std::min(j->bbits, kHistBits);
+  const int HB = 1 << hb;
   const uint64_t ntiles = (n + kTileBytes - 1) / kTileBytes;
   int grid = (int)std::min<uint64_t>((uint64_t)j->ctx->sms, std::max<uint64_t>(ntiles, 1));
   unsigned long long chunk = (ntiles + grid - 1) / grid * (unsigned long long)kTileBytes;
@@ -397,8 +402,10 @@ static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk
   j->chunk = chunk;
 
   PK_TRY(job_alloc(j, j->tile_nl, sizeof(uint32_t) * (ntiles + 1)));
-  PK_TRY(job_alloc(j, j->counts, sizeof(uint32_t) * (size_t)grid * B));
+  PK_TRY(job_alloc(j, j->counts, sizeof(uint32_t) * (size_t)grid * HB));
   PK_TRY(job_alloc(j, j->bstart, sizeof(uint32_t) * (B + 1)));
+  if (hb < j->bbits) PK_TRY(job_alloc(j, j->hstart, sizeof(uint32_t) * (HB + 1)));
+  uint32_t* hstart = (uint32_t*)(hb < j->bbits ? j->hstart.p : j->bstart.p);
   Scalars init{};
   memset(&init, 0, sizeof(init));
   init.s0 = ~0ull;
@@ -411,13 +418,13 @@ static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk
   a.k = k;
   a.lmer_m = std::min(k, p->lmer_length);
   a.drop_n = p->drop_n ? 1 : 0;
-  a.bbits = j->bbits;
+  a.bbits = hb;
   a.cbits = std::min(j->bbits, kCoarseBits);
   a.grid = grid;
   a.chunk = chunk;
   a.tile_nl = (uint32_t*)j->tile_nl.p;
   a.counts = (uint32_t*)j->counts.p;
-  a.bstart = (uint32_t*)j->bstart.p;
+  a.bstart = hstart;
   a.sc = j->d_sc;
 
   mark_begin(j, ST_LINES);
@@ -467,11 +474,19 @@ static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk
   mark_end(j, ST_SCATTER);
   mark_begin(j, ST_SCATTER_FINE);
   if (two_pass) {
+    if (hb < j->bbits) {
+      PK_CUDA(cudaMemsetAsync(j->bstart.p, 0, sizeof(uint32_t) * (size_t)(B + 1), j->stream));
+      PK_CUDA(cudaMemsetAsync(&j->d_sc->ticket_fcount, 0, sizeof(uint32_t), j->stream));
+      PK_CUDA(launch_fine_count(j->tkeys.p, (const uint32_t*)j->cstart.p, (const uint32_t*)j->slice_start.p,
+                                (uint32_t*)j->bstart.p, k, j->bbits, a.cbits, j->wide, &j->d_sc->ticket_fcount,
+                                j->stream));
+      PK_CUDA(launch_prefix((uint32_t*)j->bstart.p, B, j->stream));
+    }
     PK_CUDA(cudaMemcpyAsync(j->fcur.p, j->bstart.p, sizeof(uint32_t) * (size_t)B, cudaMemcpyDeviceToDevice,
                             j->stream));
     PK_CUDA(cudaMemsetAsync(&j->d_sc->ticket_fine, 0, sizeof(uint32_t), j->stream));
     PK_CUDA(launch_scatter_fine(j->tkeys.p, (const uint32_t*)j->cstart.p, (const uint32_t*)j->slice_start.p,
-                                (uint32_t*)j->fcur.p, j->keys.p, k, a.bbits, a.cbits, j->wide,
+                                (uint32_t*)j->fcur.p, j->keys.p, k, j->bbits, a.cbits, j->wide,
                                 &j->d_sc->ticket_fine, N, &j->d_sc->err, j->stream));
   }
   mark_end(j, ST_SCATTER_FINE);

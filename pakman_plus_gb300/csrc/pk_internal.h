@@ -30,9 +30,12 @@ constexpr int kBucketThreads = 512;
 constexpr int kMnThreads = 128;
 constexpr int kMnCap = 2048;        // items (k-mer records) per macro-node segment on chip
 constexpr int kHistSmem = 1024;     // count-histogram bins kept in shared memory
-constexpr int kBucketStack = 256;   // pending sub-ranges of one bucket (binary-trie split)
+constexpr int kBucketStack = 256;   // pending sub-ranges of one bucket
+constexpr int kSplitWays = 4;      // pieces an overflowing sub-range is cut into
 constexpr int kMaxBucketAttempts = 1 << 16;  // sub-range attempts per bucket before giving up
-constexpr int kCoarseBits = 7;      // pass-1 partition digits (coarse regions)
+constexpr int kCoarseBits = 7;     // pass-1 partition digits (coarse regions)
+constexpr int kMaxPartBits = 18;   // partition digits (table buckets) at most
+constexpr int kHistBits = 15;      // digits the counting pass histograms in shared memory
 constexpr int kSortBinBits = 10;    // top remainder bits of the per-bucket counting sort
 constexpr int kBinMax = 128;        // largest bin sorted by ranking (else radix sort)
 
@@ -47,7 +50,7 @@ struct Scalars {                    // device-side scalars of one job
   uint32_t cutoff;                  // histogram cutoff
   uint32_t ticket_filter;
   uint32_t ticket_fine;
-  uint32_t pad2;
+  uint32_t ticket_fcount;
   unsigned long long n_unique;      // U
   unsigned long long n_kept;        // V
   unsigned long long n_nodes;       // M
@@ -125,6 +128,10 @@ struct MnArgs {
 // Launchers (all stream-ordered, no host synchronisation).
 cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st);
 cudaError_t launch_bucket_count(const CountArgs& a, int wide, cudaStream_t st);
+cudaError_t launch_fine_count(const void* in, const uint32_t* cstart, const uint32_t* slice_start,
+                              uint32_t* bcount, int k, int bbits, int cbits, int wide, uint32_t* ticket,
+                              cudaStream_t st);
+cudaError_t launch_prefix(uint32_t* counts, int B, cudaStream_t st);
 cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st);
 cudaError_t launch_scatter(const CountArgs& a, void* keys_out, int wide, cudaStream_t st);
 // Two-pass partition: coarse regions (pass 1) then fine buckets inside each region.

@@ -735,7 +735,7 @@ struct FineCfg {
   static constexpr int T = 512;                             // threads
   static constexpr int PT = sizeof(KeyT) == 8 ? 16 : 8;      // keys per thread
   static constexpr int S = T * PT;                          // keys per slice (64 KB)
-  static constexpr int FBMAX = 1 << (15 - kCoarseBits);     // fine buckets per coarse
+  static constexpr int FBMAX = 1 << (kMaxPartBits - kCoarseBits);  // fine buckets per coarse
   static constexpr size_t smem = sizeof(KeyT) * S;
 };
 
@@ -792,13 +792,25 @@ __global__ void __launch_bounds__(512, 2) k_scatter_fine(const KeyT* __restrict_
     }
     __syncthreads();
     {
-      // FB <= FC::T: one fine bucket per thread
-      const uint32_t hv = tid < FB ? s_hist[tid] : 0u;
+      // each thread owns a contiguous run of FB / T fine buckets (at least one)
+      constexpr int FPT = (FC::FBMAX + FC::T - 1) / FC::T;
+      const int per = (FB + FC::T - 1) / FC::T;
+      const int f0 = min(FB, tid * per);
+      uint32_t hv[FPT], sum = 0;
+#pragma unroll
+      for (int q = 0; q < FPT; q++) {
+        hv[q] = (q < per && f0 + q < FB) ? s_hist[f0 + q] : 0u;
+        sum += hv[q];
+      }
       uint32_t tot;
-      const uint32_t ex = block_exclusive_sum(hv, s_warp, tot);
-      if (tid < FB) {
-        s_loff[tid] = ex;
-        s_goff[tid] = hv ? atomicAdd(&fcur[(g << fb) + tid], hv) : 0u;
+      uint32_t ex = block_exclusive_sum(sum, s_warp, tot);
+#pragma unroll
+      for (int q = 0; q < FPT; q++) {
+        if (q < per && f0 + q < FB) {
+          s_loff[f0 + q] = ex;
+          s_goff[f0 + q] = hv[q] ? atomicAdd(&fcur[(g << fb) + f0 + q], hv[q]) : 0u;
+          ex += hv[q];
+        }
       }
     }
     __syncthreads();
@@ -817,6 +829,50 @@ __global__ void __launch_bounds__(512, 2) k_scatter_fine(const KeyT* __restrict_
   }
 }
 
+// Fine bucket sizes when the partition has more digits than the counting pass's
+// histogram: slices of each coarse region are counted by their fine digits in shared
+// memory and added to bcount[(g << fb) + f].
+template <typename KeyT>
+__global__ void __launch_bounds__(512, 2) k_fine_count(const KeyT* __restrict__ in,
+                                                   const uint32_t* __restrict__ cstart,
+                                                   const uint32_t* __restrict__ slice_start,
+                                                   uint32_t* bcount, int k, int bbits, int cbits,
+                                                   uint32_t* ticket) {
+  using FC = FineCfg<KeyT>;
+  __shared__ uint32_t s_hist[FC::FBMAX];
+  __shared__ uint32_t s_slice, s_g;
+  const int tid = threadIdx.x;
+  const int Cn = 1 << cbits, fb = bbits - cbits, FB = 1 << fb;
+  const int fshift = 2 * k - bbits;
+  const uint32_t nslices = slice_start[Cn];
+  while (true) {
+    __syncthreads();
+    if (tid == 0) {
+      s_slice = atomicAdd(ticket, 1u);
+      if (s_slice < nslices) {
+        int lo = 0, hi = Cn - 1;
+        while (lo < hi) {
+          int mid = (lo + hi + 1) >> 1;
+          if (slice_start[mid] <= s_slice) lo = mid; else hi = mid - 1;
+        }
+        s_g = lo;
+      }
+    }
+    for (int i = tid; i < FB; i += FC::T) s_hist[i] = 0;
+    __syncthreads();
+    const uint32_t sl = s_slice;
+    if (sl >= nslices) break;
+    const uint32_t g = s_g;
+    const uint32_t r0 = cstart[g] + (sl - slice_start[g]) * FC::S;
+    const uint32_t r1 = min(r0 + (uint32_t)FC::S, cstart[g + 1]);
+    for (uint32_t i = r0 + tid; i < r1; i += FC::T)
+      atomicAdd(&s_hist[(uint32_t)(in[i] >> fshift) & (uint32_t)(FB - 1)], 1u);
+    __syncthreads();
+    for (int f = tid; f < FB; f += FC::T)
+      if (s_hist[f]) atomicAdd(&bcount[((uint32_t)g << fb) + f], s_hist[f]);
+  }
+}
+
 // counts[c][b] -> exclusive prefix over chunks (in place); totals into bstart[b].
 __global__ void __launch_bounds__(256) k_col_prefix(uint32_t* counts, int grid, int B, uint32_t* totals) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -831,18 +887,23 @@ __global__ void __launch_bounds__(256) k_col_prefix(uint32_t* counts, int grid, 
   totals[b] = run;
 }
 
+// Exclusive prefix of bstart[0..B) in place, bstart[B] = total.  One block: each
+// thread sums a contiguous run of ceil(B / 1024) entries, one block scan gives the run
+// offsets, and each thread writes its run (B up to 2^18).
 __global__ void __launch_bounds__(1024) k_bucket_prefix(uint32_t* bstart, int B) {
   __shared__ uint32_t s_warp[33];
-  uint32_t carry = 0;
-  for (int base = 0; base < B; base += blockDim.x) {
-    int i = base + threadIdx.x;
-    uint32_t v = i < B ? bstart[i] : 0;
-    uint32_t tot;
-    uint32_t ex = block_exclusive_sum(v, s_warp, tot);
-    if (i < B) bstart[i] = carry + ex;
-    carry += tot;
+  const int per = (B + (int)blockDim.x - 1) / (int)blockDim.x;
+  const int b0 = min(B, (int)threadIdx.x * per), b1 = min(B, b0 + per);
+  uint32_t sum = 0;
+  for (int b = b0; b < b1; b++) sum += bstart[b];
+  uint32_t tot;
+  uint32_t run = block_exclusive_sum(sum, s_warp, tot);
+  for (int b = b0; b < b1; b++) {
+    const uint32_t v = bstart[b];
+    bstart[b] = run;
+    run += v;
   }
-  if (threadIdx.x == 0) bstart[B] = carry;
+  if (threadIdx.x == 0) bstart[B] = tot;
 }
 
 // ------------------------------------------------------------- per-bucket table ------
@@ -868,27 +929,29 @@ struct BucketSmem {
   static constexpr size_t bytes = off_hist + sizeof(uint32_t) * kHistSmem;
 };
 
+// Insert (r, c) into the open-addressing table: 0 = r was present, 1 = r is new,
+// 2 = no slot within kMaxProbe probes (treated as an overflow of the sub-range).
+constexpr int kMaxProbe = 256;
 template <typename KeyT>
-__device__ __forceinline__ bool hash_insert(KeyT* skey, uint32_t* scnt, uint32_t hmask, KeyT r,
-                                            uint32_t c) {
+__device__ __forceinline__ int hash_insert(KeyT* skey, uint32_t* scnt, uint32_t hmask, KeyT r, uint32_t c) {
   const KeyT EMPTY = ~(KeyT)0;
   uint32_t h = (uint32_t)(KeyOps<KeyT>::hash(r) >> 40) & hmask;
-  for (uint32_t probe = 0; probe <= hmask; probe++) {
+  for (int probe = 0; probe < kMaxProbe; probe++) {
     KeyT cur = *(volatile KeyT*)&skey[h];
     if (cur == r) {
       atomicAdd(&scnt[h], c);
-      return true;
+      return 0;
     }
     if (cur == EMPTY) {
       KeyT old = KeyOps<KeyT>::cas(&skey[h], EMPTY, r);
       if (old == EMPTY || old == r) {
         atomicAdd(&scnt[h], c);
-        return true;
+        return old == EMPTY ? 1 : 0;
       }
     }
     h = (h + 1) & hmask;
   }
-  return false;
+  return 2;
 }
 
 // Rows [base+acc, base+acc+u) of a bucket from the sorted on-chip run (sk, sc), plus the
@@ -950,24 +1013,25 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   uint16_t* wc = reinterpret_cast<uint16_t*>(smem + SM::off_wc);
   uint32_t* shist = reinterpret_cast<uint32_t*>(smem + SM::off_hist);
   __shared__ uint32_t s_warp[33];
-  __shared__ uint32_t s_beta, s_ovf, s_d[3], s_fail, s_nb[2];
+  __shared__ uint32_t s_beta, s_ovf, s_d[3], s_fail, s_nb[2], s_unew;
   __shared__ int s_sp;
-  __shared__ KeyT s_stk_v[kBucketStack];
-  __shared__ int s_stk_l[kBucketStack];
-  __shared__ KeyT s_red_k[2 * (kBucketThreads / 32)];
+  __shared__ KeyT s_stk_lo[kBucketStack];  // pending sub-ranges [lo, hi) of the bucket
+  __shared__ KeyT s_stk_hi[kBucketStack];
+  __shared__ KeyT s_split[kSplitWays];
   __shared__ float s_ratio;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int B = 1 << a.bbits;
   const int rem = 2 * a.k - a.bbits;  // remainder bits below the bucket id
   const KeyT rmask = KeyOps<KeyT>::mask(rem);
+  const KeyT rtop = KeyOps<KeyT>::shl((KeyT)1, rem);  // end of the remainder range
   const KeyT EMPTY = ~(KeyT)0;
   const KeyT* __restrict__ keys = reinterpret_cast<const KeyT*>(a.keys);
   KeyT* __restrict__ tkeys = reinterpret_cast<KeyT*>(a.tkeys);
   const int hbins = a.t < kHistSmem ? a.t : kHistSmem;
   for (int i = tid; i < hbins; i += kBucketThreads) shist[i] = 0;
   if (tid == 0) s_ratio = 0.5f;  // running distinct/keys ratio of this CTA's buckets
-  const int slog_max = rem < 7 ? rem : 7;  // initial split guess (<= 128 sub-ranges)
+  const int slog_max = rem < 4 ? rem : 4;  // initial split guess (<= 16 sub-ranges)
 
   // the next bucket's ticket and extent are fetched while the current one is counted
   uint32_t next_beta = 0, next_base = 0, next_end = 0;
@@ -1000,17 +1064,18 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       continue;
     }
     // Sub-ranges of the bucket are counted one at a time, in key order.  A sub-range
-    // is the set of remainders whose top `plen` bits equal `pv`.  The first split
-    // guesses from the distinct/keys ratio seen so far; a sub-range whose distinct
-    // keys overflow the on-chip table is split at the first bit where its keys differ
-    // (a binary trie), so any skew terminates.
+    // is an interval [lo, hi) of remainders.  The first split guesses from the
+    // distinct/keys ratio seen so far; a sub-range whose distinct keys overflow the
+    // on-chip table is cut at quantiles of a sample of its distinct keys, so skewed
+    // buckets (a heavy k-mer and its error variants) split evenly.
     int slog = 0;
     while (slog < slog_max && (float)(n >> slog) * s_ratio * 1.2f > (float)HALF) slog++;
     if (tid == 0) {
       s_sp = 0;
+      const int psh0 = rem - slog;
       for (int j = (1 << slog) - 1; j >= 0; j--) {
-        s_stk_v[s_sp] = (KeyT)j;
-        s_stk_l[s_sp] = slog;
+        s_stk_lo[s_sp] = KeyOps<KeyT>::shl((KeyT)(uint32_t)j, psh0);
+        s_stk_hi[s_sp] = KeyOps<KeyT>::shl((KeyT)(uint32_t)(j + 1), psh0);
         s_sp++;
       }
       s_d[0] = s_d[1] = s_d[2] = 0;
@@ -1020,30 +1085,39 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
     bool failed = false;
     __syncthreads();
     while (s_sp > 0) {
-      const KeyT pv = s_stk_v[s_sp - 1];
-      const int plen = s_stk_l[s_sp - 1];
+      const KeyT lo = s_stk_lo[s_sp - 1];
+      const KeyT hi = s_stk_hi[s_sp - 1];
       __syncthreads();
       if (tid == 0) s_sp--;
       if (++attempts > kMaxBucketAttempts) { failed = true; break; }
-      const int psh = rem - plen;
+      const bool whole = lo == (KeyT)0 && hi == rtop;
+      // bits below the interval's common prefix (all its keys share the bits above)
+      const KeyT span = lo ^ (hi - (KeyT)1);
+      const int psh = span == (KeyT)0 ? 0 : KeyOps<KeyT>::top_bit(span) + 1;
       // table sized for the distinct keys expected (2.5x), at least 1024 slots; an
       // overflow splits the sub-range
       uint32_t Heff = 1024;
       {
         const float uest = (float)n * s_ratio * 2.5f;
         while ((float)Heff < uest && Heff < (uint32_t)H) Heff <<= 1;
-        if (plen > 0) Heff = H;
+        if (!whole) Heff = H;
       }
       const uint32_t hmask = Heff - 1;
       for (uint32_t i = tid; i < Heff; i += kBucketThreads) {
         skey[i] = EMPTY;
         scnt[i] = 0;
       }
-      if (tid == 0) s_ovf = 0;
+      if (tid == 0) {
+        s_ovf = 0;
+        s_unew = 0;
+      }
       __syncthreads();
-      // --- hash aggregation of this sub-range
+      // --- hash aggregation of this sub-range; it stops as soon as the distinct keys
+      //     exceed half the table (the sort needs the other half)
       constexpr int PF = 4;  // keys loaded per thread before inserting
+      const uint32_t ulimit = Heff / 2;
       for (uint32_t i0 = 0; i0 < n; i0 += PF * kBucketThreads) {
+        if (*(volatile uint32_t*)&s_ovf) break;
         KeyT rr[PF];
 #pragma unroll
         for (int q = 0; q < PF; q++) {
@@ -1053,8 +1127,11 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
 #pragma unroll
         for (int q = 0; q < PF; q++) {
           const KeyT r = rr[q];
-          const bool v = r != EMPTY && (plen == 0 || KeyOps<KeyT>::shr(r, psh) == pv);
-          if (v && !hash_insert<KeyT>(skey, scnt, hmask, r, 1u)) s_ovf = 1;
+          const bool v = r != EMPTY && (whole || (!(r < lo) && r < hi));
+          if (v) {
+            const int res = hash_insert<KeyT>(skey, scnt, hmask, r, 1u);
+            if (res == 2 || (res == 1 && atomicAdd(&s_unew, 1u) >= ulimit)) s_ovf = 1;
+          }
         }
       }
       __syncthreads();
@@ -1071,7 +1148,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       for (int q = 0; q < SPT; q++) {
         rk[q] = EMPTY;
         rc[q] = 0;
-        if (!ovf && (uint32_t)q < spt) {
+        if ((uint32_t)q < spt) {
           rk[q] = skey[q * kBucketThreads + tid];
           rc[q] = scnt[q * kBucketThreads + tid];
           occ += rk[q] != EMPTY;
@@ -1081,31 +1158,44 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       uint32_t off = block_exclusive_sum(occ, s_warp, u);
       if (u > Heff / 2) ovf = true;  // the sort needs a second half
       if (ovf) {
-        // split at the highest bit (below the prefix) where the sub-range's keys
-        // differ: OR and AND of the sub-range's remainders (overflow is rare, so they
-        // are gathered here rather than during the inserts)
-        KeyT kor = 0, kand = ~(KeyT)0;
-        for (uint32_t i = tid; i < n; i += kBucketThreads) {
-          const KeyT r = keys[base + i] & rmask;
-          if (plen == 0 || KeyOps<KeyT>::shr(r, psh) == pv) {
-            kor |= r;
-            kand &= r;
+        // cut [lo, hi) at quantiles of a sample of the distinct keys in the table
+        // (one per thread: the first occupied slot of its stride)
+        KeyT* samp = reinterpret_cast<KeyT*>(wc);  // kBucketThreads keys
+        KeyT mine = EMPTY;
+#pragma unroll
+        for (int q = SPT - 1; q >= 0; q--)
+          if (rk[q] != EMPTY) mine = rk[q];
+        samp[tid] = mine;
+        const int m = __syncthreads_count(mine != EMPTY);
+        const int ways = m < kSplitWays ? m : kSplitWays;
+        if (ways < 2) {
+          if (tid == 0) s_fail = 1;
+        } else if (mine != EMPTY) {
+          int rank = 0;
+          for (int j = 0; j < kBucketThreads; j++) {
+            const KeyT o = samp[j];
+            rank += (o != EMPTY && o < mine);
           }
+          // splitter w (1 <= w < ways) is the sample of rank floor(w * m / ways)
+          for (int w = 1; w < ways; w++)
+            if (rank == (w * m) / ways) s_split[w] = mine;
         }
-        block_or_and<KeyT>(kor, kand, s_red_k);
-        if (tid == 0) {
-          const KeyT diff = (kor ^ kand) & KeyOps<KeyT>::mask(psh);
-          if (diff == 0 || s_sp + 2 > kBucketStack) {
+        __syncthreads();
+        if (tid == 0 && !s_fail) {
+          if (s_sp + ways > kBucketStack) {
             s_fail = 1;
           } else {
-            const int bit = KeyOps<KeyT>::top_bit(diff);  // bit index from the bottom
-            const int clen = rem - bit;                   // child prefix length
-            const KeyT cp = KeyOps<KeyT>::shr(kand, bit + 1) << 1;  // common bits, then 0
-            s_stk_v[s_sp] = cp | (KeyT)1;
-            s_stk_l[s_sp] = clen;
-            s_stk_v[s_sp + 1] = cp;
-            s_stk_l[s_sp + 1] = clen;
-            s_sp += 2;
+            // push the pieces highest first, so the lowest is counted next
+            KeyT top = hi;
+            for (int w = ways - 1; w >= 1; w--) {
+              s_stk_lo[s_sp] = s_split[w];
+              s_stk_hi[s_sp] = top;
+              top = s_split[w];
+              s_sp++;
+            }
+            s_stk_lo[s_sp] = lo;
+            s_stk_hi[s_sp] = top;
+            s_sp++;
           }
         }
         __syncthreads();
@@ -1485,7 +1575,7 @@ __device__ uint32_t upper_bound_rows(const KeyT* __restrict__ kk, uint32_t lo, u
 // macro-nodes in key order.  A bucket larger than kMnCap rows is processed in
 // segments split at node-key pivots.
 template <typename KeyT>
-__global__ void __launch_bounds__(kMnThreads) k_macro_nodes(MnArgs a) {
+__global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
   using SM = MnSmem<KeyT>;
   extern __shared__ __align__(16) unsigned char smem[];
   KeyT* ikey = reinterpret_cast<KeyT*>(smem + SM::off_key);
@@ -1720,8 +1810,10 @@ cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st) {
 template <typename KeyT, bool SCATTER>
 static cudaError_t launch_extract_t(const CountArgs& a, KeyT* out, cudaStream_t st) {
   const size_t smem = sizeof(uint32_t) << a.bbits;
-  cudaError_t e = cudaFuncSetAttribute(k_extract<KeyT, SCATTER>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the attribute is shared by every thread launching this kernel, so it is always
+  // set to the largest histogram (15 partition digits), never to this launch's size
+  cudaError_t e = cudaFuncSetAttribute(k_extract<KeyT, SCATTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(uint32_t) << 15));
   if (e != cudaSuccess) return e;
   k_extract<KeyT, SCATTER><<<a.grid, kExtractThreads, smem, st>>>(a, out);
   return cudaGetLastError();
@@ -1777,6 +1869,23 @@ cudaError_t launch_scatter_fine(const void* in, const uint32_t* cstart, const ui
               : launch_fine_t<uint64_t>(reinterpret_cast<const uint64_t*>(in), cstart, slice_start, fcur,
                                         reinterpret_cast<uint64_t*>(out), k, bbits, cbits, ticket, cap, err,
                                         st);
+}
+
+cudaError_t launch_fine_count(const void* in, const uint32_t* cstart, const uint32_t* slice_start,
+                              uint32_t* bcount, int k, int bbits, int cbits, int wide, uint32_t* ticket,
+                              cudaStream_t st) {
+  if (wide)
+    k_fine_count<u128><<<sm_count() * 2, 512, 0, st>>>(reinterpret_cast<const u128*>(in), cstart, slice_start,
+                                                      bcount, k, bbits, cbits, ticket);
+  else
+    k_fine_count<uint64_t><<<sm_count() * 2, 512, 0, st>>>(reinterpret_cast<const uint64_t*>(in), cstart,
+                                                          slice_start, bcount, k, bbits, cbits, ticket);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prefix(uint32_t* counts, int B, cudaStream_t st) {
+  k_bucket_prefix<<<1, 1024, 0, st>>>(counts, B);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st) {

@@ -67,14 +67,14 @@ namespace {
 
 // Device bytes a request may need: the FASTA, two key arrays and the count array
 // over N windows, kept rows and the macro-node arrays over V kept k-mers.  N is
-// bounded by the FASTA size (a window needs at least one byte) and V by N; the
-// estimate takes N = F and V = N / 4 (a read set whose kept k-mers exceed that
-// still runs exactly, through the allocator's own budget check and a retry).
+// bounded by the FASTA size (a window needs at least one byte); V, the k-mers at or
+// above the cutoff, is taken as N / 8 (a read set whose kept k-mers exceed that still
+// runs exactly, through the allocator's own budget check and a retry).
 uint64_t footprint(const pk_request& r) {
   const uint64_t F = r.fasta_bytes;
   const uint64_t W = r.params.k > 32 ? 16 : 8;
   const uint64_t N = F;
-  const uint64_t V = N / 4;
+  const uint64_t V = N / 8;
   const uint64_t fixed = 64ull << 20;  // per-bucket tables, histograms, look-back flags
   return F + N * (2 * W + 4) + V * (W + 4) + 2 * V * (W + 32) + fixed;
 }

@@ -144,45 +144,59 @@ def _header_block(first_index: int, n: int):
 
 
 def matrix_to_fasta(mat: np.ndarray, first_index: int = 0) -> bytes:
-    """FASTA for equal-length reads given as an (n, L) uint8 ASCII matrix."""
+    """FASTA for equal-length reads given as an (n, L) uint8 ASCII matrix.  Reads whose
+    ids have the same number of digits form a regular block of records, so each block
+    is filled as a 2-D array."""
     n, L = mat.shape
     if n == 0:
         return b""
-    hb, hl = _header_block(first_index, n)
-    rec = hl + L + 1
-    off = np.zeros(n + 1, dtype=np.int64)
-    np.cumsum(rec, out=off[1:])
-    buf = np.empty(int(off[-1]), dtype=np.uint8)
-    hoff = np.zeros(n + 1, dtype=np.int64)
-    np.cumsum(hl, out=hoff[1:])
-    hpos = np.repeat(off[:-1] - hoff[:-1], hl) + np.arange(hb.size)
-    buf[hpos] = hb
-    spos = (off[:-1] + hl)[:, None] + np.arange(L)[None, :]
-    buf[spos] = mat
-    buf[off[1:] - 1] = ord("\n")
-    return buf.tobytes()
+    parts = []
+    lo = first_index
+    end = first_index + n
+    while lo < end:
+        d = len(str(lo))
+        hi = min(end, 10 ** d)
+        m = hi - lo
+        rec = np.empty((m, 3 + d + L + 1), dtype=np.uint8)
+        rec[:, 0] = ord(">")
+        rec[:, 1] = ord("r")
+        v = np.arange(lo, hi, dtype=np.int64)
+        for c in range(d - 1, -1, -1):
+            rec[:, 2 + c] = 48 + (v % 10)
+            v //= 10
+        rec[:, 2 + d] = ord("\n")
+        rec[:, 3 + d:3 + d + L] = mat[lo - first_index:hi - first_index]
+        rec[:, -1] = ord("\n")
+        parts.append(rec.reshape(-1))
+        lo = hi
+    return np.concatenate(parts).tobytes()
 
 
 def sample_read_matrix(rng, genome: np.ndarray, n_reads: int, read_len: int, err: float,
                        random_strand: bool = True, n_rate: float = 0.0) -> np.ndarray:
-    """Equal-length reads as an (n, L) ASCII matrix."""
+    """Equal-length reads as an (n, L) ASCII matrix: uniform start positions, random
+    strand, iid substitutions to one of the three other bases."""
     out = np.empty((n_reads, read_len), dtype=np.uint8)
+    win = np.lib.stride_tricks.sliding_window_view(genome, read_len)
     chunk = 1 << 18
     for c0 in range(0, n_reads, chunk):
         c1 = min(n_reads, c0 + chunk)
         m = c1 - c0
         starts = rng.integers(0, genome.size - read_len + 1, size=m)
-        codes = genome[starts[:, None] + np.arange(read_len)[None, :]]
+        codes = win[starts]
+        flat = codes.reshape(-1)
         if err > 0:
-            e = rng.random(codes.shape) < err
-            codes = np.where(e, (codes + rng.integers(1, 4, size=codes.shape)) & 3, codes)
+            ne = int(rng.binomial(flat.size, err))
+            pos = rng.integers(0, flat.size, size=ne)
+            flat[pos] = (flat[pos] + rng.integers(1, 4, size=ne).astype(np.uint8)) & 3
         if random_strand:
             rev = rng.random(m) < 0.5
-            codes = np.where(rev[:, None], 3 - codes[:, ::-1], codes)
+            codes[rev] = 3 - codes[rev, ::-1]
         asc = _ACGT[codes]
         if n_rate > 0:
-            nm = rng.random(asc.shape) < n_rate
-            asc = np.where(nm, np.uint8(_N), asc)
+            af = asc.reshape(-1)
+            nn = int(rng.binomial(af.size, n_rate))
+            af[rng.integers(0, af.size, size=nn)] = _N
         out[c0:c1] = asc
     return out
 

@@ -34,7 +34,7 @@ def test_golden_fixture(name):
     assert np.array_equal(mn.prefix_visits, g.mn_pre_visit)
 
 
-@pytest.mark.parametrize("bucket_bits", [2, 3, 6, 11])
+@pytest.mark.parametrize("bucket_bits", [2, 3, 6, 11, 16, 18])
 @pytest.mark.parametrize("name", ["k32_basic", "k63_basic", "k11_dense", "k32_ragged"])
 def test_golden_with_forced_partition(name, bucket_bits):
     """Few, large buckets force the multi-pass (split) path of the bucket kernel."""
