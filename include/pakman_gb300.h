@@ -247,6 +247,57 @@ pk_status pk_server_get_stats(pk_server* s, pk_server_stats* out);
 /* Device footprint the admission control assumes for a request (bytes). */
 uint64_t pk_request_footprint(const pk_request* req);
 
+/* ---- Batching: many independent read sets in one CUDA-graph launch ----------------
+ *
+ * (No reference counterpart: the reference runs one read set per MPI job.)  The whole
+ * count -> cutoff -> macro-node path of every set is captured once into one CUDA graph
+ * (sets spread over `branches` concurrent graph branches, each with buffers sized for
+ * its largest set) and replayed with a single launch while the batch's shape (set
+ * sizes and parameters) stays the same.  The partition digits of each size class are
+ * autotuned once (the fastest of the automatic choice and its neighbours, timed on
+ * the class's largest set) unless params.bucket_bits is set.  Inside the graph a set's
+ * window count is bounded by its size, its kept k-mers by 1/8 of that and all sets'
+ * macro-nodes by the batch output capacity; a set that exceeds a bound (or fails) is
+ * run again on its own, so every result equals the set run alone. */
+typedef struct pk_batch pk_batch;
+
+typedef struct pk_batch_set {
+  const char* fasta;          /* host FASTA of the set (pinned memory copies fastest) */
+  uint64_t fasta_bytes;
+  pk_params params;
+} pk_batch_set;
+
+typedef struct pk_batch_result {
+  pk_status status;           /* PK_OK, PK_ERR_EMPTY, PK_ERR_FORMAT, ... of this set */
+  int32_t rerun;              /* 1 if the set was run again outside the graph */
+  pk_summary summary;
+  uint64_t mn_first;          /* first row of this set in the batch's macro-node table */
+} pk_batch_result;
+
+typedef struct pk_batch_stats {
+  uint64_t graph_launches;    /* graph launches so far (one per pk_batch_run) */
+  uint64_t graph_captures;    /* captures (the shape changed) */
+  uint64_t kernels_per_launch;/* kernel nodes in the current graph */
+  uint64_t reruns;            /* sets run again on their own */
+  uint64_t tuned_classes;     /* size classes with autotuned partition digits */
+  uint64_t total_nodes;       /* rows of the last run's macro-node table */
+  double last_graph_ms;       /* device time of the last graph launch */
+  double tune_ms;             /* host time spent autotuning */
+} pk_batch_stats;
+
+pk_status pk_batch_create(pk_ctx* ctx, int32_t branches, pk_batch** out);
+void pk_batch_destroy(pk_batch* b);
+/* Runs all sets; results[i] describes set i, whose macro-node rows are
+ * [mn_first, mn_first + summary.n_nodes) of the batch table. */
+pk_status pk_batch_run(pk_batch* b, const pk_batch_set* sets, int32_t n_sets, pk_batch_result* results);
+/* The batch's macro-node table: every set's rows contiguous, at its mn_first (sets
+ * are not in set order); capacity in rows. */
+pk_status pk_batch_copy_macro_nodes(pk_batch* b, void* keys, uint32_t* suffix_counts,
+                                    uint32_t* prefix_counts, uint64_t capacity);
+pk_status pk_batch_get_stats(pk_batch* b, pk_batch_stats* out);
+/* Autotuned partition digits for a set of this size and k (0 if not tuned yet). */
+int32_t pk_batch_tuned_bits(pk_batch* b, uint64_t fasta_bytes, int32_t k);
+
 #ifdef __cplusplus
 }
 #endif

@@ -475,3 +475,89 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+@dataclass
+class BatchResult:
+    """One set of a batch: its status (0 = ok), summary and its rows of the batch's
+    macro-node table; `rerun` is True when it ran again outside the graph."""
+    status: int
+    rerun: bool
+    summary: Summary
+    mn_first: int
+
+
+class Batch:
+    """Many independent read sets in one CUDA-graph launch (``pk_batch_run``).  The
+    graph is captured on the first run of a batch shape and replayed while the shape
+    stays the same; partition digits are autotuned per size class."""
+
+    def __init__(self, ctx: Context, branches: int = 4):
+        self.ctx = ctx
+        h = c_void_p()
+        check(capi.lib().pk_batch_create(ctx.handle, branches, byref(h)), "pk_batch_create")
+        self._h = h
+        self._keep = None
+        self._k = 32
+
+    def run(self, sets) -> list:
+        """`sets`: sequence of (fasta, params).  Returns one BatchResult per set."""
+        n = len(sets)
+        arr = (capi.PkBatchSet * max(1, n))()
+        keep = []
+        for i, (fasta, params) in enumerate(sets):
+            buf = _as_bytes_ptr(fasta)
+            keep.append((fasta, buf))
+            arr[i].fasta = buf[0]
+            arr[i].fasta_bytes = buf[1]
+            arr[i].params = params
+            self._k = params.k
+        res = (capi.PkBatchResult * max(1, n))()
+        check(capi.lib().pk_batch_run(self._h, arr, n, res), "pk_batch_run")
+        self._keep = keep
+        return [BatchResult(r.status, bool(r.rerun), Summary.from_c(r.summary), r.mn_first) for r in res[:n]]
+
+    def table(self, out=None):
+        """(keys, suffix, prefix) of the last run, every set's rows at its mn_first."""
+        m = self.stats()["total_nodes"]
+        if out is None:
+            keys = np.empty(m, key_dtype(self._k))
+            suf = np.empty((m, 4), np.uint32)
+            pre = np.empty((m, 4), np.uint32)
+        else:
+            keys, suf, pre = out
+        check(capi.lib().pk_batch_copy_macro_nodes(self._h, keys.ctypes.data, suf.ctypes.data,
+                                                   pre.ctypes.data, min(keys.shape[0], suf.shape[0],
+                                                                        pre.shape[0])),
+              "pk_batch_copy_macro_nodes")
+        return keys[:m], suf[:m], pre[:m]
+
+    def macro_nodes(self, result: BatchResult, table, coverage: int) -> MacroNodeTable:
+        keys, suf, pre = table
+        a, m = result.mn_first, result.summary.n_nodes
+        return MacroNodeTable(keys[a:a + m], suf[a:a + m], pre[a:a + m], coverage, self._k)
+
+    def stats(self) -> Dict[str, float]:
+        s = capi.PkBatchStats()
+        check(capi.lib().pk_batch_get_stats(self._h, byref(s)), "pk_batch_get_stats")
+        return {n: getattr(s, n) for n, _ in capi.PkBatchStats._fields_}
+
+    def tuned_bits(self, fasta_bytes: int, k: int) -> int:
+        return int(capi.lib().pk_batch_tuned_bits(self._h, fasta_bytes, k))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.lib().pk_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

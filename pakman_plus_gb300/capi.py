@@ -57,6 +57,20 @@ class PkServerStats(ctypes.Structure):
                                         "admitted_bytes", "peak_admitted_bytes", "requeued")]
 
 
+class PkBatchSet(ctypes.Structure):
+    _fields_ = [("fasta", c_void_p), ("fasta_bytes", c_uint64), ("params", PkParams)]
+
+
+class PkBatchResult(ctypes.Structure):
+    _fields_ = [("status", c_int), ("rerun", c_int32), ("summary", PkSummary), ("mn_first", c_uint64)]
+
+
+class PkBatchStats(ctypes.Structure):
+    _fields_ = [("graph_launches", c_uint64), ("graph_captures", c_uint64),
+                ("kernels_per_launch", c_uint64), ("reruns", c_uint64), ("tuned_classes", c_uint64),
+                ("total_nodes", c_uint64), ("last_graph_ms", ctypes.c_double), ("tune_ms", ctypes.c_double)]
+
+
 class PakmanError(RuntimeError):
     """A failed C-ABI call; `status` is the pk_status code."""
 
@@ -132,6 +146,12 @@ _SIGS = {
     "pk_result_release": (c_int, [c_void_p, c_uint64]),
     "pk_server_get_stats": (c_int, [c_void_p, POINTER(PkServerStats)]),
     "pk_request_footprint": (c_uint64, [POINTER(PkRequest)]),
+    "pk_batch_create": (c_int, [c_void_p, c_int32, POINTER(c_void_p)]),
+    "pk_batch_destroy": (None, [c_void_p]),
+    "pk_batch_run": (c_int, [c_void_p, POINTER(PkBatchSet), c_int32, POINTER(PkBatchResult)]),
+    "pk_batch_copy_macro_nodes": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
+    "pk_batch_get_stats": (c_int, [c_void_p, POINTER(PkBatchStats)]),
+    "pk_batch_tuned_bits": (c_int32, [c_void_p, c_uint64, c_int32]),
     "pk_host_alloc": (c_int, [c_uint64, POINTER(c_void_p)]),
     "pk_host_free": (None, [c_void_p]),
 }

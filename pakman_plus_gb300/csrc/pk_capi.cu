@@ -15,6 +15,7 @@
 
 #include "../../include/pakman_gb300.h"
 #include "pk_internal.h"
+#include "pk_runtime.h"
 
 using namespace pk;
 
@@ -30,83 +31,15 @@ static pk_status fail(pk_status s, const std::string& msg) {
 
 pk_status pk::set_error(pk_status s, const std::string& msg) { return fail(s, msg); }
 
-#define PK_CUDA(call)                                                                     \
-  do {                                                                                    \
-    cudaError_t e_ = (call);                                                              \
-    if (e_ != cudaSuccess)                                                                \
-      return fail(e_ == cudaErrorMemoryAllocation ? PK_ERR_NOMEM : PK_ERR_CUDA,           \
-                  std::string(#call) + ": " + cudaGetErrorString(e_));                     \
-  } while (0)
 
-#define PK_TRY(expr)              \
-  do {                            \
-    pk_status s_ = (expr);        \
-    if (s_ != PK_OK) return s_;   \
-  } while (0)
-
-// ---------------------------------------------------------------- context -------
-struct pk_ctx {
-  int device = 0;
-  uint64_t budget = 0;
-  std::atomic<uint64_t> used{0};
-  cudaMemPool_t pool = nullptr;
-  int sms = 0;
-};
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-};
-
-enum Stage {
-  ST_H2D = 0,
-  ST_LINES,
-  ST_BUCKET_COUNT,
-  ST_OFFSETS,
-  ST_SCATTER,
-  ST_SCATTER_FINE,
-  ST_TABLE,
-  ST_CUTOFF,
-  ST_FILTER,
-  ST_MN,
-  ST_COUNT_
-};
-static const char* kStageNames[ST_COUNT_] = {"h2d",          "line_scan",      "bucket_count",
-                                             "bucket_offsets", "scatter_coarse", "scatter_fine",
-                                             "bucket_table", "cutoff",         "kept_filter",
-                                             "macro_nodes"};
-
-struct pk_job {
-  pk_ctx* ctx = nullptr;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  pk_params params{};
-  int wide = 0;
-  int bbits = 0;
-  int grid = 0;
-  unsigned long long chunk = 0;
-  uint64_t F = 0, N = 0;
-  int t_hist = 0;
-  int stage = 0;  // 0 none, 1 counted, 2 cutoff, 3 macro-nodes
-  uint64_t mn_cap = 0;
-  Scalars* d_sc = nullptr;
-  Scalars* h_sc = nullptr;  // pinned mirror
-  DevBuf fasta, tile_nl, counts, bstart, hstart, keys, tkeys, tcounts, tu, tsub, flags_m, hist, hist2,
-      nkeys, nsuf, npre, packed, doff, dkeys, dcounts, flags_f, kkeys, kcounts, kstart, kcount, ksub,
-      coff, cstart, slice_start, fcur;
-  bool dense_valid = false;
-  bool timing = false;
-  cudaEvent_t ev0[ST_COUNT_] = {}, ev1[ST_COUNT_] = {};
-  bool ev_rec[ST_COUNT_] = {};
-};
-
-static pk_status set_device(pk_ctx* c) {
+pk_status pk::set_device(pk_ctx* c) {
   PK_CUDA(cudaSetDevice(c->device));
   return PK_OK;
 }
 
-static pk_status job_alloc(pk_job* j, DevBuf& b, size_t bytes) {
+pk_status pk::job_alloc(pk_job* j, DevBuf& b, size_t bytes) {
   if (b.p && b.bytes >= bytes) return PK_OK;
+  if (j->graph_mode) return fail(PK_ERR_STATE, "batch buffers are smaller than a set needs");
   if (b.p) {
     PK_CUDA(cudaFreeAsync(b.p, j->stream));
     j->ctx->used -= b.bytes;
@@ -141,7 +74,7 @@ static void job_free(pk_job* j, DevBuf& b) {
   b.bytes = 0;
 }
 
-static void job_free_all(pk_job* j) {
+void pk::job_free_all(pk_job* j) {
   DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->hstart, &j->keys,  &j->tkeys,
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
@@ -164,8 +97,6 @@ static void mark_end(pk_job* j, int st) {
 }
 
 // ---------------------------------------------------------------- C ABI ---------
-extern "C" {
-
 void pk_params_default(pk_params* p) {
   if (!p) return;
   memset(p, 0, sizeof(*p));
@@ -352,7 +283,7 @@ void pk_host_free(void* p) {
   if (p) cudaFreeHost(p);
 }
 
-static pk_status check_params(const pk_params* p) {
+pk_status pk::check_params(const pk_params* p) {
   if (!p) return fail(PK_ERR_INVALID, "params is null");
   if (p->k < 2 || p->k > 64) return fail(PK_ERR_INVALID, "k must be in 2..64");
   if (p->lmer_length < 1 || p->lmer_length > 32) return fail(PK_ERR_INVALID, "lmer_length must be in 1..32");
@@ -366,7 +297,7 @@ static pk_status check_params(const pk_params* p) {
 // bucket holds a few thousand keys (the per-bucket kernel counts a bucket on chip).
 // The keys reach their buckets in two passes (kCoarseBits coarse regions, then fine
 // buckets inside each region), so the digit count is not tied to L2 capacity.
-static int auto_bucket_bits(uint64_t F, int k, int wide) {
+int pk::auto_bucket_bits(uint64_t F, int k, int wide) {
   // keys per bucket aimed at: large enough to amortise the per-bucket work of the
   // table and macro-node kernels, small enough that a bucket's distinct keys usually
   // fit one on-chip hash table (8192 64-bit or 4096 128-bit slots at load <= 1/2)
@@ -378,7 +309,7 @@ static int auto_bucket_bits(uint64_t F, int k, int wide) {
 }
 
 // Stages 1-5: device FASTA -> sorted (k-mer, count) table, resident.
-static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_params* p) {
+pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_params* p) {
   const int k = p->k;
   j->params = *p;
   j->wide = k > 32;
@@ -406,11 +337,13 @@ static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk
   PK_TRY(job_alloc(j, j->bstart, sizeof(uint32_t) * (B + 1)));
   if (hb < j->bbits) PK_TRY(job_alloc(j, j->hstart, sizeof(uint32_t) * (HB + 1)));
   uint32_t* hstart = (uint32_t*)(hb < j->bbits ? j->hstart.p : j->bstart.p);
-  Scalars init{};
-  memset(&init, 0, sizeof(init));
-  init.s0 = ~0ull;
-  *j->h_sc = init;
-  PK_CUDA(cudaMemcpyAsync(j->d_sc, j->h_sc, sizeof(Scalars), cudaMemcpyHostToDevice, j->stream));
+  if (!j->graph_mode) {
+    Scalars init{};
+    memset(&init, 0, sizeof(init));
+    init.s0 = ~0ull;
+    *j->h_sc = init;
+    PK_CUDA(cudaMemcpyAsync(j->d_sc, j->h_sc, sizeof(Scalars), cudaMemcpyHostToDevice, j->stream));
+  }
 
   CountArgs a{};
   a.fasta = (const uint8_t*)d_fasta;
@@ -436,13 +369,17 @@ static pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk
   mark_begin(j, ST_OFFSETS);
   PK_CUDA(launch_bucket_offsets(a, j->stream));
   mark_end(j, ST_OFFSETS);
-  // the key buffer is sized by the exact window count
-  PK_CUDA(cudaMemcpyAsync(j->h_sc, j->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost, j->stream));
-  PK_CUDA(cudaStreamSynchronize(j->stream));
-  if (j->h_sc->err & ERR_FORMAT)
-    return fail(PK_ERR_FORMAT, "a FASTA record start is not '>' (one '>' header line and one "
-                               "sequence line per record expected)");
-  const uint64_t N = j->h_sc->n_windows;
+  // the key buffer is sized by the exact window count (graph mode: by the bound the
+  // caller sized its buffers for)
+  uint64_t N = j->ncap;
+  if (!j->graph_mode) {
+    PK_CUDA(cudaMemcpyAsync(j->h_sc, j->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost, j->stream));
+    PK_CUDA(cudaStreamSynchronize(j->stream));
+    if (j->h_sc->err & ERR_FORMAT)
+      return fail(PK_ERR_FORMAT, "a FASTA record start is not '>' (one '>' header line and one "
+                                 "sequence line per record expected)");
+    N = j->h_sc->n_windows;
+  }
   if (N >= (1ull << 32) - 1)
     return fail(PK_ERR_LIMIT, "more than 2^32-2 k-mer windows in one job; split the input");
   j->N = N;
@@ -597,7 +534,7 @@ pk_status pk_table_load(pk_job* j, const void* keys, const uint32_t* counts, uin
   return PK_OK;
 }
 
-static pk_status sync_scalars(pk_job* j) {
+pk_status pk::sync_scalars(pk_job* j) {
   PK_CUDA(cudaMemcpyAsync(j->h_sc, j->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost, j->stream));
   PK_CUDA(cudaStreamSynchronize(j->stream));
   const uint32_t err = j->h_sc->err;
@@ -682,7 +619,7 @@ pk_status pk_table_device(pk_job* j, const void** k, const uint32_t** c) {
 }
 
 // cutoff on the device; no host synchronisation
-static pk_status cutoff_enqueue(pk_job* j, int t) {
+pk_status pk::cutoff_enqueue(pk_job* j, int t) {
   const unsigned long long* hist = (const unsigned long long*)j->hist.p;
   if (t != j->t_hist) {
     // histogram for a different -t than the one fused into counting
@@ -718,7 +655,7 @@ pk_status pk_cutoff(pk_job* j, int32_t t, uint32_t* cutoff, uint64_t* hist, uint
   return PK_OK;
 }
 
-static pk_status mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
+pk_status pk::mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
   const int B = 1 << j->bbits;
   const size_t W = j->wide ? 16 : 8;
   const uint64_t kcap = kept_bound ? kept_bound : 1;
@@ -771,6 +708,7 @@ static pk_status mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) 
   m.nsuf = (uint32_t*)j->nsuf.p;
   m.npre = (uint32_t*)j->npre.p;
   m.cap = cap;
+  m.kcap = kcap;
   m.k = j->params.k;
   m.bbits = j->bbits;
   m.sc = j->d_sc;
@@ -857,4 +795,3 @@ pk_status pk_run_device(pk_job* j, const void* d_fasta, uint64_t n, const pk_par
   return run_rest(j, p, out);
 }
 
-}  // extern "C"

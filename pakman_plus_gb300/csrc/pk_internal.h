@@ -120,6 +120,7 @@ struct MnArgs {
   uint32_t* nsuf;            // 4 * cap
   uint32_t* npre;            // 4 * cap
   unsigned long long cap;
+  unsigned long long kcap;   // kept rows the kept buffers hold
   int k;
   int bbits;
   Scalars* sc;
@@ -132,6 +133,10 @@ cudaError_t launch_fine_count(const void* in, const uint32_t* cstart, const uint
                               uint32_t* bcount, int k, int bbits, int cbits, int wide, uint32_t* ticket,
                               cudaStream_t st);
 cudaError_t launch_prefix(uint32_t* counts, int B, cudaStream_t st);
+// batch: reserve a set's rows in the batch macro-node table and copy them there
+cudaError_t launch_batch_emit(const Scalars* sc, unsigned long long* counter, unsigned long long cap,
+                              unsigned long long* res, const void* nkeys, const void* nsuf, const void* npre,
+                              int wide, void* okeys, void* osuf, void* opre, cudaStream_t st);
 cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st);
 cudaError_t launch_scatter(const CountArgs& a, void* keys_out, int wide, cudaStream_t st);
 // Two-pass partition: coarse regions (pass 1) then fine buckets inside each region.

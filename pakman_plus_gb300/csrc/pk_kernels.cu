@@ -1597,6 +1597,12 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
   KeyT* __restrict__ nkeys = reinterpret_cast<KeyT*>(a.nkeys);
   constexpr uint32_t CAP = kMnCap - 16;  // rows per segment before ties
 
+  // kept rows beyond the kept buffers were not written: nothing to merge (every CTA
+  // reads the same flag, so all of them leave)
+  if (tid == 0) s_beta = (a.sc->err & ERR_BOUNDS) ? 1u : 0u;
+  __syncthreads();
+  if (s_beta) return;
+
   while (true) {
     __syncthreads();
     if (tid == 0) s_beta = atomicAdd(&a.sc->ticket_mn, 1u);
@@ -1613,6 +1619,11 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
         s_cur[f + 1] = b0 + (d == 0 ? 0u : a.ksub[3 * bp + d - 1]);
         s_end[f + 1] = b0 + (d == 3 ? a.kcount[bp] : a.ksub[3 * bp + d]);
       }
+      for (int st = 0; st < 5; st++)
+        if (s_end[st] > a.kcap || s_cur[st] > s_end[st]) {  // never read past the kept rows
+          atomicOr(&a.sc->err, ERR_BOUNDS);
+          s_cur[st] = s_end[st] = 0;
+        }
     }
     if (tid == 0)
       for (int st = 0; st < 5; st++) s_beg[st] = s_cur[st];
@@ -1812,9 +1823,13 @@ static cudaError_t launch_extract_t(const CountArgs& a, KeyT* out, cudaStream_t 
   const size_t smem = sizeof(uint32_t) << a.bbits;
   // the attribute is shared by every thread launching this kernel, so it is always
   // set to the largest histogram (15 partition digits), never to this launch's size
-  cudaError_t e = cudaFuncSetAttribute(k_extract<KeyT, SCATTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(sizeof(uint32_t) << 15));
-  if (e != cudaSuccess) return e;
+  static bool attr_set = false;  // same value from every thread, so a race is benign
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_extract<KeyT, SCATTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(uint32_t) << 15));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
   k_extract<KeyT, SCATTER><<<a.grid, kExtractThreads, smem, st>>>(a, out);
   return cudaGetLastError();
 }
@@ -1827,9 +1842,12 @@ cudaError_t launch_bucket_count(const CountArgs& a, int wide, cudaStream_t st) {
 template <typename KeyT>
 static cudaError_t launch_coarse_t(const CountArgs& a, const uint32_t* coff, KeyT* out, cudaStream_t st) {
   const size_t smem = CoarseCfg<KeyT>::smem;
-  cudaError_t e = cudaFuncSetAttribute(k_scatter_coarse<KeyT>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+  static bool attr_set = false;  // a constant, so concurrent first calls agree
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_scatter_coarse<KeyT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
   k_scatter_coarse<KeyT><<<a.grid, kExtractThreads, smem, st>>>(a, coff, out);
   return cudaGetLastError();
 }
@@ -1853,9 +1871,12 @@ static cudaError_t launch_fine_t(const KeyT* in, const uint32_t* cstart, const u
                                  uint32_t* fcur, KeyT* out, int k, int bbits, int cbits, uint32_t* ticket,
                                  unsigned long long cap, uint32_t* err, cudaStream_t st) {
   const size_t smem = FineCfg<KeyT>::smem;
-  cudaError_t e = cudaFuncSetAttribute(k_scatter_fine<KeyT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
+  static bool attr_set = false;  // a constant, so concurrent first calls agree
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_scatter_fine<KeyT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
   k_scatter_fine<KeyT><<<sm_count() * 2, FineCfg<KeyT>::T, smem, st>>>(in, cstart, slice_start, fcur, out,
                                                                         k, bbits, cbits, ticket, cap, err);
   return cudaGetLastError();
@@ -1903,9 +1924,12 @@ cudaError_t launch_scatter(const CountArgs& a, void* keys_out, int wide, cudaStr
 template <typename KeyT>
 static cudaError_t launch_bucket_t(const BucketArgs& a, int grid, cudaStream_t st) {
   const size_t smem = BucketSmem<KeyT>::bytes;
-  cudaError_t e = cudaFuncSetAttribute(k_bucket_table<KeyT>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+  static bool attr_set = false;  // a constant, so concurrent first calls agree
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_bucket_table<KeyT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
   if (grid <= 0) grid = sm_count() * bucket_ctas_per_sm(sizeof(KeyT) == 16);
   k_bucket_table<KeyT><<<grid, kBucketThreads, smem, st>>>(a);
   return cudaGetLastError();
@@ -1943,9 +1967,12 @@ cudaError_t launch_filter_kept(const FilterArgs& a, int wide, int grid, cudaStre
 template <typename KeyT>
 static cudaError_t launch_mn_t(const MnArgs& a, int grid, cudaStream_t st) {
   const size_t smem = MnSmem<KeyT>::bytes;
-  cudaError_t e = cudaFuncSetAttribute(k_macro_nodes<KeyT>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+  static bool attr_set = false;  // a constant, so concurrent first calls agree
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_macro_nodes<KeyT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
   if (grid <= 0) grid = sm_count() * mn_ctas_per_sm(sizeof(KeyT) == 16);
   k_macro_nodes<KeyT><<<grid, kMnThreads, smem, st>>>(a);
   return cudaGetLastError();
@@ -2010,4 +2037,57 @@ cudaError_t launch_table_bounds(const void* keys, unsigned long long n, int bbit
   }
   return cudaGetLastError();
 }
+}  // namespace pk
+
+// ----------------------------------------------------------------- batch output ----
+namespace pk {
+
+// One set of a captured batch: reserve its rows in the batch's macro-node table.
+// res = {first row, rows, state}; state 1 ok, 2 table full, 3 device error, 4 nothing kept.
+__global__ void k_batch_reserve(const Scalars* sc, unsigned long long* counter, unsigned long long cap,
+                                unsigned long long* res) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (sc->err != 0) {
+    res[0] = 0; res[1] = 0; res[2] = 3;
+    return;
+  }
+  if (sc->n_kept == 0) {
+    res[0] = 0; res[1] = 0; res[2] = 4;
+    return;
+  }
+  const unsigned long long m = sc->n_nodes;
+  const unsigned long long off = atomicAdd(counter, m);
+  if (off + m > cap) {
+    res[0] = 0; res[1] = 0; res[2] = 2;
+    return;
+  }
+  res[0] = off; res[1] = m; res[2] = 1;
+}
+
+// Copy the set's nodes (key words, 4 suffix and 4 prefix counts) to its reserved rows.
+__global__ void __launch_bounds__(256) k_batch_copy(const unsigned long long* __restrict__ nkeys,
+                                                    const uint4* __restrict__ nsuf,
+                                                    const uint4* __restrict__ npre, int key_words,
+                                                    const unsigned long long* res,
+                                                    unsigned long long* okeys, uint4* osuf, uint4* opre) {
+  if (res[2] != 1) return;
+  const unsigned long long off = res[0], m = res[1];
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < m;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    for (int w = 0; w < key_words; w++) okeys[(off + i) * key_words + w] = nkeys[i * key_words + w];
+    osuf[off + i] = nsuf[i];
+    opre[off + i] = npre[i];
+  }
+}
+
+cudaError_t launch_batch_emit(const Scalars* sc, unsigned long long* counter, unsigned long long cap,
+                              unsigned long long* res, const void* nkeys, const void* nsuf, const void* npre,
+                              int wide, void* okeys, void* osuf, void* opre, cudaStream_t st) {
+  k_batch_reserve<<<1, 32, 0, st>>>(sc, counter, cap, res);
+  k_batch_copy<<<sm_count() * 2, 256, 0, st>>>((const unsigned long long*)nkeys, (const uint4*)nsuf,
+                                               (const uint4*)npre, wide ? 2 : 1, res,
+                                               (unsigned long long*)okeys, (uint4*)osuf, (uint4*)opre);
+  return cudaGetLastError();
+}
+
 }  // namespace pk

@@ -326,8 +326,8 @@ def config4_set(index: int, scale: float = 1.0) -> ReadSet:
     cov = int(g.integers(20, 81))
     genome = random_genome(g, glen, 0.5)
     n = max(1, int(round(cov * glen / rl)))
-    reads = sample_reads(g, genome, n, rl, 0.005)
-    return ReadSet(f"batch-set-{index}", reads_to_fasta(reads), 32, cov, rl, n, glen)
+    mat = sample_read_matrix(g, genome, n, rl, 0.005)
+    return ReadSet(f"batch-set-{index}", matrix_to_fasta(mat), 32, cov, rl, n, glen)
 
 
 def config5_job(index: int, scale: float = 1.0) -> ReadSet:

@@ -75,3 +75,11 @@ def test_serving_structs_and_footprint(lib):
     assert lib.pk_request_footprint(None) == 0
     assert lib.pk_server_create(None, 2, None) == capi.PK_ERR_INVALID
     assert lib.pk_submit(None, None, None) == capi.PK_ERR_INVALID
+
+
+def test_batch_structs(lib):
+    assert ctypes.sizeof(capi.PkBatchSet) == 8 + 8 + 64
+    assert ctypes.sizeof(capi.PkBatchResult) == 4 + 4 + 48 + 8
+    assert ctypes.sizeof(capi.PkBatchStats) == 6 * 8 + 2 * 8
+    assert lib.pk_batch_create(None, 2, None) == capi.PK_ERR_INVALID
+    assert lib.pk_batch_tuned_bits(None, 100, 32) == 0
