@@ -143,6 +143,29 @@ pk_status pk_macro_nodes_device(pk_job* job, const void** d_keys, const uint32_t
 pk_status pk_run(pk_job* job, const char* fasta, uint64_t n, const pk_params* p, pk_summary* out);
 pk_status pk_run_device(pk_job* job, const void* d_fasta, uint64_t n, const pk_params* p,
                         pk_summary* out);
+/* ---- initial wiring: replaces initiate_mnode_wiring (src/wire.cpp:66-121) ---------
+ * Per macro-node, MacroNode::setup_wiring (includes/distribute_kmers.h:549-655) after a
+ * terminal entry is appended to both lists.  List entries: the present extensions in
+ * ascending base code, then the terminal one (visit max(other side's visit sum - own
+ * side's, 0)).  wire[w] = {suffix list index, offset in that suffix's visits, visits};
+ * prefix_begin[p] = {first wire of prefix p, its wires}; unused entries are 0, as in
+ * the reference.  The reference leaves the order of equal-ranked prefixes to an
+ * unstable sort; here equal entries keep list order. */
+typedef struct pk_wiring {
+  int32_t n_suffixes;             /* list sizes including the terminal entry */
+  int32_t n_prefixes;
+  int32_t terminal_suffix_visit;
+  int32_t terminal_prefix_visit;
+  int32_t n_wires;
+  int32_t wire[9][3];
+  int32_t prefix_begin[5][2];
+} pk_wiring;
+
+/* After pk_build_macro_nodes; coverage 0 uses the job's params.coverage. */
+pk_status pk_wire_macro_nodes(pk_job* job, int32_t coverage);
+pk_status pk_copy_wiring(pk_job* job, pk_wiring* out, uint64_t capacity);
+pk_status pk_wiring_device(pk_job* job, const pk_wiring** d_wiring);
+
 pk_status pk_summary_get(pk_job* job, pk_summary* out);
 
 /* ---- per-kernel timing (CUDA events on the job's stream) ---------------------------- */

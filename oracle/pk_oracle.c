@@ -522,4 +522,82 @@ int pko_visit(int count, int coverage) {
   return q;
 }
 
+/*
+ * Initial wiring of macro-nodes (src/wire.cpp:66-121 with MacroNode::setup_wiring,
+ * includes/distribute_kmers.h:549-655).  Per node the suffix list holds the present
+ * extensions in ascending base code then one terminal entry, the prefix list likewise
+ * (the reference's suffix lists come out in that order; its prefix order is left to an
+ * unstable sort, so ties below are broken in this canonical order).  Each entry has a
+ * (count, visit) pair; a terminal gets count 1 and visit max(other side's visit sum -
+ * own side's, 0).  Entries are ranked by visit, then count, both descending (Comp_rev,
+ * :495-506; the lists have at most 5 entries, where std::sort is an insertion sort and
+ * keeps equal entries in list order), and a two-pointer walk pairs prefix visits with
+ * suffix visits: wire w = (suffix list index, offset into that suffix's visits, count);
+ * when a prefix is used up, begin[prefix] = (index of its first wire, its wires).
+ * Wires and begin entries that are never set stay 0, as in the reference.
+ */
+typedef struct {
+  int32_t ns, np;             /* list sizes including the terminal entry */
+  int32_t term_suf, term_pre; /* visits of the terminal entries */
+  int32_t nw;                 /* wires written */
+  int32_t wire[9][3];         /* suffix_id, offset_in_suffix, count */
+  int32_t begin[5][2];        /* prefix_pos, num_wires */
+} pko_wire;
+
+static void rank_entries(const int32_t* cnt, const int32_t* vis, int n, int* order) {
+  for (int i = 0; i < n; i++) order[i] = i;
+  for (int i = 1; i < n; i++) { /* insertion sort, equal entries keep their order */
+    int x = order[i], j = i - 1;
+    while (j >= 0 && (vis[x] > vis[order[j]] || (vis[x] == vis[order[j]] && cnt[x] > cnt[order[j]]))) {
+      order[j + 1] = order[j];
+      j--;
+    }
+    order[j + 1] = x;
+  }
+}
+
+int pko_wire_nodes(const uint32_t* suf, const uint32_t* pre, size_t m, int coverage, pko_wire* out) {
+  if (coverage == 0) return PKO_EARG;
+  for (size_t nidx = 0; nidx < m; nidx++) {
+    pko_wire* w = &out[nidx];
+    memset(w, 0, sizeof(*w));
+    int32_t scnt[5], svis[5], pcnt[5], pvis[5];
+    int ns = 0, np = 0, sc = 0, pc = 0;
+    for (int e = 0; e < 4; e++) {
+      const uint32_t c = suf[4 * nidx + e];
+      if (c) { scnt[ns] = (int32_t)c; svis[ns] = pko_visit((int)c, coverage); sc += svis[ns]; ns++; }
+    }
+    for (int e = 0; e < 4; e++) {
+      const uint32_t c = pre[4 * nidx + e];
+      if (c) { pcnt[np] = (int32_t)c; pvis[np] = pko_visit((int)c, coverage); pc += pvis[np]; np++; }
+    }
+    scnt[ns] = 1; svis[ns] = pc - sc > 0 ? pc - sc : 0; ns++;
+    pcnt[np] = 1; pvis[np] = sc - pc > 0 ? sc - pc : 0; np++;
+    w->ns = ns; w->np = np; w->term_suf = svis[ns - 1]; w->term_pre = pvis[np - 1];
+    int os[5], op[5];
+    rank_entries(scnt, svis, ns, os);
+    rank_entries(pcnt, pvis, np, op);
+    int leftover = sc + svis[ns - 1];
+    int off_s[5] = {0, 0, 0, 0, 0};
+    int top_p = 0, top_s = 0, var_p = 0, var_s = 0, wi = 0, p_size = 0, last_pid = -1, begin_pos = -1;
+    while (leftover > 0 && wi < 9) {
+      const int sid = os[top_s], pid = op[top_p];
+      const int a = pvis[pid] - var_p, b = svis[sid] - var_s;
+      const int cnt = a < b ? a : b;
+      w->wire[wi][0] = sid; w->wire[wi][1] = off_s[sid]; w->wire[wi][2] = cnt;
+      if (last_pid != pid) { begin_pos = wi; last_pid = pid; }
+      p_size++; wi++;
+      leftover -= cnt; var_p += cnt; var_s += cnt; off_s[sid] += cnt;
+      if (var_p == pvis[pid]) {
+        var_p = 0; top_p++;
+        w->begin[pid][0] = begin_pos; w->begin[pid][1] = p_size;
+        p_size = 0;
+      }
+      if (var_s == svis[sid]) { var_s = 0; top_s++; }
+    }
+    w->nw = wi;
+  }
+  return PKO_OK;
+}
+
 void pko_free(void* p) { free(p); }

@@ -82,6 +82,7 @@ def lib():
                                       ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
                                       ctypes.POINTER(sz), ctypes.POINTER(sz)]
         L.pko_visit.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.pko_wire_nodes.argtypes = [vp, vp, sz, ctypes.c_int, vp]
         L.pko_free.argtypes = [vp]
         _lib = L
     return _lib
@@ -177,6 +178,63 @@ def macro_nodes(table: Table, k: int, cut: int) -> MacroNodes:
                       _take(np_.value, 4 * M, np.uint32).reshape(M, 4), v.value)
 
 
+# one node's initial wiring (pko_wire in pk_oracle.c)
+WIRE_DTYPE = np.dtype([("ns", "<i4"), ("np", "<i4"), ("term_suf", "<i4"), ("term_pre", "<i4"),
+                       ("nw", "<i4"), ("wire", "<i4", (9, 3)), ("begin", "<i4", (5, 2))])
+
+
+def wire(suf: np.ndarray, pre: np.ndarray, coverage: int) -> np.ndarray:
+    """Initial wiring of every node of a macro-node table (suf/pre: (M, 4) counts)."""
+    L = lib()
+    suf = np.ascontiguousarray(suf, dtype=np.uint32)
+    pre = np.ascontiguousarray(pre, dtype=np.uint32)
+    m = suf.shape[0]
+    out = np.zeros(max(1, m), WIRE_DTYPE)
+    rc = L.pko_wire_nodes(suf.ctypes.data, pre.ctypes.data, m, int(coverage), out.ctypes.data)
+    if rc != PKO_OK:
+        raise OracleError(rc, "pko_wire_nodes")
+    return out[:m]
+
+
+def read_wire_dump(path: str):
+    """The reference's wiring dump as WIRE_DTYPE rows plus each node's list order:
+    (wiring, suffix_exts, prefix_exts) where *_exts[i] lists the entries' base codes
+    in the reference's order (4 = terminal)."""
+    data = open(path, "rb").read()
+    assert data[:4] == b"PKW1"
+    m = int.from_bytes(data[4:12], "little")
+    off = 12
+    out = np.zeros(m, WIRE_DTYPE)
+    sexts, pexts = [], []
+    for i in range(m):
+        lists = []
+        for side in range(2):
+            n = int.from_bytes(data[off:off + 4], "little")
+            off += 4
+            ent = np.frombuffer(data, np.dtype([("ext", "u1"), ("count", "<i4"), ("visit", "<i4")]), n, off)
+            off += 9 * n
+            lists.append(ent)
+        nw = int.from_bytes(data[off:off + 4], "little")
+        off += 4
+        wires = np.frombuffer(data, "<i4", 3 * nw, off).reshape(nw, 3)
+        off += 12 * nw
+        nb = int.from_bytes(data[off:off + 4], "little")
+        off += 4
+        beg = np.frombuffer(data, "<i4", 2 * nb, off).reshape(nb, 2)
+        off += 8 * nb
+        s, p = lists
+        out[i]["ns"], out[i]["np"] = len(s), len(p)
+        out[i]["term_suf"] = int(s["visit"][s["ext"] == 0xff][0])
+        out[i]["term_pre"] = int(p["visit"][p["ext"] == 0xff][0])
+        used = int(np.count_nonzero(wires[:, 2]))
+        out[i]["nw"] = used
+        out[i]["wire"][:min(9, nw)] = wires[:9]
+        out[i]["begin"][:min(5, nb)] = beg[:5]
+        sexts.append([4 if e == 0xff else int(e) for e in s["ext"]])
+        pexts.append([4 if e == 0xff else int(e) for e in p["ext"]])
+    return out, sexts, pexts
+
+
 def visit(count_: int, coverage: int) -> int:
     return lib().pko_visit(int(count_), int(coverage))
 
@@ -219,6 +277,7 @@ class RefRun:
     aborted: bool
     seconds: dict
     stdout: str
+    wiring: Optional[tuple] = None  # read_wire_dump(): (WIRE_DTYPE rows, suffix exts, prefix exts)
 
 
 def read_table_dump(path: str):
@@ -310,4 +369,5 @@ def run_reference(fasta: bytes, k: int, read_len: int, coverage: int, t: int = 2
         if aborted or not want_mn or not os.path.exists(out + ".mn"):
             return RefRun(tk, tc, cut, kept, None, None, None, None, None, True, aborted, secs, txt)
         mk, ms, mp, sv, pv, ok = read_mn_dump(out + ".mn", coverage)
-        return RefRun(tk, tc, cut, kept, mk, ms, mp, sv, pv, ok, aborted, secs, txt)
+        wires = read_wire_dump(out + ".wire") if os.path.exists(out + ".wire") else None
+        return RefRun(tk, tc, cut, kept, mk, ms, mp, sv, pv, ok, aborted, secs, txt, wires)

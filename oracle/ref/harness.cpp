@@ -18,6 +18,11 @@
 //                    u64 lo, u64 hi, u32 k1len, k1len x u8 base,
 //                    u32 nsuf, nsuf x {u8 ext, i32 count, i32 visit, u8 term},
 //                    u32 npre, npre x {u8 ext, i32 count, i32 visit, u8 term}
+// OUT_PREFIX.wire  : "PKW1" u64 M, per node after initiate_mnode_wiring
+//                    (src/wire.cpp:66-121): for suffixes then prefixes u32 n,
+//                    n x {u8 ext (0xff = terminal), i32 count, i32 visit};
+//                    u32 nw, nw x {i32 suffix_id, i32 offset_in_suffix, i32 count};
+//                    u32 np, np x {i32 prefix_pos, i32 num_wires}
 // stdout last line : {"count_s": .., "mn_s": .., "U": .., "M": ..}
 #include <stdio.h>
 #include <stdint.h>
@@ -114,6 +119,43 @@ int main(int argc, char** argv) {
       }
       put_ext_list(f, mn.suffixes, mn.suffix_count, mn.suffixes_terminal);
       put_ext_list(f, mn.prefixes, mn.prefix_count, mn.prefixes_terminal);
+    }
+    fclose(f);
+  }
+  // initial wiring on the same map, then its dump
+  initiate_mnode_wiring(MN_map);
+  {
+    FILE* f = fopen((out + ".wire").c_str(), "wb");
+    uint64_t m = MN_map.size();
+    fwrite("PKW1", 1, 4, f);
+    fwrite(&m, 8, 1, f);
+    for (const auto& kv : MN_map) {
+      const MacroNode& mn = kv.second;
+      const std::vector<BasePairVector>* lists[2] = {&mn.suffixes, &mn.prefixes};
+      const std::vector<std::pair<int, int>>* counts[2] = {&mn.suffix_count, &mn.prefix_count};
+      for (int side = 0; side < 2; side++) {
+        uint32_t n = (uint32_t)lists[side]->size();
+        fwrite(&n, 4, 1, f);
+        for (uint32_t i = 0; i < n; i++) {
+          uint8_t e = (*lists[side])[i].size() ? (uint8_t)(*lists[side])[i][0] : (uint8_t)0xff;
+          int32_t c = (*counts[side])[i].first, v = (*counts[side])[i].second;
+          fwrite(&e, 1, 1, f);
+          fwrite(&c, 4, 1, f);
+          fwrite(&v, 4, 1, f);
+        }
+      }
+      uint32_t nw = (uint32_t)mn.wiring_info.size();
+      fwrite(&nw, 4, 1, f);
+      for (const WireInfo& w : mn.wiring_info) {
+        int32_t a[3] = {w.suffix_id, w.offset_in_suffix, w.count};
+        fwrite(a, 4, 3, f);
+      }
+      uint32_t np = (uint32_t)mn.prefix_begin_info.size();
+      fwrite(&np, 4, 1, f);
+      for (const PrefixInfo& pi : mn.prefix_begin_info) {
+        int32_t a[2] = {pi.prefix_pos, pi.num_wires};
+        fwrite(a, 4, 2, f);
+      }
     }
     fclose(f);
   }

@@ -28,6 +28,9 @@ from .capi import EmptyAfterCutoff, FormatError, PakmanError, check, default_par
 KEY128 = np.dtype([("lo", "<u8"), ("hi", "<u8")])
 KMERPAIRS64 = np.dtype([("seq", "<u8"), ("k_count", "<i4")])  # packed, 12 bytes
 KMERPAIRS128 = np.dtype([("seq_lo", "<u8"), ("seq_hi", "<u8"), ("k_count", "<i4")])  # 20 bytes
+# pk_wiring: one macro-node's initial wiring
+WIRING = np.dtype([("ns", "<i4"), ("np", "<i4"), ("term_suf", "<i4"), ("term_pre", "<i4"), ("nw", "<i4"),
+                   ("wire", "<i4", (9, 3)), ("begin", "<i4", (5, 2))])
 
 
 def key_dtype(k: int):
@@ -237,6 +240,15 @@ class Job:
                                              pre.ctypes.data, cap), "pk_copy_macro_nodes")
         cov = coverage if coverage is not None else self.params.coverage
         return MacroNodeTable(keys[:m], suf[:m], pre[:m], cov, self.params.k)
+
+    # -- initial wiring
+    def wire(self, coverage: int = 0) -> np.ndarray:
+        """Initial wiring of every macro-node (WIRING rows, in node order)."""
+        check(capi.lib().pk_wire_macro_nodes(self._h, coverage), "pk_wire_macro_nodes")
+        m = self.summary().n_nodes
+        out = np.zeros(max(1, m), WIRING)
+        check(capi.lib().pk_copy_wiring(self._h, out.ctypes.data, m), "pk_copy_wiring")
+        return out[:m]
 
     # -- whole path
     def run(self, fasta, params: capi.PkParams) -> Summary:

@@ -71,6 +71,12 @@ class PkBatchStats(ctypes.Structure):
                 ("total_nodes", c_uint64), ("last_graph_ms", ctypes.c_double), ("tune_ms", ctypes.c_double)]
 
 
+class PkWiring(ctypes.Structure):
+    _fields_ = [("n_suffixes", c_int32), ("n_prefixes", c_int32), ("terminal_suffix_visit", c_int32),
+                ("terminal_prefix_visit", c_int32), ("n_wires", c_int32), ("wire", (c_int32 * 3) * 9),
+                ("prefix_begin", (c_int32 * 2) * 5)]
+
+
 class PakmanError(RuntimeError):
     """A failed C-ABI call; `status` is the pk_status code."""
 
@@ -131,6 +137,9 @@ _SIGS = {
     "pk_run_device": (c_int, [c_void_p, c_void_p, c_uint64, POINTER(PkParams),
                               POINTER(PkSummary)]),
     "pk_summary_get": (c_int, [c_void_p, POINTER(PkSummary)]),
+    "pk_wire_macro_nodes": (c_int, [c_void_p, c_int32]),
+    "pk_copy_wiring": (c_int, [c_void_p, c_void_p, c_uint64]),
+    "pk_wiring_device": (c_int, [c_void_p, POINTER(c_void_p)]),
     "pk_job_enable_timing": (c_int, [c_void_p, c_int]),
     "pk_job_stage_times": (c_int, [c_void_p, POINTER(c_float), c_int, POINTER(c_int)]),
     "pk_stage_name": (c_char_p, [c_int]),

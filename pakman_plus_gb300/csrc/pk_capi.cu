@@ -79,7 +79,7 @@ void pk::job_free_all(pk_job* j) {
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
-                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur};
+                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring};
   for (DevBuf* b : all) job_free(j, *b);
   j->dense_valid = false;
 }
@@ -228,6 +228,7 @@ pk_status pk_job_reset(pk_job* j) {
   PK_TRY(set_device(j->ctx));
   job_free_all(j);
   j->stage = 0;
+  j->wired = false;
   PK_CUDA(cudaStreamSynchronize(j->stream));
   return PK_OK;
 }
@@ -245,7 +246,7 @@ pk_status pk_job_memory(pk_job* j, uint64_t* bytes) {
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
-                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur};
+                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring};
   uint64_t s = 0;
   for (DevBuf* b : all) s += b->bytes;
   *bytes = s;
@@ -315,6 +316,7 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   j->wide = k > 32;
   j->F = n;
   j->stage = 0;
+  j->wired = false;
   const int W = j->wide ? 16 : 8;
   const int bb = p->bucket_bits ? std::min(p->bucket_bits, std::min(kMaxPartitionBits, 2 * k - 2))
                                 : auto_bucket_bits(n, k, j->wide);
@@ -716,6 +718,7 @@ pk_status pk::mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
   PK_CUDA(launch_macro_nodes(m, j->wide, 0, j->stream));
   mark_end(j, ST_MN);
   j->stage = 3;
+  j->wired = false;
   return PK_OK;
 }
 
@@ -755,6 +758,39 @@ pk_status pk_macro_nodes_device(pk_job* j, const void** k, const uint32_t** s, c
   if (k) *k = j->nkeys.p;
   if (s) *s = (const uint32_t*)j->nsuf.p;
   if (p) *p = (const uint32_t*)j->npre.p;
+  return PK_OK;
+}
+
+pk_status pk_wire_macro_nodes(pk_job* j, int32_t coverage) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  if (j->stage < 3) return fail(PK_ERR_STATE, "no macro-nodes: call pk_build_macro_nodes first");
+  const int cov = coverage ? coverage : j->params.coverage;
+  if (cov <= 0) return fail(PK_ERR_INVALID, "coverage must be >= 1");
+  PK_TRY(set_device(j->ctx));
+  PK_TRY(sync_scalars(j));
+  const uint64_t m = j->h_sc->n_nodes;
+  PK_TRY(job_alloc(j, j->wiring, sizeof(WireRow) * (m ? m : 1)));
+  PK_CUDA(launch_wire(j->nsuf.p, j->npre.p, m, cov, (WireRow*)j->wiring.p, j->stream));
+  j->wired = true;
+  return PK_OK;
+}
+
+pk_status pk_copy_wiring(pk_job* j, pk_wiring* out, uint64_t cap) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  if (!j->wired) return fail(PK_ERR_STATE, "no wiring: call pk_wire_macro_nodes first");
+  PK_TRY(set_device(j->ctx));
+  PK_TRY(sync_scalars(j));
+  const uint64_t m = j->h_sc->n_nodes;
+  if (cap < m) return fail(PK_ERR_INVALID, "capacity smaller than the node count");
+  if (m && out) PK_CUDA(cudaMemcpyAsync(out, j->wiring.p, sizeof(pk_wiring) * m, cudaMemcpyDeviceToHost, j->stream));
+  PK_CUDA(cudaStreamSynchronize(j->stream));
+  return PK_OK;
+}
+
+pk_status pk_wiring_device(pk_job* j, const pk_wiring** d) {
+  if (!j || !d) return fail(PK_ERR_INVALID, "null argument");
+  if (!j->wired) return fail(PK_ERR_STATE, "no wiring: call pk_wire_macro_nodes first");
+  *d = (const pk_wiring*)j->wiring.p;
   return PK_OK;
 }
 

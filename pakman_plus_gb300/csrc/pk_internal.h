@@ -126,6 +126,13 @@ struct MnArgs {
   Scalars* sc;
 };
 
+// One macro-node's initial wiring (the pk_wiring layout of the C ABI).
+struct WireRow {
+  int32_t ns, np, term_suf, term_pre, nw;
+  int32_t wire[9][3];
+  int32_t begin[5][2];
+};
+
 // Launchers (all stream-ordered, no host synchronisation).
 cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st);
 cudaError_t launch_bucket_count(const CountArgs& a, int wide, cudaStream_t st);
@@ -133,6 +140,8 @@ cudaError_t launch_fine_count(const void* in, const uint32_t* cstart, const uint
                               uint32_t* bcount, int k, int bbits, int cbits, int wide, uint32_t* ticket,
                               cudaStream_t st);
 cudaError_t launch_prefix(uint32_t* counts, int B, cudaStream_t st);
+cudaError_t launch_wire(const void* nsuf, const void* npre, unsigned long long m, int coverage, WireRow* out,
+                        cudaStream_t st);
 // batch: reserve a set's rows in the batch macro-node table and copy them there
 cudaError_t launch_batch_emit(const Scalars* sc, unsigned long long* counter, unsigned long long cap,
                               unsigned long long* res, const void* nkeys, const void* nsuf, const void* npre,

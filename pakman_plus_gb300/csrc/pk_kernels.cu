@@ -2091,3 +2091,115 @@ cudaError_t launch_batch_emit(const Scalars* sc, unsigned long long* counter, un
 }
 
 }  // namespace pk
+
+// ------------------------------------------------------------------ initial wiring --
+namespace pk {
+
+// One thread per macro-node: the initial wiring of src/wire.cpp:66-121 /
+// MacroNode::setup_wiring (includes/distribute_kmers.h:549-655).  Lists: present
+// extensions in ascending base code, then the terminal entry (count 1, visit =
+// max(other side's visit sum - own side's, 0)); entries ranked by visit then count,
+// both descending, equal entries in list order; a two-pointer walk pairs prefix
+// visits with suffix visits.
+__global__ void __launch_bounds__(256) k_wire(const uint4* __restrict__ nsuf, const uint4* __restrict__ npre,
+                                              unsigned long long m, int coverage, WireRow* __restrict__ out) {
+  const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const uint4 s4 = nsuf[i], p4 = npre[i];
+  const uint32_t sraw[4] = {s4.x, s4.y, s4.z, s4.w}, praw[4] = {p4.x, p4.y, p4.z, p4.w};
+  int32_t scnt[5], svis[5], pcnt[5], pvis[5];
+  int ns = 0, np = 0, sc = 0, pc = 0;
+  const uint32_t cov = (uint32_t)coverage;
+#pragma unroll
+  for (int e = 0; e < 4; e++) {
+    if (sraw[e]) {
+      scnt[ns] = (int32_t)sraw[e];
+      svis[ns] = (int32_t)((sraw[e] + cov - 1) / cov);
+      sc += svis[ns];
+      ns++;
+    }
+    if (praw[e]) {
+      pcnt[np] = (int32_t)praw[e];
+      pvis[np] = (int32_t)((praw[e] + cov - 1) / cov);
+      pc += pvis[np];
+      np++;
+    }
+  }
+  scnt[ns] = 1;
+  svis[ns] = max(pc - sc, 0);
+  ns++;
+  pcnt[np] = 1;
+  pvis[np] = max(sc - pc, 0);
+  np++;
+  // rank the entries (insertion sort: equal entries keep list order)
+  int os[5], op[5];
+  for (int a = 0; a < ns; a++) os[a] = a;
+  for (int a = 0; a < np; a++) op[a] = a;
+  for (int a = 1; a < ns; a++) {
+    const int x = os[a];
+    int b = a - 1;
+    while (b >= 0 && (svis[x] > svis[os[b]] || (svis[x] == svis[os[b]] && scnt[x] > scnt[os[b]]))) {
+      os[b + 1] = os[b];
+      b--;
+    }
+    os[b + 1] = x;
+  }
+  for (int a = 1; a < np; a++) {
+    const int x = op[a];
+    int b = a - 1;
+    while (b >= 0 && (pvis[x] > pvis[op[b]] || (pvis[x] == pvis[op[b]] && pcnt[x] > pcnt[op[b]]))) {
+      op[b + 1] = op[b];
+      b--;
+    }
+    op[b + 1] = x;
+  }
+  WireRow r;
+  r.ns = ns;
+  r.np = np;
+  r.term_suf = svis[ns - 1];
+  r.term_pre = pvis[np - 1];
+  for (int a = 0; a < 27; a++) (&r.wire[0][0])[a] = 0;
+  for (int a = 0; a < 10; a++) (&r.begin[0][0])[a] = 0;
+  int leftover = sc + svis[ns - 1];
+  int off_s[5] = {0, 0, 0, 0, 0};
+  int top_p = 0, top_s = 0, var_p = 0, var_s = 0, wi = 0, p_size = 0, last_pid = -1, begin_pos = -1;
+  while (leftover > 0 && wi < 9) {
+    const int sid = os[top_s], pid = op[top_p];
+    const int cnt = min(pvis[pid] - var_p, svis[sid] - var_s);
+    r.wire[wi][0] = sid;
+    r.wire[wi][1] = off_s[sid];
+    r.wire[wi][2] = cnt;
+    if (last_pid != pid) {
+      begin_pos = wi;
+      last_pid = pid;
+    }
+    p_size++;
+    wi++;
+    leftover -= cnt;
+    var_p += cnt;
+    var_s += cnt;
+    off_s[sid] += cnt;
+    if (var_p == pvis[pid]) {
+      var_p = 0;
+      top_p++;
+      r.begin[pid][0] = begin_pos;
+      r.begin[pid][1] = p_size;
+      p_size = 0;
+    }
+    if (var_s == svis[sid]) {
+      var_s = 0;
+      top_s++;
+    }
+  }
+  r.nw = wi;
+  out[i] = r;
+}
+
+cudaError_t launch_wire(const void* nsuf, const void* npre, unsigned long long m, int coverage, WireRow* out,
+                        cudaStream_t st) {
+  if (m == 0) return cudaSuccess;
+  k_wire<<<(unsigned)((m + 255) / 256), 256, 0, st>>>((const uint4*)nsuf, (const uint4*)npre, m, coverage, out);
+  return cudaGetLastError();
+}
+
+}  // namespace pk

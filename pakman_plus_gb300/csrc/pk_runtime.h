@@ -75,8 +75,9 @@ struct pk_job {
   pk::Scalars* h_sc = nullptr;  // pinned mirror
   DevBuf fasta, tile_nl, counts, bstart, hstart, keys, tkeys, tcounts, tu, tsub, flags_m, hist, hist2,
       nkeys, nsuf, npre, packed, doff, dkeys, dcounts, flags_f, kkeys, kcounts, kstart, kcount, ksub,
-      coff, cstart, slice_start, fcur;
+      coff, cstart, slice_start, fcur, wiring;
   bool dense_valid = false;
+  bool wired = false;  // wiring matches the current macro-nodes
   bool timing = false;
   // graph mode (batch capture): no host synchronisation and no allocation; the
   // window count is bounded by ncap and scalars were initialised by the caller

@@ -142,6 +142,12 @@ def main():
             rec.update(expect="ok", cutoff=ref.cutoff, n_kept=ref.n_kept, hist=pipe.hist,
                        mn_lo=ref.mn_keys["lo"], mn_hi=ref.mn_keys["hi"], mn_suf=ref.mn_suf,
                        mn_pre=ref.mn_pre, mn_suf_visit=ref.mn_suf_visit, mn_pre_visit=ref.mn_pre_visit)
+            # the reference's initial wiring (src/wire.cpp) and its list orders (4 = terminal)
+            rw, sexts, pexts = ref.wiring
+            pad = lambda lists: np.array([l + [-1] * (5 - len(l)) for l in lists], np.int8).reshape(-1, 5)  # noqa: E731
+            rec.update(w_ns=rw["ns"], w_np=rw["np"], w_term_suf=rw["term_suf"], w_term_pre=rw["term_pre"],
+                       w_nw=rw["nw"], w_wire=rw["wire"], w_begin=rw["begin"], w_sext=pad(sexts),
+                       w_pext=pad(pexts))
         assert table_ok, case["name"]
         # the batched flush (-b) and the concurrent counters (-p) must give the same table
         for var in case.get("variants", []):

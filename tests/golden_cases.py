@@ -32,6 +32,7 @@ class Golden:
     mn_pre: Optional[np.ndarray]
     mn_suf_visit: Optional[np.ndarray]
     mn_pre_visit: Optional[np.ndarray]
+    wiring: Optional[dict] = None  # the reference's initial wiring: w_* arrays, list orders
 
 
 def _keys(lo, hi):
@@ -51,7 +52,8 @@ def load(name: str) -> Golden:
                   int(z["n_windows"]) if "n_windows" in z.files else None,
                   int(z["cutoff"]) if "cutoff" in z.files else None,
                   int(z["n_kept"]) if "n_kept" in z.files else None, g("hist"), mk, g("mn_suf"),
-                  g("mn_pre"), g("mn_suf_visit"), g("mn_pre_visit"))
+                  g("mn_pre"), g("mn_suf_visit"), g("mn_pre_visit"),
+                  {f: z[f] for f in z.files if f.startswith("w_")} or None)
 
 
 def names():
