@@ -65,7 +65,9 @@ typedef struct pk_params {
                            window); 1: windows containing 'N'/'n' are skipped */
   uint64_t batch_kmers; /* -b: MAX_KMER_COUNT; the table is the same for any value */
   int32_t bucket_bits;  /* partition digits (leading key bits), 2..18; 0 = automatic */
-  int32_t reserved[7];
+  int32_t mn_units;     /* macro-node work units: 0 = automatic (about 1000 kept rows
+                           each); n > 0 = units of 4^(n-1) partition buckets */
+  int32_t reserved[6];
 } pk_params;
 
 /* Counts reported by a run. */

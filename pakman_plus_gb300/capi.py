@@ -31,7 +31,8 @@ PK_ERR_NO_DEVICE = 10
 class PkParams(ctypes.Structure):
     _fields_ = [("k", c_int32), ("lmer_length", c_int32), ("num_buckets", c_int32),
                 ("coverage", c_int32), ("read_length", c_int32), ("drop_n", c_int32),
-                ("batch_kmers", c_uint64), ("bucket_bits", c_int32), ("reserved", c_int32 * 7)]
+                ("batch_kmers", c_uint64), ("bucket_bits", c_int32), ("mn_units", c_int32),
+                ("reserved", c_int32 * 6)]
 
 
 class PkSummary(ctypes.Structure):

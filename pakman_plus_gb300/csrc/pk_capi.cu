@@ -289,6 +289,7 @@ pk_status pk::check_params(const pk_params* p) {
   if (p->k < 2 || p->k > 64) return fail(PK_ERR_INVALID, "k must be in 2..64");
   if (p->lmer_length < 1 || p->lmer_length > 32) return fail(PK_ERR_INVALID, "lmer_length must be in 1..32");
   if (p->num_buckets < 1) return fail(PK_ERR_INVALID, "num_buckets (-t) must be >= 1");
+  if (p->mn_units < 0 || p->mn_units > 16) return fail(PK_ERR_INVALID, "mn_units must be in 0..16");
   if (p->bucket_bits < 0 || p->bucket_bits > kMaxPartitionBits)
     return fail(PK_ERR_INVALID, "bucket_bits must be in 0.." + std::to_string(kMaxPartitionBits));
   return PK_OK;
@@ -713,6 +714,17 @@ pk_status pk::mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
   m.kcap = kcap;
   m.k = j->params.k;
   m.bbits = j->bbits;
+  // node units of about 1000 kept rows: each unit merges up to 2V / units rows
+  {
+    const double units = std::max(1.0, 2.0 * (double)kept_bound / 1000.0);
+    int ub = 0;
+    while ((double)(1u << ub) < units && ub < 30) ub++;
+    int level = (j->bbits - ub) / 2;
+    if (level < 1) level = 0;
+    if (j->params.mn_units > 0) level = j->params.mn_units - 1;
+    if (2 * level > j->bbits) level = j->bbits / 2;
+    m.level = level;
+  }
   m.sc = j->d_sc;
   mark_begin(j, ST_MN);
   PK_CUDA(launch_macro_nodes(m, j->wide, 0, j->stream));

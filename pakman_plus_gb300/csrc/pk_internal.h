@@ -123,6 +123,7 @@ struct MnArgs {
   unsigned long long kcap;   // kept rows the kept buffers hold
   int k;
   int bbits;
+  int level;                 // node units cover 4^level table buckets (0: one bucket, split)
   Scalars* sc;
 };
 

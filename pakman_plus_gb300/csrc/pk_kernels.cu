@@ -1588,6 +1588,7 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
   __shared__ unsigned long long s_NO;
 
   const int tid = threadIdx.x;
+  const int Bu = 1 << (a.bbits - 2 * a.level);  // node units
   const int B = 1 << a.bbits;
   const int k = a.k;
   const int nb = 2 * (k - 1);
@@ -1608,16 +1609,34 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
     if (tid == 0) s_beta = atomicAdd(&a.sc->ticket_mn, 1u);
     __syncthreads();
     const uint32_t beta = s_beta;
-    if (beta >= (uint32_t)B) break;
+    if (beta >= (uint32_t)Bu) break;
     if (tid == 0) {
-      s_cur[0] = a.kstart[beta];
-      s_end[0] = a.kstart[beta] + a.kcount[beta];
-      for (int f = 0; f < 4; f++) {
-        const uint32_t bp = ((uint32_t)f << (a.bbits - 2)) | (beta >> 2);
-        const uint32_t d = beta & 3;
-        const uint32_t b0 = a.kstart[bp];
-        s_cur[f + 1] = b0 + (d == 0 ? 0u : a.ksub[3 * bp + d - 1]);
-        s_end[f + 1] = b0 + (d == 3 ? a.kcount[bp] : a.ksub[3 * bp + d]);
+      if (a.level == 0) {
+        // node bucket = table bucket: suffix stream = the bucket's kept rows, prefix
+        // streams = the part of bucket (f, beta >> 2) whose next two bits are beta & 3
+        s_cur[0] = a.kstart[beta];
+        s_end[0] = a.kstart[beta] + a.kcount[beta];
+        for (int f = 0; f < 4; f++) {
+          const uint32_t bp = ((uint32_t)f << (a.bbits - 2)) | (beta >> 2);
+          const uint32_t d = beta & 3;
+          const uint32_t b0 = a.kstart[bp];
+          s_cur[f + 1] = b0 + (d == 0 ? 0u : a.ksub[3 * bp + d - 1]);
+          s_end[f + 1] = b0 + (d == 3 ? a.kcount[bp] : a.ksub[3 * bp + d]);
+        }
+      } else {
+        // node unit = the node keys whose top bbits - 2 level bits are beta: suffix
+        // stream = table buckets [beta << 2L, (beta + 1) << 2L), prefix stream f =
+        // table buckets (f, beta, any 2L - 2 bits) -- contiguous kept rows each
+        const int L2 = 2 * a.level;
+        const uint32_t s0b = beta << L2, s1b = s0b + (1u << L2) - 1;
+        s_cur[0] = a.kstart[s0b];
+        s_end[0] = a.kstart[s1b] + a.kcount[s1b];
+        for (int f = 0; f < 4; f++) {
+          const uint32_t p0 = ((uint32_t)f << (a.bbits - 2)) | (beta << (L2 - 2));
+          const uint32_t p1 = p0 + (1u << (L2 - 2)) - 1;
+          s_cur[f + 1] = a.kstart[p0];
+          s_end[f + 1] = a.kstart[p1] + a.kcount[p1];
+        }
       }
       for (int st = 0; st < 5; st++)
         if (s_end[st] > a.kcap || s_cur[st] > s_end[st]) {  // never read past the kept rows
@@ -1699,17 +1718,23 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
           ord[rank] = (uint16_t)i;
         }
         __syncthreads();
-        // ---- node boundaries and node index per merged position
+        // ---- node boundaries and node index per merged position: each thread takes
+        //      a contiguous run of positions, so one block scan serves the segment
         uint32_t nodes = 0;
-        for (uint32_t r0 = 0; r0 < mm; r0 += kMnThreads) {
-          const uint32_t r = r0 + tid;
-          uint32_t flag = 0;
-          if (r < mm) flag = (r == 0) || !(ikey[ord[r - 1]] == ikey[ord[r]]);
+        {
+          const uint32_t per = (mm + kMnThreads - 1) / kMnThreads;
+          const uint32_t r0 = min(mm, tid * per), r1 = min(mm, r0 + per);
+          uint32_t cnt = 0;
+          for (uint32_t r = r0; r < r1; r++) cnt += (r == 0) || !(ikey[ord[r - 1]] == ikey[ord[r]]);
           uint32_t tot;
-          const uint32_t ex = block_exclusive_sum(flag, s_warp, tot);
-          if (r < mm) nid[r] = (uint16_t)(nodes + ex + flag - 1);
-          nodes += tot;
+          uint32_t run = block_exclusive_sum(cnt, s_warp, tot);
+          for (uint32_t r = r0; r < r1; r++) {
+            run += (r == 0) || !(ikey[ord[r - 1]] == ikey[ord[r]]);
+            nid[r] = (uint16_t)(run - 1);
+          }
+          nodes = tot;
         }
+        __syncthreads();  // nid is read across threads below
         if (!counting) {
           // ---- node offset: decoupled look-back over node buckets
           if (first) {
@@ -1761,7 +1786,7 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
         for (int st = 0; st < 5; st++) s_cur[st] = s_beg[st];
       __syncthreads();
     }
-    if (tid == 0 && beta == (uint32_t)B - 1) a.sc->n_nodes = NO + total;
+    if (tid == 0 && beta == (uint32_t)Bu - 1) a.sc->n_nodes = NO + total;
   }
 }
 

@@ -191,3 +191,19 @@ def test_hbm_budget_is_enforced():
         with pytest.raises(pk.capi.OutOfMemory):
             job.count(rs.fasta, pk.default_params(k=32))
     small.close()
+
+
+@pytest.mark.parametrize("mn_units", [1, 2, 3, 5])
+@pytest.mark.parametrize("name,bucket_bits", [("k32_basic", 8), ("k63_basic", 9), ("k11_dense", 11),
+                                              ("k32_ragged", 12), ("k32_t1", 7)])
+def test_golden_with_macro_node_units(name, bucket_bits, mn_units):
+    """Macro-node work units spanning 4^level partition buckets give the same nodes."""
+    g = load(name)
+    p = pk.default_params(k=g.k, num_buckets=g.t, coverage=g.coverage, drop_n=int(g.drop_n),
+                          bucket_bits=bucket_bits, mn_units=mn_units)
+    with pk.Job(ctx()) as job:
+        job.count(g.fasta, p)
+        job.cutoff(g.t)
+        job.build_macro_nodes(0)
+        mn = job.macro_nodes(g.coverage)
+    assert_mn_equal(mn, g.mn_keys, g.mn_suf, g.mn_pre)
