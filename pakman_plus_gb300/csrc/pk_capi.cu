@@ -408,7 +408,8 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   const bool two_pass = a.cbits < a.bbits;
   mark_begin(j, ST_SCATTER);
   PK_CUDA(launch_coarse_offsets(a, (uint32_t*)j->coff.p, (uint32_t*)j->cstart.p,
-                                (uint32_t*)j->slice_start.p, j->wide, j->stream));
+                                (uint32_t*)j->slice_start.p, fine_slice_keys(j->wide, j->bbits - a.cbits),
+                                j->stream));
   PK_CUDA(launch_scatter_coarse(a, (const uint32_t*)j->coff.p, two_pass ? j->tkeys.p : j->keys.p,
                                 j->wide, j->stream));
   mark_end(j, ST_SCATTER);

@@ -150,8 +150,10 @@ cudaError_t launch_batch_emit(const Scalars* sc, unsigned long long* counter, un
 cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st);
 cudaError_t launch_scatter(const CountArgs& a, void* keys_out, int wide, cudaStream_t st);
 // Two-pass partition: coarse regions (pass 1) then fine buckets inside each region.
+// keys per pass-2 slice for a fan-out of 2^fb fine buckets per coarse region
+int fine_slice_keys(int wide, int fb);
 cudaError_t launch_coarse_offsets(const CountArgs& a, uint32_t* coff, uint32_t* cstart,
-                                  uint32_t* slice_start, int wide, cudaStream_t st);
+                                  uint32_t* slice_start, int slice_keys, cudaStream_t st);
 cudaError_t launch_scatter_coarse(const CountArgs& a, const uint32_t* coff, void* out, int wide,
                                   cudaStream_t st);
 cudaError_t launch_scatter_fine(const void* in, const uint32_t* cstart, const uint32_t* slice_start,

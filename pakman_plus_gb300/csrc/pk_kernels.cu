@@ -829,6 +829,120 @@ __global__ void __launch_bounds__(512, 2) k_scatter_fine(const KeyT* __restrict_
   }
 }
 
+// Wide fan-out (2048 fine buckets per coarse region): a slice of 192 KB is
+// staged in shared memory so that each fine bucket still gets runs of several keys.
+// The slice is read twice (counting, then placing; the second read mostly hits L2),
+// four keys per thread per round.
+template <typename KeyT>
+struct FineBigCfg {
+  static constexpr int T = 1024;
+  static constexpr int S = (192 * 1024) / (int)sizeof(KeyT);  // keys per slice
+  static constexpr int PR = 4;                                 // keys per thread per round
+  static constexpr size_t smem = sizeof(KeyT) * S;
+};
+
+template <typename KeyT>
+__global__ void __launch_bounds__(1024, 1) k_scatter_fine_big(const KeyT* __restrict__ in,
+                                                             const uint32_t* __restrict__ cstart,
+                                                             const uint32_t* __restrict__ slice_start,
+                                                             uint32_t* fcur, KeyT* __restrict__ out,
+                                                             int k, int bbits, int cbits, uint32_t* ticket,
+                                                             unsigned long long cap, uint32_t* err) {
+  using FC = FineBigCfg<KeyT>;
+  constexpr int FBMAX = FineCfg<KeyT>::FBMAX;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  KeyT* stage = reinterpret_cast<KeyT*>(smem_raw);
+  __shared__ uint32_t s_hist[FBMAX], s_loff[FBMAX], s_goff[FBMAX], s_fill[FBMAX];
+  __shared__ uint32_t s_warp[33];
+  __shared__ uint32_t s_slice, s_g;
+  const int tid = threadIdx.x;
+  const int Cn = 1 << cbits, fb = bbits - cbits, FB = 1 << fb;
+  const int fshift = 2 * k - bbits;
+  const uint32_t nslices = slice_start[Cn];
+  while (true) {
+    __syncthreads();
+    if (tid == 0) {
+      s_slice = atomicAdd(ticket, 1u);
+      if (s_slice < nslices) {
+        int lo = 0, hi = Cn - 1;
+        while (lo < hi) {
+          int mid = (lo + hi + 1) >> 1;
+          if (slice_start[mid] <= s_slice) lo = mid; else hi = mid - 1;
+        }
+        s_g = lo;
+      }
+    }
+    for (int i = tid; i < FB; i += FC::T) { s_hist[i] = 0; s_fill[i] = 0; }
+    __syncthreads();
+    const uint32_t sl = s_slice;
+    if (sl >= nslices) break;
+    const uint32_t g = s_g;
+    const uint32_t r0 = cstart[g] + (sl - slice_start[g]) * FC::S;
+    const uint32_t r1 = min(r0 + (uint32_t)FC::S, cstart[g + 1]);
+    const uint32_t m = r1 - r0;
+    for (uint32_t i0 = 0; i0 < m; i0 += FC::PR * FC::T) {
+      KeyT xs[FC::PR];
+#pragma unroll
+      for (int q = 0; q < FC::PR; q++) {
+        const uint32_t i = i0 + q * FC::T + tid;
+        xs[q] = i < m ? in[r0 + i] : (KeyT)0;
+      }
+#pragma unroll
+      for (int q = 0; q < FC::PR; q++)
+        if (i0 + q * FC::T + tid < m) atomicAdd(&s_hist[(uint32_t)(xs[q] >> fshift) & (uint32_t)(FB - 1)], 1u);
+    }
+    __syncthreads();
+    {
+      constexpr int FPT = (FBMAX + FC::T - 1) / FC::T;
+      const int per = (FB + FC::T - 1) / FC::T;
+      const int f0 = min(FB, tid * per);
+      uint32_t hv[FPT], sum = 0;
+#pragma unroll
+      for (int q = 0; q < FPT; q++) {
+        hv[q] = (q < per && f0 + q < FB) ? s_hist[f0 + q] : 0u;
+        sum += hv[q];
+      }
+      uint32_t tot;
+      uint32_t ex = block_exclusive_sum(sum, s_warp, tot);
+#pragma unroll
+      for (int q = 0; q < FPT; q++) {
+        if (q < per && f0 + q < FB) {
+          s_loff[f0 + q] = ex;
+          s_goff[f0 + q] = hv[q] ? atomicAdd(&fcur[(g << fb) + f0 + q], hv[q]) : 0u;
+          ex += hv[q];
+        }
+      }
+    }
+    __syncthreads();
+    for (uint32_t i0 = 0; i0 < m; i0 += FC::PR * FC::T) {
+      KeyT xs[FC::PR];
+#pragma unroll
+      for (int q = 0; q < FC::PR; q++) {
+        const uint32_t i = i0 + q * FC::T + tid;
+        xs[q] = i < m ? in[r0 + i] : (KeyT)0;
+      }
+#pragma unroll
+      for (int q = 0; q < FC::PR; q++) {
+        if (i0 + q * FC::T + tid < m) {
+          const uint32_t f = (uint32_t)(xs[q] >> fshift) & (uint32_t)(FB - 1);
+          stage[s_loff[f] + atomicAdd(&s_fill[f], 1u)] = xs[q];
+        }
+      }
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < m; i += FC::T) {
+      const KeyT x = stage[i];
+      const uint32_t f = (uint32_t)(x >> fshift) & (uint32_t)(FB - 1);
+      guarded_store(out, s_goff[f] + (i - s_loff[f]), x, cap, err);
+    }
+  }
+}
+
+int fine_slice_keys(int wide, int fb) {
+  if (fb >= 11) return wide ? FineBigCfg<u128>::S : FineBigCfg<uint64_t>::S;
+  return wide ? FineCfg<u128>::S : FineCfg<uint64_t>::S;
+}
+
 // Fine bucket sizes when the partition has more digits than the counting pass's
 // histogram: slices of each coarse region are counted by their fine digits in shared
 // memory and added to bcount[(g << fb) + f].
@@ -837,7 +951,7 @@ __global__ void __launch_bounds__(512, 2) k_fine_count(const KeyT* __restrict__ 
                                                    const uint32_t* __restrict__ cstart,
                                                    const uint32_t* __restrict__ slice_start,
                                                    uint32_t* bcount, int k, int bbits, int cbits,
-                                                   uint32_t* ticket) {
+                                                   uint32_t* ticket, uint32_t slice_keys) {
   using FC = FineCfg<KeyT>;
   __shared__ uint32_t s_hist[FC::FBMAX];
   __shared__ uint32_t s_slice, s_g;
@@ -863,8 +977,8 @@ __global__ void __launch_bounds__(512, 2) k_fine_count(const KeyT* __restrict__ 
     const uint32_t sl = s_slice;
     if (sl >= nslices) break;
     const uint32_t g = s_g;
-    const uint32_t r0 = cstart[g] + (sl - slice_start[g]) * FC::S;
-    const uint32_t r1 = min(r0 + (uint32_t)FC::S, cstart[g + 1]);
+    const uint32_t r0 = cstart[g] + (sl - slice_start[g]) * slice_keys;
+    const uint32_t r1 = min(r0 + slice_keys, cstart[g + 1]);
     for (uint32_t i = r0 + tid; i < r1; i += FC::T)
       atomicAdd(&s_hist[(uint32_t)(in[i] >> fshift) & (uint32_t)(FB - 1)], 1u);
     __syncthreads();
@@ -1884,8 +1998,8 @@ cudaError_t launch_scatter_coarse(const CountArgs& a, const uint32_t* coff, void
 }
 
 cudaError_t launch_coarse_offsets(const CountArgs& a, uint32_t* coff, uint32_t* cstart,
-                                  uint32_t* slice_start, int wide, cudaStream_t st) {
-  const int sk = wide ? FineCfg<u128>::S : FineCfg<uint64_t>::S;
+                                  uint32_t* slice_start, int slice_keys, cudaStream_t st) {
+  const int sk = slice_keys;
   k_coarse_offsets<<<a.grid, 256, 0, st>>>(a.counts, a.bstart, a.grid, a.bbits, a.cbits, coff, cstart,
                                            slice_start, sk);
   return cudaGetLastError();
@@ -1901,6 +2015,19 @@ static cudaError_t launch_fine_t(const KeyT* in, const uint32_t* cstart, const u
     cudaError_t e = cudaFuncSetAttribute(k_scatter_fine<KeyT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr_set = true;
+  }
+  if (bbits - cbits >= 11) {
+    const size_t bsmem = FineBigCfg<KeyT>::smem;
+    static bool big_attr_set = false;
+    if (!big_attr_set) {
+      cudaError_t e = cudaFuncSetAttribute(k_scatter_fine_big<KeyT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)bsmem);
+      if (e != cudaSuccess) return e;
+      big_attr_set = true;
+    }
+    k_scatter_fine_big<KeyT><<<sm_count(), FineBigCfg<KeyT>::T, bsmem, st>>>(in, cstart, slice_start, fcur, out, k,
+                                                                             bbits, cbits, ticket, cap, err);
+    return cudaGetLastError();
   }
   k_scatter_fine<KeyT><<<sm_count() * 2, FineCfg<KeyT>::T, smem, st>>>(in, cstart, slice_start, fcur, out,
                                                                         k, bbits, cbits, ticket, cap, err);
@@ -1920,12 +2047,13 @@ cudaError_t launch_scatter_fine(const void* in, const uint32_t* cstart, const ui
 cudaError_t launch_fine_count(const void* in, const uint32_t* cstart, const uint32_t* slice_start,
                               uint32_t* bcount, int k, int bbits, int cbits, int wide, uint32_t* ticket,
                               cudaStream_t st) {
+  const uint32_t sk = (uint32_t)fine_slice_keys(wide, bbits - cbits);
   if (wide)
     k_fine_count<u128><<<sm_count() * 2, 512, 0, st>>>(reinterpret_cast<const u128*>(in), cstart, slice_start,
-                                                      bcount, k, bbits, cbits, ticket);
+                                                      bcount, k, bbits, cbits, ticket, sk);
   else
     k_fine_count<uint64_t><<<sm_count() * 2, 512, 0, st>>>(reinterpret_cast<const uint64_t*>(in), cstart,
-                                                          slice_start, bcount, k, bbits, cbits, ticket);
+                                                          slice_start, bcount, k, bbits, cbits, ticket, sk);
   return cudaGetLastError();
 }
 
