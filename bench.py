@@ -184,6 +184,22 @@ def cpu_baseline(rs, sample_windows: int):
                       f"macro-nodes, {dt:.2f} s on {threads} threads"}
 
 
+def max_over_ranks(x: float, dist, device: str) -> float:
+    """The slowest rank's time (every rank gets it); `dist` is None for one process."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(windows_per_rank: int, world: int, ms: float) -> float:
+    """Whole-job k-mers/s: every replica counts its own read set of the same size, so
+    the job processes world x windows in the slowest rank's time."""
+    return windows_per_rank * world / (ms / 1000.0)
+
+
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return 0
@@ -490,11 +506,8 @@ def main():
         dist.barrier()
     clocks = sampler.stop()
     ms_step = e0.elapsed_time(e1) / args.steps
-    if dist:
-        t = torch.tensor([ms_step], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = s.n_windows * world / (ms_step / 1000.0)
+    ms_step = max_over_ranks(ms_step, dist, f"cuda:{local}")
+    value = job_throughput(s.n_windows, world, ms_step)
 
     # end to end through the public API: pinned host FASTA in, macro-node table out,
     # every step; requests go through the serving front end (pk_submit / pk_wait) with
@@ -543,11 +556,8 @@ def main():
     se = infos[-1].summary
     srv.close()
     e2e_ms = 1000.0 * (t1 - t0) / e2e_steps
-    if dist:
-        t = torch.tensor([e2e_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = {"value": se.n_windows * world / (e2e_ms / 1000.0), "unit": UNIT,
+    e2e_ms = max_over_ranks(e2e_ms, dist, f"cuda:{local}")
+    e2e = {"value": job_throughput(se.n_windows, world, e2e_ms), "unit": UNIT,
            "h2d_bytes_per_step": F, "d2h_bytes_per_step": int(se.n_nodes * (W + 32) + 48),
            "ms_per_step": e2e_ms, "steps": e2e_steps,
            "mode": f"pk_submit/pk_wait, {depth} jobs in flight, pinned host buffers",
