@@ -90,6 +90,18 @@ __device__ __forceinline__ void st_release(unsigned long long* p, unsigned long 
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+// Hint the L2 to fetch bytes [lo, hi) of `base` (one thread; the copy engine of the
+// SM runs it in the background).  The range is shrunk to 16-byte boundaries, as the
+// bulk prefetch requires, so it never reaches past `hi`.
+__device__ __forceinline__ void prefetch_l2(const void* base, unsigned long long lo, unsigned long long hi) {
+  const unsigned long long a = (reinterpret_cast<unsigned long long>(base) + lo + 15) & ~15ull;
+  const unsigned long long e = (reinterpret_cast<unsigned long long>(base) + hi) & ~15ull;
+  for (unsigned long long p = a; p < e; p += 65536) {
+    const uint32_t sz = (uint32_t)(e - p < 65536 ? e - p : 65536);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(sz) : "memory");
+  }
+}
+
 // Decoupled look-back words: status in bits 62-63 (1 = aggregate, 2 = inclusive).
 constexpr unsigned long long kLbAgg = 1ull << 62;
 constexpr unsigned long long kLbIncl = 2ull << 62;
@@ -1068,6 +1080,22 @@ __device__ __forceinline__ int hash_insert(KeyT* skey, uint32_t* scnt, uint32_t 
   return 2;
 }
 
+// One table row, plus its count in the count histogram (counts below t).
+template <typename KeyT>
+__device__ __forceinline__ void emit_row(const BucketArgs& a, KeyT* __restrict__ tkeys, unsigned long long row,
+                                         KeyT key, uint32_t cnt, uint32_t* shist) {
+  if (row < a.cap) {
+    tkeys[row] = key;
+    a.tcounts[row] = cnt;
+  } else {
+    atomicOr(&a.sc->err, ERR_BOUNDS);
+  }
+  if (cnt < (uint32_t)a.t) {
+    if (cnt < (uint32_t)kHistSmem) atomicAdd(&shist[cnt], 1u);
+    else atomicAdd(&a.hist[cnt], 1ull);
+  }
+}
+
 // Rows [base+acc, base+acc+u) of a bucket from the sorted on-chip run (sk, sc), plus the
 // per-bucket counts of rows by the next two key bits (s_d).
 template <typename KeyT>
@@ -1083,18 +1111,7 @@ __device__ void write_bucket_rows(const KeyT* sk, const uint32_t* sc, uint32_t u
     uint32_t d2 = 3;
     if (v) {
       const KeyT r = sk[i];
-      const uint32_t cnt = sc[i];
-      const unsigned long long row = (unsigned long long)base + acc + i;
-      if (row < a.cap) {
-        tkeys[row] = hi_bits | r;
-        a.tcounts[row] = cnt;
-      } else {
-        atomicOr(&a.sc->err, ERR_BOUNDS);
-      }
-      if (cnt < (uint32_t)a.t) {
-        if (cnt < (uint32_t)kHistSmem) atomicAdd(&shist[cnt], 1u);
-        else atomicAdd(&a.hist[cnt], 1ull);
-      }
+      emit_row<KeyT>(a, tkeys, (unsigned long long)base + acc + i, hi_bits | r, sc[i], shist);
       d2 = (uint32_t)(KeyOps<KeyT>::shr(r, rem - 2) & 3);
     }
     dl0 += __popc(__ballot_sync(FULLMASK, v && d2 == 0));
@@ -1144,7 +1161,10 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   KeyT* __restrict__ tkeys = reinterpret_cast<KeyT*>(a.tkeys);
   const int hbins = a.t < kHistSmem ? a.t : kHistSmem;
   for (int i = tid; i < hbins; i += kBucketThreads) shist[i] = 0;
-  if (tid == 0) s_ratio = 0.5f;  // running distinct/keys ratio of this CTA's buckets
+  // running distinct/keys ratio of this CTA's buckets; read sets at 20x-80x coverage
+  // with sub-percent errors start near 0.2 (a high guess splits the first buckets
+  // needlessly, a low one costs one overflowing pass)
+  if (tid == 0) s_ratio = 0.2f;
   const int slog_max = rem < 4 ? rem : 4;  // initial split guess (<= 16 sub-ranges)
 
   // the next bucket's ticket and extent are fetched while the current one is counted
@@ -1161,7 +1181,14 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       s_nb[1] = next_end;
       if (next_beta < (uint32_t)B) {
         next_beta = atomicAdd(&a.sc->ticket_bucket, 1u);
-        if (next_beta < (uint32_t)B) { next_base = a.bstart[next_beta]; next_end = a.bstart[next_beta + 1]; }
+        if (next_beta < (uint32_t)B) {
+          next_base = a.bstart[next_beta];
+          next_end = a.bstart[next_beta + 1];
+          // the next bucket's keys stream into L2 while this one is counted, so its
+          // hash pass reads at L2 latency
+          const unsigned long long e = min((unsigned long long)next_end, a.cap);
+          if (next_base < e) prefetch_l2(keys, sizeof(KeyT) * (unsigned long long)next_base, sizeof(KeyT) * e);
+        }
       }
     }
     __syncthreads();
@@ -1221,6 +1248,17 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
         skey[i] = EMPTY;
         scnt[i] = 0;
       }
+      // sort bins (counts, then fill cursors) of the distinct remainders: the top
+      // bits below the sub-range's common prefix
+      const int dbits = psh < kSortBinBits ? psh : kSortBinBits;
+      const uint32_t nbins = 1u << dbits;
+      const int dsh = psh - dbits;
+      uint32_t* bh = reinterpret_cast<uint32_t*>(wc);  // [nbins] counts -> offsets
+      uint32_t* bf = bh + (1u << kSortBinBits);        // [nbins] fill
+      for (uint32_t i = tid; i < nbins; i += kBucketThreads) {
+        bh[i] = 0;
+        bf[i] = 0;
+      }
       if (tid == 0) {
         s_ovf = 0;
         s_unew = 0;
@@ -1250,9 +1288,9 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       }
       __syncthreads();
       bool ovf = s_ovf != 0;
-      // --- compaction of occupied slots into [0, u)
-      // order is irrelevant here (the run is sorted next), so slots are read with a
-      // stride of one block: conflict-free shared-memory access
+      // --- occupied slots into registers, counted, with their sort bins histogrammed;
+      // order is irrelevant here, so slots are read with a stride of one block:
+      // conflict-free shared-memory access
       constexpr int SPT = H / kBucketThreads;
       const uint32_t spt = Heff / kBucketThreads;
       KeyT rk[SPT];
@@ -1265,11 +1303,14 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
         if ((uint32_t)q < spt) {
           rk[q] = skey[q * kBucketThreads + tid];
           rc[q] = scnt[q * kBucketThreads + tid];
-          occ += rk[q] != EMPTY;
+          if (rk[q] != EMPTY) {
+            occ++;
+            if (!ovf) atomicAdd(&bh[(uint32_t)KeyOps<KeyT>::shr(rk[q], dsh) & (nbins - 1)], 1u);
+          }
         }
       }
       uint32_t u;
-      uint32_t off = block_exclusive_sum(occ, s_warp, u);
+      block_exclusive_sum(occ, s_warp, u);
       if (u > Heff / 2) ovf = true;  // the sort needs a second half
       if (ovf) {
         // cut [lo, hi) at quantiles of a sample of the distinct keys in the table
@@ -1316,33 +1357,12 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
         if (s_fail) { failed = true; break; }
         continue;
       }
-#pragma unroll
-      for (int q = 0; q < SPT; q++) {
-        if (rk[q] != EMPTY) {
-          skey[off] = rk[q];
-          scnt[off] = rc[q];
-          off++;
-        }
-      }
-      __syncthreads();
-      // --- sort the u distinct remainders: counting sort by their top bits below the
-      //     prefix, then each element's rank among its bin (bins hold one error
-      //     family of a k-mer, a few dozen keys); a bin above kBinMax falls back to
-      //     a stable LSD radix sort
-      KeyT* sk = skey;
-      uint32_t* sc = scnt;
+      // --- sort the u distinct remainders: bins (top bits below the prefix) are offset
+      //     by a block scan and the slots go from registers straight into their bins;
+      //     each element's rank among its bin (a bin holds a few keys) then gives its
+      //     row, written at once.  A bin above kBinMax falls back to a stable LSD
+      //     radix sort of the binned run.
       {
-        const int dbits = psh < kSortBinBits ? psh : kSortBinBits;
-        const uint32_t nbins = 1u << dbits;
-        const int dsh = psh - dbits;
-        uint32_t* bh = reinterpret_cast<uint32_t*>(wc);  // [nbins] counts -> offsets
-        uint32_t* bf = bh + (1u << kSortBinBits);        // [nbins] fill
-        for (uint32_t i = tid; i < nbins; i += kBucketThreads) { bh[i] = 0; bf[i] = 0; }
-        if (tid == 0) s_ovf = 0;
-        __syncthreads();
-        for (uint32_t i = tid; i < u; i += kBucketThreads)
-          atomicAdd(&bh[(uint32_t)KeyOps<KeyT>::shr(skey[i], dsh) & (nbins - 1)], 1u);
-        __syncthreads();
         constexpr int BPT = (1 << kSortBinBits) / kBucketThreads;
         uint32_t hv[BPT], hs = 0, hm = 0;
 #pragma unroll
@@ -1360,35 +1380,50 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
           if (bi < nbins) bh[bi] = ex;
           ex += hv[q];
         }
-        if (hm > (uint32_t)kBinMax) s_ovf = 1;
-        __syncthreads();
-        KeyT* bk = skey + Heff / 2;
-        uint32_t* bc = scnt + Heff / 2;
-        for (uint32_t i = tid; i < u; i += kBucketThreads) {
-          const KeyT x = skey[i];
-          const uint32_t bi = (uint32_t)KeyOps<KeyT>::shr(x, dsh) & (nbins - 1);
-          const uint32_t pos = bh[bi] + atomicAdd(&bf[bi], 1u);
-          bk[pos] = x;
-          bc[pos] = scnt[i];
+        const bool radix = __syncthreads_or(hm > (uint32_t)kBinMax) != 0;
+#pragma unroll
+        for (int q = 0; q < SPT; q++) {
+          if (rk[q] != EMPTY) {
+            const uint32_t bi = (uint32_t)KeyOps<KeyT>::shr(rk[q], dsh) & (nbins - 1);
+            const uint32_t pos = bh[bi] + atomicAdd(&bf[bi], 1u);
+            skey[pos] = rk[q];
+            scnt[pos] = rc[q];
+          }
         }
         __syncthreads();
-        if (!s_ovf) {
-          for (uint32_t i = tid; i < u; i += kBucketThreads) {
-            const KeyT x = bk[i];
-            const uint32_t bi = (uint32_t)KeyOps<KeyT>::shr(x, dsh) & (nbins - 1);
-            const uint32_t b0 = bh[bi], b1 = b0 + bf[bi];
-            uint32_t rank = 0;
-            for (uint32_t j = b0; j < b1; j++) rank += bk[j] < x;
-            skey[b0 + rank] = x;
-            scnt[b0 + rank] = bc[i];
+        if (!radix) {
+          // element i of the binned run lands at row b0 + rank, within its bin's rows,
+          // so neighbouring threads store to neighbouring rows
+          const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
+          uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
+          for (uint32_t i0 = 0; i0 < u; i0 += kBucketThreads) {
+            const uint32_t i = i0 + tid;
+            const bool v = i < u;
+            uint32_t d2 = 3;
+            if (v) {
+              const KeyT x = skey[i];
+              const uint32_t bi = (uint32_t)KeyOps<KeyT>::shr(x, dsh) & (nbins - 1);
+              const uint32_t b0 = bh[bi], b1 = b0 + bf[bi];
+              uint32_t rank = 0;
+              for (uint32_t j = b0; j < b1; j++) rank += skey[j] < x;
+              emit_row<KeyT>(a, tkeys, (unsigned long long)base + acc + b0 + rank, hi_bits | x, scnt[i], shist);
+              d2 = (uint32_t)(KeyOps<KeyT>::shr(x, rem - 2) & 3);
+            }
+            dl0 += __popc(__ballot_sync(FULLMASK, v && d2 == 0));
+            dl1 += __popc(__ballot_sync(FULLMASK, v && d2 == 1));
+            dl2 += __popc(__ballot_sync(FULLMASK, v && d2 == 2));
           }
-          __syncthreads();
+          if (lane == 0) {
+            if (dl0) atomicAdd(&s_d[0], dl0);
+            if (dl1) atomicAdd(&s_d[1], dl1);
+            if (dl2) atomicAdd(&s_d[2], dl2);
+          }
         } else {
-          // stable LSD radix sort of the binned run (bins already in order)
-          sk = bk;
-          sc = bc;
-          KeyT* dk = skey;
-          uint32_t* dc = scnt;
+          // stable LSD radix sort of the binned run in [0, u) through [H/2, H/2 + u)
+          KeyT* sk = skey;
+          uint32_t* sc = scnt;
+          KeyT* dk = skey + Heff / 2;
+          uint32_t* dc = scnt + Heff / 2;
           const int npass = (psh + 7) / 8;
           const uint32_t E = (u + NW - 1) / NW;
           const uint32_t e0 = (uint32_t)warp * E;
@@ -1461,9 +1496,9 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
             KeyT* tk = sk; sk = dk; dk = tk;
             uint32_t* tc = sc; sc = dc; dc = tc;
           }
+          write_bucket_rows<KeyT>(sk, sc, u, a, beta, rem, base, acc, tkeys, s_d, shist);
         }
       }
-      write_bucket_rows<KeyT>(sk, sc, u, a, beta, rem, base, acc, tkeys, s_d, shist);
       acc += u;
       __syncthreads();
     }
