@@ -108,24 +108,46 @@ constexpr unsigned long long kLbIncl = 2ull << 62;
 constexpr unsigned long long kLbVal = (1ull << 62) - 1;
 constexpr int kLbSpinLimit = 1 << 24;  // ~1-2 s with the back-off below
 
-// Exclusive prefix of `flags[0..idx)`; called by one thread.  Every wait is bounded:
-// on expiry the error bit is set and the partial sum is returned.
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULLMASK, v, o);
+  return v;
+}
+
+// Exclusive prefix of `flags[0..idx)`, computed by a whole warp (all 32 lanes call it
+// and all get the sum).  Each step reads the 32 nearest unread predecessors at once
+// (lane 0 = nearest): it stops at the nearest inclusive word, otherwise adds the
+// aggregates up to the first word still unpublished and moves past them.  Waiting on
+// an unpublished word is bounded: on expiry the error bit is set and the partial sum
+// is returned.
 __device__ unsigned long long lookback_exclusive(unsigned long long* flags, int idx, uint32_t* err) {
+  const int lane = threadIdx.x & 31;
   unsigned long long sum = 0;
-  for (int j = idx - 1; j >= 0; --j) {
-    unsigned long long f = 0;
-    int spins = 0;
-    while (true) {
-      f = ld_acquire(&flags[j]);
-      if (f >> 62) break;
-      if (++spins >= kLbSpinLimit) {
-        atomicOr(err, ERR_LOOKBACK);
-        return sum;
-      }
-      __nanosleep(spins < 64 ? 32 : 256);
+  int top = idx - 1;  // nearest predecessor not yet added
+  int spins = 0;
+  while (top >= 0) {
+    const int j = top - lane;
+    const unsigned long long f = j >= 0 ? ld_acquire(&flags[j]) : kLbIncl;  // below 0: inclusive 0
+    const unsigned st = (unsigned)(f >> 62);
+    const unsigned waiting = __ballot_sync(FULLMASK, st == 0);
+    const unsigned incl = __ballot_sync(FULLMASK, st == 2);
+    const int first_wait = waiting ? __ffs(waiting) - 1 : 32;
+    const int first_incl = incl ? __ffs(incl) - 1 : 32;
+    if (first_incl < first_wait) {
+      sum += warp_sum_u64(lane <= first_incl ? (f & kLbVal) : 0ull);
+      return sum;
     }
-    sum += f & kLbVal;
-    if ((f & ~kLbVal) == kLbIncl) break;
+    if (first_wait > 0) {
+      sum += warp_sum_u64(lane < first_wait ? (f & kLbVal) : 0ull);
+      top -= first_wait;
+      spins = 0;
+      continue;
+    }
+    if (++spins >= kLbSpinLimit) {
+      if (lane == 0) atomicOr(err, ERR_LOOKBACK);
+      return sum;
+    }
+    __nanosleep(spins < 64 ? 32 : 256);
   }
   return sum;
 }
@@ -1655,14 +1677,13 @@ __global__ void __launch_bounds__(256) k_filter_kept(FilterArgs a) {
       const uint32_t i = i0 + lane;
       v += __popc(__ballot_sync(FULLMASK, i < u && a.tcounts[r0 + i] >= cut));
     }
-    unsigned long long K = 0;
+    if (lane == 0) st_release(&a.flags[beta], kLbAgg | (unsigned long long)v);
+    __syncwarp();
+    unsigned long long K = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
     if (lane == 0) {
-      st_release(&a.flags[beta], kLbAgg | (unsigned long long)v);
-      K = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
       st_release(&a.flags[beta], kLbIncl | (K + v));
       if (beta == (uint32_t)B - 1) a.sc->n_kept_rows = K + v;
     }
-    K = __shfl_sync(FULLMASK, K, 0);
     uint32_t pos = (uint32_t)K;
     uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
     for (uint32_t i0 = 0; i0 < u; i0 += 32) {
@@ -1887,12 +1908,15 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
         if (!counting) {
           // ---- node offset: decoupled look-back over node buckets
           if (first) {
-            if (tid == 0) {
+            if (tid < 32) {  // warp 0 looks back
               const unsigned long long mine = pass == 0 ? nodes : total;
-              st_release(&a.flags[beta], kLbAgg | mine);
+              if (tid == 0) st_release(&a.flags[beta], kLbAgg | mine);
+              __syncwarp();
               const unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
-              st_release(&a.flags[beta], kLbIncl | (ex + mine));
-              s_NO = ex;
+              if (tid == 0) {
+                st_release(&a.flags[beta], kLbIncl | (ex + mine));
+                s_NO = ex;
+              }
             }
             __syncthreads();
             NO = s_NO;
