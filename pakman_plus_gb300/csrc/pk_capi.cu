@@ -695,6 +695,7 @@ pk_status pk::mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
   f.kcount = (uint32_t*)j->kcount.p;
   f.ksub = (uint32_t*)j->ksub.p;
   f.cap = kcap;
+  f.trows = j->tcounts.bytes / sizeof(uint32_t);
   f.k = j->params.k;
   f.bbits = j->bbits;
   f.sc = j->d_sc;

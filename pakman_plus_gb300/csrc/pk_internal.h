@@ -104,6 +104,7 @@ struct FilterArgs {
   uint32_t* kcount;          // 2^bbits
   uint32_t* ksub;            // 3 * 2^bbits
   unsigned long long cap;    // kept-row capacity
+  unsigned long long trows;  // rows the table count buffer holds (reads stay below)
   int k;
   int bbits;
   Scalars* sc;

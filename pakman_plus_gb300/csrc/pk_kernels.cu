@@ -1652,14 +1652,37 @@ __device__ __forceinline__ uint32_t upper_bound_s(const KeyT* k, uint32_t lo, ui
   return lo;
 }
 
+// Counts of table rows [q, q+4) (one 16-byte load when the four rows lie inside the
+// count buffer) and the mask of those rows that are inside [r0, e) and kept.
+__device__ __forceinline__ uint32_t kept_group(const FilterArgs& a, uint32_t q, uint32_t r0, uint32_t e,
+                                               uint32_t cut, uint32_t c[4]) {
+  c[0] = c[1] = c[2] = c[3] = 0;
+  if (q >= e) return 0;
+  if ((unsigned long long)q + 4 <= a.trows) {
+    const uint4 v = *reinterpret_cast<const uint4*>(a.tcounts + q);
+    c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+  } else {
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+      if ((unsigned long long)q + t < a.trows) c[t] = a.tcounts[q + t];
+  }
+  uint32_t m = 0;
+#pragma unroll
+  for (int t = 0; t < 4; t++)
+    if (q + t >= r0 && q + t < e && c[t] >= cut) m |= 1u << t;
+  return m;
+}
+
 // Kept rows (count >= cutoff) of every table bucket, written densely in key order --
 // the k-mers construct_kmer_histogram hands to macro-node construction.  Per bucket:
 // kstart (first kept row), kcount, and ksub (kept rows whose next two key bits are
-// < 1, 2, 3).  Warps scan 32-row steps with ballots; bucket offsets come from a
-// decoupled look-back (every bucket publishes its aggregate before waiting).
+// < 1, 2, 3).  Bucket offsets come from a decoupled look-back (every bucket publishes
+// its aggregate before waiting).
 template <typename KeyT>
 __global__ void __launch_bounds__(256) k_filter_kept(FilterArgs a) {
-  // one warp per table bucket: no block-wide barriers
+  // one warp per table bucket: no block-wide barriers.  Lane l takes the rows
+  // [g + 4l, g + 4l + 4) of each 128-row step, with g aligned to four rows, so one
+  // 16-byte load brings its four counts and lane order is row order.
   const int lane = threadIdx.x & 31;
   const int B = 1 << a.bbits;
   const int rem = 2 * a.k - a.bbits;
@@ -1671,12 +1694,14 @@ __global__ void __launch_bounds__(256) k_filter_kept(FilterArgs a) {
     if (lane == 0) beta = atomicAdd(&a.sc->ticket_filter, 1u);
     beta = __shfl_sync(FULLMASK, beta, 0);
     if (beta >= (uint32_t)B) break;
-    const uint32_t r0 = a.bstart[beta], u = a.tu[beta];
+    const uint32_t r0 = a.bstart[beta], e = r0 + a.tu[beta];
+    const uint32_t g0 = r0 & ~3u;
     uint32_t v = 0;
-    for (uint32_t i0 = 0; i0 < u; i0 += 32) {
-      const uint32_t i = i0 + lane;
-      v += __popc(__ballot_sync(FULLMASK, i < u && a.tcounts[r0 + i] >= cut));
+    for (uint32_t g = g0; g < e; g += 128) {
+      uint32_t c[4];
+      v += __popc(kept_group(a, g + 4 * lane, r0, e, cut, c));
     }
+    v = __reduce_add_sync(FULLMASK, v);
     if (lane == 0) st_release(&a.flags[beta], kLbAgg | (unsigned long long)v);
     __syncwarp();
     unsigned long long K = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
@@ -1686,28 +1711,39 @@ __global__ void __launch_bounds__(256) k_filter_kept(FilterArgs a) {
     }
     uint32_t pos = (uint32_t)K;
     uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
-    for (uint32_t i0 = 0; i0 < u; i0 += 32) {
-      const uint32_t i = i0 + lane;
-      const uint32_t c = i < u ? a.tcounts[r0 + i] : 0;
-      const bool keep = i < u && c >= cut;
-      const unsigned bal = __ballot_sync(FULLMASK, keep);
-      uint32_t d2 = 3;
-      if (keep) {
-        const KeyT x = tkeys[r0 + i];
-        const uint32_t o = pos + __popc(bal & lanemask_lt());
+    for (uint32_t g = g0; g < e; g += 128) {
+      const uint32_t q = g + 4 * lane;
+      uint32_t c[4];
+      const uint32_t m = kept_group(a, q, r0, e, cut, c);
+      const uint32_t n = __popc(m);
+      uint32_t inc = n;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULLMASK, inc, o);
+        if (lane >= o) inc += y;
+      }
+      uint32_t o = pos + inc - n;
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        if (!((m >> t) & 1u)) continue;
+        const KeyT x = tkeys[q + t];
         if (o < a.cap) {
           kkeys[o] = x;
-          a.kcounts[o] = c;
+          a.kcounts[o] = c[t];
         } else {
           atomicOr(&a.sc->err, ERR_BOUNDS);
         }
-        d2 = (uint32_t)(KeyOps<KeyT>::shr(x, rem - 2) & 3);
+        o++;
+        const uint32_t d2 = (uint32_t)(KeyOps<KeyT>::shr(x, rem - 2) & 3);
+        dl0 += d2 == 0;
+        dl1 += d2 == 1;
+        dl2 += d2 == 2;
       }
-      dl0 += __popc(__ballot_sync(FULLMASK, keep && d2 == 0));
-      dl1 += __popc(__ballot_sync(FULLMASK, keep && d2 == 1));
-      dl2 += __popc(__ballot_sync(FULLMASK, keep && d2 == 2));
-      pos += __popc(bal);
+      pos += __shfl_sync(FULLMASK, inc, 31);
     }
+    dl0 = __reduce_add_sync(FULLMASK, dl0);
+    dl1 = __reduce_add_sync(FULLMASK, dl1);
+    dl2 = __reduce_add_sync(FULLMASK, dl2);
     if (lane == 0) {
       a.kstart[beta] = (uint32_t)K;
       a.kcount[beta] = v;
