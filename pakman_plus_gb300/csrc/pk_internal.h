@@ -28,7 +28,7 @@ constexpr int kExtractThreads = 512;
 constexpr int kSegBytes = 64;       // bytes per thread per extraction step
 constexpr int kBucketThreads = 512;
 constexpr int kMnThreads = 128;
-constexpr int kMnCap = 2048;        // items (k-mer records) per macro-node segment on chip
+constexpr int kMnCap = 1536;        // items (k-mer records) per macro-node segment on chip
 constexpr int kHistSmem = 1024;     // count-histogram bins kept in shared memory
 constexpr int kBucketStack = 256;   // pending sub-ranges of one bucket
 constexpr int kSplitWays = 4;      // pieces an overflowing sub-range is cut into

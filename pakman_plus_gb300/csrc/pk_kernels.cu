@@ -2043,7 +2043,7 @@ size_t bucket_smem_bytes(int wide) {
 }
 size_t mn_smem_bytes(int wide) { return wide ? MnSmem<u128>::bytes : MnSmem<uint64_t>::bytes; }
 int bucket_ctas_per_sm(int) { return 2; }
-int mn_ctas_per_sm(int wide) { return wide ? 4 : 6; }
+int mn_ctas_per_sm(int wide) { return wide ? 5 : 8; }
 
 cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st) {
   const int ntiles = (int)((a.F + kTileBytes - 1) / kTileBytes);
