@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--serve-pool", type=int, default=32, help="distinct generated read sets")
     ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--serve-budget-gb", type=float, default=160.0)
+    ap.add_argument("--ingest", action="store_true",
+                    help="file ingest benchmark: FASTA file -> macro-node table on the host, read "
+                         "into memory then counted, against streamed by pk_count_file")
     return ap.parse_args()
 
 
@@ -443,6 +446,92 @@ def run_batch(args, rank, world):
     return 0
 
 
+def run_ingest(args, rank, world):
+    """FASTA file -> macro-node table in host memory, two ways, on one GPU: (a) the file
+    read into pinned host memory, then pk_run (copy, count, cutoff, macro-nodes); (b)
+    pk_count_file, whose reader threads stream the file to the device while earlier
+    pieces are copied and line-scanned, then cutoff and macro-nodes.  Both copy the
+    macro-node table back.  The file is read once before timing, so both read it from
+    the page cache; the timings are host wall-clock per file."""
+    if rank != 0:
+        return 0
+    import numpy as np
+    import torch
+
+    import pakman_plus_gb300 as pk
+    from pakman_plus_gb300 import build as pkbuild
+
+    pkbuild.build()
+    rs = workload(args.workload, args.scale)
+    F = len(rs.fasta)
+    tmpdir = tempfile.mkdtemp(prefix="pk_ingest_")
+    path = os.path.join(tmpdir, "reads.fa")
+    with open(path, "wb") as f:
+        f.write(rs.fasta)
+    with open(path, "rb") as f:
+        while f.read(1 << 26):
+            pass
+    params = pk.default_params(k=rs.k, num_buckets=rs.t, coverage=rs.coverage, read_length=rs.read_len,
+                               drop_n=int(rs.drop_n), batch_kmers=rs.batch)
+    ctx = pk.Context(0)
+    pinned = torch.empty(F, dtype=torch.uint8, pin_memory=True).numpy()
+    with pk.Job(ctx) as job:  # macro-node count, to size the pinned output buffers
+        cap = job.run(rs.fasta, params).n_nodes + 16
+    kd = pk.key_dtype(rs.k)
+    out = (torch.empty(cap * kd.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(kd),
+           torch.empty(cap * 16, dtype=torch.uint8, pin_memory=True).numpy().view(np.uint32).reshape(cap, 4),
+           torch.empty(cap * 16, dtype=torch.uint8, pin_memory=True).numpy().view(np.uint32).reshape(cap, 4))
+
+    def read_only():
+        with open(path, "rb") as f:
+            return f.readinto(memoryview(pinned))
+
+    def via_memory(job):
+        n = read_only()
+        s = job.run(pinned[:n], params)
+        job.macro_nodes(out=out)
+        return s
+
+    def via_file(job):
+        job.count_file(path, params)
+        job.cutoff(rs.t)
+        job.build_macro_nodes(0)
+        job.macro_nodes(out=out)
+        return job.summary()
+
+    def timed(fn, *a):
+        t0 = time.perf_counter()
+        r = fn(*a)
+        return r, (time.perf_counter() - t0) * 1e3
+
+    res = {"read_only": [], "memory": [], "file": []}
+    with pk.Job(ctx) as job:
+        for step in range(args.warmup + args.steps):
+            _, t_read = timed(read_only)
+            sm, t_mem = timed(via_memory, job)
+            sf, t_file = timed(via_file, job)
+            assert (sm.n_windows, sm.n_unique, sm.n_kept, sm.n_nodes) == (sf.n_windows, sf.n_unique, sf.n_kept,
+                                                                         sf.n_nodes)
+            if step >= args.warmup:
+                res["read_only"].append(t_read)
+                res["memory"].append(t_mem)
+                res["file"].append(t_file)
+    med = {k: statistics.median(v) for k, v in res.items()}
+    line = {"metric": "file_to_macro_nodes_ms", "impl": "ours", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": False, "data": "synthetic",
+            "value": round(med["file"], 3), "unit": "ms",
+            "memory_path_ms": round(med["memory"], 3), "file_read_only_ms": round(med["read_only"], 3),
+            "file_read_gbs": round(F / med["read_only"] / 1e6, 2),
+            "kmers_per_s_file_path": sm.n_windows / (med["file"] * 1e-3),
+            "config": {"workload": rs.name, "fasta_bytes": F, "kmer_windows": sm.n_windows,
+                       "page_cache": "warm", "host_threads": os.cpu_count()}}
+    print(json.dumps(line), flush=True)
+    os.remove(path)
+    os.rmdir(tmpdir)
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -454,6 +543,8 @@ def main():
         return run_serve(args, rank, world)
     if args.batch:
         return run_batch(args, rank, world)
+    if args.ingest:
+        return run_ingest(args, rank, world)
 
     import numpy as np
     import torch

@@ -22,6 +22,11 @@
  *   pk_copy_macro_nodes           the MN_map contents (MacroNode suffix/prefix counts,
  *                                 includes/distribute_kmers.h:533-658)
  *   pk_run / pk_run_device        the driver sequence src/distribute_kmers.cpp:147-168
+ *   pk_fasta_slice / pk_count_file
+ *                                 perform_input_reading + DivideReads,
+ *                                 src/input_reading.cpp:68-243, 246-303 (a rank's
+ *                                 record-aligned slice of the FASTA file), streamed
+ *                                 to the device and counted
  */
 #ifndef PAKMAN_GB300_H
 #define PAKMAN_GB300_H
@@ -47,7 +52,10 @@ typedef enum pk_status {
   PK_ERR_DEVICE = 8,    /* a kernel reported failure (bounded wait expired,
                            on-chip capacity exceeded); results are not valid */
   PK_ERR_BUSY = 9,      /* serving: no capacity right now, retry later */
-  PK_ERR_NO_DEVICE = 10 /* no usable CUDA device */
+  PK_ERR_NO_DEVICE = 10, /* no usable CUDA device */
+  PK_ERR_IO = 11         /* the input file cannot be opened or read (the reference
+                            prints "Couldn't open the input FASTA file" and exits 2,
+                            src/input_reading.cpp:260-265) */
 } pk_status;
 
 typedef struct pk_ctx pk_ctx;
@@ -108,6 +116,24 @@ pk_status pk_job_memory(pk_job* job, uint64_t* bytes);
 pk_status pk_count(pk_job* job, const char* fasta, uint64_t n, const pk_params* p);
 pk_status pk_count_device(pk_job* job, const void* d_fasta, uint64_t n, const pk_params* p);
 pk_status pk_table_info(pk_job* job, uint64_t* n_unique, uint64_t* n_windows, uint64_t* n_reads);
+
+/* ---- file ingest: replaces perform_input_reading ----------------------------------
+ * The slice of a FASTA file that MPI rank `rank` of `n_ranks` reads in the reference
+ * (DivideReads): rank r nominally owns bytes [r*(S/n), (r+1)*(S/n)) of the S-byte
+ * file (the last rank to the end); its data start at the first '>' at or after its
+ * nominal start (rank 0: byte 0) and end at the first '>' at or after the next rank's
+ * nominal start (the last rank: end of file).  The reference looks for that '>'
+ * inside an overlap of read_length + 100 bytes; here the search runs on to the end
+ * of the file, which gives the same slice whenever the reference's search ends inside
+ * its overlap.  The slices of ranks 0..n-1 tile the file.  Host only (no device). */
+pk_status pk_fasta_slice(const char* path, int32_t rank, int32_t n_ranks, int32_t read_length,
+                         uint64_t* offset, uint64_t* length);
+/* pk_count on rank `rank`'s slice of the file, streamed: reader threads fill pinned
+ * staging pieces from the file while earlier pieces are copied to the device and
+ * line-scanned, so reading, copying and scanning overlap.  n_ranks = 1 counts the
+ * whole file.  PK_ERR_IO when the file cannot be opened or read. */
+pk_status pk_count_file(pk_job* job, const char* path, int32_t rank, int32_t n_ranks, const pk_params* p);
+
 /* Load an existing frequency table instead of counting (the input of the PaK-Graph
  * builder, Pakman_Subgraph::build_graph, src/pakman_graph.hpp:592-673, whose table
  * comes from elsewhere).  Rows ascending and unique, keys below 4^k in the layout of

@@ -60,6 +60,19 @@ def build_reference(k: int) -> Optional[str]:
     return exe if os.path.exists(exe) else None
 
 
+def build_divide_reference() -> Optional[str]:
+    """Build oracle/_ref/divide_reads_ref (the reference's DivideReads called alone for
+    any rank and rank count), if the reference tree is present."""
+    exe = os.path.join(REF_OUT, "divide_reads_ref")
+    if os.path.exists(exe):
+        return exe
+    if not os.path.isdir(REFERENCE_TREE):
+        return None
+    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), "divide", "K=32", "-j8"],
+                          stdout=subprocess.DEVNULL)
+    return exe if os.path.exists(exe) else None
+
+
 _lib = None
 
 
@@ -278,6 +291,38 @@ class RefRun:
     seconds: dict
     stdout: str
     wiring: Optional[tuple] = None  # read_wire_dump(): (WIRE_DTYPE rows, suffix exts, prefix exts)
+
+
+def divide_reads(data: bytes, rank: int, size: int, overlap: int) -> Optional[bytes]:
+    """One MPI rank's input data as the reference's DivideReads computes it from the
+    file bytes (src/input_reading.cpp:68-243): rank r reads bytes
+    [r*L, r*L + L - 1 + overlap] with L = filesize // size (the last rank up to the end
+    of the file), skips the bytes before the first '>' of that chunk (ranks > 0) and
+    ends at the first '>' at or after chunk offset L (every rank but the last).  The
+    overlap is read_length + 100 (src/input_reading.cpp:251).  Returns None where the
+    reference's scans would run past its chunk, which its loops do not bound."""
+    fs = len(data)
+    local = fs // size
+    start = rank * local
+    end = start + local - 1 + overlap
+    if rank == size - 1:
+        end = fs - 1
+    n = end - start + 1                  # the chunk length the reference allocates
+    chunk = data[start:end + 1]          # a read past the end of the file comes back short
+    locstart, locend = 0, n
+    if rank != 0:
+        i = chunk.find(b">")
+        if i < 0:
+            return None
+        locstart = i
+    if rank != size - 1:
+        i = chunk.find(b">", n - overlap)
+        if i < 0:
+            return None
+        locend = i
+    if locend < locstart:
+        return None
+    return chunk[locstart:locend]
 
 
 def read_table_dump(path: str):

@@ -5,9 +5,9 @@ ABI in ``include/pakman_gb300.h``; this package is the host-side mirror of the
 reference's interface for that path.  There is no CPU fallback.
 """
 from .api import (KEY128, KMERPAIRS64, KMERPAIRS128, Batch, BatchResult, Context, EmptyAfterCutoff,  # noqa: F401
-                  FormatError, Job, MacroNodeTable, PakmanError, PakmanSession, RequestInfo,
+                  FormatError, InputFileError, Job, MacroNodeTable, PakmanError, PakmanSession, RequestInfo,
                   Server, Summary,
-                  default_params, key_dtype, to_key128)
+                  default_params, fasta_slice, key_dtype, to_key128)
 from .capi import lib as load_library  # noqa: F401
 
 __all__ = ["Context", "Job", "Server", "Batch", "BatchResult", "RequestInfo", "PakmanSession", "MacroNodeTable", "Summary", "default_params",

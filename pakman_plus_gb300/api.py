@@ -16,6 +16,7 @@ Two layers over the C ABI:
 from __future__ import annotations
 
 import ctypes
+import os
 from ctypes import byref, c_float, c_int, c_uint32, c_uint64, c_void_p
 from dataclasses import dataclass
 from typing import Dict, Optional, Tuple
@@ -23,7 +24,7 @@ from typing import Dict, Optional, Tuple
 import numpy as np
 
 from . import capi
-from .capi import EmptyAfterCutoff, FormatError, PakmanError, check, default_params  # noqa: F401
+from .capi import EmptyAfterCutoff, FormatError, InputFileError, PakmanError, check, default_params  # noqa: F401
 
 KEY128 = np.dtype([("lo", "<u8"), ("hi", "<u8")])
 KMERPAIRS64 = np.dtype([("seq", "<u8"), ("k_count", "<i4")])  # packed, 12 bytes
@@ -45,6 +46,15 @@ def to_key128(keys: np.ndarray) -> np.ndarray:
     out["lo"] = keys
     out["hi"] = 0
     return out
+
+
+def fasta_slice(path: str, rank: int = 0, n_ranks: int = 1, read_length: int = 0) -> Tuple[int, int]:
+    """(offset, length) of the slice of a FASTA file that rank `rank` of `n_ranks` reads
+    (the reference's DivideReads rule; pk_fasta_slice).  Needs no device."""
+    off, ln = c_uint64(), c_uint64()
+    check(capi.lib().pk_fasta_slice(os.fsencode(path), rank, n_ranks, read_length, byref(off), byref(ln)),
+          "pk_fasta_slice")
+    return off.value, ln.value
 
 
 class Context:
@@ -169,6 +179,13 @@ class Job:
     def count_device(self, ptr: int, n: int, params: capi.PkParams):
         self.params = params
         check(capi.lib().pk_count_device(self._h, c_void_p(ptr), n, byref(params)), "pk_count_device")
+
+    def count_file(self, path: str, params: capi.PkParams, rank: int = 0, n_ranks: int = 1):
+        """Count rank `rank`'s slice of a FASTA file (the whole file for one rank),
+        streamed from disk to the device (pk_count_file)."""
+        self.params = params
+        check(capi.lib().pk_count_file(self._h, os.fsencode(path), rank, n_ranks, byref(params)),
+              "pk_count_file")
 
     def load_table(self, keys: np.ndarray, counts: np.ndarray, params: capi.PkParams):
         """Use an existing ascending, unique (k-mer, count) table instead of counting."""

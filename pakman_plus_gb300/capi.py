@@ -26,6 +26,7 @@ PK_ERR_LIMIT = 7
 PK_ERR_DEVICE = 8
 PK_ERR_BUSY = 9
 PK_ERR_NO_DEVICE = 10
+PK_ERR_IO = 11
 
 
 class PkParams(ctypes.Structure):
@@ -103,8 +104,12 @@ class Busy(PakmanError):
     pass
 
 
+class InputFileError(PakmanError):
+    """The FASTA file cannot be opened or read (the reference exits with status 2)."""
+
+
 _ERR_CLASSES = {PK_ERR_FORMAT: FormatError, PK_ERR_EMPTY: EmptyAfterCutoff,
-                PK_ERR_NOMEM: OutOfMemory, PK_ERR_BUSY: Busy}
+                PK_ERR_NOMEM: OutOfMemory, PK_ERR_BUSY: Busy, PK_ERR_IO: InputFileError}
 
 _lib = None
 
@@ -124,6 +129,8 @@ _SIGS = {
     "pk_job_memory": (c_int, [c_void_p, POINTER(c_uint64)]),
     "pk_count": (c_int, [c_void_p, c_void_p, c_uint64, POINTER(PkParams)]),
     "pk_count_device": (c_int, [c_void_p, c_void_p, c_uint64, POINTER(PkParams)]),
+    "pk_count_file": (c_int, [c_void_p, c_char_p, c_int32, c_int32, POINTER(PkParams)]),
+    "pk_fasta_slice": (c_int, [c_char_p, c_int32, c_int32, c_int32, POINTER(c_uint64), POINTER(c_uint64)]),
     "pk_table_load": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64, POINTER(PkParams)]),
     "pk_table_info": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64)]),
     "pk_copy_table": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64]),

@@ -86,10 +86,10 @@ void pk::job_free_all(pk_job* j) {
 
 // per-stage CUDA events on the job's stream (begin/end pairs, so host-side gaps
 // between stages are not charged to a kernel)
-static void mark_begin(pk_job* j, int st) {
+void pk::mark_begin(pk_job* j, int st) {
   if (j->timing) cudaEventRecord(j->ev0[st], j->stream);
 }
-static void mark_end(pk_job* j, int st) {
+void pk::mark_end(pk_job* j, int st) {
   if (j->timing) {
     cudaEventRecord(j->ev1[st], j->stream);
     j->ev_rec[st] = true;
@@ -123,6 +123,7 @@ const char* pk_status_string(pk_status s) {
     case PK_ERR_DEVICE: return "device-side failure";
     case PK_ERR_BUSY: return "busy";
     case PK_ERR_NO_DEVICE: return "no CUDA device";
+    case PK_ERR_IO: return "input file cannot be read";
   }
   return "unknown status";
 }
@@ -219,6 +220,10 @@ void pk_job_destroy(pk_job* j) {
   }
   if (j->d_sc) cudaFree(j->d_sc);
   if (j->h_sc) cudaFreeHost(j->h_sc);
+  for (int i = 0; i < pk_job::kIngestBufs; i++) {
+    if (j->ing_host[i]) cudaFreeHost(j->ing_host[i]);
+    if (j->ing_ev[i]) cudaEventDestroy(j->ing_ev[i]);
+  }
   if (j->own_stream) cudaStreamDestroy(j->stream);
   delete j;
 }
@@ -340,7 +345,7 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   PK_TRY(job_alloc(j, j->bstart, sizeof(uint32_t) * (B + 1)));
   if (hb < j->bbits) PK_TRY(job_alloc(j, j->hstart, sizeof(uint32_t) * (HB + 1)));
   uint32_t* hstart = (uint32_t*)(hb < j->bbits ? j->hstart.p : j->bstart.p);
-  if (!j->graph_mode) {
+  if (!j->graph_mode && !j->lines_ready) {
     Scalars init{};
     memset(&init, 0, sizeof(init));
     init.s0 = ~0ull;
@@ -364,7 +369,8 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   a.sc = j->d_sc;
 
   mark_begin(j, ST_LINES);
-  PK_CUDA(launch_line_scan(a, j->stream));
+  if (j->lines_ready) PK_CUDA(launch_tile_prefix(a, j->stream));
+  else PK_CUDA(launch_line_scan(a, j->stream));
   mark_end(j, ST_LINES);
   mark_begin(j, ST_BUCKET_COUNT);
   PK_CUDA(launch_bucket_count(a, j->wide, j->stream));

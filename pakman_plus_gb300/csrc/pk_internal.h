@@ -137,6 +137,11 @@ struct WireRow {
 
 // Launchers (all stream-ordered, no host synchronisation).
 cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st);
+// the line scan in two halves: per-tile newline counts for tiles [tile0, tile0 + ntiles)
+// (any order, any number of launches), then the prefix over all tiles
+cudaError_t launch_line_tiles(const uint8_t* buf, unsigned long long F, uint32_t* tile_nl, Scalars* sc,
+                              unsigned long long tile0, unsigned long long ntiles, cudaStream_t st);
+cudaError_t launch_tile_prefix(const CountArgs& a, cudaStream_t st);
 cudaError_t launch_bucket_count(const CountArgs& a, int wide, cudaStream_t st);
 cudaError_t launch_fine_count(const void* in, const uint32_t* cstart, const uint32_t* slice_start,
                               uint32_t* bcount, int k, int bbits, int cbits, int wide, uint32_t* ticket,

@@ -209,8 +209,9 @@ __device__ void block_or_and(KeyT& x_or, KeyT& x_and, KeyT* s_red) {
 // Newlines per 64 KB tile, the first '>' and the number of '>' bytes.
 __global__ void __launch_bounds__(256) k_line_scan(const uint8_t* __restrict__ buf,
                                                    unsigned long long F, uint32_t* tile_nl,
-                                                   Scalars* sc) {
-  const unsigned long long t0 = (unsigned long long)blockIdx.x * kTileBytes;
+                                                   Scalars* sc, unsigned long long tile0) {
+  const unsigned long long tile = tile0 + blockIdx.x;
+  const unsigned long long t0 = tile * kTileBytes;
   const unsigned long long t1 = min(t0 + (unsigned long long)kTileBytes, F);
   uint32_t nl = 0, gt = 0;
   unsigned long long first = ~0ull;
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(256) k_line_scan(const uint8_t* __restrict__ b
     uint32_t a = 0, b = 0;
     unsigned long long f = ~0ull;
     for (int i = 0; i < (int)(blockDim.x >> 5); i++) { a += s_nl[i]; b += s_gt[i]; f = min(f, s_first[i]); }
-    tile_nl[blockIdx.x] = a;
+    tile_nl[tile] = a;
     if (b) atomicAdd(&sc->n_reads, (unsigned long long)b);
     if (f != ~0ull) atomicMin(&sc->s0, f);
   }
@@ -2045,11 +2046,23 @@ size_t mn_smem_bytes(int wide) { return wide ? MnSmem<u128>::bytes : MnSmem<uint
 int bucket_ctas_per_sm(int) { return 2; }
 int mn_ctas_per_sm(int wide) { return wide ? 5 : 8; }
 
-cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st) {
+cudaError_t launch_line_tiles(const uint8_t* buf, unsigned long long F, uint32_t* tile_nl, Scalars* sc,
+                              unsigned long long tile0, unsigned long long ntiles, cudaStream_t st) {
+  if (ntiles > 0) k_line_scan<<<(unsigned)ntiles, 256, 0, st>>>(buf, F, tile_nl, sc, tile0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_prefix(const CountArgs& a, cudaStream_t st) {
   const int ntiles = (int)((a.F + kTileBytes - 1) / kTileBytes);
-  if (ntiles > 0) k_line_scan<<<ntiles, 256, 0, st>>>(a.fasta, a.F, a.tile_nl, a.sc);
   k_tile_prefix<<<1, 1024, 0, st>>>(a.fasta, a.F, a.tile_nl, ntiles, a.sc);
   return cudaGetLastError();
+}
+
+cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st) {
+  const unsigned long long ntiles = (a.F + kTileBytes - 1) / kTileBytes;
+  cudaError_t e = launch_line_tiles(a.fasta, a.F, a.tile_nl, a.sc, 0, ntiles, st);
+  if (e != cudaSuccess) return e;
+  return launch_tile_prefix(a, st);
 }
 
 template <typename KeyT, bool SCATTER>

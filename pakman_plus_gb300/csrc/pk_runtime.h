@@ -83,6 +83,12 @@ struct pk_job {
   // window count is bounded by ncap and scalars were initialised by the caller
   bool graph_mode = false;
   uint64_t ncap = 0;
+  // file ingest (pk_count_file): the tiles were line-scanned and the scalars set up
+  // as the pieces landed, so counting starts at the tile prefix
+  bool lines_ready = false;
+  static constexpr int kIngestBufs = 8;  // pinned staging pieces (two per reader thread)
+  void* ing_host[kIngestBufs] = {};
+  cudaEvent_t ing_ev[kIngestBufs] = {};
   cudaEvent_t ev0[ST_COUNT_] = {}, ev1[ST_COUNT_] = {};
   bool ev_rec[ST_COUNT_] = {};
 };
@@ -100,6 +106,9 @@ pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_params
 pk_status sync_scalars(pk_job* j);
 pk_status cutoff_enqueue(pk_job* j, int t);
 pk_status mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound);
+// per-stage CUDA events on the job's stream (when timing is on)
+void mark_begin(pk_job* j, int st);
+void mark_end(pk_job* j, int st);
 }  // namespace pk
 
 #endif  // PK_RUNTIME_H

@@ -136,26 +136,15 @@ int main(int argc, char** argv) {
          node_threshold);
   fflush(stdout);
 
-  // ---- input reading: the whole file into pinned host memory
-  double t0 = now_s();
+  // ---- input reading (perform_input_reading): the file is streamed to the device
+  // by pk_count_file below; an unreadable file ends the run as the reference's does
   FILE* fin = fopen(input.c_str(), "rb");
   if (!fin) {
     fprintf(stderr, "Couldn't open the input FASTA file\n");
     exit(2);
   }
-  fseek(fin, 0, SEEK_END);
-  const long flen = ftell(fin);
-  fseek(fin, 0, SEEK_SET);
-  void* host = nullptr;
-  pk_status st = pk_host_alloc((uint64_t)(flen > 0 ? flen : 1), &host);
-  if (st != PK_OK) die_pk("pk_host_alloc", st);
-  if (flen > 0 && fread(host, 1, (size_t)flen, fin) != (size_t)flen) {
-    fprintf(stderr, "Couldn't open the input FASTA file\n");
-    exit(2);
-  }
   fclose(fin);
-  double t1 = now_s();
-  printf("File reading time (secs): %f, bytes: %ld\n", t1 - t0, flen);
+  pk_status st = PK_OK;
 
   pk_ctx* ctx = nullptr;
   pk_job* job = nullptr;
@@ -171,13 +160,18 @@ int main(int argc, char** argv) {
   p.drop_n = drop_n;
   p.batch_kmers = max_kmer_count;
 
-  // ---- counting (perform_kmer_counting)
+  // ---- input reading streamed into counting (perform_kmer_counting)
   double t2 = now_s();
-  if ((st = pk_count(job, (const char*)host, (uint64_t)flen, &p)) != PK_OK) die_pk("k-mer counting", st);
+  st = pk_count_file(job, input.c_str(), 0, 1, &p);
+  if (st == PK_ERR_IO) {
+    fprintf(stderr, "Couldn't open the input FASTA file\n");
+    exit(2);
+  }
+  if (st != PK_OK) die_pk("k-mer counting", st);
   uint64_t u = 0, nwin = 0, nreads = 0;
   pk_table_info(job, &u, &nwin, &nreads);
   double t3 = now_s();
-  printf("performing k-mer counting (secs): %f, reads: %llu, k-mer instances: %llu, unique k-mers: %llu\n",
+  printf("input reading and k-mer counting (secs): %f, reads: %llu, k-mer instances: %llu, unique k-mers: %llu\n",
          t3 - t2, (unsigned long long)nreads, (unsigned long long)nwin, (unsigned long long)u);
   const int wide = k > 32;
   if (!out_prefix.empty()) {
@@ -244,6 +238,5 @@ int main(int argc, char** argv) {
   printf("pakman-gb300-elapsed-time-no-io (secs): %f\n", t5 - t2);
   pk_job_destroy(job);
   pk_ctx_destroy(ctx);
-  pk_host_free(host);
   return 0;
 }
