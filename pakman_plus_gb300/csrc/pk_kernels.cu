@@ -90,17 +90,6 @@ __device__ __forceinline__ void st_release(unsigned long long* p, unsigned long 
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// Hint the L2 to fetch bytes [lo, hi) of `base` (one thread; the copy engine of the
-// SM runs it in the background).  The range is shrunk to 16-byte boundaries, as the
-// bulk prefetch requires, so it never reaches past `hi`.
-__device__ __forceinline__ void prefetch_l2(const void* base, unsigned long long lo, unsigned long long hi) {
-  const unsigned long long a = (reinterpret_cast<unsigned long long>(base) + lo + 15) & ~15ull;
-  const unsigned long long e = (reinterpret_cast<unsigned long long>(base) + hi) & ~15ull;
-  for (unsigned long long p = a; p < e; p += 65536) {
-    const uint32_t sz = (uint32_t)(e - p < 65536 ? e - p : 65536);
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(sz) : "memory");
-  }
-}
 
 // Decoupled look-back words: status in bits 62-63 (1 = aggregate, 2 = inclusive).
 constexpr unsigned long long kLbAgg = 1ull << 62;
@@ -1204,14 +1193,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       s_nb[1] = next_end;
       if (next_beta < (uint32_t)B) {
         next_beta = atomicAdd(&a.sc->ticket_bucket, 1u);
-        if (next_beta < (uint32_t)B) {
-          next_base = a.bstart[next_beta];
-          next_end = a.bstart[next_beta + 1];
-          // the next bucket's keys stream into L2 while this one is counted, so its
-          // hash pass reads at L2 latency
-          const unsigned long long e = min((unsigned long long)next_end, a.cap);
-          if (next_base < e) prefetch_l2(keys, sizeof(KeyT) * (unsigned long long)next_base, sizeof(KeyT) * e);
-        }
+        if (next_beta < (uint32_t)B) { next_base = a.bstart[next_beta]; next_end = a.bstart[next_beta + 1]; }
       }
     }
     __syncthreads();
