@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["bacterial", "plain", "longk"], default="bacterial")
     ap.add_argument("--scale", type=float, default=1.0)
-    ap.add_argument("--e2e-workers", type=int, default=2,
+    ap.add_argument("--e2e-workers", type=int, default=3,
                     help="jobs in flight in the end-to-end (serving API) measurement")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
