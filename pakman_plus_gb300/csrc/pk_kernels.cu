@@ -1281,15 +1281,21 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
           const uint32_t i = i0 + q * kBucketThreads + tid;
           rr[q] = i < n ? (keys[base + i] & rmask) : EMPTY;
         }
+        uint32_t fresh = 0;  // distinct keys this thread added in this round
 #pragma unroll
         for (int q = 0; q < PF; q++) {
           const KeyT r = rr[q];
           const bool v = r != EMPTY && (whole || (!(r < lo) && r < hi));
           if (v) {
             const int res = hash_insert<KeyT>(skey, scnt, hmask, r, 1u);
-            if (res == 2 || (res == 1 && atomicAdd(&s_unew, 1u) >= ulimit)) s_ovf = 1;
+            if (res == 2) s_ovf = 1;
+            fresh += res == 1;
           }
         }
+        // the distinct-key count grows once per warp and round (one shared atomic per
+        // new key cost 7 % of the kernel)
+        fresh = __reduce_add_sync(FULLMASK, fresh);
+        if (lane == 0 && fresh && atomicAdd(&s_unew, fresh) + fresh > ulimit) s_ovf = 1;
       }
       __syncthreads();
       bool ovf = s_ovf != 0;
