@@ -30,9 +30,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "k-mers/sec count+macro-node on 1 GB300 (% HBM roofline); served p50/p99 latency"
 UNIT = "k-mers/s"
-KERNELS_PER_STEP = 12  # line scan, tile prefix, bucket count, column prefix, bucket prefix,
-#                        coarse offsets, coarse scatter, fine scatter, bucket table, cutoff,
-#                        kept filter, macro-nodes
+KERNELS_PER_STEP = 14  # line scan, tile prefix, bucket count, column prefix, bucket prefix,
+#                        coarse offsets, coarse scatter, fine scatter, giant-chunk prefix, bucket
+#                        table (two launches: the plain and the giant-bucket kernel, one of
+#                        which returns at once), cutoff, kept filter, macro-nodes
 
 
 def parse():

@@ -143,6 +143,11 @@ pk_status presize(pk_job* j, uint64_t fmax, int k, int bbits, int t, int sms) {
   PK_TRY(job_alloc(j, j->nsuf, 16 * 2 * vcap));
   PK_TRY(job_alloc(j, j->npre, 16 * 2 * vcap));
   PK_TRY(job_alloc(j, j->flags_m, 8 * (size_t)B));
+  PK_TRY(job_alloc(j, j->gfirst, 4 * (size_t)B));
+  PK_TRY(job_alloc(j, j->gcount, 4 * (size_t)B));
+  PK_TRY(job_alloc(j, j->chunk_bucket, 4 * (fmax / kChunkKeys + 1)));
+  PK_TRY(job_alloc(j, j->gdone, 4 * (size_t)B));
+  PK_TRY(job_alloc(j, j->chunk_u, 4 * (fmax / kChunkKeys + 1)));
   return PK_OK;
 }
 

@@ -79,7 +79,9 @@ void pk::job_free_all(pk_job* j) {
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
-                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring};
+                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring,
+                   &j->gfirst, &j->gcount, &j->chunk_bucket, &j->gdone,
+                   &j->chunk_u};
   for (DevBuf* b : all) job_free(j, *b);
   j->dense_valid = false;
 }
@@ -251,7 +253,9 @@ pk_status pk_job_memory(pk_job* j, uint64_t* bytes) {
                    &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
-                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring};
+                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring,
+                   &j->gfirst, &j->gcount, &j->chunk_bucket, &j->gdone,
+                   &j->chunk_u};
   uint64_t s = 0;
   for (DevBuf* b : all) s += b->bytes;
   *bytes = s;
@@ -438,8 +442,22 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   }
   mark_end(j, ST_SCATTER_FINE);
   mark_begin(j, ST_TABLE);
+  // giant buckets are reduced chunk by chunk first (chunk items ahead of the buckets)
+  PK_TRY(job_alloc(j, j->gfirst, sizeof(uint32_t) * (size_t)B));
+  PK_TRY(job_alloc(j, j->gcount, sizeof(uint32_t) * (size_t)B));
+  PK_TRY(job_alloc(j, j->gdone, sizeof(uint32_t) * (size_t)B));
+  PK_TRY(job_alloc(j, j->chunk_bucket, sizeof(uint32_t) * (size_t)(N / kChunkKeys + 1)));
+  PK_TRY(job_alloc(j, j->chunk_u, sizeof(uint32_t) * (size_t)(N / kChunkKeys + 1)));
+  PK_CUDA(launch_giant_chunks((const uint32_t*)j->bstart.p, j->bbits, (uint32_t*)j->gfirst.p,
+                              (uint32_t*)j->gcount.p, (uint32_t*)j->chunk_bucket.p, (uint32_t*)j->gdone.p,
+                              j->d_sc, j->stream));
   BucketArgs b{};
   b.keys = j->keys.p;
+  b.gfirst = (const uint32_t*)j->gfirst.p;
+  b.gcount = (const uint32_t*)j->gcount.p;
+  b.chunk_bucket = (const uint32_t*)j->chunk_bucket.p;
+  b.gdone = (uint32_t*)j->gdone.p;
+  b.chunk_u = (uint32_t*)j->chunk_u.p;
   b.bstart = (const uint32_t*)j->bstart.p;
   b.tkeys = j->tkeys.p;
   b.tcounts = (uint32_t*)j->tcounts.p;

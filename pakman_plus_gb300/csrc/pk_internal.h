@@ -38,6 +38,11 @@ constexpr int kMaxPartBits = 18;   // partition digits (table buckets) at most
 constexpr int kHistBits = 15;      // digits the counting pass histograms in shared memory
 constexpr int kSortBinBits = 10;    // top remainder bits of the per-bucket counting sort
 constexpr int kBinMax = 128;        // largest bin sorted by ranking (else radix sort)
+// Giant buckets (skewed input: a homopolymer or tandem repeat and its error variants)
+// are first reduced chunk by chunk, by many CTAs, to (key, count) pairs.
+constexpr int kChunkKeys = 32768;                   // keys per chunk of a giant bucket
+constexpr uint32_t kGiantKeys = 16u * kChunkKeys;   // a bucket this large is giant
+constexpr uint32_t kChunkRaw = 0xffffffffu;         // chunk left as keys (too many distinct)
 
 struct Scalars {                    // device-side scalars of one job
   unsigned long long s0;            // index of the first '>' (F if none)
@@ -51,6 +56,7 @@ struct Scalars {                    // device-side scalars of one job
   uint32_t ticket_filter;
   uint32_t ticket_fine;
   uint32_t ticket_fcount;
+  uint32_t n_chunk_items;           // chunk items of giant buckets (table kernel)
   unsigned long long n_unique;      // U
   unsigned long long n_kept;        // V
   unsigned long long n_nodes;       // M
@@ -77,7 +83,8 @@ struct CountArgs {
 // The table is kept "sparse": the u rows of bucket b sit at [bstart[b], bstart[b] + u),
 // inside the bucket's own key range, ascending.
 struct BucketArgs {
-  const void* keys;          // bucketed keys (uint64 or u128), N entries
+  void* keys;                // bucketed keys (uint64 or u128), N entries; chunks of giant
+                             // buckets are rewritten in place as (key, count) pairs
   const uint32_t* bstart;    // 2^bbits + 1
   void* tkeys;               // table keys out (N capacity)
   uint32_t* tcounts;         // table counts out (N capacity)
@@ -88,6 +95,11 @@ struct BucketArgs {
   int k;
   int bbits;
   unsigned long long cap;    // table capacity (rows)
+  const uint32_t* gfirst;    // 2^bbits: first chunk item of each giant bucket (null: none)
+  const uint32_t* gcount;    // 2^bbits: its chunk items (0: not giant)
+  const uint32_t* chunk_bucket;  // per chunk item: its bucket
+  uint32_t* gdone;           // 2^bbits: chunk items of the bucket finished
+  uint32_t* chunk_u;         // per chunk item: pairs it left, or kChunkRaw
   Scalars* sc;
 };
 
@@ -137,6 +149,11 @@ struct WireRow {
 
 // Launchers (all stream-ordered, no host synchronisation).
 cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st);
+// chunk items of the giant buckets (n_b >= kGiantKeys): floor(n_b / kChunkKeys)
+// consecutive items each, from gfirst[b], gcount[b] of them; chunk_bucket maps an item
+// to its bucket; sc->n_chunk_items = all items; gdone = 0
+cudaError_t launch_giant_chunks(const uint32_t* bstart, int bbits, uint32_t* gfirst, uint32_t* gcount,
+                                uint32_t* chunk_bucket, uint32_t* gdone, Scalars* sc, cudaStream_t st);
 // the line scan in two halves: per-tile newline counts for tiles [tile0, tile0 + ntiles)
 // (any order, any number of launches), then the prefix over all tiles
 cudaError_t launch_line_tiles(const uint8_t* buf, unsigned long long F, uint32_t* tile_nl, Scalars* sc,

@@ -74,6 +74,15 @@ struct KeyOps<u128> {
   __device__ __forceinline__ static u128 cas(u128* p, u128 cmp, u128 val) { return atomicCAS(p, cmp, val); }
 };
 
+// A key loaded through L2 only (data another CTA of the same kernel wrote).
+__device__ __forceinline__ uint64_t ldcg_key(const uint64_t* p) {
+  return (uint64_t)__ldcg(reinterpret_cast<const unsigned long long*>(p));
+}
+__device__ __forceinline__ u128 ldcg_key(const u128* p) {
+  const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2*>(p));
+  return ((u128)v.y << 64) | v.x;
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned r;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
@@ -88,6 +97,12 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
 
 __device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
 
 
@@ -1137,13 +1152,167 @@ __device__ void write_bucket_rows(const KeyT* sk, const uint32_t* sc, uint32_t u
   }
 }
 
+// Chunk items of the giant buckets (one thread per bucket): a bucket of at least
+// kGiantKeys keys reserves floor(n / kChunkKeys) consecutive chunk items, gfirst[b] the
+// first and gcount[b] how many, and marks them as its own in chunk_bucket; the number
+// of chunk items ends in sc->n_chunk_items (zero beforehand); gdone = 0.
+__global__ void __launch_bounds__(256) k_giant_chunks(const uint32_t* __restrict__ bstart, int B,
+                                                      uint32_t* gfirst, uint32_t* gcount,
+                                                      uint32_t* chunk_bucket, uint32_t* gdone, Scalars* sc) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const uint32_t n = bstart[b + 1] - bstart[b];
+  const uint32_t c = n >= kGiantKeys ? n / kChunkKeys : 0u;
+  gdone[b] = 0;
+  gcount[b] = c;
+  uint32_t g0 = 0;
+  if (c) {
+    g0 = atomicAdd(&sc->n_chunk_items, c);
+    for (uint32_t i = 0; i < c; i++) chunk_bucket[g0 + i] = (uint32_t)b;
+  }
+  gfirst[b] = g0;
+}
+
+// One chunk item: keys [cb, cb + kChunkKeys) of a giant bucket are aggregated on chip.
+// When their distinct keys fit half the table they are written back over the chunk's
+// own slots as (remainder, count) pairs -- remainders in slots [cb, cb + u), counts as
+// uint32 from slot cb + kChunkKeys / 2 on -- and chunk_u = u; otherwise the chunk keeps
+// its keys and chunk_u = kChunkRaw.  The bucket item reads the pairs in place of the
+// keys, so a heavy k-mer's copies are summed by many CTAs instead of one.
+template <typename KeyT>
+__device__ __forceinline__ void aggregate_chunk(const BucketArgs& a, KeyT* keys_rw, unsigned long long cb, uint32_t item,
+                                uint32_t beta, KeyT rmask, KeyT* skey, uint32_t* scnt, uint32_t* s_warp,
+                                uint32_t* s_flag, uint32_t* s_cnt) {
+  constexpr int H = BucketCfg<KeyT>::H;
+  constexpr int PF = 4;
+  const KeyT EMPTY = ~(KeyT)0;
+  const int tid = threadIdx.x, lane = tid & 31;
+  for (uint32_t i = tid; i < (uint32_t)H; i += kBucketThreads) {
+    skey[i] = EMPTY;
+    scnt[i] = 0;
+  }
+  if (tid == 0) {
+    *s_flag = 0;
+    *s_cnt = 0;
+  }
+  __syncthreads();
+  for (uint32_t i0 = 0; i0 < (uint32_t)kChunkKeys; i0 += PF * kBucketThreads) {
+    if (*(volatile uint32_t*)s_flag) break;
+    KeyT rr[PF];
+#pragma unroll
+    for (int q = 0; q < PF; q++) rr[q] = keys_rw[cb + i0 + q * kBucketThreads + tid] & rmask;
+    uint32_t fresh = 0;
+#pragma unroll
+    for (int q = 0; q < PF; q++) {
+      const int res = hash_insert<KeyT>(skey, scnt, H - 1, rr[q], 1u);
+      if (res == 2) *s_flag = 1;
+      fresh += res == 1;
+    }
+    fresh = __reduce_add_sync(FULLMASK, fresh);
+    if (lane == 0 && fresh && atomicAdd(s_cnt, fresh) + fresh > (uint32_t)(H / 2)) *s_flag = 1;
+  }
+  __syncthreads();
+  const bool raw = *(volatile uint32_t*)s_flag != 0;
+  constexpr int SPT = H / kBucketThreads;
+  KeyT rk[SPT];
+  uint32_t rc[SPT];
+  uint32_t occ = 0;
+#pragma unroll
+  for (int q = 0; q < SPT; q++) {
+    rk[q] = skey[q * kBucketThreads + tid];
+    rc[q] = scnt[q * kBucketThreads + tid];
+    occ += rk[q] != EMPTY;
+  }
+  uint32_t u;
+  uint32_t off = block_exclusive_sum(occ, s_warp, u);  // ends with a barrier: every key was read
+  if (!raw && u <= (uint32_t)(H / 2)) {
+    uint32_t* pc = reinterpret_cast<uint32_t*>(keys_rw + cb + kChunkKeys / 2);
+#pragma unroll
+    for (int q = 0; q < SPT; q++) {
+      if (rk[q] != EMPTY) {
+        keys_rw[cb + off] = rk[q];
+        pc[off] = rc[q];
+        off++;
+      }
+    }
+  } else {
+    u = kChunkRaw;
+  }
+  if (tid == 0) a.chunk_u[item] = u;
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) atomicAdd(&a.gdone[beta], 1u);
+}
+
+// A giant bucket's item waits (bounded) until its chunk items are done and returns the
+// entries it will read: the chunks' pairs (or keys, where a chunk stayed raw) and the
+// keys after the last chunk.  On expiry it sets ERR_LOOKBACK and *s_fail.
+__device__ __forceinline__ uint32_t giant_entries(const BucketArgs& a, uint32_t beta, uint32_t n, uint32_t g0,
+                                               uint32_t nch, uint32_t* s_warp, uint32_t* s_fail) {
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    int spins = 0;
+    while (ld_acquire_u32(&a.gdone[beta]) < nch) {
+      if (++spins >= kLbSpinLimit) {
+        atomicOr(&a.sc->err, ERR_LOOKBACK);
+        *s_fail = 1;
+        break;
+      }
+      __nanosleep(spins < 64 ? 32 : 256);
+    }
+  }
+  __syncthreads();
+  uint32_t part = 0;
+  for (uint32_t j = tid; j < nch; j += kBucketThreads) {
+    const uint32_t cu = __ldcg(&a.chunk_u[g0 + j]);
+    part += cu == kChunkRaw ? (uint32_t)kChunkKeys : cu;
+  }
+  uint32_t tot;
+  block_exclusive_sum(part, s_warp, tot);
+  return tot + (n - nch * (uint32_t)kChunkKeys);
+}
+
+// One hash pass of a giant bucket's sub-range [lo, hi): chunk by chunk (pairs carry
+// their counts), then the tail keys.  Loads go through L2, as other CTAs wrote the
+// pairs during this kernel.
+template <typename KeyT>
+__device__ __forceinline__ void giant_pass(const BucketArgs& a, const KeyT* keys_rw, uint32_t base, uint32_t n,
+                                        uint32_t g0, uint32_t nch, bool whole, KeyT lo, KeyT hi, KeyT rmask,
+                                        KeyT* skey, uint32_t* scnt, uint32_t hmask, uint32_t ulimit,
+                                        uint32_t* s_ovf, uint32_t* s_unew) {
+  const int tid = threadIdx.x, lane = tid & 31;
+  for (uint32_t j = 0; j <= nch; j++) {
+    if (*(volatile uint32_t*)s_ovf) break;
+    const unsigned long long cb = (unsigned long long)base + (unsigned long long)j * kChunkKeys;
+    uint32_t len = n - nch * (uint32_t)kChunkKeys;
+    bool pairs = false;
+    if (j < nch) {
+      const uint32_t cu = __ldcg(&a.chunk_u[g0 + j]);
+      pairs = cu != kChunkRaw;
+      len = pairs ? cu : (uint32_t)kChunkKeys;
+    }
+    const uint32_t* pc = reinterpret_cast<const uint32_t*>(keys_rw + cb + kChunkKeys / 2);
+    uint32_t fresh = 0;
+    for (uint32_t i = tid; i < len; i += kBucketThreads) {
+      const KeyT r = ldcg_key(keys_rw + cb + i) & rmask;
+      if (whole || (!(r < lo) && r < hi)) {
+        const int res = hash_insert<KeyT>(skey, scnt, hmask, r, pairs ? __ldcg(pc + i) : 1u);
+        if (res == 2) *s_ovf = 1;
+        fresh += res == 1;
+      }
+    }
+    fresh = __reduce_add_sync(FULLMASK, fresh);
+    if (lane == 0 && fresh && atomicAdd(s_unew, fresh) + fresh > ulimit) *s_ovf = 1;
+  }
+}
+
 // Per bucket: aggregate the bucket's keys into (remainder, count) in an on-chip
 // hash table, radix-sort the distinct remainders and write them as table rows at
 // the bucket's own key range [bstart, bstart + u) ("sparse" table: no inter-bucket
 // dependency).  When the distinct keys of a bucket exceed the on-chip capacity the
 // bucket is counted in 2^slog sub-passes, each taking the keys whose next slog
 // remainder bits equal the sub-pass index (so sub-passes come out in key order).
-template <typename KeyT>
+template <typename KeyT, bool GIANT>
 __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a) {
   using SM = BucketSmem<KeyT>;
   constexpr int H = SM::H;
@@ -1179,26 +1348,61 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   if (tid == 0) s_ratio = 0.2f;
   const int slog_max = rem < 4 ? rem : 4;  // initial split guess (<= 16 sub-ranges)
 
-  // the next bucket's ticket and extent are fetched while the current one is counted
-  uint32_t next_beta = 0, next_base = 0, next_end = 0;
+  // Work tickets: the chunk items of giant buckets first (tickets [0, nci)), then the
+  // buckets.  A giant bucket waits (bounded) until its chunks are reduced; every chunk
+  // ticket was taken before any bucket ticket, by a CTA that waits on nothing, so the
+  // wait ends.  The next ticket and its bucket's extent are fetched while the current
+  // one is counted.
+  // Two instantiations are launched back to back and exactly one of them works: GIANT
+  // = false when the partition has no giant bucket (it carries none of their code, so
+  // the common case keeps its registers), GIANT = true otherwise, taking the chunk
+  // items first and then every bucket, so the giant buckets' own passes overlap the
+  // other buckets.
+  const uint32_t ng = a.gfirst ? a.sc->n_chunk_items : 0u;
+  if ((ng != 0) != GIANT) return;
+  const uint32_t nci = GIANT ? ng : 0u;
+  const uint32_t nt = nci + (uint32_t)B;
+  uint32_t* ticket = &a.sc->ticket_bucket;
+  KeyT* keys_rw = reinterpret_cast<KeyT*>(a.keys);
+  uint32_t next_t = 0, next_base = 0, next_end = 0;
+  auto bucket_of = [&](uint32_t tk) { return tk - nci; };
   if (tid == 0) {
-    next_beta = atomicAdd(&a.sc->ticket_bucket, 1u);
-    if (next_beta < (uint32_t)B) { next_base = a.bstart[next_beta]; next_end = a.bstart[next_beta + 1]; }
+    next_t = atomicAdd(ticket, 1u);
+    if (next_t >= nci && next_t < nt) {
+      const uint32_t b = bucket_of(next_t);
+      next_base = a.bstart[b];
+      next_end = a.bstart[b + 1];
+    }
   }
   while (true) {
     __syncthreads();
     if (tid == 0) {
-      s_beta = next_beta;
+      s_beta = next_t;
       s_nb[0] = next_base;
       s_nb[1] = next_end;
-      if (next_beta < (uint32_t)B) {
-        next_beta = atomicAdd(&a.sc->ticket_bucket, 1u);
-        if (next_beta < (uint32_t)B) { next_base = a.bstart[next_beta]; next_end = a.bstart[next_beta + 1]; }
+      if (next_t < nt) {
+        next_t = atomicAdd(ticket, 1u);
+        if (next_t >= nci && next_t < nt) {
+          const uint32_t b = bucket_of(next_t);
+          next_base = a.bstart[b];
+          next_end = a.bstart[b + 1];
+        }
       }
     }
     __syncthreads();
-    const uint32_t beta = s_beta;
-    if (beta >= (uint32_t)B) break;
+    const uint32_t t = s_beta;
+    if (t >= nt) break;
+    if (t < nci) {
+      if (tid == 0) {
+        const uint32_t gb = a.chunk_bucket[t];
+        s_nb[0] = gb;
+        s_nb[1] = a.bstart[gb] + (t - a.gfirst[gb]) * (uint32_t)kChunkKeys;
+      }
+      __syncthreads();
+      aggregate_chunk<KeyT>(a, keys_rw, s_nb[1], t, s_nb[0], rmask, skey, scnt, s_warp, &s_ovf, &s_unew);
+      continue;
+    }
+    const uint32_t beta = bucket_of(t);
     const uint32_t base = s_nb[0];
     const uint32_t n = s_nb[1] - base;
     if (tid == 0) s_fail = 0;
@@ -1209,14 +1413,20 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       }
       continue;
     }
+    // a giant bucket reads its chunks' pairs (or keys, where a chunk stayed raw) and the
+    // keys after its last chunk; n_eff = entries it reads
+    const uint32_t g0 = GIANT ? a.gfirst[beta] : 0u;
+    const uint32_t nch = GIANT ? a.gcount[beta] : 0u;
+    const uint32_t n_eff = nch ? giant_entries(a, beta, n, g0, nch, s_warp, &s_fail) : n;
     // Sub-ranges of the bucket are counted one at a time, in key order.  A sub-range
     // is an interval [lo, hi) of remainders.  The first split guesses from the
     // distinct/keys ratio seen so far; a sub-range whose distinct keys overflow the
     // on-chip table is cut at quantiles of a sample of its distinct keys, so skewed
     // buckets (a heavy k-mer and its error variants) split evenly.
     int slog = 0;
-    while (slog < slog_max && (float)(n >> slog) * s_ratio * 1.2f > (float)HALF) slog++;
-    if (tid == 0) {
+    while (slog < slog_max && (float)(n_eff >> slog) * s_ratio * 1.2f > (float)HALF) slog++;
+    if (tid == 0 && s_fail) s_sp = 0;
+    if (tid == 0 && !s_fail) {
       s_sp = 0;
       const int psh0 = rem - slog;
       for (int j = (1 << slog) - 1; j >= 0; j--) {
@@ -1228,8 +1438,8 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
     }
     uint32_t acc = 0;
     int attempts = 0;
-    bool failed = false;
     __syncthreads();
+    bool failed = s_fail != 0;  // a giant bucket whose chunks did not finish in time
     while (s_sp > 0) {
       const KeyT lo = s_stk_lo[s_sp - 1];
       const KeyT hi = s_stk_hi[s_sp - 1];
@@ -1244,7 +1454,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       // overflow splits the sub-range
       uint32_t Heff = 1024;
       {
-        const float uest = (float)n * s_ratio * 2.5f;
+        const float uest = (float)n_eff * s_ratio * 2.5f;
         while ((float)Heff < uest && Heff < (uint32_t)H) Heff <<= 1;
         if (!whole) Heff = H;
       }
@@ -1273,7 +1483,10 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       //     exceed half the table (the sort needs the other half)
       constexpr int PF = 4;  // keys loaded per thread before inserting
       const uint32_t ulimit = Heff / 2;
-      for (uint32_t i0 = 0; i0 < n; i0 += PF * kBucketThreads) {
+      if (nch)
+        giant_pass<KeyT>(a, keys_rw, base, n, g0, nch, whole, lo, hi, rmask, skey, scnt, hmask, ulimit, &s_ovf,
+                         &s_unew);
+      for (uint32_t i0 = 0; i0 < n && !nch; i0 += PF * kBucketThreads) {
         if (*(volatile uint32_t*)&s_ovf) break;
         KeyT rr[PF];
 #pragma unroll
@@ -1524,7 +1737,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       a.tsub[3 * beta + 1] = s_d[0] + s_d[1];
       a.tsub[3 * beta + 2] = s_d[0] + s_d[1] + s_d[2];
       atomicAdd(&a.sc->n_unique, (unsigned long long)acc);
-      s_ratio = 0.5f * s_ratio + 0.5f * ((float)acc / (float)n);
+      s_ratio = 0.5f * s_ratio + 0.5f * ((float)acc / (float)n_eff);
     }
   }
   __syncthreads();
@@ -2175,17 +2388,29 @@ static cudaError_t launch_bucket_t(const BucketArgs& a, int grid, cudaStream_t s
   const size_t smem = BucketSmem<KeyT>::bytes;
   static bool attr_set = false;  // a constant, so concurrent first calls agree
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_bucket_table<KeyT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_bucket_table<KeyT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_bucket_table<KeyT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
   if (grid <= 0) grid = sm_count() * bucket_ctas_per_sm(sizeof(KeyT) == 16);
-  k_bucket_table<KeyT><<<grid, kBucketThreads, smem, st>>>(a);
+  // exactly one of the two works (giant buckets present or not); the other returns
+  k_bucket_table<KeyT, false><<<grid, kBucketThreads, smem, st>>>(a);
+  k_bucket_table<KeyT, true><<<grid, kBucketThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_bucket_table(const BucketArgs& a, int wide, int grid, cudaStream_t st) {
   return wide ? launch_bucket_t<u128>(a, grid, st) : launch_bucket_t<uint64_t>(a, grid, st);
+}
+
+cudaError_t launch_giant_chunks(const uint32_t* bstart, int bbits, uint32_t* gfirst, uint32_t* gcount,
+                                uint32_t* chunk_bucket, uint32_t* gdone, Scalars* sc, cudaStream_t st) {
+  const int B = 1 << bbits;
+  k_giant_chunks<<<(B + 255) / 256, 256, 0, st>>>(bstart, B, gfirst, gcount, chunk_bucket, gdone, sc);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_histogram(const uint32_t* tcounts, unsigned long long u, int t,

@@ -75,7 +75,7 @@ struct pk_job {
   pk::Scalars* h_sc = nullptr;  // pinned mirror
   DevBuf fasta, tile_nl, counts, bstart, hstart, keys, tkeys, tcounts, tu, tsub, flags_m, hist, hist2,
       nkeys, nsuf, npre, packed, doff, dkeys, dcounts, flags_f, kkeys, kcounts, kstart, kcount, ksub,
-      coff, cstart, slice_start, fcur, wiring;
+      coff, cstart, slice_start, fcur, wiring, gfirst, gcount, chunk_bucket, gdone, chunk_u;
   bool dense_valid = false;
   bool wired = false;  // wiring matches the current macro-nodes
   bool timing = false;

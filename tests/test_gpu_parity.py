@@ -91,11 +91,10 @@ def test_every_key_width(k):
     assert_table_equal(pk.to_key128(keys), counts, ora.keys, ora.counts)
 
 
-def test_skewed_low_complexity_input():
-    """Tandem repeats and homopolymers: a few buckets hold most windows."""
-    rng = np.random.Generator(np.random.PCG64(5))
+def _low_complexity_fasta(n_reads, seed=5):
+    rng = np.random.Generator(np.random.PCG64(seed))
     reads = []
-    for i in range(3000):
+    for i in range(n_reads):
         kind = i % 3
         if kind == 0:
             s = np.resize(np.frombuffer(b"AC", np.uint8), 150)
@@ -106,7 +105,12 @@ def test_skewed_low_complexity_input():
         m = rng.random(150) < 0.01
         s = np.where(m, np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, 150)], s)
         reads.append(s.astype(np.uint8))
-    fa = synth.reads_to_fasta(reads)
+    return synth.reads_to_fasta(reads)
+
+
+def test_skewed_low_complexity_input():
+    """Tandem repeats and homopolymers: a few buckets hold most windows."""
+    fa = _low_complexity_fasta(3000)
     for k, bb in ((32, 0), (32, 4), (63, 0)):
         ora = po.run(fa, k, 21)
         s, keys, counts, hist, mn, err = run_gpu(fa, k, 21, 10, bucket_bits=bb)
@@ -114,6 +118,21 @@ def test_skewed_low_complexity_input():
         assert s.cutoff == ora.cutoff
         if ora.mn is not None:
             assert_mn_equal(mn, ora.mn.keys, ora.mn.suf, ora.mn.pre)
+
+
+@pytest.mark.parametrize("k,bb", [(32, 0), (32, 2), (63, 0), (21, 3)])
+def test_giant_buckets(k, bb):
+    """Buckets of hundreds of thousands of keys (a homopolymer, a dinucleotide repeat and
+    their error variants) are reduced chunk by chunk by many CTAs to (key, count) pairs
+    before the bucket is counted; with 2 or 3 partition digits every bucket is giant and
+    the chunks of random k-mers stay raw (too many distinct keys)."""
+    fa = _low_complexity_fasta(36000, seed=6)
+    ora = po.run(fa, k, 21)
+    s, keys, counts, hist, mn, err = run_gpu(fa, k, 21, 10, bucket_bits=bb)
+    assert_table_equal(keys, counts, ora.table.keys, ora.table.counts)
+    assert s.cutoff == ora.cutoff
+    if ora.mn is not None:
+        assert_mn_equal(mn, ora.mn.keys, ora.mn.suf, ora.mn.pre)
 
 
 def test_cutoff_with_other_t_and_explicit_min_count():
