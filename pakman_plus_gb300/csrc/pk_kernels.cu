@@ -2009,6 +2009,9 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
   // kept rows beyond the kept buffers were not written: nothing to merge (every CTA
   // reads the same flag, so all of them leave)
   if (tid == 0) s_beta = (a.sc->err & ERR_BOUNDS) ? 1u : 0u;
+  // merge positions start in range, so even runs that break the sorted-input contract
+  // only ever index the segment arrays
+  for (int i = tid; i < kMnCap; i += kMnThreads) ord[i] = 0;
   __syncthreads();
   if (s_beta) return;
 
