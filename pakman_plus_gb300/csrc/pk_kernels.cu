@@ -746,9 +746,14 @@ __global__ void __launch_bounds__(256) k_coarse_offsets(const uint32_t* __restri
   __shared__ uint32_t s_c[1 << kCoarseBits];
   const int c = blockIdx.x;
   const int B = 1 << bbits, Cn = 1 << cbits, fb = bbits - cbits;
-  for (int i = threadIdx.x; i < Cn; i += blockDim.x) s_c[i] = 0;
-  __syncthreads();
-  for (int b = threadIdx.x; b < B; b += blockDim.x) atomicAdd(&s_c[b >> fb], counts[(size_t)c * B + b]);
+  // a warp sums the 2^fb fine buckets of one coarse region at a time
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int g = warp; g < Cn; g += nw) {
+    uint32_t sum = 0;
+    for (int i = lane; i < (1 << fb); i += 32) sum += counts[(size_t)c * B + ((size_t)g << fb) + i];
+    sum = __reduce_add_sync(FULLMASK, sum);
+    if (lane == 0) s_c[g] = sum;
+  }
   __syncthreads();
   for (int g = threadIdx.x; g < Cn; g += blockDim.x) coff[(size_t)c * Cn + g] = bstart[g << fb] + s_c[g];
   if (c == 0 && threadIdx.x == 0) {
@@ -1028,16 +1033,30 @@ __global__ void __launch_bounds__(512, 2) k_fine_count(const KeyT* __restrict__ 
 
 // counts[c][b] -> exclusive prefix over chunks (in place); totals into bstart[b].
 __global__ void __launch_bounds__(256) k_col_prefix(uint32_t* counts, int grid, int B, uint32_t* totals) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
+  // a CTA takes 32 bucket columns; its 8 warps take consecutive bands of chunk rows,
+  // sum them (coalesced 128-byte rows), and take their band's offset from the sums of
+  // the bands above
+  __shared__ uint32_t s_band[8][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int b = blockIdx.x * 32 + lane;
+  const int per = (grid + 7) / 8;
+  const int c0 = min(grid, warp * per), c1 = min(grid, c0 + per);
+  uint32_t sum = 0;
+  if (b < B)
+    for (int c = c0; c < c1; c++) sum += counts[(size_t)c * B + b];
+  s_band[warp][lane] = sum;
+  __syncthreads();
   uint32_t run = 0;
-  for (int c = 0; c < grid; c++) {
-    size_t i = (size_t)c * B + b;
-    uint32_t v = counts[i];
-    counts[i] = run;
-    run += v;
+  for (int w = 0; w < warp; w++) run += s_band[w][lane];
+  if (b < B) {
+    for (int c = c0; c < c1; c++) {
+      const size_t i = (size_t)c * B + b;
+      const uint32_t v = counts[i];
+      counts[i] = run;
+      run += v;
+    }
+    if (warp == 7) totals[b] = run;  // the last band ends at the last chunk
   }
-  totals[b] = run;
 }
 
 // Exclusive prefix of bstart[0..B) in place, bstart[B] = total.  One block: each
@@ -2376,7 +2395,7 @@ cudaError_t launch_prefix(uint32_t* counts, int B, cudaStream_t st) {
 
 cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st) {
   const int B = 1 << a.bbits;
-  k_col_prefix<<<(B + 255) / 256, 256, 0, st>>>(a.counts, a.grid, B, a.bstart);
+  k_col_prefix<<<(B + 31) / 32, 256, 0, st>>>(a.counts, a.grid, B, a.bstart);
   k_bucket_prefix<<<1, 1024, 0, st>>>(a.bstart, B);
   return cudaGetLastError();
 }
