@@ -171,7 +171,6 @@ cudaError_t launch_batch_emit(const Scalars* sc, unsigned long long* counter, un
                               unsigned long long* res, const void* nkeys, const void* nsuf, const void* npre,
                               int wide, void* okeys, void* osuf, void* opre, cudaStream_t st);
 cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st);
-cudaError_t launch_scatter(const CountArgs& a, void* keys_out, int wide, cudaStream_t st);
 // Two-pass partition: coarse regions (pass 1) then fine buckets inside each region.
 // keys per pass-2 slice for a fan-out of 2^fb fine buckets per coarse region
 int fine_slice_keys(int wide, int fb);

@@ -1,17 +1,21 @@
 // sm_103a kernels for PaKman's k-mer counting -> histogram cutoff -> macro-node path.
 //
 // Pipeline for one read set (FASTA bytes resident in HBM):
-//   k_line_scan      newline count per 64 KB tile, first '>' and '>' count
-//   k_tile_prefix    exclusive newline prefix over tiles, newlines before the first '>'
-//   k_extract<..,0>  per chunk: roll every k-mer window, histogram of bucket ids (smem)
-//   k_col_prefix     per bucket: prefix over chunks; k_bucket_prefix: bucket starts
-//   k_extract<..,1>  per chunk: roll again, scatter each key to its bucket slot
-//   k_bucket_table   per bucket: hash-aggregate in smem, radix-sort the distinct
-//                    keys, write the sorted (k-mer, count) table with a decoupled
-//                    look-back over buckets, count histogram and next-digit offsets
-//   k_cutoff         first minimum of the count histogram over [1, t)
-//   k_macro_nodes    per (k-1)-mer bucket: merge the suffix-side and prefix-side
-//                    streams of kept k-mers into macro-node records
+//   k_line_scan        newline count per 64 KB tile, first '>' and '>' count
+//   k_tile_prefix      exclusive newline prefix over tiles, newlines before the first '>'
+//   k_extract          per chunk: roll every k-mer window, histogram of bucket ids (smem)
+//   k_col_prefix       per bucket: prefix over chunks; k_bucket_prefix: bucket starts;
+//   k_coarse_offsets   each chunk's segment of every coarse region
+//   k_scatter_coarse   roll again, keys to their coarse region through shared-memory rings
+//   k_scatter_fine     per slice of a coarse region: keys to their bucket, staged by bucket
+//   k_giant_chunks     chunk items of buckets too large for one CTA
+//   k_bucket_table     per bucket: hash-aggregate in smem, sort the distinct keys, write
+//                      the (k-mer, count) rows, count histogram and next-digit counts
+//   k_cutoff           first minimum of the count histogram over [1, t)
+//   k_filter_kept      kept rows (count >= cutoff), dense, with a decoupled look-back
+//   k_macro_nodes      per (k-1)-mer unit: merge the suffix-side and prefix-side
+//                      streams of kept k-mers into macro-node records
+//   k_wire             initial wiring of every macro-node
 //
 // A bucket is the leading `bbits` bits of the 2k-bit key, so buckets in index order
 // are the table in key order and no global merge is needed.
@@ -419,9 +423,21 @@ __device__ void check_record_start(const uint8_t* __restrict__ buf, unsigned lon
   if (counts) atomicOr(err, ERR_FORMAT);
 }
 
-template <typename KeyT, bool SCATTER>
+// Bucket of the window whose newest byte has age sh/2, for 64-bit keys whose bucket
+// digits lie in the high word of the key (shift = 2k - digits >= 34): only the high words
+// of the code and bit-2 planes are funnel-shifted.  The bit-2 plane's carry from the low
+// word lands in bits 0-1 of the high word, below the digits.
+__device__ __forceinline__ uint32_t window_bucket_hi(const Roll& s, int sh, int shift_hi, uint32_t hmask) {
+  const uint32_t xh = __funnelshift_r((uint32_t)(s.r0 >> 32), (uint32_t)s.r1, sh);
+  const uint32_t nh = __funnelshift_r((uint32_t)(s.n0 >> 32), (uint32_t)s.n1, sh);
+  return ((xh | (nh << 2)) >> shift_hi) & hmask;
+}
+
+// Counting pass: per chunk, the bucket histogram of its windows (FASTB: the bucket is
+// taken from the high words alone, see window_bucket_hi).
+template <typename KeyT, bool FASTB>
 __global__ void __launch_bounds__(kExtractThreads, 1)
-k_extract(CountArgs a, KeyT* __restrict__ keys_out) {
+k_extract(CountArgs a) {
   extern __shared__ uint32_t s_bins[];
   __shared__ uint32_t s_wpar[kExtractThreads / 32];
   __shared__ uint32_t s_red[kExtractThreads / 32];
@@ -437,11 +453,7 @@ k_extract(CountArgs a, KeyT* __restrict__ keys_out) {
   const unsigned long long s0 = a.sc->s0;
   const int c = blockIdx.x;
 
-  if (!SCATTER) {
-    for (int i = tid; i < B; i += kExtractThreads) s_bins[i] = 0;
-  } else {
-    for (int i = tid; i < B; i += kExtractThreads) s_bins[i] = a.bstart[i] + a.counts[(size_t)c * B + i];
-  }
+  for (int i = tid; i < B; i += kExtractThreads) s_bins[i] = 0;
   __syncthreads();
 
   const unsigned long long c0 = (unsigned long long)c * a.chunk;
@@ -508,7 +520,7 @@ k_extract(CountArgs a, KeyT* __restrict__ keys_out) {
         uint32_t in = 0xffffu;
         if (p + 16 > F) in &= (1u << (uint32_t)(F - p)) - 1u;
         if (p < s0) in &= s0 - p >= 16 ? 0u : ~((1u << (uint32_t)(s0 - p)) - 1u);
-        if (!SCATTER) {
+        {
           uint32_t ends = ub.nl & odd & in;  // newlines that end sequence lines
           while (ends) {
             int q = __ffs(ends) - 1;
@@ -530,22 +542,17 @@ k_extract(CountArgs a, KeyT* __restrict__ keys_out) {
           if (!((v >> j) & 1u)) continue;
           const int age = 15 - j;
           if (!all_clear && !window_clear(s, age, k)) continue;
-          const KeyT key = window_key<KeyT>(s, 2 * age, kmask);
-          const uint32_t beta = (uint32_t)(key >> shift);
-          if (SCATTER) {
-            uint32_t pos = atomicAdd(&s_bins[beta], 1u);
-            if (pos < a.n_keys) keys_out[pos] = key;
-            else atomicOr(&a.sc->err, ERR_BOUNDS);
-          } else {
-            atomicAdd(&s_bins[beta], 1u);
-            local++;
-          }
+          uint32_t beta;
+          if (FASTB) beta = window_bucket_hi(s, 2 * age, shift - 32, (uint32_t)(B - 1));
+          else beta = (uint32_t)(window_key<KeyT>(s, 2 * age, kmask) >> shift);
+          atomicAdd(&s_bins[beta], 1u);
+          local++;
         }
       }
     }
   }
   __syncthreads();
-  if (!SCATTER) {
+  {
     for (int i = tid; i < B; i += kExtractThreads) a.counts[(size_t)c * B + i] = s_bins[i];
     uint32_t x = local;
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULLMASK, x, o);
@@ -1387,7 +1394,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   auto bucket_of = [&](uint32_t tk) { return tk - nci; };
   if (tid == 0) {
     next_t = atomicAdd(ticket, 1u);
-    if (next_t >= nci && next_t < nt) {
+    if ((!GIANT || next_t >= nci) && next_t < nt) {
       const uint32_t b = bucket_of(next_t);
       next_base = a.bstart[b];
       next_end = a.bstart[b + 1];
@@ -1401,7 +1408,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       s_nb[1] = next_end;
       if (next_t < nt) {
         next_t = atomicAdd(ticket, 1u);
-        if (next_t >= nci && next_t < nt) {
+        if ((!GIANT || next_t >= nci) && next_t < nt) {
           const uint32_t b = bucket_of(next_t);
           next_base = a.bstart[b];
           next_end = a.bstart[b + 1];
@@ -1411,7 +1418,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
     __syncthreads();
     const uint32_t t = s_beta;
     if (t >= nt) break;
-    if (t < nci) {
+    if (GIANT && t < nci) {
       if (tid == 0) {
         const uint32_t gb = a.chunk_bucket[t];
         s_nb[0] = gb;
@@ -2016,7 +2023,6 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
 
   const int tid = threadIdx.x;
   const int Bu = 1 << (a.bbits - 2 * a.level);  // node units
-  const int B = 1 << a.bbits;
   const int k = a.k;
   const int nb = 2 * (k - 1);
   const KeyT succ_mask = KeyOps<KeyT>::mask(nb);
@@ -2288,25 +2294,27 @@ cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st) {
   return launch_tile_prefix(a, st);
 }
 
-template <typename KeyT, bool SCATTER>
-static cudaError_t launch_extract_t(const CountArgs& a, KeyT* out, cudaStream_t st) {
+template <typename KeyT, bool FASTB>
+static cudaError_t launch_extract_t(const CountArgs& a, cudaStream_t st) {
   const size_t smem = sizeof(uint32_t) << a.bbits;
   // the attribute is shared by every thread launching this kernel, so it is always
   // set to the largest histogram (15 partition digits), never to this launch's size
   static bool attr_set = false;  // same value from every thread, so a race is benign
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_extract<KeyT, SCATTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_extract<KeyT, FASTB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(sizeof(uint32_t) << 15));
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  k_extract<KeyT, SCATTER><<<a.grid, kExtractThreads, smem, st>>>(a, out);
+  k_extract<KeyT, FASTB><<<a.grid, kExtractThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_bucket_count(const CountArgs& a, int wide, cudaStream_t st) {
-  return wide ? launch_extract_t<u128, false>(a, nullptr, st)
-              : launch_extract_t<uint64_t, false>(a, nullptr, st);
+  if (wide) return launch_extract_t<u128, false>(a, st);
+  // bucket digits in the key's high word: the 32-bit bucket path
+  if (2 * a.k - a.bbits >= 34) return launch_extract_t<uint64_t, true>(a, st);
+  return launch_extract_t<uint64_t, false>(a, st);
 }
 
 template <typename KeyT>
@@ -2400,10 +2408,6 @@ cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_scatter(const CountArgs& a, void* keys_out, int wide, cudaStream_t st) {
-  return wide ? launch_extract_t<u128, true>(a, reinterpret_cast<u128*>(keys_out), st)
-              : launch_extract_t<uint64_t, true>(a, reinterpret_cast<uint64_t*>(keys_out), st);
-}
 
 template <typename KeyT>
 static cudaError_t launch_bucket_t(const BucketArgs& a, int grid, cudaStream_t st) {
