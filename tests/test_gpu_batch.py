@@ -80,3 +80,24 @@ def test_batch_rejects_mixed_key_widths():
     with pk.Batch(ctx(), branches=2) as b:
         with pytest.raises(pk.PakmanError):
             b.run([s32, s63])
+
+
+def _low_complexity(n_reads, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    kind = np.arange(n_reads) % 3
+    mat = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, (n_reads, 150))].copy()
+    mat[kind == 0] = np.resize(np.frombuffer(b"AC", np.uint8), 150)
+    mat[kind == 1] = ord("A")
+    err = rng.random((n_reads, 150)) < 0.01
+    mat = np.where(err, np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, (n_reads, 150))], mat)
+    return synth.matrix_to_fasta(mat.astype(np.uint8))
+
+
+def test_batch_sets_with_giant_buckets():
+    """Sets whose homopolymer and dinucleotide buckets hold 0.5M+ keys take the chunked
+    giant-bucket path inside the captured graph, next to ordinary sets."""
+    sets = _sets(n=3, seed=1200) + [(_low_complexity(36000, s), pk.default_params(k=32, num_buckets=21, coverage=10))
+                                    for s in (7, 8)]
+    with pk.Batch(ctx(), branches=2) as b:
+        res = b.run(sets)
+        _check(b, sets, res)
