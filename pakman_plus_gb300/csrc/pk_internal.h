@@ -24,7 +24,6 @@ enum : uint32_t {
 };
 
 constexpr int kTileBytes = 65536;   // line-scan tile; chunk boundaries are multiples of it
-constexpr int kExtractThreads = 512;
 constexpr int kSegBytes = 64;       // bytes per thread per extraction step
 constexpr int kBucketThreads = 512;
 constexpr int kMnThreads = 128;

@@ -433,16 +433,24 @@ __device__ __forceinline__ uint32_t window_bucket_hi(const Roll& s, int sh, int 
   return ((xh | (nh << 2)) >> shift_hi) & hmask;
 }
 
+// Counting-pass threads: 1024 for 64-bit keys (more warps hide the decode's latency),
+// 512 for 128-bit keys (whose windows need twice the registers)
+template <typename KeyT>
+struct CountCfg {
+  static constexpr int T = sizeof(KeyT) == 8 ? 1024 : 512;
+};
+
 // Counting pass: per chunk, the bucket histogram of its windows (FASTB: the bucket is
 // taken from the high words alone, see window_bucket_hi).
 template <typename KeyT, bool FASTB>
-__global__ void __launch_bounds__(kExtractThreads, 1)
+__global__ void __launch_bounds__(CountCfg<KeyT>::T, 1)
 k_extract(CountArgs a) {
+  constexpr int NT = CountCfg<KeyT>::T;
   extern __shared__ uint32_t s_bins[];
-  __shared__ uint32_t s_wpar[kExtractThreads / 32];
-  __shared__ uint32_t s_red[kExtractThreads / 32];
+  __shared__ uint32_t s_wpar[NT / 32];
+  __shared__ uint32_t s_red[NT / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int NW = kExtractThreads / 32;
+  const int NW = NT / 32;
   const int B = 1 << a.bbits;
   const int k = a.k;
   const int shift = 2 * k - a.bbits;
@@ -453,7 +461,7 @@ k_extract(CountArgs a) {
   const unsigned long long s0 = a.sc->s0;
   const int c = blockIdx.x;
 
-  for (int i = tid; i < B; i += kExtractThreads) s_bins[i] = 0;
+  for (int i = tid; i < B; i += NT) s_bins[i] = 0;
   __syncthreads();
 
   const unsigned long long c0 = (unsigned long long)c * a.chunk;
@@ -462,7 +470,7 @@ k_extract(CountArgs a) {
   const int warm_units = (k - 1 + 15) / 16;
   if (c0 < c1 && s0 < F) {
     uint32_t carry = (a.tile_nl[c0 / kTileBytes] ^ a.sc->nl_before_s0) & 1u;
-    for (unsigned long long base = c0; base < c1; base += (unsigned long long)kExtractThreads * kSegBytes) {
+    for (unsigned long long base = c0; base < c1; base += (unsigned long long)NT * kSegBytes) {
       const unsigned long long seg = base + (unsigned long long)tid * kSegBytes;
       const bool active = seg < c1;
       uint32_t w[4][4];
@@ -553,7 +561,7 @@ k_extract(CountArgs a) {
   }
   __syncthreads();
   {
-    for (int i = tid; i < B; i += kExtractThreads) a.counts[(size_t)c * B + i] = s_bins[i];
+    for (int i = tid; i < B; i += NT) a.counts[(size_t)c * B + i] = s_bins[i];
     uint32_t x = local;
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULLMASK, x, o);
     if (lane == 0) s_red[warp] = x;
@@ -576,7 +584,11 @@ struct CoarseCfg {
   static constexpr int C = 1 << kCoarseBits;               // coarse buckets
   static constexpr int R = sizeof(KeyT) == 8 ? 128 : 64;    // ring slots per bucket
   static constexpr int FU = 128 / (int)sizeof(KeyT);        // keys per 128-byte line
-  static constexpr int BP = sizeof(KeyT) == 8 ? 16 : 8;     // window positions per batch
+  // threads: 1024 for 64-bit keys (the ring inserts and flushes are issue-bound and
+  // gain from the extra warps), 512 for 128-bit keys (whose rings hold half the slots)
+  static constexpr int T = sizeof(KeyT) == 8 ? 1024 : 512;
+  static constexpr int BP = 8;                              // window positions per batch
+                                                            // (T * BP keys between flushes)
   static constexpr size_t smem = sizeof(KeyT) * C * R;
 };
 
@@ -593,7 +605,7 @@ __device__ __forceinline__ void coarse_flush(KeyT* ring, uint32_t* w, uint32_t* 
                                              unsigned long long cap, uint32_t* err) {
   using CF = CoarseCfg<KeyT>;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int NW = kExtractThreads / 32;
+  constexpr int NW = CF::T / 32;
   for (int b = warp; b < CF::C; b += NW) {
     const uint32_t W = w[b];
     uint32_t Fv = f[b];
@@ -624,15 +636,15 @@ __device__ __forceinline__ void coarse_flush(KeyT* ring, uint32_t* w, uint32_t* 
 }
 
 template <typename KeyT>
-__global__ void __launch_bounds__(kExtractThreads, 1)
+__global__ void __launch_bounds__(CoarseCfg<KeyT>::T, 1)
 k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restrict__ out) {
   using CF = CoarseCfg<KeyT>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   KeyT* ring = reinterpret_cast<KeyT*>(smem_raw);
   __shared__ uint32_t s_w[CF::C], s_f[CF::C], s_g[CF::C];
-  __shared__ uint32_t s_wpar[kExtractThreads / 32];
+  __shared__ uint32_t s_wpar[CF::T / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int NW = kExtractThreads / 32;
+  const int NW = CF::T / 32;
   const int k = a.k;
   const int cshift = 2 * k - a.cbits;  // coarse bucket = leading cbits bits
   const KeyT kmask = KeyOps<KeyT>::mask(2 * k);
@@ -642,7 +654,7 @@ k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restric
   const unsigned long long s0 = a.sc->s0;
   const int c = blockIdx.x;
   const int Cn = 1 << a.cbits;
-  for (int i = tid; i < CF::C; i += kExtractThreads) {
+  for (int i = tid; i < CF::C; i += CF::T) {
     s_w[i] = 0;
     s_f[i] = 0;
     s_g[i] = i < Cn ? coff[(size_t)c * Cn + i] : 0;
@@ -653,7 +665,7 @@ k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restric
   const int warm_units = (k - 1 + 15) / 16;
   if (c0 < c1 && s0 < F) {
     uint32_t carry = (a.tile_nl[c0 / kTileBytes] ^ a.sc->nl_before_s0) & 1u;
-    for (unsigned long long base = c0; base < c1; base += (unsigned long long)kExtractThreads * kSegBytes) {
+    for (unsigned long long base = c0; base < c1; base += (unsigned long long)CF::T * kSegBytes) {
       const unsigned long long seg = base + (unsigned long long)tid * kSegBytes;
       const bool active = seg < c1;
       uint32_t w[4][4];
@@ -2306,7 +2318,7 @@ static cudaError_t launch_extract_t(const CountArgs& a, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  k_extract<KeyT, FASTB><<<a.grid, kExtractThreads, smem, st>>>(a);
+  k_extract<KeyT, FASTB><<<a.grid, CountCfg<KeyT>::T, smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -2326,7 +2338,7 @@ static cudaError_t launch_coarse_t(const CountArgs& a, const uint32_t* coff, Key
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  k_scatter_coarse<KeyT><<<a.grid, kExtractThreads, smem, st>>>(a, coff, out);
+  k_scatter_coarse<KeyT><<<a.grid, CoarseCfg<KeyT>::T, smem, st>>>(a, coff, out);
   return cudaGetLastError();
 }
 
