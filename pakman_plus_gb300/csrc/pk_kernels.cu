@@ -921,16 +921,23 @@ __global__ void __launch_bounds__(1024, 1) k_scatter_fine_big(const KeyT* __rest
   const int tid = threadIdx.x;
   const int Cn = 1 << cbits, fb = bbits - cbits, FB = 1 << fb;
   const int fshift = 2 * k - bbits;
+  // the region tables live in shared memory: the slice -> region search of every slice
+  // reads no global memory
+  __shared__ uint32_t s_ss[(1 << kCoarseBits) + 1], s_cs[(1 << kCoarseBits) + 1];
+  for (int i = tid; i <= Cn; i += FC::T) {
+    s_ss[i] = slice_start[i];
+    s_cs[i] = cstart[i];
+  }
   const uint32_t nslices = slice_start[Cn];
   while (true) {
     __syncthreads();
     if (tid == 0) {
       s_slice = atomicAdd(ticket, 1u);
       if (s_slice < nslices) {
-        int lo = 0, hi = Cn - 1;
+        int lo = 0, hi = Cn - 1;  // last g with slice_start[g] <= slice
         while (lo < hi) {
           int mid = (lo + hi + 1) >> 1;
-          if (slice_start[mid] <= s_slice) lo = mid; else hi = mid - 1;
+          if (s_ss[mid] <= s_slice) lo = mid; else hi = mid - 1;
         }
         s_g = lo;
       }
@@ -940,8 +947,8 @@ __global__ void __launch_bounds__(1024, 1) k_scatter_fine_big(const KeyT* __rest
     const uint32_t sl = s_slice;
     if (sl >= nslices) break;
     const uint32_t g = s_g;
-    const uint32_t r0 = cstart[g] + (sl - slice_start[g]) * FC::S;
-    const uint32_t r1 = min(r0 + (uint32_t)FC::S, cstart[g + 1]);
+    const uint32_t r0 = s_cs[g] + (sl - s_ss[g]) * FC::S;
+    const uint32_t r1 = min(r0 + (uint32_t)FC::S, s_cs[g + 1]);
     const uint32_t m = r1 - r0;
     for (uint32_t i0 = 0; i0 < m; i0 += FC::PR * FC::T) {
       KeyT xs[FC::PR];
@@ -1021,16 +1028,23 @@ __global__ void __launch_bounds__(512, 2) k_fine_count(const KeyT* __restrict__ 
   const int tid = threadIdx.x;
   const int Cn = 1 << cbits, fb = bbits - cbits, FB = 1 << fb;
   const int fshift = 2 * k - bbits;
+  // the region tables live in shared memory: the slice -> region search of every slice
+  // reads no global memory
+  __shared__ uint32_t s_ss[(1 << kCoarseBits) + 1], s_cs[(1 << kCoarseBits) + 1];
+  for (int i = tid; i <= Cn; i += FC::T) {
+    s_ss[i] = slice_start[i];
+    s_cs[i] = cstart[i];
+  }
   const uint32_t nslices = slice_start[Cn];
   while (true) {
     __syncthreads();
     if (tid == 0) {
       s_slice = atomicAdd(ticket, 1u);
       if (s_slice < nslices) {
-        int lo = 0, hi = Cn - 1;
+        int lo = 0, hi = Cn - 1;  // last g with slice_start[g] <= slice
         while (lo < hi) {
           int mid = (lo + hi + 1) >> 1;
-          if (slice_start[mid] <= s_slice) lo = mid; else hi = mid - 1;
+          if (s_ss[mid] <= s_slice) lo = mid; else hi = mid - 1;
         }
         s_g = lo;
       }
@@ -1040,8 +1054,8 @@ __global__ void __launch_bounds__(512, 2) k_fine_count(const KeyT* __restrict__ 
     const uint32_t sl = s_slice;
     if (sl >= nslices) break;
     const uint32_t g = s_g;
-    const uint32_t r0 = cstart[g] + (sl - slice_start[g]) * slice_keys;
-    const uint32_t r1 = min(r0 + slice_keys, cstart[g + 1]);
+    const uint32_t r0 = s_cs[g] + (sl - s_ss[g]) * slice_keys;
+    const uint32_t r1 = min(r0 + slice_keys, s_cs[g + 1]);
     for (uint32_t i = r0 + tid; i < r1; i += FC::T)
       atomicAdd(&s_hist[(uint32_t)(in[i] >> fshift) & (uint32_t)(FB - 1)], 1u);
     __syncthreads();
