@@ -127,7 +127,6 @@ pk_status presize(pk_job* j, uint64_t fmax, int k, int bbits, int t, int sms) {
   PK_TRY(job_alloc(j, j->tkeys, W * fmax));
   PK_TRY(job_alloc(j, j->tcounts, 4 * fmax));
   PK_TRY(job_alloc(j, j->tu, 4 * (size_t)B));
-  PK_TRY(job_alloc(j, j->tsub, 12 * (size_t)B));
   PK_TRY(job_alloc(j, j->hist, 8 * (size_t)t));
   PK_TRY(job_alloc(j, j->coff, 4 * (size_t)sms * Cn));
   PK_TRY(job_alloc(j, j->cstart, 4 * (size_t)(Cn + 1)));

@@ -76,7 +76,7 @@ static void job_free(pk_job* j, DevBuf& b) {
 
 void pk::job_free_all(pk_job* j) {
   DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->hstart, &j->keys,  &j->tkeys,
-                   &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
+                   &j->tcounts, &j->tu,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
                    &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring,
@@ -250,7 +250,7 @@ pk_status pk_job_sync(pk_job* j) {
 pk_status pk_job_memory(pk_job* j, uint64_t* bytes) {
   if (!j || !bytes) return fail(PK_ERR_INVALID, "null argument");
   DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->hstart, &j->keys,  &j->tkeys,
-                   &j->tcounts, &j->tu,    &j->tsub,    &j->flags_m, &j->hist,  &j->hist2,
+                   &j->tcounts, &j->tu,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
                    &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring,
@@ -401,7 +401,6 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   PK_TRY(job_alloc(j, j->tkeys, (size_t)W * N));
   PK_TRY(job_alloc(j, j->tcounts, sizeof(uint32_t) * N));
   PK_TRY(job_alloc(j, j->tu, sizeof(uint32_t) * (size_t)B));
-  PK_TRY(job_alloc(j, j->tsub, sizeof(uint32_t) * 3 * (size_t)B));
   const int t = p->num_buckets;
   PK_TRY(job_alloc(j, j->hist, sizeof(unsigned long long) * (size_t)t));
   PK_CUDA(cudaMemsetAsync(j->hist.p, 0, sizeof(unsigned long long) * (size_t)t, j->stream));
@@ -462,7 +461,6 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   b.tkeys = j->tkeys.p;
   b.tcounts = (uint32_t*)j->tcounts.p;
   b.tu = (uint32_t*)j->tu.p;
-  b.tsub = (uint32_t*)j->tsub.p;
   b.hist = (unsigned long long*)j->hist.p;
   b.t = t;
   b.k = k;
@@ -541,12 +539,10 @@ pk_status pk_table_load(pk_job* j, const void* keys, const uint32_t* counts, uin
   PK_TRY(job_alloc(j, j->tcounts, 4 * (n ? n : 1)));
   PK_TRY(job_alloc(j, j->bstart, sizeof(uint32_t) * (B + 1)));
   PK_TRY(job_alloc(j, j->tu, sizeof(uint32_t) * (size_t)B));
-  PK_TRY(job_alloc(j, j->tsub, sizeof(uint32_t) * 3 * (size_t)B));
   if (n) {
     PK_CUDA(cudaMemcpyAsync(j->tkeys.p, keys, W * n, cudaMemcpyHostToDevice, j->stream));
     PK_CUDA(cudaMemcpyAsync(j->tcounts.p, counts, 4 * n, cudaMemcpyHostToDevice, j->stream));
   }
-  PK_CUDA(cudaMemsetAsync(j->tsub.p, 0, sizeof(uint32_t) * 3 * (size_t)B, j->stream));
   PK_CUDA(launch_table_bounds(j->tkeys.p, n, j->bbits, k, (uint32_t*)j->bstart.p, (uint32_t*)j->tu.p,
                               wide, j->stream));
   Scalars init{};

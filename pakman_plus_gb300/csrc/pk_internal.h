@@ -88,7 +88,6 @@ struct BucketArgs {
   void* tkeys;               // table keys out (N capacity)
   uint32_t* tcounts;         // table counts out (N capacity)
   uint32_t* tu;              // 2^bbits: rows per bucket
-  uint32_t* tsub;            // 3 * 2^bbits: rows of the bucket whose next 2 key bits are < 1, 2, 3
   unsigned long long* hist;  // t bins (zeroed)
   int t;
   int k;

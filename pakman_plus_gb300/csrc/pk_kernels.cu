@@ -10,7 +10,7 @@
 //   k_scatter_fine     per slice of a coarse region: keys to their bucket, staged by bucket
 //   k_giant_chunks     chunk items of buckets too large for one CTA
 //   k_bucket_table     per bucket: hash-aggregate in smem, sort the distinct keys, write
-//                      the (k-mer, count) rows, count histogram and next-digit counts
+//                      the (k-mer, count) rows and the count histogram
 //   k_cutoff           first minimum of the count histogram over [1, t)
 //   k_filter_kept      kept rows (count >= cutoff), dense, with a decoupled look-back
 //   k_macro_nodes      per (k-1)-mer unit: merge the suffix-side and prefix-side
@@ -1175,33 +1175,14 @@ __device__ __forceinline__ void emit_row(const BucketArgs& a, KeyT* __restrict__
   }
 }
 
-// Rows [base+acc, base+acc+u) of a bucket from the sorted on-chip run (sk, sc), plus the
-// per-bucket counts of rows by the next two key bits (s_d).
+// Rows [base+acc, base+acc+u) of a bucket from the sorted on-chip run (sk, sc).
 template <typename KeyT>
 __device__ void write_bucket_rows(const KeyT* sk, const uint32_t* sc, uint32_t u, const BucketArgs& a,
                                   uint32_t beta, int rem, uint32_t base, uint32_t acc,
-                                  KeyT* __restrict__ tkeys, uint32_t* s_d, uint32_t* shist) {
-  const int tid = threadIdx.x, lane = tid & 31;
+                                  KeyT* __restrict__ tkeys, uint32_t* shist) {
   const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
-  uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
-  for (uint32_t i0 = 0; i0 < u; i0 += kBucketThreads) {
-    const uint32_t i = i0 + tid;
-    const bool v = i < u;
-    uint32_t d2 = 3;
-    if (v) {
-      const KeyT r = sk[i];
-      emit_row<KeyT>(a, tkeys, (unsigned long long)base + acc + i, hi_bits | r, sc[i], shist);
-      d2 = (uint32_t)(KeyOps<KeyT>::shr(r, rem - 2) & 3);
-    }
-    dl0 += __popc(__ballot_sync(FULLMASK, v && d2 == 0));
-    dl1 += __popc(__ballot_sync(FULLMASK, v && d2 == 1));
-    dl2 += __popc(__ballot_sync(FULLMASK, v && d2 == 2));
-  }
-  if (lane == 0) {
-    if (dl0) atomicAdd(&s_d[0], dl0);
-    if (dl1) atomicAdd(&s_d[1], dl1);
-    if (dl2) atomicAdd(&s_d[2], dl2);
-  }
+  for (uint32_t i = threadIdx.x; i < u; i += kBucketThreads)
+    emit_row<KeyT>(a, tkeys, (unsigned long long)base + acc + i, hi_bits | sk[i], sc[i], shist);
 }
 
 // Chunk items of the giant buckets (one thread per bucket): a bucket of at least
@@ -1377,7 +1358,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   uint16_t* wc = reinterpret_cast<uint16_t*>(smem + SM::off_wc);
   uint32_t* shist = reinterpret_cast<uint32_t*>(smem + SM::off_hist);
   __shared__ uint32_t s_warp[33];
-  __shared__ uint32_t s_beta, s_ovf, s_d[3], s_fail, s_nb[2], s_unew;
+  __shared__ uint32_t s_beta, s_ovf, s_fail, s_nb[2], s_unew;
   __shared__ int s_sp;
   __shared__ KeyT s_stk_lo[kBucketStack];  // pending sub-ranges [lo, hi) of the bucket
   __shared__ KeyT s_stk_hi[kBucketStack];
@@ -1459,10 +1440,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
     const uint32_t n = s_nb[1] - base;
     if (tid == 0) s_fail = 0;
     if (n == 0) {
-      if (tid == 0) {
-        a.tu[beta] = 0;
-        a.tsub[3 * beta] = a.tsub[3 * beta + 1] = a.tsub[3 * beta + 2] = 0;
-      }
+      if (tid == 0) a.tu[beta] = 0;
       continue;
     }
     // a giant bucket reads its chunks' pairs (or keys, where a chunk stayed raw) and the
@@ -1486,7 +1464,6 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
         s_stk_hi[s_sp] = KeyOps<KeyT>::shl((KeyT)(uint32_t)(j + 1), psh0);
         s_sp++;
       }
-      s_d[0] = s_d[1] = s_d[2] = 0;
     }
     uint32_t acc = 0;
     int attempts = 0;
@@ -1671,28 +1648,13 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
           // element i of the binned run lands at row b0 + rank, within its bin's rows,
           // so neighbouring threads store to neighbouring rows
           const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
-          uint32_t dl0 = 0, dl1 = 0, dl2 = 0;
-          for (uint32_t i0 = 0; i0 < u; i0 += kBucketThreads) {
-            const uint32_t i = i0 + tid;
-            const bool v = i < u;
-            uint32_t d2 = 3;
-            if (v) {
-              const KeyT x = skey[i];
-              const uint32_t bi = (uint32_t)KeyOps<KeyT>::shr(x, dsh) & (nbins - 1);
-              const uint32_t b0 = bh[bi], b1 = b0 + bf[bi];
-              uint32_t rank = 0;
-              for (uint32_t j = b0; j < b1; j++) rank += skey[j] < x;
-              emit_row<KeyT>(a, tkeys, (unsigned long long)base + acc + b0 + rank, hi_bits | x, scnt[i], shist);
-              d2 = (uint32_t)(KeyOps<KeyT>::shr(x, rem - 2) & 3);
-            }
-            dl0 += __popc(__ballot_sync(FULLMASK, v && d2 == 0));
-            dl1 += __popc(__ballot_sync(FULLMASK, v && d2 == 1));
-            dl2 += __popc(__ballot_sync(FULLMASK, v && d2 == 2));
-          }
-          if (lane == 0) {
-            if (dl0) atomicAdd(&s_d[0], dl0);
-            if (dl1) atomicAdd(&s_d[1], dl1);
-            if (dl2) atomicAdd(&s_d[2], dl2);
+          for (uint32_t i = tid; i < u; i += kBucketThreads) {
+            const KeyT x = skey[i];
+            const uint32_t bi = (uint32_t)KeyOps<KeyT>::shr(x, dsh) & (nbins - 1);
+            const uint32_t b0 = bh[bi], b1 = b0 + bf[bi];
+            uint32_t rank = 0;
+            for (uint32_t j = b0; j < b1; j++) rank += skey[j] < x;
+            emit_row<KeyT>(a, tkeys, (unsigned long long)base + acc + b0 + rank, hi_bits | x, scnt[i], shist);
           }
         } else {
           // stable LSD radix sort of the binned run in [0, u) through [H/2, H/2 + u)
@@ -1772,7 +1734,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
             KeyT* tk = sk; sk = dk; dk = tk;
             uint32_t* tc = sc; sc = dc; dc = tc;
           }
-          write_bucket_rows<KeyT>(sk, sc, u, a, beta, rem, base, acc, tkeys, s_d, shist);
+          write_bucket_rows<KeyT>(sk, sc, u, a, beta, rem, base, acc, tkeys, shist);
         }
       }
       acc += u;
@@ -1785,9 +1747,6 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
     __syncthreads();
     if (tid == 0) {
       a.tu[beta] = acc;
-      a.tsub[3 * beta + 0] = s_d[0];
-      a.tsub[3 * beta + 1] = s_d[0] + s_d[1];
-      a.tsub[3 * beta + 2] = s_d[0] + s_d[1] + s_d[2];
       atomicAdd(&a.sc->n_unique, (unsigned long long)acc);
       s_ratio = 0.5f * s_ratio + 0.5f * ((float)acc / (float)n_eff);
     }

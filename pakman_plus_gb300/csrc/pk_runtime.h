@@ -73,7 +73,7 @@ struct pk_job {
   uint64_t mn_cap = 0;
   pk::Scalars* d_sc = nullptr;
   pk::Scalars* h_sc = nullptr;  // pinned mirror
-  DevBuf fasta, tile_nl, counts, bstart, hstart, keys, tkeys, tcounts, tu, tsub, flags_m, hist, hist2,
+  DevBuf fasta, tile_nl, counts, bstart, hstart, keys, tkeys, tcounts, tu, flags_m, hist, hist2,
       nkeys, nsuf, npre, packed, doff, dkeys, dcounts, flags_f, kkeys, kcounts, kstart, kcount, ksub,
       coff, cstart, slice_start, fcur, wiring, gfirst, gcount, chunk_bucket, gdone, chunk_u;
   bool dense_valid = false;
