@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--serve-jobs", type=int, default=5000)
     ap.add_argument("--serve-rate", type=float, default=200.0, help="mean arrivals per second")
     ap.add_argument("--serve-pool", type=int, default=32, help="distinct generated read sets")
-    ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--serve-workers", type=int, default=8)
     ap.add_argument("--serve-budget-gb", type=float, default=160.0)
     ap.add_argument("--ingest", action="store_true",
                     help="file ingest benchmark: FASTA file -> macro-node table on the host, read "
