@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--batch", action="store_true",
                     help="batching benchmark: many read sets in one CUDA-graph launch")
     ap.add_argument("--batch-sets", type=int, default=256)
-    ap.add_argument("--batch-branches", type=int, default=4)
+    ap.add_argument("--batch-branches", type=int, default=6)
     ap.add_argument("--serve", action="store_true",
                     help="serving benchmark: Poisson stream of jobs through pk_submit, p50/p99 latency")
     ap.add_argument("--serve-jobs", type=int, default=5000)
