@@ -176,3 +176,18 @@ def test_count_file_errors(tmp_path):
         good = _write(tmp_path, "good.fa", _fasta(4))
         job.count_file(good, p)
         assert job.summary().n_windows == po.count(_fasta(4), 32).counts.sum()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("data", [b"", b"no header here\nACGT\n", b">only-header"])
+def test_count_file_without_windows(tmp_path, data):
+    """Files with no k-mer window count to an empty table; the cutoff then ends the run
+    as the reference's MPI_Abort does (PK_ERR_EMPTY)."""
+    from gpu_helpers import ctx
+    path = _write(tmp_path, "in.fa", data)
+    p = pk.default_params(k=32)
+    with pk.Job(ctx()) as job:
+        job.count_file(path, p)
+        assert job.summary().n_windows == 0
+        with pytest.raises(pk.EmptyAfterCutoff):
+            job.cutoff(21)
