@@ -1,13 +1,14 @@
 /*
  * Single-rank stand-in for the MPI calls made by PaKman's k-mer counting,
- * histogram and macro-node translation units.
+ * histogram, macro-node and compaction translation units.
  *
  * TEST INFRASTRUCTURE ONLY: this header exists so the reference's own sources
  * (src/distribute_kmers.cpp, src/input_reading.cpp, src/kmer_counting.cpp,
- * src/kmer_histogram.cpp, src/mn_construct.cpp, src/timers.cpp) compile
+ * src/kmer_histogram.cpp, src/mn_construct.cpp, src/timers.cpp, the compaction
+ * units) compile
  * unmodified on a machine without MPI and run as one rank.  With one rank every
  * collective is a local copy: Allreduce/Reduce copy send to receive, Alltoall(v)
- * copy the rank-0 block, MPI-IO reads through stdio.  Nothing in the GPU
+ * and Allgather(v) copy the rank-0 block, MPI-IO reads through stdio.  Nothing in the GPU
  * product includes or links this file.
  */
 #ifndef PK_REF_MPI_SHIM_H
@@ -68,6 +69,10 @@ int MPI_Alltoall(const void* s, int scount, MPI_Datatype st, void* r, int rcount
                  MPI_Comm c);
 int MPI_Alltoallv(const void* s, const int* scounts, const int* sdispls, MPI_Datatype st, void* r,
                   const int* rcounts, const int* rdispls, MPI_Datatype rt, MPI_Comm c);
+int MPI_Allgather(const void* s, int scount, MPI_Datatype st, void* r, int rcount, MPI_Datatype rt,
+                  MPI_Comm c);
+int MPI_Allgatherv(const void* s, int scount, MPI_Datatype st, void* r, const int* rcounts,
+                   const int* rdispls, MPI_Datatype rt, MPI_Comm c);
 
 int MPI_File_open(MPI_Comm c, const char* name, int mode, MPI_Info info, MPI_File* fh);
 int MPI_File_get_size(MPI_File fh, MPI_Offset* size);

@@ -1,0 +1,107 @@
+"""The compaction oracle (oracle/pk_compact.py) against the reference's own iterative
+compaction: golden dumps made by tests/golden/make_compact_golden.py, a live run of
+the reference built here when its sources are present, and libstdc++'s std::sort for
+the wiring's unstable ranking."""
+import os
+import subprocess
+import zlib
+
+import numpy as np
+import pytest
+
+from oracle import pk_compact as pc
+from oracle import pk_oracle as po
+from pakman_plus_gb300 import synth
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = sorted(f[len("compact_"):-4] for f in os.listdir(GOLDEN) if f.startswith("compact_"))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, "compact_%s.npz" % name))
+    unz = lambda a: zlib.decompress(a.tobytes())  # noqa: E731
+    out = {"fasta": unz(z["fasta"]), "params": [int(x) for x in z["params"]],
+           "before": unz(z["before"]), "runs": []}
+    for thr in z["thresholds"]:
+        thr = int(thr)
+        out["runs"].append((thr, unz(z["after_%d" % thr]), unz(z["contigs_%d" % thr]),
+                            int(z["rounds_%d" % thr][0])))
+    return out
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_reproduces_reference_compaction(name):
+    g = load(name)
+    for thr, after, contigs, rounds in g["runs"]:
+        k, before = pc.parse_state(g["before"])
+        o = pc.compact(before, k, thr)
+        _, ref_after = pc.parse_state(after)
+        assert o.rounds == rounds
+        assert len(o.nodes) <= thr < len(before)
+        assert pc.state_view(o.nodes) == pc.state_view(ref_after)
+        assert o.contigs == pc.parse_contigs(contigs)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_canonical_start_matches_initial_wiring(name):
+    """The oracle's own start state (lists in ascending base order) has the initial
+    wiring that the C oracle's pko_wire_nodes (pinned to src/wire.cpp) computes."""
+    g = load(name)
+    k, rl, cov, t = g["params"]
+    ora = po.run(g["fasta"], k, t)
+    nodes = pc.initial_nodes(ora.mn.keys, ora.mn.suf, ora.mn.pre, k, cov)
+    w = po.wire(ora.mn.suf, ora.mn.pre, cov)
+    assert len(nodes) == w.size
+    for nd, row in zip(nodes, w):
+        assert len(nd.suf) == row["ns"] and len(nd.pre) == row["np"]
+        assert nd.suf[-1][2] == row["term_suf"] and nd.pre[-1][2] == row["term_pre"]
+        used = [x for x in nd.wires if x[2]]
+        assert len(used) == row["nw"]
+        assert [tuple(x) for x in row["wire"][:len(used)]] == used
+        assert [tuple(x) for x in row["begin"][:len(nd.begin)]] == list(nd.begin)
+    # the reference's own map holds the same nodes and entry multisets
+    _, ref = pc.parse_state(g["before"])
+    assert [nd.key for nd in ref] == [nd.key for nd in nodes]
+    for a, b in zip(ref, nodes):
+        assert sorted(map(tuple, (e[:4] for e in a.pre))) == sorted(map(tuple, (e[:4] for e in b.pre)))
+        assert [e[:4] for e in a.suf] == [e[:4] for e in b.suf]
+
+
+@pytest.fixture(scope="module")
+def stdsort(tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("ss") / "stdsort")
+    src = os.path.join(os.path.dirname(pc.__file__), "ref", "stdsort_harness.cpp")
+    try:
+        subprocess.run(["g++", "-O1", "-o", exe, src], check=True, capture_output=True)
+    except (OSError, subprocess.CalledProcessError):
+        pytest.skip("no C++ compiler")
+    return exe
+
+
+def test_std_sort_restatement_matches_libstdcxx(stdsort):
+    rng = np.random.default_rng(11)
+    cases = []
+    for n in list(range(0, 40)) + [47, 64, 100, 257, 1000]:
+        for spread in (1, 2, 4, 50):
+            cases.append([(int(rng.integers(0, spread)), int(rng.integers(0, spread))) for _ in range(n)])
+    cases.append([(3, 1)] * 70)  # all equal
+    cases.append([(i // 3, 0) for i in range(90)])  # ascending runs (descending order wanted)
+    cases.append([(90 - i, 2) for i in range(90)])
+    inp = "".join("%d %s\n" % (len(c), " ".join("%d %d" % vc for vc in c)) for c in cases)
+    out = subprocess.run([stdsort], input=inp, capture_output=True, text=True, check=True).stdout
+    lines = out.split("\n")
+    for c, line in zip(cases, lines):
+        idx = list(range(len(c)))
+        pc._std_sort(idx, lambda i, j: c[i][0] > c[j][0] or (c[i][0] == c[j][0] and c[i][1] > c[j][1]))
+        assert idx == ([int(x) for x in line.split()] if line.strip() else []), c
+
+
+def test_live_reference_run():
+    """A fresh seed through the reference built here (skipped without its sources)."""
+    if pc.build_compact_reference(32) is None:
+        pytest.skip("the reference tree is not present")
+    rs = synth.small_case(91, genome_len=6000, n_reads=4000, read_len=100, err=0.01, k=32, coverage=30)
+    r = pc.run_reference(rs.fasta, 32, 100, 30, 20)
+    o = pc.compact(r.before, 32, 20)
+    assert pc.state_view(o.nodes) == pc.state_view(r.after)
+    assert o.contigs == r.contigs
