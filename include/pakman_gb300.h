@@ -194,6 +194,57 @@ pk_status pk_wire_macro_nodes(pk_job* job, int32_t coverage);
 pk_status pk_copy_wiring(pk_job* job, pk_wiring* out, uint64_t capacity);
 pk_status pk_wiring_device(pk_job* job, const pk_wiring** d_wiring);
 
+/* ---- iterative compaction: replaces begin_iterative_compaction
+ * (src/iterative_compaction.cpp:131-464) -------------------------------------------
+ * Rounds of independent-set merging on the device until at most node_threshold
+ * macro-nodes remain (the reference's -n; its command line turns 0 into 100000,
+ * src/distribute_kmers.cpp:300-302).  A round merges every node whose non-terminal
+ * neighbours all have smaller (k-1)-mers (generate_id_set, src/merge_mn.cpp:289-432):
+ * each of its wires hands the predecessor a longer suffix and the successor a longer
+ * prefix (iterate_and_pack_mn :433-550, push_to_pred / push_to_succ :1325-1411), or
+ * becomes a partial contig when both ends are terminal; touched nodes are re-wired
+ * (MacroNode::setup_wiring, includes/distribute_kmers.h:550-657).  The start is the
+ * wired map of pk_wire_macro_nodes (lists in ascending base order).  Needs
+ * pk_build_macro_nodes; coverage 0 uses the job's params.coverage.  Lists are held on
+ * chip up to 32 entries a side (PK_ERR_DEVICE beyond, as for a node whose visits do
+ * not balance or a transfer whose target is missing, where the reference asserts or
+ * exits). */
+typedef struct pk_compaction_info {
+  uint64_t n_nodes;       /* nodes left (<= node_threshold) */
+  uint64_t n_entries;     /* prefix + suffix entries over those nodes */
+  uint64_t n_contigs;     /* partial contigs emitted by the rounds, in emission order */
+  uint64_t ext_bases;     /* total extension length over the entries */
+  uint64_t contig_bases;  /* total partial-contig length */
+  int32_t rounds;
+  int32_t key_bytes;      /* 8, or 16 for k > 32 */
+} pk_compaction_info;
+
+/* One prefix or suffix entry of a remaining node (MacroNode's per-entry vectors). */
+typedef struct pk_compact_entry {
+  uint64_t ext_offset;  /* into ext_bases: the extension's bases, one code per byte */
+  uint32_t ext_length;  /* 0 for the terminal null entry */
+  int32_t count;        /* first of the (count, visit) pair */
+  int32_t visit;
+  int32_t terminal;
+  int32_t prefix_pos;   /* prefix_begin_info (prefix entries; 0 on suffix entries) */
+  int32_t num_wires;
+} pk_compact_entry;
+
+pk_status pk_compact(pk_job* job, uint64_t node_threshold, int32_t coverage, pk_compaction_info* info);
+pk_status pk_compaction_get_info(pk_job* job, pk_compaction_info* info);
+/* Remaining nodes, ascending by key.  Node i's entries are entries[entry_offsets[i] ..
+ * entry_offsets[i+1]): n_prefixes[i] prefixes, then its suffixes, each list in the
+ * reference's order; its wiring_info is wires[3 * (entry_offsets[i] + i) ..] with
+ * (n_entries of the node + 1) slots of {suffix_id, offset_in_suffix, count}.  Sizes
+ * come from pk_compaction_info (keys n_nodes * key_bytes, entry_offsets n_nodes + 1,
+ * wires 3 * (n_entries + n_nodes) int32, ext_bases ext_bases bytes); any pointer may
+ * be NULL. */
+pk_status pk_copy_compacted(pk_job* job, void* keys, uint64_t* entry_offsets, uint32_t* n_prefixes,
+                            pk_compact_entry* entries, int32_t* wires, uint8_t* ext_bases);
+/* Partial contigs in emission order: contig c is bases[offsets[c] .. offsets[c+1])
+ * (base codes A=0 C=1 T=2 G=3); offsets has n_contigs + 1 slots. */
+pk_status pk_copy_partial_contigs(pk_job* job, uint64_t* offsets, uint8_t* bases);
+
 pk_status pk_summary_get(pk_job* job, pk_summary* out);
 
 /* ---- per-kernel timing (CUDA events on the job's stream) ---------------------------- */

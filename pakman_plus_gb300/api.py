@@ -19,7 +19,7 @@ import ctypes
 import os
 from ctypes import byref, c_float, c_int, c_uint32, c_uint64, c_void_p
 from dataclasses import dataclass
-from typing import Dict, Optional, Tuple
+from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 
@@ -153,6 +153,80 @@ def _visit(counts: np.ndarray, coverage: int) -> np.ndarray:
     return np.where(c != 0, q, 0)
 
 
+COMPACT_ENTRY = np.dtype([("ext_offset", "<u8"), ("ext_length", "<u4"), ("count", "<i4"),
+                          ("visit", "<i4"), ("terminal", "<i4"), ("prefix_pos", "<i4"),
+                          ("num_wires", "<i4")])
+
+
+@dataclass
+class Compaction:
+    """The map left by pk_compact and the partial contigs of its rounds (host copies).
+    Node i: keys[i]; entries[entry_offsets[i]:entry_offsets[i+1]] = n_prefixes[i]
+    prefixes then its suffixes; wires[entry_offsets[i] + i :][:n_entries_i + 1]."""
+    rounds: int
+    keys: np.ndarray
+    entry_offsets: np.ndarray
+    n_prefixes: np.ndarray
+    entries: np.ndarray
+    wires: np.ndarray
+    ext_bases: np.ndarray
+    contig_offsets: np.ndarray
+    contig_bases: np.ndarray
+
+    @staticmethod
+    def fetch(handle, info) -> "Compaction":
+        n, e = info.n_nodes, info.n_entries
+        kb = info.key_bytes
+        keys = np.zeros(max(1, n), np.uint64 if kb == 8 else np.dtype([("lo", "<u8"), ("hi", "<u8")]))
+        eo = np.zeros(n + 1, np.uint64)
+        npre = np.zeros(max(1, n), np.uint32)
+        ent = np.zeros(max(1, e), COMPACT_ENTRY)
+        wires = np.zeros((max(1, e + n), 3), np.int32)
+        xb = np.zeros(max(1, info.ext_bases), np.uint8)
+        check(capi.lib().pk_copy_compacted(handle, keys.ctypes.data, eo.ctypes.data, npre.ctypes.data,
+                                           ent.ctypes.data, wires.ctypes.data, xb.ctypes.data),
+              "pk_copy_compacted")
+        co = np.zeros(info.n_contigs + 1, np.uint64)
+        cb = np.zeros(max(1, info.contig_bases), np.uint8)
+        check(capi.lib().pk_copy_partial_contigs(handle, co.ctypes.data, cb.ctypes.data),
+              "pk_copy_partial_contigs")
+        return Compaction(info.rounds, keys[:n], eo, npre[:n], ent[:e], wires[:e + n],
+                          xb[:info.ext_bases], co, cb[:info.contig_bases])
+
+    @property
+    def n_nodes(self) -> int:
+        return int(self.keys.shape[0])
+
+    def key(self, i: int) -> int:
+        k = self.keys[i]
+        return int(k) if self.keys.dtype.names is None else int(k["lo"]) | (int(k["hi"]) << 64)
+
+    def contigs(self) -> List[bytes]:
+        o = self.contig_offsets
+        b = self.contig_bases.tobytes()
+        return [b[int(o[c]):int(o[c + 1])] for c in range(o.shape[0] - 1)]
+
+    def state_view(self):
+        """Per node (key, suffixes, prefixes, wires, begin) with entries as
+        (ext bytes, count, visit, terminal) -- the oracle's comparable form."""
+        xb = self.ext_bases.tobytes()
+        out = []
+        for i in range(self.n_nodes):
+            e0, e1 = int(self.entry_offsets[i]), int(self.entry_offsets[i + 1])
+            npf = int(self.n_prefixes[i])
+            ents = self.entries[e0:e1]
+
+            def row(x):
+                o, ln = int(x["ext_offset"]), int(x["ext_length"])
+                return (xb[o:o + ln], int(x["count"]), int(x["visit"]), bool(x["terminal"]))
+            pre = [row(x) for x in ents[:npf]]
+            suf = [row(x) for x in ents[npf:]]
+            w = self.wires[e0 + i:e1 + i + 1]
+            out.append((self.key(i), suf, pre, [tuple(int(v) for v in r) for r in w],
+                        [(int(x["prefix_pos"]), int(x["num_wires"])) for x in ents[:npf]]))
+        return out
+
+
 class Job:
     """One read set on the device: count -> cutoff -> macro-nodes; buffers stay
     resident until :meth:`reset` or :meth:`close`."""
@@ -266,6 +340,15 @@ class Job:
         out = np.zeros(max(1, m), WIRING)
         check(capi.lib().pk_copy_wiring(self._h, out.ctypes.data, m), "pk_copy_wiring")
         return out[:m]
+
+    # -- iterative compaction
+    def compact(self, node_threshold: int, coverage: int = 0) -> "Compaction":
+        """Rounds of independent-set merging on the device until at most
+        `node_threshold` macro-nodes remain (begin_iterative_compaction); the result is
+        copied to the host."""
+        info = capi.PkCompactionInfo()
+        check(capi.lib().pk_compact(self._h, node_threshold, coverage, byref(info)), "pk_compact")
+        return Compaction.fetch(self._h, info)
 
     # -- whole path
     def run(self, fasta, params: capi.PkParams) -> Summary:

@@ -79,6 +79,12 @@ class PkWiring(ctypes.Structure):
                 ("prefix_begin", (c_int32 * 2) * 5)]
 
 
+class PkCompactionInfo(ctypes.Structure):
+    _fields_ = [("n_nodes", c_uint64), ("n_entries", c_uint64), ("n_contigs", c_uint64),
+                ("ext_bases", c_uint64), ("contig_bases", c_uint64), ("rounds", c_int32),
+                ("key_bytes", c_int32)]
+
+
 class PakmanError(RuntimeError):
     """A failed C-ABI call; `status` is the pk_status code."""
 
@@ -148,6 +154,10 @@ _SIGS = {
     "pk_wire_macro_nodes": (c_int, [c_void_p, c_int32]),
     "pk_copy_wiring": (c_int, [c_void_p, c_void_p, c_uint64]),
     "pk_wiring_device": (c_int, [c_void_p, POINTER(c_void_p)]),
+    "pk_compact": (c_int, [c_void_p, c_uint64, c_int32, POINTER(PkCompactionInfo)]),
+    "pk_compaction_get_info": (c_int, [c_void_p, POINTER(PkCompactionInfo)]),
+    "pk_copy_compacted": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pk_copy_partial_contigs": (c_int, [c_void_p, c_void_p, c_void_p]),
     "pk_job_enable_timing": (c_int, [c_void_p, c_int]),
     "pk_job_stage_times": (c_int, [c_void_p, POINTER(c_float), c_int, POINTER(c_int)]),
     "pk_stage_name": (c_char_p, [c_int]),

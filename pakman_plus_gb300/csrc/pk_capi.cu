@@ -83,6 +83,8 @@ void pk::job_free_all(pk_job* j) {
                    &j->gfirst, &j->gcount, &j->chunk_bucket, &j->gdone,
                    &j->chunk_u};
   for (DevBuf* b : all) job_free(j, *b);
+  cp_free(j);
+  j->compacted = false;
   j->dense_valid = false;
 }
 
@@ -327,6 +329,7 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   j->F = n;
   j->stage = 0;
   j->wired = false;
+  j->compacted = false;
   const int W = j->wide ? 16 : 8;
   const int bb = p->bucket_bits ? std::min(p->bucket_bits, std::min(kMaxPartitionBits, 2 * k - 2))
                                 : auto_bucket_bits(n, k, j->wide);
@@ -753,6 +756,7 @@ pk_status pk::mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
   mark_end(j, ST_MN);
   j->stage = 3;
   j->wired = false;
+  j->compacted = false;
   return PK_OK;
 }
 

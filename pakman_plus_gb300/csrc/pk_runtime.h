@@ -51,12 +51,17 @@ enum Stage {
   ST_CUTOFF,
   ST_FILTER,
   ST_MN,
+  ST_COMPACT,
   ST_COUNT_
 };
 static const char* kStageNames[ST_COUNT_] = {"h2d",          "line_scan",      "bucket_count",
                                              "bucket_offsets", "scatter_coarse", "scatter_fine",
                                              "bucket_table", "cutoff",         "kept_filter",
-                                             "macro_nodes"};
+                                             "macro_nodes",  "compaction"};
+
+namespace pk {
+struct CpState;  // iterative compaction buffers (pk_compact.cu)
+}
 
 struct pk_job {
   pk_ctx* ctx = nullptr;
@@ -78,6 +83,8 @@ struct pk_job {
       coff, cstart, slice_start, fcur, wiring, gfirst, gcount, chunk_bucket, gdone, chunk_u;
   bool dense_valid = false;
   bool wired = false;  // wiring matches the current macro-nodes
+  pk::CpState* cp = nullptr;
+  bool compacted = false;  // the compaction state matches the current macro-nodes
   bool timing = false;
   // graph mode (batch capture): no host synchronisation and no allocation; the
   // window count is bounded by ncap and scalars were initialised by the caller
@@ -98,6 +105,7 @@ namespace pk {
 pk_status set_device(pk_ctx* c);
 pk_status job_alloc(pk_job* j, DevBuf& b, size_t bytes);
 void job_free_all(pk_job* j);
+void cp_free(pk_job* j);  // the compaction state, if any
 pk_status check_params(const pk_params* p);
 int auto_bucket_bits(uint64_t F, int k, int wide);
 // device FASTA -> resident table; in graph mode no host synchronisation happens and

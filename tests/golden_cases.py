@@ -57,4 +57,6 @@ def load(name: str) -> Golden:
 
 
 def names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz")))
+    """The hot-path cases (compact_*.npz hold the compaction fixtures)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz"))
+                  if not os.path.basename(p).startswith("compact_"))

@@ -1,0 +1,115 @@
+"""Device iterative compaction (pk_compact) against the oracle restatement of the
+reference's begin_iterative_compaction (oracle/pk_compact.py, pinned to the reference's
+own runs in tests/test_compact_oracle.py): the map left at the node threshold -- every
+prefix and suffix list with its extensions, counts, visits and terminal flags, the
+wiring and prefix begin slots -- and the partial contigs in emission order, exactly."""
+import os
+import zlib
+
+import numpy as np
+import pytest
+
+import pakman_plus_gb300 as pk
+from gpu_helpers import ctx
+from oracle import pk_compact as pc
+from pakman_plus_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _golden(name):
+    z = np.load(os.path.join(GOLDEN, "compact_%s.npz" % name))
+    k, rl, cov, t = (int(x) for x in z["params"])
+    return zlib.decompress(z["fasta"].tobytes()), k, cov, t, [int(x) for x in z["thresholds"]]
+
+
+def _device(fasta, k, cov, t, thr, drop_n=False):
+    p = pk.default_params(k=k, num_buckets=t, coverage=cov, drop_n=int(drop_n))
+    with pk.Job(ctx()) as job:
+        job.count(fasta, p)
+        job.cutoff(t)
+        job.build_macro_nodes(0)
+        mn = job.macro_nodes(cov)
+        res = job.compact(thr, cov)
+    return mn, res
+
+
+def _oracle(mn, k, cov, thr):
+    nodes = pc.initial_nodes(mn.keys, mn.suffix_counts, mn.prefix_counts, k, cov)
+    return pc.compact(nodes, k, thr)
+
+
+def _check(res, ora):
+    assert res.rounds == ora.rounds
+    assert res.state_view() == pc.state_view(ora.nodes)
+    assert res.contigs() == ora.contigs
+
+
+@pytest.mark.parametrize("name", ["k32_small", "k32_bact", "k32_tandem", "k63_longk"])
+def test_golden_inputs(name):
+    fasta, k, cov, t, thrs = _golden(name)
+    for thr in thrs:
+        mn, res = _device(fasta, k, cov, t, thr)
+        _check(res, _oracle(mn, k, cov, thr))
+
+
+def test_bacterial_scaled_143k_nodes():
+    """92 kbp of the 4.6 Mbp / 80x workload: 143k macro-nodes down to 100 in 27 rounds."""
+    rs = synth.config2(0.02)
+    mn, res = _device(rs.fasta, rs.k, rs.coverage, rs.t, 100)
+    assert res.rounds > 10
+    _check(res, _oracle(mn, rs.k, rs.coverage, 100))
+
+
+def test_longk_dropn_scaled():
+    rs = synth.config3(0.003)
+    mn, res = _device(rs.fasta, rs.k, rs.coverage, rs.t, 20, rs.drop_n)
+    _check(res, _oracle(mn, rs.k, rs.coverage, 20))
+
+
+@pytest.mark.parametrize("k", [17, 21, 31, 33, 48, 64])
+def test_key_widths(k):
+    rs = synth.small_case(300 + k, genome_len=4000, n_reads=3000, read_len=120, err=0.005, k=k,
+                          coverage=40)
+    mn, res = _device(rs.fasta, k, 40, 21, 5)
+    _check(res, _oracle(mn, k, 40, 5))
+
+
+def test_threshold_above_node_count_is_the_initial_wiring():
+    rs = synth.small_case(5, genome_len=3000, n_reads=1500, k=32, coverage=20)
+    p = pk.default_params(k=32, coverage=20)
+    with pk.Job(ctx()) as job:
+        job.count(rs.fasta, p)
+        job.cutoff(21)
+        m = job.build_macro_nodes(0)
+        w = job.wire(20)
+        res = job.compact(m, 20)
+    assert res.rounds == 0 and res.n_nodes == m and not res.contigs()
+    view = res.state_view()
+    for row, (key, suf, pre, wires, begin) in zip(w, view):
+        assert len(suf) == row["ns"] and len(pre) == row["np"]
+        assert suf[-1][2] == row["term_suf"] and pre[-1][2] == row["term_pre"]
+        used = [x for x in wires if x[2]]
+        assert len(used) == row["nw"]
+        assert used == [tuple(int(v) for v in r) for r in row["wire"][:len(used)]]
+        assert begin == [tuple(int(v) for v in r) for r in row["begin"][:len(begin)]]
+
+
+def test_compact_twice_and_state_errors():
+    rs = synth.small_case(6, genome_len=4000, n_reads=2500, k=32, coverage=25)
+    p = pk.default_params(k=32, coverage=25)
+    with pk.Job(ctx()) as job:
+        with pytest.raises(pk.PakmanError) as e:
+            job.compact(10)
+        assert e.value.status == pk.capi.PK_ERR_STATE
+        job.count(rs.fasta, p)
+        job.cutoff(21)
+        job.build_macro_nodes(0)
+        mn = job.macro_nodes(25)
+        a = job.compact(50, 25)
+        b = job.compact(3, 25)
+        a2 = job.compact(50, 25)
+    assert a.state_view() == a2.state_view() and a.contigs() == a2.contigs()
+    _check(b, _oracle(mn, 32, 25, 3))
