@@ -51,6 +51,11 @@ def parse():
     ap.add_argument("--cpu-sample-windows", type=int, default=0,
                     help="windows in the CPU baseline's sample (0: the whole read set)")
     ap.add_argument("--bucket-bits", type=int, default=0, help="partition digits (0 = automatic)")
+    ap.add_argument("--compact-threshold", type=int, default=100000,
+                    help="node threshold of the compaction measurement (the reference's -n default)")
+    ap.add_argument("--no-compaction", action="store_true")
+    ap.add_argument("--compact-cpu-scale", type=float, default=0.02,
+                    help="genome scale of the compaction CPU baseline's sample")
     ap.add_argument("--batch", action="store_true",
                     help="batching benchmark: many read sets in one CUDA-graph launch")
     ap.add_argument("--batch-sets", type=int, default=256)
@@ -202,6 +207,53 @@ def job_throughput(windows_per_rank: int, world: int, ms: float) -> float:
     """Whole-job k-mers/s: every replica counts its own read set of the same size, so
     the job processes world x windows in the slowest rank's time."""
     return windows_per_rank * world / (ms / 1000.0)
+
+
+def measure_compaction(job, rs, args, M, reps=3):
+    """Iterative compaction (pk_compact) of this workload's macro-node table down to
+    --compact-threshold nodes: device time of the whole call (CUDA events around it on
+    the job's stream, host round trips between rounds included), median of `reps`."""
+    import ctypes
+
+    from pakman_plus_gb300 import capi
+    L = capi.lib()
+    info = capi.PkCompactionInfo()
+
+    def once():
+        st = L.pk_compact(job.handle, args.compact_threshold, rs.coverage, ctypes.byref(info))
+        if st != 0:
+            raise RuntimeError("pk_compact: " + L.pk_last_error().decode())
+        return job.stage_times()["compaction"]
+
+    once()
+    ms = statistics.median(once() for _ in range(reps))
+    return {"workload": f"{rs.name} macro-node table -> at most {args.compact_threshold} nodes",
+            "nodes_in": int(M), "nodes_out": int(info.n_nodes), "rounds": int(info.rounds),
+            "partial_contigs": int(info.n_contigs), "ms": ms, "nodes_per_s": M / (ms / 1000.0),
+            "launches_per_round": 15}
+
+
+def compaction_cpu_baseline(name, scale, threshold):
+    """The oracle's compaction (pure Python, one thread) on a scaled sample of the same
+    workload: macro-nodes per second."""
+    import pakman_plus_gb300 as pk
+    from oracle import pk_compact as pc
+    rs = workload(name, scale)
+    p = pk.default_params(k=rs.k, num_buckets=rs.t, coverage=rs.coverage, drop_n=int(rs.drop_n))
+    ctx = pk.Context(0)
+    with pk.Job(ctx) as job:
+        job.count(rs.fasta, p)
+        job.cutoff(rs.t)
+        job.build_macro_nodes(0)
+        mn = job.macro_nodes(rs.coverage)
+    ctx.close()
+    nodes = pc.initial_nodes(mn.keys, mn.suffix_counts, mn.prefix_counts, rs.k, rs.coverage)
+    t0 = time.perf_counter()
+    r = pc.compact(nodes, rs.k, threshold)
+    sec = time.perf_counter() - t0
+    return {"value": len(mn.keys) / sec, "unit": "macro-nodes/s", "cores": 1, "kind": "port",
+            "sample": f"{rs.name} at scale {scale}: {len(mn.keys)} macro-nodes -> {len(r.nodes)} "
+                      f"in {r.rounds} rounds ({sec:.1f} s)"}
 
 
 def run_reference_arm(args, rank, world):
@@ -600,6 +652,9 @@ def main():
     ms_step = e0.elapsed_time(e1) / args.steps
     ms_step = max_over_ranks(ms_step, dist, f"cuda:{local}")
     value = job_throughput(s.n_windows, world, ms_step)
+    compaction = None
+    if not args.no_compaction and rank == 0:
+        compaction = measure_compaction(job, rs, args, s.n_nodes)
 
     # end to end through the public API: pinned host FASTA in, macro-node table out,
     # every step; requests go through the serving front end (pk_submit / pk_wait) with
@@ -695,6 +750,11 @@ def main():
         }
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(rs, args.cpu_sample_windows)
+        if compaction is not None:
+            if world == 1 and not args.no_cpu_baseline:
+                compaction["cpu_baseline"] = compaction_cpu_baseline(args.workload, args.compact_cpu_scale,
+                                                                     min(100, args.compact_threshold))
+            line["compaction"] = compaction
         print(json.dumps(line), flush=True)
     job.close()
     ctx.close()
