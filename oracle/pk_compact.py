@@ -10,6 +10,8 @@ baseline call it.  It restates, on plain Python lists and byte strings of base c
   retrieve_mn_pinfo / _sinfo   src/walk.cpp:117-167 / :69-115
   push_to_pred / push_to_succ  src/merge_mn.cpp:1325-1365 / :1368-1411
   MacroNode::setup_wiring      includes/distribute_kmers.h:550-657 (Comp_rev :495-506)
+  identify_begin_kmers         src/iterative_compaction.cpp:65-93
+  walk / traverse_pakgraph     src/walk.cpp:268-399 / :401-533
 
 A node is keyed by its (k-1)-mer; each prefix / suffix entry is [ext, count, visit,
 terminal] where ext is the extension's bases in reading order.  The packed
@@ -369,6 +371,86 @@ def compact(nodes: List[Node], k: int, threshold: int, max_rounds: int = 1 << 30
     return Compacted(nodes, contigs, rounds)
 
 
+# ----------------------------------------------------------------- walk -----------
+WALK_MAX_BASES = 500000  # the reference asserts a partial contig stays below this (src/walk.cpp:285)
+
+
+def begin_kmers(nodes: List[Node]) -> List[Tuple[int, int]]:
+    """identify_begin_kmers (src/iterative_compaction.cpp:65-93): every terminal prefix
+    with visits, in map order then prefix-list order."""
+    return [(i, p) for i, nd in enumerate(nodes) for p, e in enumerate(nd.pre) if e[VIS] > 0 and e[TERM]]
+
+
+def walk(nodes: List[Node], k: int) -> List[bytes]:
+    """traverse_pakgraph on one thread (src/walk.cpp:401-533): from each begin k-mer,
+    the depth-first `walk` (:268-399) over the wires of the prefix it entered by, each
+    wire taking its share [offset, offset + frequency) of the prefix's visits; a
+    terminal suffix ends a contig.  Contigs in begin order, then depth-first order (the
+    reference's order with one thread)."""
+    L = k - 1
+    pos = {nd.key: i for i, nd in enumerate(nodes)}
+    out: List[bytes] = []
+    for bi, bp in begin_kmers(nodes):
+        nd = nodes[bi]
+        contig = bytearray(nd.pre[bp][EXT] + key_bases(nd.key, L))
+        # frame: [node, prefix, offset_in_prefix, wire index, off, freq_remaining, child share, length]
+        stack = [[bi, bp, 0, 0, 0, nd.pre[bp][VIS], None, len(contig)]]
+        while stack:
+            f = stack[-1]
+            cur = nodes[f[0]]
+            bpos, num = cur.begin[f[1]]
+            if f[6] is not None:  # back from the child walk
+                f[5] -= f[6]
+                f[6] = None
+                del contig[f[7]:]
+                f[4] += cur.wires[bpos + f[3]][2]
+                f[3] += 1
+                continue
+            if f[3] >= num:
+                stack.pop()
+                continue
+            sid, off_in_suffix, sz = cur.wires[bpos + f[3]]
+            off, oip, rem = f[4], f[2], f[5]
+            if off + sz <= oip or off > oip + rem:
+                f[4] += sz
+                f[3] += 1
+                continue
+            off_in_wire = 0 if oip <= off else oip - off
+            next_off = off_in_suffix + off_in_wire
+            share = min(rem, sz - off_in_wire)
+            S = cur.suf[sid]
+            f[7] = len(contig)
+            contig += S[EXT]
+            if S[TERM]:
+                out.append(bytes(contig))
+                f[5] -= share
+                del contig[f[7]:]
+                f[4] += sz
+                f[3] += 1
+                continue
+            nxt_i = pos.get(S[NBR])
+            if nxt_i is None:
+                raise CompactionError("walk: successor node not in the map")
+            nxt = nodes[nxt_i]
+            search = (key_bases(cur.key, L) + S[EXT])[:len(S[EXT])]
+            q = next((j for j, e in enumerate(nxt.pre) if e[EXT] == search), -1)
+            if q < 0:  # the reference prints "prefix not found" and exits
+                raise CompactionError("walk: no prefix of the successor matches")
+            if share <= 0:  # the reference asserts freq_in_wire > 0
+                raise CompactionError("walk: empty share of a wire")
+            if len(contig) >= WALK_MAX_BASES:
+                raise CompactionError("walk: a contig reached 500000 bases")
+            f[6] = share
+            stack.append([nxt_i, q, next_off, 0, 0, share, None, len(contig)])
+    return out
+
+
+def read_fasta_contigs(data: bytes) -> List[bytes]:
+    """Sequences of a contigs_*.fa file as base codes (A=0, C=1, T=2, G=3)."""
+    code = {ord("A"): 0, ord("C"): 1, ord("T"): 2, ord("G"): 3}
+    return [bytes(code[c] for c in line) for line in data.split(b"\n") if line and not line.startswith(b">")]
+
+
 # ----------------------------------------------------------------- construction ---
 def initial_nodes(keys, suf, pre, k: int, coverage: int) -> List[Node]:
     """The wired map the reference hands to compaction, lists in canonical order:
@@ -493,9 +575,10 @@ class RefCompaction:
 
 
 def run_reference(fasta: bytes, k: int, read_len: int, coverage: int, threshold: int,
-                  t: int = 21) -> Optional[RefCompaction]:
+                  t: int = 21, walk: bool = False) -> Optional[RefCompaction]:
     """The reference's compaction on `fasta` (one rank, one thread); None if it cannot
-    be built here."""
+    be built here.  walk=True also runs its walk: raw["walk_fa"] / raw["partial_fa"] hold
+    the contigs_out_r0.fa / contigs_par_r0.fa it writes (contigs longer than 400)."""
     import json
     exe = build_compact_reference(k)
     if exe is None or not os.path.exists(exe):
@@ -506,8 +589,8 @@ def run_reference(fasta: bytes, k: int, read_len: int, coverage: int, threshold:
             f.write(fasta)
         out = os.path.join(d, "out")
         p = subprocess.run([exe, out, "-f", fa, "-r", str(read_len), "-c", str(coverage), "-t", str(t),
-                            "-n", str(threshold)], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
-                           env=dict(os.environ, OMP_NUM_THREADS="1"))
+                            "-n", str(threshold)], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, cwd=d,
+                           env=dict(os.environ, OMP_NUM_THREADS="1", PK_REF_WALK="1" if walk else "0"))
         if p.returncode != 0:
             raise CompactionError("reference compaction failed: " + p.stdout.decode(errors="replace")[-400:])
         line = [x for x in p.stdout.decode().splitlines() if x.startswith("{")][-1]
@@ -515,6 +598,10 @@ def run_reference(fasta: bytes, k: int, read_len: int, coverage: int, threshold:
         for part in ("before", "after", "contigs"):
             with open(out + "." + part, "rb") as f:
                 raw[part] = f.read()
+        if walk:
+            for key, name in (("walk_fa", "contigs_out_r0.fa"), ("partial_fa", "contigs_par_r0.fa")):
+                with open(os.path.join(d, name), "rb") as f:
+                    raw[key] = f.read()
         kk, before = parse_state(raw["before"])
         _, after = parse_state(raw["after"])
         return RefCompaction(kk, before, after, parse_contigs(raw["contigs"]), json.loads(line)["compact_s"], raw)

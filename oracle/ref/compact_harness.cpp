@@ -18,9 +18,16 @@
 //     u32 nw, nw x {i32 suffix_id, i32 offset_in_suffix, i32 count},
 //     u32 np, np x {i32 prefix_pos, i32 num_wires}
 // OUT_PREFIX.contigs : "PKP1" u64 n, n x {u32 len, len x u8 base}
-// stdout last line : {"compact_s": .., "M0": .., "M1": .., "contigs": ..}
-#include <stdio.h>
+// stdout last line : {"compact_s": .., "walk_s": .., "M0": .., "M1": .., "contigs": ..}
+//
+// With PK_REF_WALK=1 in the environment the harness then runs the reference's walk on
+// the compacted map (identify_begin_kmers, src/iterative_compaction.cpp:65-93, and
+// traverse_pakgraph, src/walk.cpp:401-533), which writes contigs_out_r0.fa (walk
+// contigs longer than 400 bases) and contigs_par_r0.fa (partial contigs longer than
+// 400 bases) into the working directory.
 #include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string>
 #include <vector>
 
@@ -32,6 +39,9 @@ void parseCommandLine(const int argc, char* const argv[]);
 void set_num_threads();
 size_t begin_iterative_compaction(std::vector<std::pair<kmer_t, MacroNode>>& MN_map,
                                   std::vector<BasePairVector>& partial_contig_list);
+void identify_begin_kmers(std::vector<std::pair<kmer_t, MacroNode>>& MN_map, std::vector<BeginMN>& list_of_begin_kmers);
+void traverse_pakgraph(std::vector<std::pair<kmer_t, MacroNode>>& global_MN_map,
+                       std::vector<BeginMN>& list_of_begin_kmers, std::vector<BasePairVector>& partial_contig_list);
 
 static void put_key(FILE* f, kmer_t key) {
   uint64_t lo = (uint64_t)key;
@@ -130,8 +140,18 @@ int main(int argc, char** argv) {
     for (const BasePairVector& c : contigs) put_bases(f, c);
     fclose(f);
   }
-  printf("{\"compact_s\": %.6f, \"M0\": %llu, \"M1\": %llu, \"contigs\": %llu}\n", t1 - t0,
-         (unsigned long long)m0, (unsigned long long)MN_map.size(), (unsigned long long)contigs.size());
+  const uint64_t m1 = MN_map.size(), np = contigs.size();
+  double t2 = t1, t3 = t1;
+  const char* w = getenv("PK_REF_WALK");
+  if (w && w[0] == '1') {
+    std::vector<BeginMN> begins;
+    t2 = MPI_Wtime();
+    identify_begin_kmers(MN_map, begins);
+    traverse_pakgraph(MN_map, begins, contigs);
+    t3 = MPI_Wtime();
+  }
+  printf("{\"compact_s\": %.6f, \"walk_s\": %.6f, \"M0\": %llu, \"M1\": %llu, \"contigs\": %llu}\n",
+         t1 - t0, t3 - t2, (unsigned long long)m0, (unsigned long long)m1, (unsigned long long)np);
   fflush(stdout);
   MPI_Finalize();
   return 0;

@@ -7,7 +7,8 @@ Run from the repository root in a tree where the reference sources are present:
 
 For every case it writes ``compact_<case>.npz`` holding the input FASTA (zlib), the
 run's parameters and the reference's own dumps (zlib): the wired macro-node map before
-compaction, the map left at the node threshold and the partial contigs, after checking
+compaction, the map left at the node threshold, the partial contigs, and the contig
+files its walk writes (walk and partial contigs longer than 400 bases), after checking
 that the oracle (oracle/pk_compact.py) reproduces them from the map before.  The
 binary is built from the unmodified reference sources by ``oracle/ref/Makefile``
 (``make -C oracle/ref compact``, single-rank MPI shim).
@@ -63,18 +64,23 @@ def main():
         arrays = {"fasta": z(fasta), "params": np.array([k, rl, cov, t], np.int64),
                   "thresholds": np.array(thrs, np.int64)}
         for thr in thrs:
-            r = pc.run_reference(fasta, k, rl, cov, thr, t)
+            r = pc.run_reference(fasta, k, rl, cov, thr, t, walk=True)
             if r is None:
                 raise SystemExit("the reference compaction cannot be built here")
             o = pc.compact(r.before, r.k, thr)
             if pc.state_view(o.nodes) != pc.state_view(r.after) or o.contigs != r.contigs:
                 raise SystemExit("oracle disagrees with the reference on %s n=%d" % (name, thr))
+            w = pc.walk(o.nodes, r.k)
+            if [c for c in w if len(c) > 400] != pc.read_fasta_contigs(r.raw["walk_fa"]):
+                raise SystemExit("oracle walk disagrees with the reference on %s n=%d" % (name, thr))
+            arrays["walk_%d" % thr] = z(r.raw["walk_fa"])
+            arrays["partial_fa_%d" % thr] = z(r.raw["partial_fa"])
             arrays["before"] = z(r.raw["before"])
             arrays["after_%d" % thr] = z(r.raw["after"])
             arrays["contigs_%d" % thr] = z(r.raw["contigs"])
             arrays["rounds_%d" % thr] = np.array([o.rounds], np.int64)
             print(name, "n", thr, "M0", len(r.before), "M1", len(r.after), "contigs", len(r.contigs),
-                  "rounds", o.rounds)
+                  "rounds", o.rounds, "walk", len(w), ">400", len(pc.read_fasta_contigs(r.raw["walk_fa"])))
         np.savez(os.path.join(OUT, "compact_%s.npz" % name), **arrays)
 
 

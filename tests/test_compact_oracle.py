@@ -1,7 +1,7 @@
-"""The compaction oracle (oracle/pk_compact.py) against the reference's own iterative
-compaction: golden dumps made by tests/golden/make_compact_golden.py, a live run of
-the reference built here when its sources are present, and libstdc++'s std::sort for
-the wiring's unstable ranking."""
+"""The compaction and walk oracle (oracle/pk_compact.py) against the reference's own
+iterative compaction and walk: golden dumps made by tests/golden/make_compact_golden.py,
+a live run of the reference built here when its sources are present, and libstdc++'s
+std::sort for the wiring's unstable ranking."""
 import os
 import subprocess
 import zlib
@@ -25,14 +25,15 @@ def load(name):
     for thr in z["thresholds"]:
         thr = int(thr)
         out["runs"].append((thr, unz(z["after_%d" % thr]), unz(z["contigs_%d" % thr]),
-                            int(z["rounds_%d" % thr][0])))
+                            int(z["rounds_%d" % thr][0]), unz(z["walk_%d" % thr]),
+                            unz(z["partial_fa_%d" % thr])))
     return out
 
 
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_reproduces_reference_compaction(name):
     g = load(name)
-    for thr, after, contigs, rounds in g["runs"]:
+    for thr, after, contigs, rounds, _, _ in g["runs"]:
         k, before = pc.parse_state(g["before"])
         o = pc.compact(before, k, thr)
         _, ref_after = pc.parse_state(after)
@@ -40,6 +41,18 @@ def test_oracle_reproduces_reference_compaction(name):
         assert len(o.nodes) <= thr < len(before)
         assert pc.state_view(o.nodes) == pc.state_view(ref_after)
         assert o.contigs == pc.parse_contigs(contigs)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_walk_reproduces_reference_contig_files(name):
+    """The walk on the compacted map: the reference writes, with one thread, its walk
+    contigs and its partial contigs longer than 400 bases in generation order."""
+    g = load(name)
+    for thr, after, contigs, rounds, walk_fa, partial_fa in g["runs"]:
+        k, nodes = pc.parse_state(after)
+        w = pc.walk(nodes, k)
+        assert [c for c in w if len(c) > 400] == pc.read_fasta_contigs(walk_fa)
+        assert [c for c in pc.parse_contigs(contigs) if len(c) > 400] == pc.read_fasta_contigs(partial_fa)
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -101,7 +114,8 @@ def test_live_reference_run():
     if pc.build_compact_reference(32) is None:
         pytest.skip("the reference tree is not present")
     rs = synth.small_case(91, genome_len=6000, n_reads=4000, read_len=100, err=0.01, k=32, coverage=30)
-    r = pc.run_reference(rs.fasta, 32, 100, 30, 20)
+    r = pc.run_reference(rs.fasta, 32, 100, 30, 20, walk=True)
     o = pc.compact(r.before, 32, 20)
     assert pc.state_view(o.nodes) == pc.state_view(r.after)
     assert o.contigs == r.contigs
+    assert [c for c in pc.walk(o.nodes, 32) if len(c) > 400] == pc.read_fasta_contigs(r.raw["walk_fa"])
