@@ -27,6 +27,13 @@
  *                                 src/input_reading.cpp:68-243, 246-303 (a rank's
  *                                 record-aligned slice of the FASTA file), streamed
  *                                 to the device and counted
+ *   pk_wire_macro_nodes           initiate_mnode_wiring, src/wire.cpp:66-121
+ *   pk_compact / pk_copy_compacted / pk_copy_partial_contigs
+ *                                 begin_iterative_compaction (MN_map after the rounds,
+ *                                 partial_contig_list), src/iterative_compaction.cpp:131-464
+ *   pk_walk / pk_copy_walk_contigs
+ *                                 identify_begin_kmers + traverse_pakgraph,
+ *                                 src/iterative_compaction.cpp:65-93, src/walk.cpp:268-533
  */
 #ifndef PAKMAN_GB300_H
 #define PAKMAN_GB300_H
@@ -244,6 +251,28 @@ pk_status pk_copy_compacted(pk_job* job, void* keys, uint64_t* entry_offsets, ui
 /* Partial contigs in emission order: contig c is bases[offsets[c] .. offsets[c+1])
  * (base codes A=0 C=1 T=2 G=3); offsets has n_contigs + 1 slots. */
 pk_status pk_copy_partial_contigs(pk_job* job, uint64_t* offsets, uint8_t* bases);
+
+/* ---- walk: replaces identify_begin_kmers + traverse_pakgraph
+ * (src/iterative_compaction.cpp:65-93, src/walk.cpp:268-533) -------------------------
+ * On the map left by pk_compact: from every terminal prefix with visits (map order,
+ * then prefix-list order) a depth-first walk over the wires, each wire taking its share
+ * of the prefix's visits, emits a contig at every terminal suffix.  Contigs come in
+ * begin order, then depth-first order -- the reference's order with one thread; all
+ * contigs are returned (the reference writes those longer than 400 bases).  A missing
+ * successor or prefix, an empty share, a contig of 500000 bases (the reference exits
+ * or asserts) or a path deeper than max_depth nodes gives PK_ERR_DEVICE. */
+typedef struct pk_walk_info {
+  uint64_t n_begins;
+  uint64_t n_contigs;
+  uint64_t contig_bases;
+  uint32_t max_depth;  /* frames on each walk's stack */
+  uint32_t reserved;
+} pk_walk_info;
+
+pk_status pk_walk(pk_job* job, pk_walk_info* info);
+/* contig c is bases[offsets[c] .. offsets[c+1]) (codes A=0 C=1 T=2 G=3); offsets has
+ * n_contigs + 1 slots, bases contig_bases bytes. */
+pk_status pk_copy_walk_contigs(pk_job* job, uint64_t* offsets, uint8_t* bases);
 
 pk_status pk_summary_get(pk_job* job, pk_summary* out);
 

@@ -350,6 +350,17 @@ class Job:
         check(capi.lib().pk_compact(self._h, node_threshold, coverage, byref(info)), "pk_compact")
         return Compaction.fetch(self._h, info)
 
+    def walk(self) -> List[bytes]:
+        """Contigs of the walk over the map left by :meth:`compact` (traverse_pakgraph),
+        as base codes, in begin order then depth-first order."""
+        info = capi.PkWalkInfo()
+        check(capi.lib().pk_walk(self._h, byref(info)), "pk_walk")
+        off = np.zeros(info.n_contigs + 1, np.uint64)
+        b = np.zeros(max(1, info.contig_bases), np.uint8)
+        check(capi.lib().pk_copy_walk_contigs(self._h, off.ctypes.data, b.ctypes.data), "pk_copy_walk_contigs")
+        raw = b.tobytes()
+        return [raw[int(off[c]):int(off[c + 1])] for c in range(info.n_contigs)]
+
     # -- whole path
     def run(self, fasta, params: capi.PkParams) -> Summary:
         buf = _as_bytes_ptr(fasta)

@@ -85,6 +85,11 @@ class PkCompactionInfo(ctypes.Structure):
                 ("key_bytes", c_int32)]
 
 
+class PkWalkInfo(ctypes.Structure):
+    _fields_ = [("n_begins", c_uint64), ("n_contigs", c_uint64), ("contig_bases", c_uint64),
+                ("max_depth", c_uint32), ("reserved", c_uint32)]
+
+
 class PakmanError(RuntimeError):
     """A failed C-ABI call; `status` is the pk_status code."""
 
@@ -158,6 +163,8 @@ _SIGS = {
     "pk_compaction_get_info": (c_int, [c_void_p, POINTER(PkCompactionInfo)]),
     "pk_copy_compacted": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "pk_copy_partial_contigs": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "pk_walk": (c_int, [c_void_p, POINTER(PkWalkInfo)]),
+    "pk_copy_walk_contigs": (c_int, [c_void_p, c_void_p, c_void_p]),
     "pk_job_enable_timing": (c_int, [c_void_p, c_int]),
     "pk_job_stage_times": (c_int, [c_void_p, POINTER(c_float), c_int, POINTER(c_int)]),
     "pk_stage_name": (c_char_p, [c_int]),

@@ -30,6 +30,7 @@
 //                 target in generation order and sizes the new lists
 //   k_cp_apply<1> writes the lists and re-wires touched nodes (MacroNode::setup_wiring,
 //                 includes/distribute_kmers.h:550-657); other nodes keep their wiring
+// and, on the compacted map, the walk (pk_walk; k_walk, below).
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -54,7 +55,18 @@ constexpr uint32_t kLenMask = 0x7fffffffu;
 constexpr int kScanT = 1024, kScanPer = 4, kScanTile = kScanT * kScanPer;
 
 // device error bits of a compaction
-enum : uint32_t { CE_LIST = 1u, CE_TARGET = 2u, CE_BALANCE = 4u, CE_TERMINAL = 8u, CE_BOUNDS = 16u };
+enum : uint32_t {
+  CE_LIST = 1u,
+  CE_TARGET = 2u,
+  CE_BALANCE = 4u,
+  CE_TERMINAL = 8u,
+  CE_BOUNDS = 16u,
+  CE_WALK_PREFIX = 32u,  // no prefix of the successor matches (the reference exits)
+  CE_WALK_SHARE = 64u,   // a wire's share of the visits is empty (the reference asserts)
+  CE_WALK_LONG = 128u,   // a contig reached 500000 bases (the reference asserts)
+  CE_WALK_DEPTH = 256u,  // a walk went deeper than its stack
+};
+constexpr uint32_t kWalkMaxBases = 500000;  // src/walk.cpp:285
 
 struct Tr {            // one TransferNode (src/merge_mn.cpp:483-525)
   uint64_t w;          // arena base offset of W = P + K + S
@@ -834,6 +846,196 @@ __global__ void __launch_bounds__(128) k_cp_apply(Side<KeyT> a, Side<KeyT> b, ui
   for (int j = 0; j < r.ns; j++) b.cnt[d0 + r.np + j] = scnt[j], b.vis[d0 + r.np + j] = svis[j];
 }
 
+// ------------------------------------------------------------------ walk ---------
+// traverse_pakgraph / walk (src/walk.cpp:268-533) on the compacted map: one thread per
+// begin k-mer (identify_begin_kmers, src/iterative_compaction.cpp:65-93) runs the
+// depth-first walk with its frames on a bounded stack in HBM.  Pass 0 counts each
+// begin's contigs and bases; pass 1 writes them (one byte per base), each contig
+// rebuilt from the stack: the begin prefix and key, then every frame's suffix.
+struct WFrame {
+  uint32_t node;
+  int32_t p, oip, wi, off, rem, share;
+  uint32_t len;  // contig length when this frame's current suffix was appended
+  int32_t sid;   // suffix being explored
+  int32_t pad;
+};
+
+__global__ void k_wk_begin_count(const uint32_t* __restrict__ eoff, const uint32_t* __restrict__ npre,
+                                 const uint32_t* __restrict__ xlen, const int32_t* __restrict__ vis, uint32_t n,
+                                 uint4* __restrict__ col) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t c = 0;
+  for (uint32_t e = eoff[i], e1 = eoff[i] + npre[i]; e < e1; e++) c += (vis[e] > 0 && (xlen[e] & kTerm)) ? 1u : 0u;
+  col[i] = make_uint4(c, 0, 0, 0);
+}
+
+__global__ void k_wk_begins(const uint32_t* __restrict__ eoff, const uint32_t* __restrict__ npre,
+                            const uint32_t* __restrict__ xlen, const int32_t* __restrict__ vis, uint32_t n,
+                            const uint4* __restrict__ off, uint2* __restrict__ begins) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t o = off[i].x;
+  const uint32_t e0 = eoff[i];
+  for (uint32_t q = 0; q < npre[i]; q++)
+    if (vis[e0 + q] > 0 && (xlen[e0 + q] & kTerm)) begins[o++] = make_uint2(i, q);
+}
+
+// m (<= 32) bases of key + S from position q, right-aligned
+template <typename KeyT>
+__device__ __forceinline__ uint64_t ks_bases(const uint64_t* __restrict__ ar, KeyT key, int L, uint64_t soff,
+                                             uint32_t q, int m) {
+  uint64_t v = 0;
+  const uint32_t a = q, b = q + m;
+  if (a < (uint32_t)L) {
+    const int mk = (int)(min(b, (uint32_t)L) - a);
+    v = key_bases(key, L, (int)a, mk);
+    if (b > (uint32_t)L) {
+      const int ms = (int)(b - L);
+      v = (v << (2 * ms)) | (ar_get(ar, soff) >> (64 - 2 * ms));
+    }
+  } else {
+    v = ar_get(ar, soff + (a - L)) >> (64 - 2 * m);
+  }
+  return v;
+}
+
+__device__ __forceinline__ void put_bases(uint8_t* __restrict__ out, uint64_t v, int m) {
+  for (int x = 0; x < m; x++) out[x] = (uint8_t)((v >> (2 * (m - 1 - x))) & 3);
+}
+
+template <typename KeyT, int PASS>
+__global__ void __launch_bounds__(128) k_walk(Side<KeyT> s, uint32_t n, int L, const uint2* __restrict__ begins,
+                                              uint32_t nb, const uint64_t* __restrict__ ar, WFrame* __restrict__ stk,
+                                              uint32_t cap, uint4* __restrict__ col, const uint4* __restrict__ off,
+                                              uint64_t* __restrict__ ct_off, uint8_t* __restrict__ out,
+                                              uint32_t* err) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  WFrame* st = stk + (uint64_t)b * cap;
+  const uint2 bg = begins[b];
+  const uint32_t be = s.eoff[bg.x] + bg.y;
+  const KeyT bkey = s.key[bg.x];
+  const uint32_t plen0 = s.xlen[be] & kLenMask;
+  uint32_t nct = 0, nbases = 0;
+  uint32_t ci = PASS ? off[b].x : 0u;
+  uint64_t bo = PASS ? off[b].y : 0ull;
+  int d = 0;
+  st[0] = WFrame{bg.x, (int32_t)bg.y, 0, 0, 0, s.vis[be], -1, plen0 + (uint32_t)L, -1, 0};
+  uint32_t len = plen0 + (uint32_t)L;  // current contig length
+  auto emit = [&](uint32_t clen) {
+    if (PASS) {
+      ct_off[ci] = bo;
+      uint8_t* o = out + bo;
+      // begin prefix, then the begin key
+      for (uint32_t i = 0; i < plen0; i += 32) {
+        const int m = (int)min(32u, plen0 - i);
+        put_bases(o + i, ar_get(ar, s.xoff[be] + i) >> (64 - 2 * m), m);
+      }
+      for (int i = 0; i < L; i += 32) {
+        const int m = min(32, L - i);
+        put_bases(o + plen0 + i, key_bases(bkey, L, i, m), m);
+      }
+      for (int f = 0; f <= d; f++) {
+        const uint32_t se = s.eoff[st[f].node] + s.npre[st[f].node] + (uint32_t)st[f].sid;
+        const uint32_t sl = s.xlen[se] & kLenMask, at = st[f].len;
+        for (uint32_t i = 0; i < sl; i += 32) {
+          const int m = (int)min(32u, sl - i);
+          put_bases(o + at + i, ar_get(ar, s.xoff[se] + i) >> (64 - 2 * m), m);
+        }
+      }
+      ci++;
+      bo += clen;
+    }
+    nct++;
+    nbases += clen;
+  };
+  while (d >= 0) {
+    WFrame& f = st[d];
+    const uint32_t e0 = s.eoff[f.node], np = s.npre[f.node];
+    const int2 bp = s.beg[e0 + f.p];
+    const int3* wire = s.wire + e0 + f.node;
+    if (f.share >= 0) {  // back from the child walk
+      f.rem -= f.share;
+      f.share = -1;
+      len = f.len;
+      f.off += wire[bp.x + f.wi].z;
+      f.wi++;
+      continue;
+    }
+    if (f.wi >= bp.y) {
+      d--;
+      continue;
+    }
+    const int3 w = wire[bp.x + f.wi];
+    if (f.off + w.z <= f.oip || f.off > f.oip + f.rem) {
+      f.off += w.z;
+      f.wi++;
+      continue;
+    }
+    const int oiw = f.oip <= f.off ? 0 : f.oip - f.off;
+    const int next_off = w.y + oiw;
+    const int share = min(f.rem, w.z - oiw);
+    const uint32_t se = e0 + np + (uint32_t)w.x;
+    const uint32_t sl = s.xlen[se] & kLenMask;
+    f.len = len;
+    f.sid = w.x;
+    len += sl;
+    if (s.xlen[se] & kTerm) {
+      emit(len);
+      f.rem -= share;
+      len = f.len;
+      f.off += w.z;
+      f.wi++;
+      continue;
+    }
+    // successor: binary search of the neighbour key, then its prefix equal to the
+    // first |S| bases of key + S
+    const KeyT nk = s.nbr[se];
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (s.key[mid] < nk) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo >= n || s.key[lo] != nk) {
+      atomicOr(err, CE_TARGET);
+      break;
+    }
+    const KeyT ckey = s.key[f.node];
+    const uint32_t q0 = s.eoff[lo], qn = s.npre[lo];
+    int q = -1;
+    for (uint32_t j = 0; j < qn && q < 0; j++) {
+      if ((s.xlen[q0 + j] & kLenMask) != sl) continue;
+      bool eq = true;
+      for (uint32_t i = 0; i < sl && eq; i += 32) {
+        const int m = (int)min(32u, sl - i);
+        eq = (ar_get(ar, s.xoff[q0 + j] + i) >> (64 - 2 * m)) == ks_bases(ar, ckey, L, s.xoff[se], i, m);
+      }
+      if (eq) q = (int)j;
+    }
+    if (q < 0) {
+      atomicOr(err, CE_WALK_PREFIX);
+      break;
+    }
+    if (share <= 0) {
+      atomicOr(err, CE_WALK_SHARE);
+      break;
+    }
+    if (len >= kWalkMaxBases) {
+      atomicOr(err, CE_WALK_LONG);
+      break;
+    }
+    if (d + 1 >= (int)cap) {
+      atomicOr(err, CE_WALK_DEPTH);
+      break;
+    }
+    f.share = share;
+    st[++d] = WFrame{lo, q, next_off, 0, 0, share, -1, len, -1, 0};
+  }
+  if (!PASS) col[b] = make_uint4(nct, nbases, 0, 0);
+}
+
 // ------------------------------------------------------------- copy-out ---------
 __global__ void k_cp_lengths(const uint32_t* __restrict__ xlen, uint32_t E, uint4* __restrict__ col) {
   const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -891,7 +1093,10 @@ struct CpState {
   };
   DevBuf side[2][NSIDE];
   DevBuf arena, col, off, part, is_id, tkey, tr, tgt, incnt, inoff, fill, inlist, ecol, eoff2, old_of, ct, tot,
-      epos, cpos, ubuf;
+      epos, cpos, ubuf, wk_begins, wk_stack, wk_col, wk_pos, wk_off, wk_out;
+  uint64_t wk_begins_n = 0, wk_n = 0, wk_bases = 0;
+  uint32_t wk_depth = 0;
+  bool wk_done = false;
   int cur = 0;
   uint64_t n = 0, E = 0, arena_words = 0, arena_cap = 0, C = 0, ct_cap = 0;
   uint64_t ext_bases = 0, ct_bases = 0;
@@ -977,6 +1182,10 @@ pk_status check_err(CpState& c) {
   if (e & CE_BALANCE) m += "a node's visits do not balance (the reference asserts); ";
   if (e & CE_TERMINAL) m += "a node lost its terminal entry; ";
   if (e & CE_BOUNDS) m += "an index fell outside its buffer; ";
+  if (e & CE_WALK_PREFIX) m += "walk: no prefix of a successor matches (the reference exits); ";
+  if (e & CE_WALK_SHARE) m += "walk: a wire's share of the visits is empty (the reference asserts); ";
+  if (e & CE_WALK_LONG) m += "walk: a contig reached 500000 bases (the reference asserts); ";
+  if (e & CE_WALK_DEPTH) m += "walk: a path went deeper than the walk stack; ";
   return set_error(PK_ERR_DEVICE, m);
 }
 
@@ -1104,6 +1313,53 @@ pk_status cp_finish(pk_job* j, CpState& c) {
   return PK_OK;
 }
 
+template <typename KeyT>
+pk_status cp_walk(pk_job* j, CpState& c) {
+  Side<KeyT> a = side_of<KeyT>(c, c.cur);
+  const uint64_t n = c.n;
+  cudaStream_t st = j->stream;
+  PK_TRY(cp_alloc(j, c.col, sizeof(uint4) * (n + 1)));
+  PK_TRY(cp_alloc(j, c.off, sizeof(uint4) * (n + 1)));
+  if (n) k_wk_begin_count<<<blocks(n, 256), 256, 0, st>>>(a.eoff, a.npre, a.xlen, a.vis, (uint32_t)n, (uint4*)c.col.p);
+  PK_TRY(scan4(j, c, (const uint4*)c.col.p, (uint4*)c.off.p, n));
+  uint4 t;
+  PK_TRY(read_total(j, c, (const uint4*)c.off.p + n, &t));
+  const uint64_t B = t.x;
+  PK_TRY(cp_alloc(j, c.wk_begins, sizeof(uint2) * (B + 1)));
+  if (n) k_wk_begins<<<blocks(n, 256), 256, 0, st>>>(a.eoff, a.npre, a.xlen, a.vis, (uint32_t)n, (const uint4*)c.off.p,
+                                                      (uint2*)c.wk_begins.p);
+  // frames per walk: 2^26 over all walks, at least 256 and at most 2^20 each
+  const uint64_t cap = std::min<uint64_t>(1u << 20, std::max<uint64_t>(256, (1ull << 26) / std::max<uint64_t>(B, 1)));
+  PK_TRY(cp_alloc(j, c.wk_stack, sizeof(WFrame) * cap * std::max<uint64_t>(B, 1)));
+  PK_TRY(cp_alloc(j, c.wk_col, sizeof(uint4) * (B + 1)));
+  PK_TRY(cp_alloc(j, c.wk_pos, sizeof(uint4) * (B + 1)));
+  if (B)
+    k_walk<KeyT, 0><<<blocks(B, 128), 128, 0, st>>>(a, (uint32_t)n, c.L, (const uint2*)c.wk_begins.p, (uint32_t)B,
+                                                     (const uint64_t*)c.arena.p, (WFrame*)c.wk_stack.p, (uint32_t)cap,
+                                                     (uint4*)c.wk_col.p, nullptr, nullptr, nullptr, c.d_err);
+  PK_TRY(scan4(j, c, (const uint4*)c.wk_col.p, (uint4*)c.wk_pos.p, B));
+  PK_TRY(read_total(j, c, (const uint4*)c.wk_pos.p + B, &t));
+  PK_TRY(check_err(c));
+  const uint64_t NC = t.x, NB = t.y;
+  PK_TRY(cp_alloc(j, c.wk_off, 8 * (NC + 1)));
+  PK_TRY(cp_alloc(j, c.wk_out, NB + 1));
+  if (B)
+    k_walk<KeyT, 1><<<blocks(B, 128), 128, 0, st>>>(a, (uint32_t)n, c.L, (const uint2*)c.wk_begins.p, (uint32_t)B,
+                                                     (const uint64_t*)c.arena.p, (WFrame*)c.wk_stack.p, (uint32_t)cap,
+                                                     nullptr, (const uint4*)c.wk_pos.p, (uint64_t*)c.wk_off.p,
+                                                     (uint8_t*)c.wk_out.p, c.d_err);
+  PK_CUDA(cudaMemcpyAsync((uint64_t*)c.wk_off.p + NC, &NB, 8, cudaMemcpyHostToDevice, st));
+  PK_CUDA(cudaGetLastError());
+  PK_TRY(read_total(j, c, (const uint4*)c.wk_pos.p + B, &t));
+  PK_TRY(check_err(c));
+  c.wk_begins_n = B;
+  c.wk_n = NC;
+  c.wk_bases = NB;
+  c.wk_depth = (uint32_t)cap;
+  c.wk_done = true;
+  return PK_OK;
+}
+
 }  // namespace
 
 void pk::cp_free(pk_job* j) {
@@ -1117,9 +1373,11 @@ void pk::cp_free(pk_job* j) {
         j->ctx->used -= d.bytes;
       }
     }
-  DevBuf* rest[] = {&c->arena, &c->col,   &c->off,   &c->part, &c->is_id,  &c->tkey,  &c->tr,   &c->tgt,
-                    &c->incnt, &c->inoff, &c->fill,  &c->inlist, &c->ecol, &c->eoff2, &c->old_of, &c->ct,
-                    &c->tot,   &c->epos,  &c->cpos,  &c->ubuf};
+  DevBuf* rest[] = {&c->arena,  &c->col,      &c->off,    &c->part,   &c->is_id,  &c->tkey,
+                    &c->tr,     &c->tgt,      &c->incnt,  &c->inoff,  &c->fill,   &c->inlist,
+                    &c->ecol,   &c->eoff2,    &c->old_of, &c->ct,     &c->tot,    &c->epos,
+                    &c->cpos,   &c->ubuf,     &c->wk_begins, &c->wk_stack, &c->wk_col, &c->wk_pos,
+                    &c->wk_off, &c->wk_out};
   for (DevBuf* d : rest)
     if (d->p) {
       cudaFreeAsync(d->p, j->stream);
@@ -1244,5 +1502,39 @@ extern "C" pk_status pk_copy_partial_contigs(pk_job* j, uint64_t* offsets, uint8
   PK_CUDA(cudaStreamSynchronize(st));
   if (offsets)
     for (uint64_t i = 0; i <= c.C; i++) offsets[i] = pos[i].x;
+  return PK_OK;
+}
+
+extern "C" pk_status pk_walk(pk_job* j, pk_walk_info* info) {
+  if (!j) return set_error(PK_ERR_INVALID, "job is null");
+  if (!j->cp || !j->cp->done || !j->compacted)
+    return set_error(PK_ERR_STATE, "no compaction of the current macro-nodes: call pk_compact first");
+  CpState& c = *j->cp;
+  PK_TRY(set_device(j->ctx));
+  c.wk_done = false;
+  mark_begin(j, ST_WALK);
+  const pk_status s = c.wide ? cp_walk<u128>(j, c) : cp_walk<uint64_t>(j, c);
+  mark_end(j, ST_WALK);
+  PK_TRY(s);
+  if (info) {
+    memset(info, 0, sizeof(*info));
+    info->n_begins = c.wk_begins_n;
+    info->n_contigs = c.wk_n;
+    info->contig_bases = c.wk_bases;
+    info->max_depth = c.wk_depth;
+  }
+  return PK_OK;
+}
+
+extern "C" pk_status pk_copy_walk_contigs(pk_job* j, uint64_t* offsets, uint8_t* bases) {
+  if (!j) return set_error(PK_ERR_INVALID, "job is null");
+  if (!j->cp || !j->cp->wk_done || !j->compacted)
+    return set_error(PK_ERR_STATE, "no walk of the current compaction: call pk_walk first");
+  CpState& c = *j->cp;
+  PK_TRY(set_device(j->ctx));
+  cudaStream_t st = j->stream;
+  if (offsets) PK_CUDA(cudaMemcpyAsync(offsets, c.wk_off.p, 8 * (c.wk_n + 1), cudaMemcpyDeviceToHost, st));
+  if (bases && c.wk_bases) PK_CUDA(cudaMemcpyAsync(bases, c.wk_out.p, c.wk_bases, cudaMemcpyDeviceToHost, st));
+  PK_CUDA(cudaStreamSynchronize(st));
   return PK_OK;
 }

@@ -52,12 +52,13 @@ enum Stage {
   ST_FILTER,
   ST_MN,
   ST_COMPACT,
+  ST_WALK,
   ST_COUNT_
 };
 static const char* kStageNames[ST_COUNT_] = {"h2d",          "line_scan",      "bucket_count",
                                              "bucket_offsets", "scatter_coarse", "scatter_fine",
                                              "bucket_table", "cutoff",         "kept_filter",
-                                             "macro_nodes",  "compaction"};
+                                             "macro_nodes",  "compaction",     "walk"};
 
 namespace pk {
 struct CpState;  // iterative compaction buffers (pk_compact.cu)

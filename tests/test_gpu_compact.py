@@ -1,8 +1,10 @@
-"""Device iterative compaction (pk_compact) against the oracle restatement of the
-reference's begin_iterative_compaction (oracle/pk_compact.py, pinned to the reference's
-own runs in tests/test_compact_oracle.py): the map left at the node threshold -- every
-prefix and suffix list with its extensions, counts, visits and terminal flags, the
-wiring and prefix begin slots -- and the partial contigs in emission order, exactly."""
+"""Device iterative compaction (pk_compact) and walk (pk_walk) against the oracle
+restatement of the reference's begin_iterative_compaction and traverse_pakgraph
+(oracle/pk_compact.py, pinned to the reference's own runs in
+tests/test_compact_oracle.py): the map left at the node threshold -- every prefix and
+suffix list with its extensions, counts, visits and terminal flags, the wiring and
+prefix begin slots -- the partial contigs in emission order, and the walk's contigs in
+begin then depth-first order, exactly."""
 import os
 import zlib
 
@@ -33,6 +35,7 @@ def _device(fasta, k, cov, t, thr, drop_n=False):
         job.build_macro_nodes(0)
         mn = job.macro_nodes(cov)
         res = job.compact(thr, cov)
+        res.walk_contigs = job.walk()
     return mn, res
 
 
@@ -41,10 +44,12 @@ def _oracle(mn, k, cov, thr):
     return pc.compact(nodes, k, thr)
 
 
-def _check(res, ora):
+def _check(res, ora, k=None):
     assert res.rounds == ora.rounds
     assert res.state_view() == pc.state_view(ora.nodes)
     assert res.contigs() == ora.contigs
+    if k is not None:
+        assert res.walk_contigs == pc.walk(ora.nodes, k)
 
 
 @pytest.mark.parametrize("name", ["k32_small", "k32_bact", "k32_tandem", "k63_longk"])
@@ -52,7 +57,7 @@ def test_golden_inputs(name):
     fasta, k, cov, t, thrs = _golden(name)
     for thr in thrs:
         mn, res = _device(fasta, k, cov, t, thr)
-        _check(res, _oracle(mn, k, cov, thr))
+        _check(res, _oracle(mn, k, cov, thr), k)
 
 
 def test_bacterial_scaled_143k_nodes():
@@ -60,13 +65,14 @@ def test_bacterial_scaled_143k_nodes():
     rs = synth.config2(0.02)
     mn, res = _device(rs.fasta, rs.k, rs.coverage, rs.t, 100)
     assert res.rounds > 10
-    _check(res, _oracle(mn, rs.k, rs.coverage, 100))
+    assert len(res.walk_contigs) > 0
+    _check(res, _oracle(mn, rs.k, rs.coverage, 100), rs.k)
 
 
 def test_longk_dropn_scaled():
     rs = synth.config3(0.003)
     mn, res = _device(rs.fasta, rs.k, rs.coverage, rs.t, 20, rs.drop_n)
-    _check(res, _oracle(mn, rs.k, rs.coverage, 20))
+    _check(res, _oracle(mn, rs.k, rs.coverage, 20), rs.k)
 
 
 @pytest.mark.parametrize("k", [17, 21, 31, 33, 48, 64])
@@ -74,7 +80,7 @@ def test_key_widths(k):
     rs = synth.small_case(300 + k, genome_len=4000, n_reads=3000, read_len=120, err=0.005, k=k,
                           coverage=40)
     mn, res = _device(rs.fasta, k, 40, 21, 5)
-    _check(res, _oracle(mn, k, 40, 5))
+    _check(res, _oracle(mn, k, 40, 5), k)
 
 
 def test_threshold_above_node_count_is_the_initial_wiring():
@@ -104,6 +110,9 @@ def test_compact_twice_and_state_errors():
         with pytest.raises(pk.PakmanError) as e:
             job.compact(10)
         assert e.value.status == pk.capi.PK_ERR_STATE
+        with pytest.raises(pk.PakmanError) as e:
+            job.walk()
+        assert e.value.status == pk.capi.PK_ERR_STATE
         job.count(rs.fasta, p)
         job.cutoff(21)
         job.build_macro_nodes(0)
@@ -113,3 +122,12 @@ def test_compact_twice_and_state_errors():
         a2 = job.compact(50, 25)
     assert a.state_view() == a2.state_view() and a.contigs() == a2.contigs()
     _check(b, _oracle(mn, 32, 25, 3))
+
+
+def test_walk_of_a_larger_map():
+    """The walk straight after a shallow compaction (threshold 5000 of 143k nodes):
+    many begins, long branching walks."""
+    rs = synth.config2(0.02)
+    mn, res = _device(rs.fasta, rs.k, rs.coverage, rs.t, 5000)
+    ora = _oracle(mn, rs.k, rs.coverage, 5000)
+    _check(res, ora, rs.k)
