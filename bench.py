@@ -227,10 +227,22 @@ def measure_compaction(job, rs, args, M, reps=3):
 
     once()
     ms = statistics.median(once() for _ in range(reps))
+    winfo = capi.PkWalkInfo()
+
+    def walk_once():
+        st = L.pk_walk(job.handle, ctypes.byref(winfo))
+        if st != 0:
+            raise RuntimeError("pk_walk: " + L.pk_last_error().decode())
+        return job.stage_times()["walk"]
+
+    walk_once()
+    wms = statistics.median(walk_once() for _ in range(reps))
     return {"workload": f"{rs.name} macro-node table -> at most {args.compact_threshold} nodes",
             "nodes_in": int(M), "nodes_out": int(info.n_nodes), "rounds": int(info.rounds),
             "partial_contigs": int(info.n_contigs), "ms": ms, "nodes_per_s": M / (ms / 1000.0),
-            "launches_per_round": 15}
+            "launches_per_round": 15,
+            "walk": {"ms": wms, "begin_kmers": int(winfo.n_begins), "contigs": int(winfo.n_contigs),
+                     "contig_bases": int(winfo.contig_bases), "launches": 10}}
 
 
 def compaction_cpu_baseline(name, scale, threshold):

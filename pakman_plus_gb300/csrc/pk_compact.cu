@@ -847,17 +847,26 @@ __global__ void __launch_bounds__(128) k_cp_apply(Side<KeyT> a, Side<KeyT> b, ui
 }
 
 // ------------------------------------------------------------------ walk ---------
-// traverse_pakgraph / walk (src/walk.cpp:268-533) on the compacted map: one thread per
-// begin k-mer (identify_begin_kmers, src/iterative_compaction.cpp:65-93) runs the
-// depth-first walk with its frames on a bounded stack in HBM.  Pass 0 counts each
-// begin's contigs and bases; pass 1 writes them (one byte per base), each contig
-// rebuilt from the stack: the begin prefix and key, then every frame's suffix.
+// traverse_pakgraph / walk (src/walk.cpp:268-533) on the compacted map.
+//   k_wk_links   every suffix entry's successor: the node its neighbour key names
+//                (find_mnode_exists) and that node's first prefix equal to the first
+//                |S| bases of key + S, resolved for all entries in parallel
+//   k_walk<0>    one thread per begin k-mer (identify_begin_kmers,
+//                src/iterative_compaction.cpp:65-93) runs the depth-first walk over the
+//                links, the current frame in registers and the path's frames on a
+//                bounded stack in HBM; it counts contigs, bases and pieces
+//   k_walk<1>    the same walk writes each contig's begin key and its pieces (the begin
+//                prefix and every frame's suffix, as arena views)
+//   k_wk_expand  one warp per piece writes its bases (one byte per base)
 struct WFrame {
-  uint32_t node;
-  int32_t p, oip, wi, off, rem, share;
-  uint32_t len;  // contig length when this frame's current suffix was appended
-  int32_t sid;   // suffix being explored
-  int32_t pad;
+  uint32_t node, e0, np;
+  int32_t p, oip, wi, off, rem, share, bpx, bpy, wz, sid;
+  uint32_t lenb;  // contig length before this frame's current suffix
+};
+struct WPiece {
+  uint64_t src;  // arena base offset
+  uint64_t dst;  // output byte offset
+  uint32_t len, pad;
 };
 
 __global__ void k_wk_begin_count(const uint32_t* __restrict__ eoff, const uint32_t* __restrict__ npre,
@@ -900,97 +909,18 @@ __device__ __forceinline__ uint64_t ks_bases(const uint64_t* __restrict__ ar, Ke
   return v;
 }
 
-__device__ __forceinline__ void put_bases(uint8_t* __restrict__ out, uint64_t v, int m) {
-  for (int x = 0; x < m; x++) out[x] = (uint8_t)((v >> (2 * (m - 1 - x))) & 3);
-}
-
-template <typename KeyT, int PASS>
-__global__ void __launch_bounds__(128) k_walk(Side<KeyT> s, uint32_t n, int L, const uint2* __restrict__ begins,
-                                              uint32_t nb, const uint64_t* __restrict__ ar, WFrame* __restrict__ stk,
-                                              uint32_t cap, uint4* __restrict__ col, const uint4* __restrict__ off,
-                                              uint64_t* __restrict__ ct_off, uint8_t* __restrict__ out,
-                                              uint32_t* err) {
-  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  WFrame* st = stk + (uint64_t)b * cap;
-  const uint2 bg = begins[b];
-  const uint32_t be = s.eoff[bg.x] + bg.y;
-  const KeyT bkey = s.key[bg.x];
-  const uint32_t plen0 = s.xlen[be] & kLenMask;
-  uint32_t nct = 0, nbases = 0;
-  uint32_t ci = PASS ? off[b].x : 0u;
-  uint64_t bo = PASS ? off[b].y : 0ull;
-  int d = 0;
-  st[0] = WFrame{bg.x, (int32_t)bg.y, 0, 0, 0, s.vis[be], -1, plen0 + (uint32_t)L, -1, 0};
-  uint32_t len = plen0 + (uint32_t)L;  // current contig length
-  auto emit = [&](uint32_t clen) {
-    if (PASS) {
-      ct_off[ci] = bo;
-      uint8_t* o = out + bo;
-      // begin prefix, then the begin key
-      for (uint32_t i = 0; i < plen0; i += 32) {
-        const int m = (int)min(32u, plen0 - i);
-        put_bases(o + i, ar_get(ar, s.xoff[be] + i) >> (64 - 2 * m), m);
-      }
-      for (int i = 0; i < L; i += 32) {
-        const int m = min(32, L - i);
-        put_bases(o + plen0 + i, key_bases(bkey, L, i, m), m);
-      }
-      for (int f = 0; f <= d; f++) {
-        const uint32_t se = s.eoff[st[f].node] + s.npre[st[f].node] + (uint32_t)st[f].sid;
-        const uint32_t sl = s.xlen[se] & kLenMask, at = st[f].len;
-        for (uint32_t i = 0; i < sl; i += 32) {
-          const int m = (int)min(32u, sl - i);
-          put_bases(o + at + i, ar_get(ar, s.xoff[se] + i) >> (64 - 2 * m), m);
-        }
-      }
-      ci++;
-      bo += clen;
-    }
-    nct++;
-    nbases += clen;
-  };
-  while (d >= 0) {
-    WFrame& f = st[d];
-    const uint32_t e0 = s.eoff[f.node], np = s.npre[f.node];
-    const int2 bp = s.beg[e0 + f.p];
-    const int3* wire = s.wire + e0 + f.node;
-    if (f.share >= 0) {  // back from the child walk
-      f.rem -= f.share;
-      f.share = -1;
-      len = f.len;
-      f.off += wire[bp.x + f.wi].z;
-      f.wi++;
-      continue;
-    }
-    if (f.wi >= bp.y) {
-      d--;
-      continue;
-    }
-    const int3 w = wire[bp.x + f.wi];
-    if (f.off + w.z <= f.oip || f.off > f.oip + f.rem) {
-      f.off += w.z;
-      f.wi++;
-      continue;
-    }
-    const int oiw = f.oip <= f.off ? 0 : f.oip - f.off;
-    const int next_off = w.y + oiw;
-    const int share = min(f.rem, w.z - oiw);
-    const uint32_t se = e0 + np + (uint32_t)w.x;
+// link[e] for suffix entry e of node i: (successor node, its prefix index);
+// (~0, 0) when no node has the neighbour key, (node, ~0) when no prefix matches
+template <typename KeyT>
+__global__ void __launch_bounds__(256) k_wk_links(Side<KeyT> s, uint32_t n, int L, const uint64_t* __restrict__ ar,
+                                                  uint2* __restrict__ link) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t e0 = s.eoff[i], e1 = s.eoff[i + 1], np = s.npre[i];
+  const KeyT ckey = s.key[i];
+  for (uint32_t se = e0 + np; se < e1; se++) {
+    if (s.xlen[se] & kTerm) continue;
     const uint32_t sl = s.xlen[se] & kLenMask;
-    f.len = len;
-    f.sid = w.x;
-    len += sl;
-    if (s.xlen[se] & kTerm) {
-      emit(len);
-      f.rem -= share;
-      len = f.len;
-      f.off += w.z;
-      f.wi++;
-      continue;
-    }
-    // successor: binary search of the neighbour key, then its prefix equal to the
-    // first |S| bases of key + S
     const KeyT nk = s.nbr[se];
     uint32_t lo = 0, hi = n;
     while (lo < hi) {
@@ -999,22 +929,116 @@ __global__ void __launch_bounds__(128) k_walk(Side<KeyT> s, uint32_t n, int L, c
       else hi = mid;
     }
     if (lo >= n || s.key[lo] != nk) {
+      link[se] = make_uint2(~0u, 0u);
+      continue;
+    }
+    const uint32_t q0 = s.eoff[lo], qn = s.npre[lo];
+    uint32_t q = ~0u;
+    for (uint32_t j = 0; j < qn && q == ~0u; j++) {
+      if ((s.xlen[q0 + j] & kLenMask) != sl) continue;
+      bool eq = true;
+      for (uint32_t x = 0; x < sl && eq; x += 32) {
+        const int m = (int)min(32u, sl - x);
+        eq = (ar_get(ar, s.xoff[q0 + j] + x) >> (64 - 2 * m)) == ks_bases(ar, ckey, L, s.xoff[se], x, m);
+      }
+      if (eq) q = j;
+    }
+    link[se] = make_uint2(lo, q);
+  }
+}
+
+template <typename KeyT, int PASS>
+__global__ void __launch_bounds__(128) k_walk(Side<KeyT> s, int L, const uint2* __restrict__ begins, uint32_t nb,
+                                              const uint2* __restrict__ link, WFrame* __restrict__ stk, uint32_t cap,
+                                              uint4* __restrict__ col, const uint4* __restrict__ off,
+                                              uint64_t* __restrict__ ct_off, WPiece* __restrict__ pieces,
+                                              uint8_t* __restrict__ out, uint32_t* err) {
+  // one walk per warp (lane 0): independent walks diverge completely, so they do not
+  // share a warp
+  const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if ((threadIdx.x & 31) != 0 || b >= nb) return;
+  WFrame* st = stk + (uint64_t)b * cap;
+  const uint2 bg = begins[b];
+  const uint32_t be = s.eoff[bg.x] + bg.y;
+  const uint32_t plen0 = s.xlen[be] & kLenMask;
+  uint32_t nct = 0, npc = 0;
+  uint64_t nbases = 0;
+  uint32_t ci = PASS ? off[b].x : 0u, pc = PASS ? off[b].z : 0u;
+  uint64_t bo = PASS ? off[b].y : 0ull;
+  int d = 0;
+  WFrame f;
+  f.node = bg.x;
+  f.e0 = s.eoff[bg.x];
+  f.np = s.npre[bg.x];
+  f.p = (int32_t)bg.y;
+  f.oip = 0;
+  f.wi = 0;
+  f.off = 0;
+  f.rem = s.vis[be];
+  f.share = -1;
+  {
+    const int2 bp = s.beg[f.e0 + f.p];
+    f.bpx = bp.x;
+    f.bpy = bp.y;
+  }
+  f.wz = 0;
+  f.sid = -1;
+  f.lenb = 0;
+  uint32_t len = plen0 + (uint32_t)L;
+  while (true) {
+    if (f.wi >= f.bpy) {  // this walk is done: back to the parent
+      if (d == 0) break;
+      f = st[--d];
+      f.rem -= f.share;
+      f.share = -1;
+      len = f.lenb;
+      f.off += f.wz;
+      f.wi++;
+      continue;
+    }
+    const int3 w = s.wire[f.e0 + f.node + f.bpx + f.wi];
+    if (f.off + w.z <= f.oip || f.off > f.oip + f.rem) {
+      f.off += w.z;
+      f.wi++;
+      continue;
+    }
+    const int oiw = f.oip <= f.off ? 0 : f.oip - f.off;
+    const int next_off = w.y + oiw;
+    const int share = min(f.rem, w.z - oiw);
+    const uint32_t se = f.e0 + f.np + (uint32_t)w.x;
+    const uint32_t xl = s.xlen[se], sl = xl & kLenMask;
+    if (xl & kTerm) {  // a contig: begin prefix, begin key, the frames' suffixes, this one
+      const uint32_t clen = len + sl;
+      if (PASS) {
+        ct_off[ci++] = bo;
+        for (int x = 0; x < L; x++)
+          out[bo + plen0 + x] = (uint8_t)key_bases(s.key[bg.x], L, x, 1);
+        if (plen0) pieces[pc++] = WPiece{s.xoff[be], bo, plen0, 0};
+        for (int q = 0; q < d; q++) {
+          const WFrame& g = st[q];
+          const uint32_t ge = g.e0 + g.np + (uint32_t)g.sid;
+          const uint32_t gl = s.xlen[ge] & kLenMask;
+          if (gl) pieces[pc++] = WPiece{s.xoff[ge], bo + g.lenb, gl, 0};
+        }
+        if (sl) pieces[pc++] = WPiece{s.xoff[se], bo + len, sl, 0};
+        bo += clen;
+      } else {
+        npc += (plen0 ? 1u : 0u) + (sl ? 1u : 0u);
+        for (int q = 0; q < d; q++) npc++;
+      }
+      nct++;
+      nbases += clen;
+      f.rem -= share;
+      f.off += w.z;
+      f.wi++;
+      continue;
+    }
+    const uint2 lk = link[se];
+    if (lk.x == ~0u) {
       atomicOr(err, CE_TARGET);
       break;
     }
-    const KeyT ckey = s.key[f.node];
-    const uint32_t q0 = s.eoff[lo], qn = s.npre[lo];
-    int q = -1;
-    for (uint32_t j = 0; j < qn && q < 0; j++) {
-      if ((s.xlen[q0 + j] & kLenMask) != sl) continue;
-      bool eq = true;
-      for (uint32_t i = 0; i < sl && eq; i += 32) {
-        const int m = (int)min(32u, sl - i);
-        eq = (ar_get(ar, s.xoff[q0 + j] + i) >> (64 - 2 * m)) == ks_bases(ar, ckey, L, s.xoff[se], i, m);
-      }
-      if (eq) q = (int)j;
-    }
-    if (q < 0) {
+    if (lk.y == ~0u) {
       atomicOr(err, CE_WALK_PREFIX);
       break;
     }
@@ -1022,7 +1046,7 @@ __global__ void __launch_bounds__(128) k_walk(Side<KeyT> s, uint32_t n, int L, c
       atomicOr(err, CE_WALK_SHARE);
       break;
     }
-    if (len >= kWalkMaxBases) {
+    if (len + sl >= kWalkMaxBases) {
       atomicOr(err, CE_WALK_LONG);
       break;
     }
@@ -1031,9 +1055,34 @@ __global__ void __launch_bounds__(128) k_walk(Side<KeyT> s, uint32_t n, int L, c
       break;
     }
     f.share = share;
-    st[++d] = WFrame{lo, q, next_off, 0, 0, share, -1, len, -1, 0};
+    f.sid = w.x;
+    f.wz = w.z;
+    f.lenb = len;
+    st[d++] = f;
+    len += sl;
+    f.node = lk.x;
+    f.e0 = s.eoff[lk.x];
+    f.np = s.npre[lk.x];
+    f.p = (int32_t)lk.y;
+    f.oip = next_off;
+    f.wi = 0;
+    f.off = 0;
+    f.rem = share;
+    f.share = -1;
+    const int2 bp = s.beg[f.e0 + f.p];
+    f.bpx = bp.x;
+    f.bpy = bp.y;
   }
-  if (!PASS) col[b] = make_uint4(nct, nbases, 0, 0);
+  if (!PASS) col[b] = make_uint4(nct, (uint32_t)nbases, npc, 0);
+}
+
+// one warp per piece: its bases, one byte each
+__global__ void k_wk_expand(const WPiece* __restrict__ pieces, uint32_t np, const uint64_t* __restrict__ ar,
+                            uint8_t* __restrict__ out) {
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= np) return;
+  const WPiece pc = pieces[w];
+  for (uint32_t i = lane; i < pc.len; i += 32) out[pc.dst + i] = (uint8_t)(ar_get(ar, pc.src + i) >> 62);
 }
 
 // ------------------------------------------------------------- copy-out ---------
@@ -1093,7 +1142,7 @@ struct CpState {
   };
   DevBuf side[2][NSIDE];
   DevBuf arena, col, off, part, is_id, tkey, tr, tgt, incnt, inoff, fill, inlist, ecol, eoff2, old_of, ct, tot,
-      epos, cpos, ubuf, wk_begins, wk_stack, wk_col, wk_pos, wk_off, wk_out;
+      epos, cpos, ubuf, wk_begins, wk_stack, wk_col, wk_pos, wk_off, wk_out, wk_links, wk_pieces;
   uint64_t wk_begins_n = 0, wk_n = 0, wk_bases = 0;
   uint32_t wk_depth = 0;
   bool wk_done = false;
@@ -1326,28 +1375,37 @@ pk_status cp_walk(pk_job* j, CpState& c) {
   PK_TRY(read_total(j, c, (const uint4*)c.off.p + n, &t));
   const uint64_t B = t.x;
   PK_TRY(cp_alloc(j, c.wk_begins, sizeof(uint2) * (B + 1)));
-  if (n) k_wk_begins<<<blocks(n, 256), 256, 0, st>>>(a.eoff, a.npre, a.xlen, a.vis, (uint32_t)n, (const uint4*)c.off.p,
-                                                      (uint2*)c.wk_begins.p);
+  PK_TRY(cp_alloc(j, c.wk_links, sizeof(uint2) * (c.E + 1)));
+  if (n) {
+    k_wk_begins<<<blocks(n, 256), 256, 0, st>>>(a.eoff, a.npre, a.xlen, a.vis, (uint32_t)n, (const uint4*)c.off.p,
+                                                (uint2*)c.wk_begins.p);
+    k_wk_links<KeyT><<<blocks(n, 256), 256, 0, st>>>(a, (uint32_t)n, c.L, (const uint64_t*)c.arena.p,
+                                                     (uint2*)c.wk_links.p);
+  }
   // frames per walk: 2^26 over all walks, at least 256 and at most 2^20 each
   const uint64_t cap = std::min<uint64_t>(1u << 20, std::max<uint64_t>(256, (1ull << 26) / std::max<uint64_t>(B, 1)));
   PK_TRY(cp_alloc(j, c.wk_stack, sizeof(WFrame) * cap * std::max<uint64_t>(B, 1)));
   PK_TRY(cp_alloc(j, c.wk_col, sizeof(uint4) * (B + 1)));
   PK_TRY(cp_alloc(j, c.wk_pos, sizeof(uint4) * (B + 1)));
   if (B)
-    k_walk<KeyT, 0><<<blocks(B, 128), 128, 0, st>>>(a, (uint32_t)n, c.L, (const uint2*)c.wk_begins.p, (uint32_t)B,
-                                                     (const uint64_t*)c.arena.p, (WFrame*)c.wk_stack.p, (uint32_t)cap,
-                                                     (uint4*)c.wk_col.p, nullptr, nullptr, nullptr, c.d_err);
+    k_walk<KeyT, 0><<<blocks(B * 32, 128), 128, 0, st>>>(a, c.L, (const uint2*)c.wk_begins.p, (uint32_t)B,
+                                                   (const uint2*)c.wk_links.p, (WFrame*)c.wk_stack.p, (uint32_t)cap,
+                                                   (uint4*)c.wk_col.p, nullptr, nullptr, nullptr, nullptr, c.d_err);
   PK_TRY(scan4(j, c, (const uint4*)c.wk_col.p, (uint4*)c.wk_pos.p, B));
   PK_TRY(read_total(j, c, (const uint4*)c.wk_pos.p + B, &t));
   PK_TRY(check_err(c));
-  const uint64_t NC = t.x, NB = t.y;
+  const uint64_t NC = t.x, NB = t.y, NP = t.z;
   PK_TRY(cp_alloc(j, c.wk_off, 8 * (NC + 1)));
   PK_TRY(cp_alloc(j, c.wk_out, NB + 1));
+  PK_TRY(cp_alloc(j, c.wk_pieces, sizeof(WPiece) * (NP + 1)));
   if (B)
-    k_walk<KeyT, 1><<<blocks(B, 128), 128, 0, st>>>(a, (uint32_t)n, c.L, (const uint2*)c.wk_begins.p, (uint32_t)B,
-                                                     (const uint64_t*)c.arena.p, (WFrame*)c.wk_stack.p, (uint32_t)cap,
-                                                     nullptr, (const uint4*)c.wk_pos.p, (uint64_t*)c.wk_off.p,
-                                                     (uint8_t*)c.wk_out.p, c.d_err);
+    k_walk<KeyT, 1><<<blocks(B * 32, 128), 128, 0, st>>>(a, c.L, (const uint2*)c.wk_begins.p, (uint32_t)B,
+                                                   (const uint2*)c.wk_links.p, (WFrame*)c.wk_stack.p, (uint32_t)cap,
+                                                   nullptr, (const uint4*)c.wk_pos.p, (uint64_t*)c.wk_off.p,
+                                                   (WPiece*)c.wk_pieces.p, (uint8_t*)c.wk_out.p, c.d_err);
+  if (NP)
+    k_wk_expand<<<blocks(NP * 32, 256), 256, 0, st>>>((const WPiece*)c.wk_pieces.p, (uint32_t)NP,
+                                                       (const uint64_t*)c.arena.p, (uint8_t*)c.wk_out.p);
   PK_CUDA(cudaMemcpyAsync((uint64_t*)c.wk_off.p + NC, &NB, 8, cudaMemcpyHostToDevice, st));
   PK_CUDA(cudaGetLastError());
   PK_TRY(read_total(j, c, (const uint4*)c.wk_pos.p + B, &t));
@@ -1377,7 +1435,7 @@ void pk::cp_free(pk_job* j) {
                     &c->tr,     &c->tgt,      &c->incnt,  &c->inoff,  &c->fill,   &c->inlist,
                     &c->ecol,   &c->eoff2,    &c->old_of, &c->ct,     &c->tot,    &c->epos,
                     &c->cpos,   &c->ubuf,     &c->wk_begins, &c->wk_stack, &c->wk_col, &c->wk_pos,
-                    &c->wk_off, &c->wk_out};
+                    &c->wk_off, &c->wk_out, &c->wk_links, &c->wk_pieces};
   for (DevBuf* d : rest)
     if (d->p) {
       cudaFreeAsync(d->p, j->stream);

@@ -14,10 +14,17 @@
 // The reference's build knobs ksize and LMER_LENGTH are run-time options here:
 //   -k K     k-mer length, 2..64 (default 32)
 //   -l L     LMER_LENGTH (default 8)
-// and three options of this driver:
+// and four options of this driver:
 //   -o PFX   write PFX.table ("PKT1") and PFX.mn ("PKM1") binary dumps
 //   -d DEV   CUDA device (default 0)
 //   -N       drop k-mers spanning N (default: the reference's behaviour, kept)
+//   -g       contig generation, as the reference's PERFORM_CONTIG_GENERATION build
+//            (src/distribute_kmers.cpp:156-203): iterative compaction down to the -n
+//            threshold, the walk, and the contig files that build writes into the
+//            working directory -- contigs_par_r0.fa (partial contigs of the rounds)
+//            and contigs_out_r0.fa (walk contigs), each contig longer than 400 bases
+//            as ">contig_<i>_l_<length>_r_0" and its bases, i counting across both
+//            files (src/walk.cpp:198-227, 488-515)
 // A failed requirement prints the reference's message and exits with status 157
 // (MPI_Abort(MPI_COMM_WORLD, -99) of a single process); an unreadable input exits 2.
 #include <getopt.h>
@@ -85,9 +92,9 @@ int main(int argc, char** argv) {
   std::string input, out_prefix;
   unsigned long max_kmer_count = 0;
   int read_length = 0, coverage = 0, num_buckets = 0, node_threshold = 0;
-  int k = 32, lmer = 8, device = 0, drop_n = 0;
+  int k = 32, lmer = 8, device = 0, drop_n = 0, gen = 0;
   int ret;
-  while ((ret = getopt(argc, argv, "f:b:r:c:t:n:ip:k:l:o:d:N")) != -1) {
+  while ((ret = getopt(argc, argv, "f:b:r:c:t:n:ip:k:l:o:d:Ng")) != -1) {
     switch (ret) {
       case 'f': input.assign(optarg); break;
       case 'b':
@@ -107,6 +114,7 @@ int main(int argc, char** argv) {
       case 'o': out_prefix.assign(optarg); break;
       case 'd': device = atoi(optarg); break;
       case 'N': drop_n = 1; break;
+      case 'g': gen = 1; break;
       default:
         fprintf(stderr, "Should not reach here!!\n");
         abort();  // the reference asserts
@@ -234,6 +242,43 @@ int main(int argc, char** argv) {
       put_side(f, &pre[4 * i], coverage);
     }
     fclose(f);
+  }
+  if (gen) {
+    double t6 = now_s();
+    pk_compaction_info ci;
+    if ((st = pk_compact(job, (uint64_t)node_threshold, coverage, &ci)) != PK_OK) die_pk("iterative compaction", st);
+    std::vector<uint64_t> poff(ci.n_contigs + 1);
+    std::vector<uint8_t> pb(ci.contig_bases + 1);
+    if ((st = pk_copy_partial_contigs(job, poff.data(), pb.data())) != PK_OK) die_pk("pk_copy_partial_contigs", st);
+    double t7 = now_s();
+    printf("iterative compaction (secs): %f, rounds: %d, macro-nodes left: %llu, partial contigs: %llu\n",
+           t7 - t6, ci.rounds, (unsigned long long)ci.n_nodes, (unsigned long long)ci.n_contigs);
+    pk_walk_info wi;
+    if ((st = pk_walk(job, &wi)) != PK_OK) die_pk("walk", st);
+    std::vector<uint64_t> woff(wi.n_contigs + 1);
+    std::vector<uint8_t> wb(wi.contig_bases + 1);
+    if ((st = pk_copy_walk_contigs(job, woff.data(), wb.data())) != PK_OK) die_pk("pk_copy_walk_contigs", st);
+    double t8 = now_s();
+    printf("walk (secs): %f, begin k-mers: %llu, contigs: %llu\n", t8 - t7, (unsigned long long)wi.n_begins,
+           (unsigned long long)wi.n_contigs);
+    int num_contigs = 0;
+    auto write_fa = [&](const char* name, const std::vector<uint64_t>& off, const std::vector<uint8_t>& b) {
+      FILE* f = fopen(name, "w");
+      if (!f) abort_run("Error opening output contig file!");
+      static const char sym[4] = {'A', 'C', 'T', 'G'};
+      std::string seq;
+      for (size_t c = 0; c + 1 < off.size(); c++) {
+        const uint64_t len = off[c + 1] - off[c];
+        if (len <= 400) continue;
+        seq.resize(len);
+        for (uint64_t i = 0; i < len; i++) seq[i] = sym[b[off[c] + i] & 3];
+        fprintf(f, ">contig_%d_l_%llu_r_0\n%s\n", ++num_contigs, (unsigned long long)len, seq.c_str());
+      }
+      fclose(f);
+    };
+    write_fa("contigs_par_r0.fa", poff, pb);
+    write_fa("contigs_out_r0.fa", woff, wb);
+    t5 = now_s();
   }
   printf("pakman-gb300-elapsed-time-no-io (secs): %f\n", t5 - t2);
   pk_job_destroy(job);

@@ -60,3 +60,25 @@ def names():
     """The hot-path cases (compact_*.npz hold the compaction fixtures)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz"))
                   if not os.path.basename(p).startswith("compact_"))
+
+
+def compact_names():
+    """The compaction cases (compact_<name>.npz, made by make_compact_golden.py)."""
+    return sorted(os.path.basename(p)[len("compact_"):-4] for p in glob.glob(os.path.join(HERE, "compact_*.npz")))
+
+
+def load_compact(name):
+    """A compaction case: the FASTA, (k, read_length, coverage, t), the reference's wired
+    map before compaction, and per node threshold (threshold, map after, partial contigs,
+    rounds, walk contig file, partial contig file) -- the reference's own dumps."""
+    import zlib
+    z = np.load(os.path.join(HERE, "compact_%s.npz" % name))
+    unz = lambda a: zlib.decompress(a.tobytes())  # noqa: E731
+    out = {"fasta": unz(z["fasta"]), "params": [int(x) for x in z["params"]],
+           "before": unz(z["before"]), "runs": []}
+    for thr in z["thresholds"]:
+        thr = int(thr)
+        out["runs"].append((thr, unz(z["after_%d" % thr]), unz(z["contigs_%d" % thr]),
+                            int(z["rounds_%d" % thr][0]), unz(z["walk_%d" % thr]),
+                            unz(z["partial_fa_%d" % thr])))
+    return out

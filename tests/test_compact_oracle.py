@@ -4,30 +4,17 @@ a live run of the reference built here when its sources are present, and libstdc
 std::sort for the wiring's unstable ranking."""
 import os
 import subprocess
-import zlib
 
 import numpy as np
 import pytest
 
+from golden_cases import compact_names, load_compact
 from oracle import pk_compact as pc
 from oracle import pk_oracle as po
 from pakman_plus_gb300 import synth
 
-GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = sorted(f[len("compact_"):-4] for f in os.listdir(GOLDEN) if f.startswith("compact_"))
-
-
-def load(name):
-    z = np.load(os.path.join(GOLDEN, "compact_%s.npz" % name))
-    unz = lambda a: zlib.decompress(a.tobytes())  # noqa: E731
-    out = {"fasta": unz(z["fasta"]), "params": [int(x) for x in z["params"]],
-           "before": unz(z["before"]), "runs": []}
-    for thr in z["thresholds"]:
-        thr = int(thr)
-        out["runs"].append((thr, unz(z["after_%d" % thr]), unz(z["contigs_%d" % thr]),
-                            int(z["rounds_%d" % thr][0]), unz(z["walk_%d" % thr]),
-                            unz(z["partial_fa_%d" % thr])))
-    return out
+CASES = compact_names()
+load = load_compact
 
 
 @pytest.mark.parametrize("name", CASES)

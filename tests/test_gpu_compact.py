@@ -6,25 +6,22 @@ suffix list with its extensions, counts, visits and terminal flags, the wiring a
 prefix begin slots -- the partial contigs in emission order, and the walk's contigs in
 begin then depth-first order, exactly."""
 import os
-import zlib
+import subprocess
 
-import numpy as np
 import pytest
 
 import pakman_plus_gb300 as pk
+from golden_cases import load_compact
 from gpu_helpers import ctx
 from oracle import pk_compact as pc
 from pakman_plus_gb300 import synth
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-
-
 def _golden(name):
-    z = np.load(os.path.join(GOLDEN, "compact_%s.npz" % name))
-    k, rl, cov, t = (int(x) for x in z["params"])
-    return zlib.decompress(z["fasta"].tobytes()), k, cov, t, [int(x) for x in z["thresholds"]]
+    g = load_compact(name)
+    k, rl, cov, t = g["params"]
+    return g["fasta"], k, cov, t, [r[0] for r in g["runs"]]
 
 
 def _device(fasta, k, cov, t, thr, drop_n=False):
@@ -131,3 +128,51 @@ def test_walk_of_a_larger_map():
     mn, res = _device(rs.fasta, rs.k, rs.coverage, rs.t, 5000)
     ora = _oracle(mn, rs.k, rs.coverage, 5000)
     _check(res, ora, rs.k)
+
+
+def _fa(partial, walk):
+    """The reference's two contig files for these contigs (src/walk.cpp:198-227,
+    488-515): contigs longer than 400 bases, numbered across both files."""
+    sym = b"ACTG"
+    n = 0
+    files = []
+    for lst in (partial, walk):
+        out = []
+        for c in lst:
+            if len(c) > 400:
+                n += 1
+                out.append(b">contig_%d_l_%d_r_0\n%s\n" % (n, len(c), bytes(sym[x] for x in c)))
+        files.append(b"".join(out))
+    return files
+
+
+# inputs whose canonical start order gives the reference's own map (no prefix-order tie
+# decides a wire), so the files must equal the reference's byte for byte
+SAME_AS_REFERENCE = {"k32_small", "k32_tandem", "k63_longk"}
+
+
+@pytest.mark.parametrize("name", ["k32_small", "k32_bact", "k32_tandem", "k63_longk"])
+def test_pkmer_contig_generation_files(name, tmp_path):
+    """pkmer -g: count, cutoff, macro-nodes, compaction, walk, contig files."""
+    from pakman_plus_gb300 import build as pkbuild
+    from oracle import pk_oracle as po
+    g = load_compact(name)
+    k, rl, cov, t = g["params"]
+    fa = tmp_path / "in.fa"
+    fa.write_bytes(g["fasta"])
+    exe = os.path.join(os.path.dirname(pkbuild.LIB), "bin", "pkmer")
+    ora = po.run(g["fasta"], k, t)
+    for thr, after, contigs, rounds, walk_fa, partial_fa in g["runs"]:
+        d = tmp_path / ("n%d" % thr)
+        d.mkdir()
+        p = subprocess.run([exe, "-f", str(fa), "-r", str(rl), "-c", str(cov), "-t", str(t), "-n", str(thr),
+                            "-k", str(k), "-g"], cwd=str(d), capture_output=True, text=True)
+        assert p.returncode == 0, p.stdout + p.stderr
+        par = (d / "contigs_par_r0.fa").read_bytes()
+        out = (d / "contigs_out_r0.fa").read_bytes()
+        nodes = pc.initial_nodes(ora.mn.keys, ora.mn.suf, ora.mn.pre, k, cov)
+        o = pc.compact(nodes, k, thr)
+        exp_par, exp_out = _fa(o.contigs, pc.walk(o.nodes, k))
+        assert par == exp_par and out == exp_out
+        if name in SAME_AS_REFERENCE:
+            assert par == partial_fa and out == walk_fa
