@@ -39,7 +39,6 @@ from typing import List, Optional, Tuple
 EXT, CNT, VIS, TERM, NBR = 0, 1, 2, 3, 4  # entry fields (NBR: cached neighbour key)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_REF_TREE = "/root/reference"
 
 
 class CompactionError(RuntimeError):
@@ -556,8 +555,9 @@ def state_view(nodes: List[Node]):
 def build_compact_reference(k: int) -> Optional[str]:
     """oracle/_ref/pakman_compact_k<k>, built from the reference sources in place; None
     when the reference tree is absent."""
+    from oracle.pk_oracle import REFERENCE_TREE
     exe = os.path.join(_HERE, "_ref", "pakman_compact_k%d" % k)
-    if not os.path.isdir(_REF_TREE):
+    if not os.path.isdir(REFERENCE_TREE):
         return exe if os.path.exists(exe) else None
     subprocess.run(["make", "-s", "-C", os.path.join(_HERE, "ref"), "compact", "K=%d" % k],
                    check=True, stdout=subprocess.DEVNULL)
