@@ -41,6 +41,23 @@ def test_null_arguments_are_rejected(lib):
     assert lib.pk_count(None, None, 0, None) == capi.PK_ERR_INVALID
     assert lib.pk_cutoff(None, 21, None, None, None) == capi.PK_ERR_INVALID
     assert lib.pk_ctx_create(0, 0, None) == capi.PK_ERR_INVALID
+    info = capi.PkCompactionInfo()
+    assert lib.pk_compact(None, 100, 0, ctypes.byref(info)) == capi.PK_ERR_INVALID
+    assert lib.pk_compaction_get_info(None, ctypes.byref(info)) == capi.PK_ERR_INVALID
+    assert lib.pk_copy_compacted(None, None, None, None, None, None, None) == capi.PK_ERR_INVALID
+    assert lib.pk_copy_partial_contigs(None, None, None) == capi.PK_ERR_INVALID
+    assert lib.pk_walk(None, None) == capi.PK_ERR_INVALID
+    assert lib.pk_copy_walk_contigs(None, None, None) == capi.PK_ERR_INVALID
+
+
+def test_compaction_structs_match_c(lib):
+    """pk_compaction_info, pk_compact_entry and pk_walk_info as the header lays them out."""
+    import pakman_plus_gb300.api as api
+    assert ctypes.sizeof(capi.PkCompactionInfo) == 5 * 8 + 2 * 4
+    assert api.COMPACT_ENTRY.itemsize == 32
+    assert [api.COMPACT_ENTRY.fields[f][1] for f in ("ext_offset", "ext_length", "count", "visit", "terminal",
+                                                     "prefix_pos", "num_wires")] == [0, 8, 12, 16, 20, 24, 28]
+    assert ctypes.sizeof(capi.PkWalkInfo) == 3 * 8 + 2 * 4
 
 
 def test_no_cpu_fallback_without_device(lib):

@@ -51,6 +51,15 @@ def test_defaults_are_announced_and_missing_file_exits_2(pkmer, tmp_path):
     assert "K-mer size: 32, L-mer size: 8, Number of Processes: 1, MAX_KMER_COUNT: 100000000" in r.stdout
 
 
+def test_contig_generation_flag_is_parsed(pkmer, tmp_path):
+    """-g (the reference's contig-generation build) is accepted; the run then fails on
+    the missing file exactly as without it."""
+    r = _run(pkmer, "-f", str(tmp_path / "none.fa"), "-r", "150", "-c", "40", "-n", "500", "-g")
+    assert r.returncode == 2
+    assert "Couldn't open the input FASTA file" in r.stderr
+    assert "node_threashold=100K" not in r.stdout
+
+
 def test_unknown_option_aborts(pkmer):
     r = _run(pkmer, "-Z")
     assert r.returncode < 0 or r.returncode == 134  # SIGABRT, as the reference's assert
