@@ -450,6 +450,72 @@ def read_fasta_contigs(data: bytes) -> List[bytes]:
     return [bytes(code[c] for c in line) for line in data.split(b"\n") if line and not line.startswith(b">")]
 
 
+# ----------------------------------------------------------------- C restatement --
+class _CResult(__import__("ctypes").Structure):
+    import ctypes as _c
+    _fields_ = [("rounds", _c.c_uint64), ("n_nodes", _c.c_uint64), ("n_contigs", _c.c_uint64),
+                ("walk_contigs", _c.c_uint64), ("walk_bases", _c.c_uint64), ("contig_bases", _c.c_uint64),
+                ("hash", _c.c_uint64)]
+
+
+def compact_walk_c(keys, suf, pre, k: int, coverage: int, threshold: int) -> _CResult:
+    """The same compaction and walk in C (oracle/pk_compact.c); the result carries
+    counts and a hash of everything (`result_hash`)."""
+    import ctypes
+
+    import numpy as np
+
+    from oracle import pk_oracle as po
+    L = po.lib()
+    fn = L.pko_compact_walk
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                   ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_CResult)]
+    m = len(keys)
+    kw = np.zeros((max(1, m), 2), np.uint64)
+    if m:
+        if getattr(keys, "dtype", None) is not None and keys.dtype.names:
+            kw[:m, 0] = keys["lo"]
+            kw[:m, 1] = keys["hi"]
+        else:
+            kw[:m, 0] = np.asarray(keys, np.uint64)
+    s = np.ascontiguousarray(suf, np.uint32).reshape(-1)
+    p = np.ascontiguousarray(pre, np.uint32).reshape(-1)
+    out = _CResult()
+    rc = fn(kw.ctypes.data, s.ctypes.data, p.ctypes.data, m, k, coverage, threshold, ctypes.byref(out))
+    if rc != 0:
+        raise CompactionError("pko_compact_walk failed with %d" % rc)
+    return out
+
+
+def result_hash(nodes: List[Node], contigs: List[bytes], walk_contigs: List[bytes]) -> int:
+    """FNV-1a 64 of a map, its partial contigs and its walk contigs, serialised the way
+    oracle/pk_compact.c hashes them."""
+    import struct
+    M = (1 << 64) - 1
+
+    def fnv(h, b):
+        for x in b:
+            h = ((h ^ x) * 1099511628211) & M
+        return h
+
+    h = 1469598103934665603
+    for key, suf, pre, wires, begin in state_view(nodes):
+        h = fnv(h, struct.pack("<QQ", key & M, key >> 64))
+        for lst in (suf, pre):
+            h = fnv(h, struct.pack("<I", len(lst)))
+            for ext, c, v, t in lst:
+                h = fnv(h, struct.pack("<I", len(ext)) + ext + struct.pack("<iiB", c, v, int(t)))
+        h = fnv(h, struct.pack("<I", len(wires)) + b"".join(struct.pack("<iii", *w) for w in wires))
+        h = fnv(h, struct.pack("<I", len(begin)) + b"".join(struct.pack("<ii", *b) for b in begin))
+    h = fnv(h, struct.pack("<Q", len(contigs)))
+    for c in contigs:
+        h = fnv(h, struct.pack("<I", len(c)) + c)
+    hw = 1469598103934665603
+    for c in walk_contigs:
+        hw = fnv(hw, struct.pack("<I", len(c)) + c)
+    return fnv(fnv(h, struct.pack("<Q", len(walk_contigs))), struct.pack("<Q", hw))
+
+
 # ----------------------------------------------------------------- construction ---
 def initial_nodes(keys, suf, pre, k: int, coverage: int) -> List[Node]:
     """The wired map the reference hands to compaction, lists in canonical order:

@@ -38,12 +38,12 @@ class OracleError(RuntimeError):
 
 
 def build(force: bool = False) -> str:
-    """Compile pk_oracle.c (gcc, -O2) into oracle/_build/libpk_oracle.so."""
-    src = os.path.join(HERE, "pk_oracle.c")
+    """Compile pk_oracle.c and pk_compact.c (gcc, -O2) into oracle/_build/libpk_oracle.so."""
+    srcs = [os.path.join(HERE, "pk_oracle.c"), os.path.join(HERE, "pk_compact.c")]
     os.makedirs(BUILD, exist_ok=True)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(x) for x in srcs):
         tmp = LIB + ".tmp"
-        subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-pthread", "-shared", "-fPIC", "-o", tmp, src])
+        subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-pthread", "-shared", "-fPIC", "-o", tmp, *srcs])
         os.replace(tmp, LIB)
     return LIB
 

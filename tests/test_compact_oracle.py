@@ -106,3 +106,28 @@ def test_live_reference_run():
     assert pc.state_view(o.nodes) == pc.state_view(r.after)
     assert o.contigs == r.contigs
     assert [c for c in pc.walk(o.nodes, 32) if len(c) > 400] == pc.read_fasta_contigs(r.raw["walk_fa"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_c_restatement_matches_the_python_oracle(name):
+    """oracle/pk_compact.c (the bench's CPU baseline) gives the same map, partial
+    contigs and walk contigs as oracle/pk_compact.py, through a hash of all three."""
+    g = load(name)
+    k, rl, cov, t = g["params"]
+    ora = po.run(g["fasta"], k, t)
+    for thr, *_ in g["runs"]:
+        o = pc.compact(pc.initial_nodes(ora.mn.keys, ora.mn.suf, ora.mn.pre, k, cov), k, thr)
+        w = pc.walk(o.nodes, k)
+        c = pc.compact_walk_c(ora.mn.keys, ora.mn.suf, ora.mn.pre, k, cov, thr)
+        assert (c.rounds, c.n_nodes, c.n_contigs, c.walk_contigs) == (o.rounds, len(o.nodes), len(o.contigs), len(w))
+        assert c.hash == pc.result_hash(o.nodes, o.contigs, w)
+
+
+def test_c_restatement_other_widths():
+    for k in (17, 33, 48, 64):
+        rs = synth.small_case(300 + k, genome_len=3000, n_reads=2500, read_len=120, err=0.005, k=k, coverage=40)
+        ora = po.run(rs.fasta, k, 21)
+        o = pc.compact(pc.initial_nodes(ora.mn.keys, ora.mn.suf, ora.mn.pre, k, 40), k, 5)
+        w = pc.walk(o.nodes, k)
+        c = pc.compact_walk_c(ora.mn.keys, ora.mn.suf, ora.mn.pre, k, 40, 5)
+        assert c.hash == pc.result_hash(o.nodes, o.contigs, w), k
