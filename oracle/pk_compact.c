@@ -222,6 +222,22 @@ static void std_sort(int* a, int n, const rank_t* r) {
   }
 }
 
+/* The ranking alone, for pinning against libstdc++: out = indices 0..n-1 sorted by
+   (visit, count) descending the way std::sort leaves them. */
+int pko_rank_std_sort(const int32_t* vis, const int32_t* cnt, int n, int* out) {
+  entry_t* e = (entry_t*)calloc(n ? n : 1, sizeof(entry_t));
+  if (!e) return PKC_EMEM;
+  for (int i = 0; i < n; i++) {
+    e[i].vis = vis[i];
+    e[i].cnt = cnt[i];
+    out[i] = i;
+  }
+  rank_t r = {e};
+  std_sort(out, n, &r);
+  free(e);
+  return PKC_OK;
+}
+
 /* MacroNode::setup_wiring after wiring_info / prefix_begin_info were cleared */
 static int setup_wiring(node_t* nd) {
   const int np = nd->pre.n, ns = nd->suf.n, nw = np + ns + 1;

@@ -78,22 +78,57 @@ def stdsort(tmp_path_factory):
     return exe
 
 
-def test_std_sort_restatement_matches_libstdcxx(stdsort):
-    rng = np.random.default_rng(11)
+def _sort_cases(sizes, seed=11):
+    rng = np.random.default_rng(seed)
     cases = []
-    for n in list(range(0, 40)) + [47, 64, 100, 257, 1000]:
-        for spread in (1, 2, 4, 50):
-            cases.append([(int(rng.integers(0, spread)), int(rng.integers(0, spread))) for _ in range(n)])
+    for n in sizes:
+        for spread in (1, 2, 3, 4, 50):
+            for _ in range(3):
+                cases.append([(int(rng.integers(0, spread)), int(rng.integers(0, spread))) for _ in range(n)])
+    return cases
+
+
+def _libstdcxx(exe, cases):
+    inp = "".join("%d %s\n" % (len(c), " ".join("%d %d" % vc for vc in c)) for c in cases)
+    out = subprocess.run([exe], input=inp, capture_output=True, text=True, check=True).stdout
+    return [[int(x) for x in line.split()] for line in out.split("\n")[:len(cases)]]
+
+
+def test_std_sort_restatement_matches_libstdcxx(stdsort):
+    cases = _sort_cases(list(range(0, 40)) + [47, 64, 100, 257, 1000])
     cases.append([(3, 1)] * 70)  # all equal
     cases.append([(i // 3, 0) for i in range(90)])  # ascending runs (descending order wanted)
     cases.append([(90 - i, 2) for i in range(90)])
-    inp = "".join("%d %s\n" % (len(c), " ".join("%d %d" % vc for vc in c)) for c in cases)
-    out = subprocess.run([stdsort], input=inp, capture_output=True, text=True, check=True).stdout
-    lines = out.split("\n")
-    for c, line in zip(cases, lines):
+    for c, ref in zip(cases, _libstdcxx(stdsort, cases)):
         idx = list(range(len(c)))
         pc._std_sort(idx, lambda i, j: c[i][0] > c[j][0] or (c[i][0] == c[j][0] and c[i][1] > c[j][1]))
-        assert idx == ([int(x) for x in line.split()] if line.strip() else []), c
+        assert idx == ref, c
+
+
+def test_c_sort_matches_libstdcxx(stdsort):
+    """The C restatement's ranking (oracle/pk_compact.c) on lists of up to 1000 entries."""
+    import ctypes
+    L = po.lib()
+    L.pko_rank_std_sort.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    cases = _sort_cases(list(range(0, 40)) + [64, 257, 1000], seed=12)
+    for c, ref in zip(cases, _libstdcxx(stdsort, cases)):
+        v = np.array([x[0] for x in c] or [0], np.int32)
+        k = np.array([x[1] for x in c] or [0], np.int32)
+        out = np.zeros(max(1, len(c)), np.int32)
+        assert L.pko_rank_std_sort(v.ctypes.data, k.ctypes.data, len(c), out.ctypes.data) == 0
+        assert out[:len(c)].tolist() == ref, c
+
+
+def test_device_sort_matches_libstdcxx(stdsort, tmp_path):
+    """The device's ranking (pakman_plus_gb300/csrc/pk_stdsort.cuh, built for the host)
+    on every list size the device ranks (0..32 entries), heavy ties included: past 16
+    entries this is the introsort branch that no fixture list reaches."""
+    exe = str(tmp_path / "stdsort_host")
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cpp", "stdsort_host.cpp")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-o", exe, src], check=True, capture_output=True)
+    cases = _sort_cases(list(range(0, 33)) * 20, seed=13)
+    mine = _libstdcxx(exe, cases)
+    assert mine == _libstdcxx(stdsort, cases)
 
 
 def test_live_reference_run():
