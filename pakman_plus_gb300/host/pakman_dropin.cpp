@@ -14,6 +14,19 @@
 // table; begin_mnode_construction prints the reference's summary lines, aborts when
 // nothing reaches the cutoff, and fills MN_map sorted by (k-1)-mer with suffixes and
 // prefixes in ascending extension order and (count, ceil(count/coverage)) pairs.
+//
+// For the reference's contig-generation build (PERFORM_CONTIG_GENERATION,
+// COMPACT_PGRAGH; src/distribute_kmers.cpp:156-203) it also replaces
+// src/wire.cpp, src/iterative_compaction.cpp and src/merge_mn.cpp:
+//
+//   initiate_mnode_wiring(MN_map)                         src/wire.cpp:66-121
+//   begin_iterative_compaction(MN_map, partial_contig_list)  src/iterative_compaction.cpp:131-464
+//   identify_begin_kmers(MN_map, list_of_begin_kmers)     src/iterative_compaction.cpp:65-93
+//   generate_compacted_pakgraph(MN_map, global_MN_map)    src/iterative_compaction.cpp:96-128
+//
+// The wiring and the compaction run on the device.  MN_map is refilled from the
+// device after each call, and the reference's own walk (src/walk.cpp, linked
+// unchanged) traverses it.  With one rank the gather is a copy.
 // One MPI rank drives one GPU; the device counts the rank's whole buffer at once, so
 // the -b batch size changes nothing (the reference's table is the same for any -b).
 #include <stdio.h>
@@ -157,4 +170,104 @@ void begin_mnode_construction(std::vector<std::pair<kmer_t, MacroNode>>& MN_map)
     MN_map.push_back(std::make_pair(key, mn));
   }
   if (rank == 0) printf("Total number of macro_nodes across all proc's: %lu\n", (unsigned long)m);
+}
+
+// ---- contig generation ---------------------------------------------------------
+extern int node_threashold;
+
+namespace {
+
+void put_ext(BasePairVector& v, const uint8_t* b, uint32_t n) {
+  for (uint32_t i = 0; i < n; i++) v.push_back((BasePair)b[i]);
+}
+
+}  // namespace
+
+void initiate_mnode_wiring(std::vector<std::pair<kmer_t, MacroNode>>& MN_map) {
+  ensure_job();
+  pk_status s = pk_wire_macro_nodes(g_job, coverage);
+  if (s != PK_OK) die(s, "pk_wire_macro_nodes");
+  std::vector<pk_wiring> w(MN_map.size() + 1);
+  s = pk_copy_wiring(g_job, w.data(), MN_map.size());
+  if (s != PK_OK) die(s, "pk_copy_wiring");
+  for (size_t i = 0; i < MN_map.size(); i++) {
+    MacroNode& mn = MN_map[i].second;
+    const pk_wiring& r = w[i];
+    mn.prefixes.push_back(BasePairVector{});
+    mn.prefixes_terminal.push_back(true);
+    mn.prefix_count.push_back(std::make_pair(1, r.terminal_prefix_visit));
+    mn.suffixes.push_back(BasePairVector{});
+    mn.suffixes_terminal.push_back(true);
+    mn.suffix_count.push_back(std::make_pair(1, r.terminal_suffix_visit));
+    const int nw = (int)(mn.prefixes.size() + mn.suffixes.size() + 1);
+    mn.wiring_info.assign(nw, WireInfo{0, 0, 0});
+    for (int x = 0; x < nw && x < 9; x++) mn.wiring_info[x] = WireInfo{r.wire[x][0], r.wire[x][1], r.wire[x][2]};
+    mn.prefix_begin_info.assign(mn.prefixes.size(), PrefixInfo{0, 0});
+    for (size_t p = 0; p < mn.prefixes.size() && p < 5; p++)
+      mn.prefix_begin_info[p] = PrefixInfo{r.prefix_begin[p][0], r.prefix_begin[p][1]};
+  }
+}
+
+size_t begin_iterative_compaction(std::vector<std::pair<kmer_t, MacroNode>>& MN_map,
+                                  std::vector<BasePairVector>& partial_contig_list) {
+  ensure_job();
+  if (rank == 0) fprintf(stderr, "Starting phase 2 iterative phase\n");
+  pk_compaction_info ci;
+  pk_status s = pk_compact(g_job, (uint64_t)node_threashold, coverage, &ci);
+  if (s != PK_OK) die(s, "pk_compact");
+  const size_t words = sizeof(kmer_t) / 8;
+  std::vector<uint64_t> keys(ci.n_nodes * words + 1), eoff(ci.n_nodes + 1);
+  std::vector<uint32_t> npre(ci.n_nodes + 1);
+  std::vector<pk_compact_entry> ent(ci.n_entries + 1);
+  std::vector<int32_t> wires(3 * (ci.n_entries + ci.n_nodes) + 3);
+  std::vector<uint8_t> bases(ci.ext_bases + 1);
+  s = pk_copy_compacted(g_job, keys.data(), eoff.data(), npre.data(), ent.data(), wires.data(), bases.data());
+  if (s != PK_OK) die(s, "pk_copy_compacted");
+  MN_map.clear();
+  MN_map.reserve(ci.n_nodes);
+  for (uint64_t i = 0; i < ci.n_nodes; i++) {
+    const kmer_t key = key_at(keys, i);
+    MacroNode mn;
+    for (int b = 0; b < MN_LENGTH; b++) mn.k_1_mer.push_back(kmerel_mn(key, b));
+    for (uint64_t e = eoff[i]; e < eoff[i + 1]; e++) {
+      BasePairVector x;
+      put_ext(x, bases.data() + ent[e].ext_offset, ent[e].ext_length);
+      const bool is_pre = e - eoff[i] < npre[i];
+      (is_pre ? mn.prefixes : mn.suffixes).push_back(x);
+      (is_pre ? mn.prefix_count : mn.suffix_count).push_back(std::make_pair(ent[e].count, ent[e].visit));
+      (is_pre ? mn.prefixes_terminal : mn.suffixes_terminal).push_back(ent[e].terminal != 0);
+      if (is_pre) mn.prefix_begin_info.push_back(PrefixInfo{ent[e].prefix_pos, ent[e].num_wires});
+    }
+    for (uint64_t w = eoff[i] + i; w <= eoff[i + 1] + i; w++)
+      mn.wiring_info.push_back(WireInfo{wires[3 * w], wires[3 * w + 1], wires[3 * w + 2]});
+    MN_map.push_back(std::make_pair(key, mn));
+  }
+  std::vector<uint64_t> coff(ci.n_contigs + 1);
+  std::vector<uint8_t> cb(ci.contig_bases + 1);
+  s = pk_copy_partial_contigs(g_job, coff.data(), cb.data());
+  if (s != PK_OK) die(s, "pk_copy_partial_contigs");
+  for (uint64_t c = 0; c < ci.n_contigs; c++) {
+    BasePairVector x;
+    put_ext(x, cb.data() + coff[c], (uint32_t)(coff[c + 1] - coff[c]));
+    partial_contig_list.push_back(x);
+  }
+  if (rank == 0) fprintf(stderr, "Completed iterative phase 2\n");
+  return ci.n_nodes;
+}
+
+// every terminal prefix with visits, map order then prefix order
+void identify_begin_kmers(std::vector<std::pair<kmer_t, MacroNode>>& MN_map,
+                          std::vector<BeginMN>& list_of_begin_kmers) {
+  for (size_t i = 0; i < MN_map.size(); i++) {
+    const MacroNode& mn = MN_map[i].second;
+    for (size_t l = 0; l < mn.prefixes.size(); l++)
+      if (mn.prefix_count[l].second > 0 && mn.prefixes_terminal[l])
+        list_of_begin_kmers.push_back(BeginMN{MN_map[i].first, (int)l});
+  }
+}
+
+// one rank: every node is already local
+void generate_compacted_pakgraph(std::vector<std::pair<kmer_t, MacroNode>>& MN_map,
+                                 std::vector<std::pair<kmer_t, MacroNode>>& global_MN_map) {
+  global_MN_map = MN_map;
 }

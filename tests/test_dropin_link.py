@@ -37,3 +37,27 @@ def test_reference_driver_links_with_the_dropin(tmp_path):
     if not torch.cuda.is_available():
         assert r.returncode == 157, (r.returncode, r.stderr)
         assert "[pakman-gb300] pk_ctx_create" in r.stderr
+
+
+@pytest.mark.skipif(not os.path.isdir(po.REFERENCE_TREE), reason="reference sources not present")
+def test_contig_generation_driver_links_with_the_dropin(tmp_path):
+    """The reference's driver in its contig-generation build (PERFORM_CONTIG_GENERATION,
+    COMPACT_PGRAGH) links with the drop-in in place of its wiring and compaction
+    objects and keeps its own walk."""
+    pkbuild.build()
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "dropin_contigs", "K=32",
+                           "-j8"], stdout=subprocess.DEVNULL)
+    exe = os.path.join(ROOT, "oracle", "_ref", "pkmer_dropin_contigs_k32")
+    syms = subprocess.run(["nm", "-C", exe], capture_output=True, text=True).stdout
+    for fn in ("initiate_mnode_wiring(", "begin_iterative_compaction(", "identify_begin_kmers(",
+               "generate_compacted_pakgraph(", "traverse_pakgraph("):
+        assert fn in syms, fn
+    assert "generate_id_set" not in syms and "iterate_and_pack_mn" not in syms and "push_to_pred" not in syms
+    fa = tmp_path / "in.fa"
+    fa.write_bytes(b">r0\n" + b"ACGT" * 25 + b"\n")
+    r = subprocess.run([exe, "-f", str(fa), "-r", "100", "-c", "10"], capture_output=True, text=True,
+                       timeout=120, cwd=str(tmp_path))
+    import torch
+    if not torch.cuda.is_available():
+        assert r.returncode == 157, (r.returncode, r.stderr)
+        assert "[pakman-gb300] pk_ctx_create" in r.stderr
