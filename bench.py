@@ -242,7 +242,7 @@ def measure_compaction(job, rs, args, M, reps=3):
             "partial_contigs": int(info.n_contigs), "ms": ms, "nodes_per_s": M / (ms / 1000.0),
             "launches_per_round": 15,
             "walk": {"ms": wms, "begin_kmers": int(winfo.n_begins), "contigs": int(winfo.n_contigs),
-                     "contig_bases": int(winfo.contig_bases), "launches": 10},
+                     "contig_bases": int(winfo.contig_bases), "launches": 12},
             "nodes_per_s_with_walk": M / ((ms + wms) / 1000.0)}
 
 
