@@ -30,10 +30,6 @@ sys.path.insert(0, ROOT)
 
 METRIC = "k-mers/sec count+macro-node on 1 GB300 (% HBM roofline); served p50/p99 latency"
 UNIT = "k-mers/s"
-KERNELS_PER_STEP = 14  # line scan, tile prefix, bucket count, column prefix, bucket prefix,
-#                        coarse offsets, coarse scatter, fine scatter, giant-chunk prefix, bucket
-#                        table (two launches: the plain and the giant-bucket kernel, one of
-#                        which returns at once), cutoff, kept filter, macro-nodes
 
 
 def parse():
@@ -179,7 +175,9 @@ def _cpu_sample(rs, sample_windows: int):
 
 def cpu_baseline(rs, sample_windows: int):
     """The oracle's multi-threaded restatement of the reference's owner-partitioned
-    counting (all host cores) plus cutoff and macro-nodes, on the same read set."""
+    counting (all host cores) plus cutoff and macro-nodes, on the same read set.
+    Returns the baseline line and the oracle's result when the sample is the whole read
+    set (else None)."""
     from oracle import pk_oracle as po
     sample, reads = _cpu_sample(rs, sample_windows)
     threads = os.cpu_count() or 1
@@ -188,9 +186,51 @@ def cpu_baseline(rs, sample_windows: int):
     pipe = po.run(sample, rs.k, rs.t, rs.drop_n, threads=threads)
     dt = time.perf_counter() - t0
     n = pipe.table.n_windows
-    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+    line = {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{reads} reads ({n} k-mer windows) of the same read set, count + cutoff + "
                       f"macro-nodes, {dt:.2f} s on {threads} threads"}
+    return line, (pipe if reads == rs.n_reads else None)
+
+
+def _digest(*arrays) -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(a.tobytes())
+    return h.hexdigest()[:16]
+
+
+def device_result(job, rs):
+    """The device's whole result for the bench's read set: table, histogram, cutoff and
+    macro-node table (the macro-nodes are built again, so the job is left at stage 3)."""
+    import pakman_plus_gb300 as pk
+    keys, counts = job.table()
+    cut, hist, kept = job.cutoff(rs.t)
+    job.build_macro_nodes(0)
+    mn = job.macro_nodes()
+    return {"keys": pk.to_key128(keys), "counts": counts, "cutoff": cut, "hist": hist,
+            "mn_keys": pk.to_key128(mn.keys), "mn_suf": mn.suffix_counts, "mn_pre": mn.prefix_counts}
+
+
+def parity(dev, pipe, scale: float):
+    """Bit-exact comparison of the device result with the oracle's on the same reads."""
+    import numpy as np
+    table = bool(dev["keys"].size == pipe.table.keys.size and
+                 np.array_equal(dev["keys"], pipe.table.keys) and
+                 np.array_equal(dev["counts"], pipe.table.counts))
+    mn = pipe.mn is not None and bool(
+        dev["mn_keys"].size == pipe.mn.keys.size and np.array_equal(dev["mn_keys"], pipe.mn.keys) and
+        np.array_equal(dev["mn_suf"], pipe.mn.suf) and np.array_equal(dev["mn_pre"], pipe.mn.pre))
+    return {"table": table, "cutoff": bool(dev["cutoff"] == pipe.cutoff),
+            "hist": bool(np.array_equal(dev["hist"], pipe.hist)), "mn": bool(mn), "scale": scale,
+            "rows": int(dev["keys"].size), "nodes": int(dev["mn_keys"].size),
+            "table_sha256_16": _digest(dev["keys"], dev["counts"]),
+            "oracle_table_sha256_16": _digest(pipe.table.keys, pipe.table.counts),
+            "mn_sha256_16": _digest(dev["mn_keys"], dev["mn_suf"], dev["mn_pre"]),
+            "oracle_mn_sha256_16": (_digest(pipe.mn.keys, pipe.mn.suf, pipe.mn.pre)
+                                    if pipe.mn is not None else None),
+            "against": "the oracle's threaded restatement (equal to the serial oracle, which is "
+                       "pinned to the reference) on the same reads, whole read set"}
 
 
 def max_over_ranks(x: float, dist, device: str) -> float:
@@ -226,7 +266,9 @@ def measure_compaction(job, rs, args, M, reps=3):
         return job.stage_times()["compaction"]
 
     once()
+    l0 = L.pk_kernel_launches()
     ms = statistics.median(once() for _ in range(reps))
+    compact_launches = (L.pk_kernel_launches() - l0) / reps
     winfo = capi.PkWalkInfo()
 
     def walk_once():
@@ -236,13 +278,16 @@ def measure_compaction(job, rs, args, M, reps=3):
         return job.stage_times()["walk"]
 
     walk_once()
+    l0 = L.pk_kernel_launches()
     wms = statistics.median(walk_once() for _ in range(reps))
+    walk_launches = (L.pk_kernel_launches() - l0) / reps
     return {"workload": f"{rs.name} macro-node table -> at most {args.compact_threshold} nodes",
             "nodes_in": int(M), "nodes_out": int(info.n_nodes), "rounds": int(info.rounds),
             "partial_contigs": int(info.n_contigs), "ms": ms, "nodes_per_s": M / (ms / 1000.0),
-            "launches_per_round": 15,
+            "launches": compact_launches,
+            "launches_per_round": compact_launches / max(1, int(info.rounds)),
             "walk": {"ms": wms, "begin_kmers": int(winfo.n_begins), "contigs": int(winfo.n_contigs),
-                     "contig_bases": int(winfo.contig_bases), "launches": 12},
+                     "contig_bases": int(winfo.contig_bases), "launches": walk_launches},
             "nodes_per_s_with_walk": M / ((ms + wms) / 1000.0)}
 
 
@@ -653,6 +698,7 @@ def main():
     sampler.start()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    launches0 = pk.capi.lib().pk_kernel_launches()
     e0.record(stream)
     for _ in range(args.steps):
         s = job.run_device(d_fa.data_ptr(), F, params)
@@ -660,12 +706,14 @@ def main():
             stage_acc[name] = stage_acc.get(name, 0.0) + ms
     e1.record(stream)
     torch.cuda.synchronize()
+    launches = pk.capi.lib().pk_kernel_launches() - launches0
     if dist:
         dist.barrier()
     clocks = sampler.stop()
     ms_step = e0.elapsed_time(e1) / args.steps
     ms_step = max_over_ranks(ms_step, dist, f"cuda:{local}")
     value = job_throughput(s.n_windows, world, ms_step)
+    dev = device_result(job, rs) if rank == 0 and world == 1 and not args.no_cpu_baseline else None
     compaction = None
     if not args.no_compaction and rank == 0:
         compaction = measure_compaction(job, rs, args, s.n_nodes)
@@ -759,11 +807,14 @@ def main():
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"},
             "e2e": e2e,
-            "gpu_launches": KERNELS_PER_STEP * args.steps,
+            "gpu_launches": int(launches),
+            "gpu_launches_per_step": launches / args.steps,
             "clocks": clocks,
         }
         if world == 1 and not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(rs, args.cpu_sample_windows)
+            line["cpu_baseline"], pipe = cpu_baseline(rs, args.cpu_sample_windows)
+            if pipe is not None and dev is not None:
+                line["parity"] = parity(dev, pipe, args.scale)
         if compaction is not None:
             if world == 1 and not args.no_cpu_baseline:
                 try:
@@ -778,6 +829,10 @@ def main():
     ctx.close()
     if dist:
         dist.destroy_process_group()
+    par = line.get("parity") if rank == 0 else None
+    if par is not None and not all(par[x] for x in ("table", "cutoff", "hist", "mn")):
+        print("bench: the device result differs from the oracle's", file=sys.stderr)
+        return 3
     return 0
 
 

@@ -78,11 +78,19 @@ typedef struct pk_params {
   int32_t read_length;  /* -r: accepted and passed through; the counter does not use it */
   int32_t drop_n;       /* 0: reference behaviour (an 'N' is code 7 OR-ed into the
                            window); 1: windows containing 'N'/'n' are skipped */
-  uint64_t batch_kmers; /* -b: MAX_KMER_COUNT; the table is the same for any value */
+  uint64_t batch_kmers; /* -b: MAX_KMER_COUNT, the piece size of counting in pieces (see
+                           chunking); the table is the same for any value */
   int32_t bucket_bits;  /* partition digits (leading key bits), 2..18; 0 = automatic */
   int32_t mn_units;     /* macro-node work units: 0 = automatic (about 1000 kept rows
                            each); n > 0 = units of 4^(n-1) partition buckets */
-  int32_t reserved[6];
+  int32_t chunking;     /* -b pieces for host input (pk_count, pk_run, pk_count_file):
+                           0 = automatic -- the whole input at once when it fits the
+                           context's HBM budget and the 2^32-window limit, else in
+                           record-aligned pieces of at most batch_kmers bytes (so at most
+                           batch_kmers k-mer windows each) whose tables are merged on the
+                           device; 1 = always in such pieces; 2 = never.  The table is the
+                           same for any piece size, as the reference's is for any -b. */
+  int32_t reserved[5];
 } pk_params;
 
 /* Counts reported by a run. */
@@ -123,6 +131,10 @@ pk_status pk_job_memory(pk_job* job, uint64_t* bytes);
 pk_status pk_count(pk_job* job, const char* fasta, uint64_t n, const pk_params* p);
 pk_status pk_count_device(pk_job* job, const void* d_fasta, uint64_t n, const pk_params* p);
 pk_status pk_table_info(pk_job* job, uint64_t* n_unique, uint64_t* n_windows, uint64_t* n_reads);
+/* Pieces the last count used: 1 when the whole input was counted at once, more when it
+ * was counted in -b pieces (the reference's batch flush, src/kmer_counting.cpp:3022-3139)
+ * and their tables merged. */
+pk_status pk_count_pieces(pk_job* job, uint32_t* pieces);
 
 /* ---- file ingest: replaces perform_input_reading ----------------------------------
  * The slice of a FASTA file that MPI rank `rank` of `n_ranks` reads in the reference
@@ -276,6 +288,17 @@ pk_status pk_copy_walk_contigs(pk_job* job, uint64_t* offsets, uint8_t* bases);
 
 pk_status pk_summary_get(pk_job* job, pk_summary* out);
 
+/* ---- bounded device waits -----------------------------------------------------------
+ * Kernels that wait on other CTAs (the decoupled look-back of the kept-row filter and of
+ * the macro-node kernel, a giant bucket waiting for its chunks) poll a bounded number of
+ * times with a short sleep between polls, then set an error bit and return, so the call
+ * fails with PK_ERR_DEVICE and the context stays usable.  spins = polls before a wait
+ * gives up (0 = the default, about 1-2 s).  withhold_unit >= 0 makes that macro-node work
+ * unit publish nothing, so the waits of the units after it run out: a fault injected on
+ * the host side, for testing this error path; -1 turns it off.  Both apply to this
+ * job's later calls. */
+pk_status pk_job_set_wait_limit(pk_job* job, uint32_t spins, int32_t withhold_unit);
+
 /* ---- per-kernel timing (CUDA events on the job's stream) ---------------------------- */
 pk_status pk_job_enable_timing(pk_job* job, int on);
 /* Milliseconds per stage of the last run; n_stages receives the stage count. */
@@ -288,8 +311,10 @@ const char* pk_stage_name(int stage);
  * latency-critical loop where an allocation may block, a process whose device-memory
  * budget is already committed): the histogram of counts < num_buckets, the first-
  * minimum cutoff over [1, num_buckets) and the number of rows >= cutoff -- the same
- * results as pk_cutoff -- over a count column already in device memory (for example the
- * counts from pk_table_device).
+ * values as pk_cutoff -- over a count column already in device memory (for example the
+ * counts from pk_table_device).  The results stay on the device, so no row reaching the
+ * cutoff is not an error here: where pk_cutoff returns PK_ERR_EMPTY this call returns
+ * PK_OK with *d_kept == 0, and the caller tests *d_kept before building macro-nodes.
  *   d_counts  device array of n_rows row counts (read only)
  *   d_cutoff  device output, 1 uint32 (required)
  *   d_hist    device output, num_buckets uint64, or NULL
@@ -300,7 +325,8 @@ const char* pk_stage_name(int stage);
  * maximum returns PK_ERR_INVALID.  The function calls no cudaMalloc, cudaFree or other
  * allocating routine.  Its first call on a device, made with that device current, looks
  * up the scratch array's device address; make that first call before any stream
- * capture.  All calls share the one array and each call clears it first: calls whose
+ * capture.  The address is kept for the rest of the process: after cudaDeviceReset on
+ * that device this function must not be called again in the same process.  All calls share the one array and each call clears it first: calls whose
  * work overlaps on the GPU race and give wrong results.  Returns once the work is
  * enqueued on `stream`. */
 #define PK_NOALLOC_MAX_BUCKETS 4096
@@ -313,6 +339,9 @@ void pk_host_free(void* p);
 
 /* Library version string. */
 const char* pk_version(void);
+/* Kernel launches this library has made in this process so far (all jobs, contexts and
+ * threads; a launch recorded into a CUDA graph counts once, when it is captured). */
+uint64_t pk_kernel_launches(void);
 
 /* ---- Serving: many independent count -> cutoff -> macro-node jobs on one GPU ----
  *

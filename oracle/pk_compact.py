@@ -625,7 +625,7 @@ def build_compact_reference(k: int) -> Optional[str]:
     exe = os.path.join(_HERE, "_ref", "pakman_compact_k%d" % k)
     if not os.path.isdir(REFERENCE_TREE):
         return exe if os.path.exists(exe) else None
-    subprocess.run(["make", "-s", "-C", os.path.join(_HERE, "ref"), "compact", "K=%d" % k],
+    subprocess.run(["make", "-s", "-C", os.path.join(_HERE, "ref"), "compact", "K=%d" % k, "REF=" + REFERENCE_TREE],
                    check=True, stdout=subprocess.DEVNULL)
     return exe
 

@@ -26,7 +26,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD, "libpk_oracle.so")
-REFERENCE_TREE = "/root/reference"
+# The reference source tree: $PAKMAN_REFERENCE, else where this project's build
+# container mounts it.  Absent on machines that only run the prebuilt oracle.
+REFERENCE_TREE = os.environ.get("PAKMAN_REFERENCE", "/root/reference")
 
 PKO_OK, PKO_EFORMAT, PKO_EARG, PKO_ENOMEM, PKO_EEMPTY = 0, -1, -2, -3, -4
 
@@ -55,7 +57,7 @@ def build_reference(k: int) -> Optional[str]:
         return exe
     if not os.path.isdir(REFERENCE_TREE):
         return None
-    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"K={k}", "-j8"],
+    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"K={k}", f"REF={REFERENCE_TREE}", "-j8"],
                           stdout=subprocess.DEVNULL)
     return exe if os.path.exists(exe) else None
 
@@ -68,7 +70,7 @@ def build_divide_reference() -> Optional[str]:
         return exe
     if not os.path.isdir(REFERENCE_TREE):
         return None
-    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), "divide", "K=32", "-j8"],
+    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), "divide", "K=32", f"REF={REFERENCE_TREE}", "-j8"],
                           stdout=subprocess.DEVNULL)
     return exe if os.path.exists(exe) else None
 

@@ -392,6 +392,13 @@ class Job:
     def enable_timing(self, on: bool = True):
         check(capi.lib().pk_job_enable_timing(self._h, int(on)), "pk_job_enable_timing")
 
+    def set_wait_limit(self, spins: int = 0, withhold_unit: int = -1):
+        """Polls before a bounded device wait gives up (0: the default, about 1-2 s), and a
+        macro-node work unit that publishes nothing (-1: none) -- a host-side fault
+        injection for testing the bounded waits (pk_job_set_wait_limit)."""
+        check(capi.lib().pk_job_set_wait_limit(self._h, int(spins), int(withhold_unit)),
+              "pk_job_set_wait_limit")
+
     def stage_times(self) -> Dict[str, float]:
         arr = (c_float * 16)()
         n = c_int()

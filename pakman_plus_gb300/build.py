@@ -24,7 +24,7 @@ HOST = os.path.join(HERE, "host")
 BIN = os.path.join(HERE, "bin")
 PKMER = os.path.join(BIN, "pkmer")
 SOURCES = ["pk_kernels.cu", "pk_capi.cu", "pk_noalloc.cu", "pk_server.cu", "pk_batch.cu", "pk_ingest.cu",
-           "pk_compact.cu"]
+           "pk_compact.cu", "pk_chunked.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -33,7 +33,7 @@ class PkParams(ctypes.Structure):
     _fields_ = [("k", c_int32), ("lmer_length", c_int32), ("num_buckets", c_int32),
                 ("coverage", c_int32), ("read_length", c_int32), ("drop_n", c_int32),
                 ("batch_kmers", c_uint64), ("bucket_bits", c_int32), ("mn_units", c_int32),
-                ("reserved", c_int32 * 6)]
+                ("chunking", c_int32), ("reserved", c_int32 * 5)]
 
 
 class PkSummary(ctypes.Structure):
@@ -130,6 +130,7 @@ _SIGS = {
     "pk_status_string": (c_char_p, [c_int]),
     "pk_last_error": (c_char_p, []),
     "pk_version": (c_char_p, []),
+    "pk_kernel_launches": (c_uint64, []),
     "pk_ctx_create": (c_int, [c_int, c_uint64, POINTER(c_void_p)]),
     "pk_ctx_destroy": (None, [c_void_p]),
     "pk_ctx_memory": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
@@ -144,6 +145,7 @@ _SIGS = {
     "pk_fasta_slice": (c_int, [c_char_p, c_int32, c_int32, c_int32, POINTER(c_uint64), POINTER(c_uint64)]),
     "pk_table_load": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64, POINTER(PkParams)]),
     "pk_table_info": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64)]),
+    "pk_count_pieces": (c_int, [c_void_p, POINTER(c_uint32)]),
     "pk_copy_table": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64]),
     "pk_copy_table_packed": (c_int, [c_void_p, c_void_p, c_uint64]),
     "pk_table_device": (c_int, [c_void_p, POINTER(c_void_p), POINTER(c_void_p)]),
@@ -166,6 +168,7 @@ _SIGS = {
     "pk_walk": (c_int, [c_void_p, POINTER(PkWalkInfo)]),
     "pk_copy_walk_contigs": (c_int, [c_void_p, c_void_p, c_void_p]),
     "pk_job_enable_timing": (c_int, [c_void_p, c_int]),
+    "pk_job_set_wait_limit": (c_int, [c_void_p, c_uint32, c_int32]),
     "pk_job_stage_times": (c_int, [c_void_p, POINTER(c_float), c_int, POINTER(c_int)]),
     "pk_stage_name": (c_char_p, [c_int]),
     "pk_cutoff_noalloc": (c_int, [c_void_p, c_uint64, c_int32, c_void_p, c_void_p, c_void_p,

@@ -74,17 +74,34 @@ static void job_free(pk_job* j, DevBuf& b) {
   b.bytes = 0;
 }
 
-void pk::job_free_all(pk_job* j) {
+int pk::job_buffers(pk_job* j, DevBuf** out, int cap) {
   DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->hstart, &j->keys,  &j->tkeys,
                    &j->tcounts, &j->tu,    &j->flags_m, &j->hist,  &j->hist2,
                    &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
                    &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
                    &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring,
                    &j->gfirst, &j->gcount, &j->chunk_bucket, &j->gdone,
-                   &j->chunk_u};
-  for (DevBuf* b : all) job_free(j, *b);
+                   &j->chunk_u, &j->acc_keys[0], &j->acc_keys[1], &j->acc_counts[0], &j->acc_counts[1],
+                   &j->merge_keys, &j->merge_counts, &j->merge_part};
+  const int n = (int)(sizeof(all) / sizeof(all[0]));
+  for (int i = 0; i < n && i < cap; i++) out[i] = all[i];
+  return n;
+}
+
+void pk::job_free_all(pk_job* j) {
+  DevBuf* all[64];
+  const int n = job_buffers(j, all, 64);
+  for (int i = 0; i < n; i++) job_free(j, *all[i]);
   cp_free(j);
   j->compacted = false;
+  j->dense_valid = false;
+}
+
+void pk::release_piece_buffers(pk_job* j) {
+  DevBuf* all[64];
+  const int n = job_buffers(j, all, 64);
+  for (int i = 0; i < n; i++)
+    if (all[i] != &j->tkeys && all[i] != &j->tcounts) job_free(j, *all[i]);
   j->dense_valid = false;
 }
 
@@ -251,16 +268,19 @@ pk_status pk_job_sync(pk_job* j) {
 
 pk_status pk_job_memory(pk_job* j, uint64_t* bytes) {
   if (!j || !bytes) return fail(PK_ERR_INVALID, "null argument");
-  DevBuf* all[] = {&j->fasta, &j->tile_nl, &j->counts, &j->bstart, &j->hstart, &j->keys,  &j->tkeys,
-                   &j->tcounts, &j->tu,    &j->flags_m, &j->hist,  &j->hist2,
-                   &j->nkeys,  &j->nsuf,   &j->npre,    &j->packed,  &j->doff,  &j->dkeys,
-                   &j->dcounts, &j->flags_f, &j->kkeys, &j->kcounts, &j->kstart, &j->kcount,
-                   &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring,
-                   &j->gfirst, &j->gcount, &j->chunk_bucket, &j->gdone,
-                   &j->chunk_u};
+  DevBuf* all[64];
+  const int n = job_buffers(j, all, 64);
   uint64_t s = 0;
-  for (DevBuf* b : all) s += b->bytes;
+  for (int i = 0; i < n; i++) s += all[i]->bytes;
   *bytes = s;
+  return PK_OK;
+}
+
+pk_status pk_job_set_wait_limit(pk_job* j, uint32_t spins, int32_t withhold_unit) {
+  if (!j) return fail(PK_ERR_INVALID, "job is null");
+  if (spins > (1u << 30)) return fail(PK_ERR_INVALID, "spins must be at most 2^30");
+  j->wait_limit = spins;
+  j->withhold_unit = withhold_unit < 0 ? -1 : withhold_unit;
   return PK_OK;
 }
 
@@ -301,6 +321,7 @@ pk_status pk::check_params(const pk_params* p) {
   if (p->lmer_length < 1 || p->lmer_length > 32) return fail(PK_ERR_INVALID, "lmer_length must be in 1..32");
   if (p->num_buckets < 1) return fail(PK_ERR_INVALID, "num_buckets (-t) must be >= 1");
   if (p->mn_units < 0 || p->mn_units > 16) return fail(PK_ERR_INVALID, "mn_units must be in 0..16");
+  if (p->chunking < 0 || p->chunking > 2) return fail(PK_ERR_INVALID, "chunking must be 0, 1 or 2");
   if (p->bucket_bits < 0 || p->bucket_bits > kMaxPartitionBits)
     return fail(PK_ERR_INVALID, "bucket_bits must be in 0.." + std::to_string(kMaxPartitionBits));
   return PK_OK;
@@ -320,6 +341,8 @@ int pk::auto_bucket_bits(uint64_t F, int k, int wide) {
   while (b < kMaxPartitionBits && est / (double)(1u << b) > per_bucket) b++;
   return std::max(2, std::min(b, 2 * k - 2));
 }
+
+static pk_status table_impl(pk_job* j, uint64_t N, int t);
 
 // Stages 1-5: device FASTA -> sorted (k-mer, count) table, resident.
 pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_params* p) {
@@ -443,6 +466,13 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
                                 &j->d_sc->ticket_fine, N, &j->d_sc->err, j->stream));
   }
   mark_end(j, ST_SCATTER_FINE);
+  return table_impl(j, N, t);
+}
+
+// Stage 5: bucketed keys -> (k-mer, count) table, resident.
+static pk_status table_impl(pk_job* j, uint64_t N, int t) {
+  const int k = j->params.k;
+  const int B = 1 << j->bbits;
   mark_begin(j, ST_TABLE);
   // giant buckets are reduced chunk by chunk first (chunk items ahead of the buckets)
   PK_TRY(job_alloc(j, j->gfirst, sizeof(uint32_t) * (size_t)B));
@@ -469,9 +499,11 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   b.k = k;
   b.bbits = j->bbits;
   b.cap = N;
+  b.spin_limit = (int)j->wait_limit;
   b.sc = j->d_sc;
   PK_CUDA(launch_bucket_table(b, j->wide, 0, j->stream));
   mark_end(j, ST_TABLE);
+  j->pieces = 1;
   j->stage = 1;
   return PK_OK;
 }
@@ -486,17 +518,33 @@ pk_status pk_count_device(pk_job* j, const void* d_fasta, uint64_t n, const pk_p
   return count_impl(j, d_fasta, n, p);
 }
 
+pk_status pk::count_host(pk_job* j, const char* fasta, uint64_t n, const pk_params* p) {
+  for (int i = 0; i < ST_COUNT_; i++) j->ev_rec[i] = false;
+  // -b pieces: always (chunking 1), or when the whole input at once does not fit the
+  // HBM budget or the 2^32-window limit (chunking 0)
+  if (p->chunking == 1) return count_pieces(j, fasta, n, p, p->batch_kmers);
+  pk_status s = job_alloc(j, j->fasta, (size_t)n + 16);
+  if (s == PK_OK) {
+    mark_begin(j, ST_H2D);
+    if (n) PK_CUDA(cudaMemcpyAsync(j->fasta.p, fasta, n, cudaMemcpyHostToDevice, j->stream));
+    mark_end(j, ST_H2D);
+    s = count_impl(j, j->fasta.p, n, p);
+  }
+  if ((s == PK_ERR_NOMEM || s == PK_ERR_LIMIT) && p->chunking == 0 && n > 1) {
+    PK_CUDA(cudaStreamSynchronize(j->stream));
+    job_free_all(j);
+    const uint64_t b = p->batch_kmers ? p->batch_kmers : 100000000ull;
+    return count_pieces(j, fasta, n, p, std::min<uint64_t>(b, (n + 1) / 2));
+  }
+  return s;
+}
+
 pk_status pk_count(pk_job* j, const char* fasta, uint64_t n, const pk_params* p) {
   if (!j) return fail(PK_ERR_INVALID, "job is null");
   PK_TRY(check_params(p));
   if (n && !fasta) return fail(PK_ERR_INVALID, "fasta is null");
   PK_TRY(set_device(j->ctx));
-  for (int i = 0; i < ST_COUNT_; i++) j->ev_rec[i] = false;
-  PK_TRY(job_alloc(j, j->fasta, (size_t)n + 16));
-  mark_begin(j, ST_H2D);
-  if (n) PK_CUDA(cudaMemcpyAsync(j->fasta.p, fasta, n, cudaMemcpyHostToDevice, j->stream));
-  mark_end(j, ST_H2D);
-  return count_impl(j, j->fasta.p, n, p);
+  return count_host(j, fasta, n, p);
 }
 
 // An existing (k-mer, count) table in place of counting: host rows ascending and
@@ -585,7 +633,7 @@ pk_status pk_table_info(pk_job* j, uint64_t* u, uint64_t* w, uint64_t* r) {
 }
 
 // Dense (contiguous, ascending) copy of the resident sparse table, built on demand.
-static pk_status materialize_dense(pk_job* j) {
+pk_status pk::dense_table(pk_job* j) {
   if (j->dense_valid) return PK_OK;
   const uint64_t u = j->h_sc->n_unique;
   const int B = 1 << j->bbits;
@@ -606,7 +654,7 @@ pk_status pk_copy_table(pk_job* j, void* keys, uint32_t* counts, uint64_t cap) {
   PK_TRY(pk_table_info(j, &u, nullptr, nullptr));
   if (cap < u) return fail(PK_ERR_INVALID, "capacity smaller than the table");
   const size_t W = j->wide ? 16 : 8;
-  PK_TRY(materialize_dense(j));
+  PK_TRY(dense_table(j));
   if (u && keys) PK_CUDA(cudaMemcpyAsync(keys, j->dkeys.p, W * u, cudaMemcpyDeviceToHost, j->stream));
   if (u && counts)
     PK_CUDA(cudaMemcpyAsync(counts, j->dcounts.p, 4 * u, cudaMemcpyDeviceToHost, j->stream));
@@ -638,7 +686,7 @@ pk_status pk_table_device(pk_job* j, const void** k, const uint32_t** c) {
   if (j->stage < 1) return fail(PK_ERR_STATE, "no table: call pk_count first");
   PK_TRY(set_device(j->ctx));
   PK_TRY(sync_scalars(j));
-  PK_TRY(materialize_dense(j));
+  PK_TRY(dense_table(j));
   PK_CUDA(cudaStreamSynchronize(j->stream));
   if (k) *k = j->dkeys.p;
   if (c) *c = (const uint32_t*)j->dcounts.p;
@@ -653,7 +701,7 @@ pk_status pk::cutoff_enqueue(pk_job* j, int t) {
     PK_TRY(sync_scalars(j));
     PK_TRY(job_alloc(j, j->hist2, sizeof(unsigned long long) * (size_t)t));
     PK_CUDA(cudaMemsetAsync(j->hist2.p, 0, sizeof(unsigned long long) * (size_t)t, j->stream));
-    PK_TRY(materialize_dense(j));
+    PK_TRY(dense_table(j));
     PK_CUDA(launch_histogram((const uint32_t*)j->dcounts.p, j->h_sc->n_unique, t,
                              (unsigned long long*)j->hist2.p, j->stream));
     hist = (const unsigned long long*)j->hist2.p;
@@ -721,6 +769,7 @@ pk_status pk::mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
   f.trows = j->tcounts.bytes / sizeof(uint32_t);
   f.k = j->params.k;
   f.bbits = j->bbits;
+  f.spin_limit = (int)j->wait_limit;
   f.sc = j->d_sc;
   mark_begin(j, ST_FILTER);
   PK_CUDA(launch_filter_kept(f, j->wide, 0, j->stream));
@@ -750,6 +799,8 @@ pk_status pk::mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
     if (2 * level > j->bbits) level = j->bbits / 2;
     m.level = level;
   }
+  m.spin_limit = (int)j->wait_limit;
+  m.withhold_unit = j->withhold_unit;
   m.sc = j->d_sc;
   mark_begin(j, ST_MN);
   PK_CUDA(launch_macro_nodes(m, j->wide, 0, j->stream));

@@ -1087,9 +1087,9 @@ pk_status scan4(pk_job* j, CpState& c, const uint4* in, uint4* out, uint64_t n) 
   const uint32_t tiles = (uint32_t)((n + kScanTile - 1) / kScanTile);
   PK_TRY(cp_alloc(j, c.part, sizeof(uint4) * (tiles + 1)));
   uint4* part = (uint4*)c.part.p;
-  if (tiles) k_scan_tiles<<<tiles, kScanT, 0, j->stream>>>(in, out, part, (uint32_t)n);
-  k_scan_parts<<<1, kScanT, 0, j->stream>>>(part, tiles, out, (uint32_t)n);
-  if (n) k_scan_add<<<(uint32_t)((n + 255) / 256), 256, 0, j->stream>>>(out, part, (uint32_t)n);
+  if (tiles) pk::note_launch(), k_scan_tiles<<<tiles, kScanT, 0, j->stream>>>(in, out, part, (uint32_t)n);
+  pk::note_launch(), k_scan_parts<<<1, kScanT, 0, j->stream>>>(part, tiles, out, (uint32_t)n);
+  if (n) pk::note_launch(), k_scan_add<<<(uint32_t)((n + 255) / 256), 256, 0, j->stream>>>(out, part, (uint32_t)n);
   PK_CUDA(cudaGetLastError());
   return PK_OK;
 }
@@ -1125,7 +1125,7 @@ pk_status cp_init(pk_job* j, CpState& c, int32_t cov) {
   const uint64_t m = j->h_sc->n_nodes;
   PK_TRY(cp_alloc(j, c.col, sizeof(uint4) * (m + 1)));
   PK_TRY(cp_alloc(j, c.off, sizeof(uint4) * (m + 1)));
-  if (m) k_cp_init_count<<<blocks(m, 256), 256, 0, j->stream>>>((const uint4*)j->nsuf.p, (const uint4*)j->npre.p,
+  if (m) pk::note_launch(), k_cp_init_count<<<blocks(m, 256), 256, 0, j->stream>>>((const uint4*)j->nsuf.p, (const uint4*)j->npre.p,
                                                                   (uint32_t)m, (uint4*)c.col.p);
   PK_TRY(scan4(j, c, (const uint4*)c.col.p, (uint4*)c.off.p, m));
   uint4 tot;
@@ -1141,7 +1141,7 @@ pk_status cp_init(pk_job* j, CpState& c, int32_t cov) {
   PK_CUDA(cudaMemsetAsync(c.arena.p, 0, 16, j->stream));
   PK_CUDA(cudaMemcpyAsync(c.arena.p, &w0, 8, cudaMemcpyHostToDevice, j->stream));
   c.arena_words = 1;
-  k_cp_init<KeyT><<<blocks(m + 1, 128), 128, 0, j->stream>>>((const KeyT*)j->nkeys.p, (const uint4*)j->nsuf.p,
+  pk::note_launch(), k_cp_init<KeyT><<<blocks(m + 1, 128), 128, 0, j->stream>>>((const KeyT*)j->nkeys.p, (const uint4*)j->nsuf.p,
                                                               (const uint4*)j->npre.p, (uint32_t)m, c.L, cov,
                                                               (const uint4*)c.off.p, side_of<KeyT>(c, 0), c.d_err);
   PK_CUDA(cudaGetLastError());
@@ -1157,7 +1157,7 @@ pk_status cp_round(pk_job* j, CpState& c) {
   PK_TRY(cp_alloc(j, c.col, sizeof(uint4) * (n + 1)));
   PK_TRY(cp_alloc(j, c.off, sizeof(uint4) * (n + 1)));
   PK_TRY(cp_alloc(j, c.is_id, n + 1));
-  k_cp_mark<KeyT><<<blocks(n, 256), 256, 0, j->stream>>>(a, (uint32_t)n, c.L, (uint4*)c.col.p, (uint8_t*)c.is_id.p);
+  pk::note_launch(), k_cp_mark<KeyT><<<blocks(n, 256), 256, 0, j->stream>>>(a, (uint32_t)n, c.L, (uint4*)c.col.p, (uint8_t*)c.is_id.p);
   PK_TRY(scan4(j, c, (const uint4*)c.col.p, (uint4*)c.off.p, n));
   uint4 tot;
   PK_TRY(read_total(j, c, (const uint4*)c.off.p + n, &tot));
@@ -1182,7 +1182,7 @@ pk_status cp_round(pk_job* j, CpState& c) {
   PK_TRY(alloc_side<KeyT>(j, c, nb, n2, c.E + T));
   PK_TRY(cp_alloc(j, c.old_of, 4 * (n2 + 1)));
   Side<KeyT> b = side_of<KeyT>(c, nb);
-  k_cp_emit<KeyT><<<blocks(n, 256), 256, 0, j->stream>>>(
+  pk::note_launch(), k_cp_emit<KeyT><<<blocks(n, 256), 256, 0, j->stream>>>(
       a, (uint32_t)n, c.L, (const uint4*)c.off.p, (const uint8_t*)c.is_id.p, (uint64_t*)c.arena.p, c.arena_words,
       c.arena_cap, (KeyT*)c.tkey.p, (Tr*)c.tr.p, (Ct*)c.ct.p, c.C, b.key, (uint32_t*)c.old_of.p, c.d_err);
   PK_CUDA(cudaGetLastError());
@@ -1194,19 +1194,19 @@ pk_status cp_round(pk_job* j, CpState& c) {
   PK_CUDA(cudaMemsetAsync(c.incnt.p, 0, sizeof(uint4) * (n2 + 1), j->stream));
   PK_CUDA(cudaMemsetAsync(c.fill.p, 0, 4 * (n2 + 1), j->stream));
   if (T)
-    k_cp_resolve<KeyT><<<blocks(T, 256), 256, 0, j->stream>>>((const KeyT*)c.tkey.p, (uint32_t)T, b.key,
+    pk::note_launch(), k_cp_resolve<KeyT><<<blocks(T, 256), 256, 0, j->stream>>>((const KeyT*)c.tkey.p, (uint32_t)T, b.key,
                                                                (uint32_t)n2, (uint32_t*)c.tgt.p, (uint4*)c.incnt.p,
                                                                c.d_err);
   PK_TRY(scan4(j, c, (const uint4*)c.incnt.p, (uint4*)c.inoff.p, n2));
   if (T)
-    k_cp_fill<<<blocks(T, 256), 256, 0, j->stream>>>((const uint32_t*)c.tgt.p, (uint32_t)T,
+    pk::note_launch(), k_cp_fill<<<blocks(T, 256), 256, 0, j->stream>>>((const uint32_t*)c.tgt.p, (uint32_t)T,
                                                      (const uint4*)c.inoff.p, (uint32_t*)c.fill.p,
                                                      (uint32_t*)c.inlist.p);
-  k_cp_apply<KeyT, 0><<<blocks(n2 + 1, 128), 128, 0, j->stream>>>(
+  pk::note_launch(), k_cp_apply<KeyT, 0><<<blocks(n2 + 1, 128), 128, 0, j->stream>>>(
       a, b, (uint32_t)n2, c.L, (const uint32_t*)c.old_of.p, (const uint4*)c.inoff.p, (uint32_t*)c.inlist.p,
       (const Tr*)c.tr.p, (const uint64_t*)c.arena.p, (uint4*)c.ecol.p, c.d_err);
   PK_TRY(scan4(j, c, (const uint4*)c.ecol.p, (uint4*)c.eoff2.p, n2));
-  k_cp_apply<KeyT, 1><<<blocks(n2 + 1, 128), 128, 0, j->stream>>>(
+  pk::note_launch(), k_cp_apply<KeyT, 1><<<blocks(n2 + 1, 128), 128, 0, j->stream>>>(
       a, b, (uint32_t)n2, c.L, (const uint32_t*)c.old_of.p, (const uint4*)c.inoff.p, (uint32_t*)c.inlist.p,
       (const Tr*)c.tr.p, (const uint64_t*)c.arena.p, (uint4*)c.eoff2.p, c.d_err);
   PK_CUDA(cudaGetLastError());
@@ -1228,11 +1228,11 @@ pk_status cp_finish(pk_job* j, CpState& c) {
   PK_TRY(cp_alloc(j, c.epos, sizeof(uint4) * (c.E + 1)));
   PK_TRY(cp_alloc(j, c.cpos, sizeof(uint4) * (c.C + 1)));
   Side<KeyT> a = side_of<KeyT>(c, c.cur);
-  if (c.E) k_cp_lengths<<<blocks(c.E, 256), 256, 0, j->stream>>>(a.xlen, (uint32_t)c.E, (uint4*)c.col.p);
+  if (c.E) pk::note_launch(), k_cp_lengths<<<blocks(c.E, 256), 256, 0, j->stream>>>(a.xlen, (uint32_t)c.E, (uint4*)c.col.p);
   PK_TRY(scan4(j, c, (const uint4*)c.col.p, (uint4*)c.epos.p, c.E));
   uint4 t1, t2;
   PK_TRY(read_total(j, c, (const uint4*)c.epos.p + c.E, &t1));
-  if (c.C) k_cp_ct_lengths<<<blocks(c.C, 256), 256, 0, j->stream>>>((const Ct*)c.ct.p, (uint32_t)c.C, (uint4*)c.col.p);
+  if (c.C) pk::note_launch(), k_cp_ct_lengths<<<blocks(c.C, 256), 256, 0, j->stream>>>((const Ct*)c.ct.p, (uint32_t)c.C, (uint4*)c.col.p);
   PK_TRY(scan4(j, c, (const uint4*)c.col.p, (uint4*)c.cpos.p, c.C));
   PK_TRY(read_total(j, c, (const uint4*)c.cpos.p + c.C, &t2));
   PK_TRY(check_err(c));
@@ -1249,7 +1249,7 @@ pk_status cp_walk(pk_job* j, CpState& c) {
   cudaStream_t st = j->stream;
   PK_TRY(cp_alloc(j, c.col, sizeof(uint4) * (n + 1)));
   PK_TRY(cp_alloc(j, c.off, sizeof(uint4) * (n + 1)));
-  if (n) k_wk_begin_count<<<blocks(n, 256), 256, 0, st>>>(a.eoff, a.npre, a.xlen, a.vis, (uint32_t)n, (uint4*)c.col.p);
+  if (n) pk::note_launch(), k_wk_begin_count<<<blocks(n, 256), 256, 0, st>>>(a.eoff, a.npre, a.xlen, a.vis, (uint32_t)n, (uint4*)c.col.p);
   PK_TRY(scan4(j, c, (const uint4*)c.col.p, (uint4*)c.off.p, n));
   uint4 t;
   PK_TRY(read_total(j, c, (const uint4*)c.off.p + n, &t));
@@ -1257,9 +1257,9 @@ pk_status cp_walk(pk_job* j, CpState& c) {
   PK_TRY(cp_alloc(j, c.wk_begins, sizeof(uint2) * (B + 1)));
   PK_TRY(cp_alloc(j, c.wk_links, sizeof(uint2) * (c.E + 1)));
   if (n) {
-    k_wk_begins<<<blocks(n, 256), 256, 0, st>>>(a.eoff, a.npre, a.xlen, a.vis, (uint32_t)n, (const uint4*)c.off.p,
+    pk::note_launch(), k_wk_begins<<<blocks(n, 256), 256, 0, st>>>(a.eoff, a.npre, a.xlen, a.vis, (uint32_t)n, (const uint4*)c.off.p,
                                                 (uint2*)c.wk_begins.p);
-    k_wk_links<KeyT><<<blocks(n, 256), 256, 0, st>>>(a, (uint32_t)n, c.L, (const uint64_t*)c.arena.p,
+    pk::note_launch(), k_wk_links<KeyT><<<blocks(n, 256), 256, 0, st>>>(a, (uint32_t)n, c.L, (const uint64_t*)c.arena.p,
                                                      (uint2*)c.wk_links.p);
   }
   // frames per walk: 2^26 over all walks, at least 256 and at most 2^20 each
@@ -1268,7 +1268,7 @@ pk_status cp_walk(pk_job* j, CpState& c) {
   PK_TRY(cp_alloc(j, c.wk_col, sizeof(uint4) * (B + 1)));
   PK_TRY(cp_alloc(j, c.wk_pos, sizeof(uint4) * (B + 1)));
   if (B)
-    k_walk<KeyT, 0><<<blocks(B * 32, 128), 128, 0, st>>>(a, c.L, (const uint2*)c.wk_begins.p, (uint32_t)B,
+    pk::note_launch(), k_walk<KeyT, 0><<<blocks(B * 32, 128), 128, 0, st>>>(a, c.L, (const uint2*)c.wk_begins.p, (uint32_t)B,
                                                    (const uint2*)c.wk_links.p, (WFrame*)c.wk_stack.p, (uint32_t)cap,
                                                    (uint4*)c.wk_col.p, nullptr, nullptr, nullptr, nullptr, c.d_err);
   PK_TRY(scan4(j, c, (const uint4*)c.wk_col.p, (uint4*)c.wk_pos.p, B));
@@ -1279,12 +1279,12 @@ pk_status cp_walk(pk_job* j, CpState& c) {
   PK_TRY(cp_alloc(j, c.wk_out, NB + 1));
   PK_TRY(cp_alloc(j, c.wk_pieces, sizeof(WPiece) * (NP + 1)));
   if (B)
-    k_walk<KeyT, 1><<<blocks(B * 32, 128), 128, 0, st>>>(a, c.L, (const uint2*)c.wk_begins.p, (uint32_t)B,
+    pk::note_launch(), k_walk<KeyT, 1><<<blocks(B * 32, 128), 128, 0, st>>>(a, c.L, (const uint2*)c.wk_begins.p, (uint32_t)B,
                                                    (const uint2*)c.wk_links.p, (WFrame*)c.wk_stack.p, (uint32_t)cap,
                                                    nullptr, (const uint4*)c.wk_pos.p, (uint64_t*)c.wk_off.p,
                                                    (WPiece*)c.wk_pieces.p, (uint8_t*)c.wk_out.p, c.d_err);
   if (NP)
-    k_wk_expand<<<blocks(NP * 32, 256), 256, 0, st>>>((const WPiece*)c.wk_pieces.p, (uint32_t)NP,
+    pk::note_launch(), k_wk_expand<<<blocks(NP * 32, 256), 256, 0, st>>>((const WPiece*)c.wk_pieces.p, (uint32_t)NP,
                                                        (const uint64_t*)c.arena.p, (uint8_t*)c.wk_out.p);
   PK_CUDA(cudaMemcpyAsync((uint64_t*)c.wk_off.p + NC, &NB, 8, cudaMemcpyHostToDevice, st));
   PK_CUDA(cudaGetLastError());
@@ -1358,7 +1358,15 @@ extern "C" pk_status pk_compact(pk_job* j, uint64_t threshold, int32_t coverage,
   PK_CUDA(cudaHostAlloc(&c.h_tot, 2 * sizeof(uint4), cudaHostAllocDefault));
   mark_begin(j, ST_COMPACT);
   pk_status s = c.wide ? cp_init<u128>(j, c, cov) : cp_init<uint64_t>(j, c, cov);
-  while (s == PK_OK && c.n > threshold) s = c.wide ? cp_round<u128>(j, c) : cp_round<uint64_t>(j, c);
+  while (s == PK_OK && c.n > threshold) {
+    const uint64_t before = c.n;
+    s = c.wide ? cp_round<u128>(j, c) : cp_round<uint64_t>(j, c);
+    // the node with the largest key is always in the ID set, so every round shrinks
+    // the map; a round that does not is a fault, not a reason to loop on
+    if (s == PK_OK && c.n >= before)
+      s = set_error(PK_ERR_DEVICE, "a compaction round merged no node (" + std::to_string(before) +
+                                       " nodes before and after)");
+  }
   if (s == PK_OK) s = c.wide ? cp_finish<u128>(j, c) : cp_finish<uint64_t>(j, c);
   mark_end(j, ST_COMPACT);
   if (s != PK_OK) {
@@ -1396,7 +1404,7 @@ extern "C" pk_status pk_copy_compacted(pk_job* j, void* keys, uint64_t* entry_of
   }
   if (entries && E) {
     PK_TRY(cp_alloc(j, c.ubuf, sizeof(pk_compact_entry) * E));
-    k_cp_entries<<<blocks(E, 256), 256, 0, st>>>((const uint32_t*)d[CpState::XLEN].p,
+    pk::note_launch(), k_cp_entries<<<blocks(E, 256), 256, 0, st>>>((const uint32_t*)d[CpState::XLEN].p,
                                                   (const int32_t*)d[CpState::CNT].p, (const int32_t*)d[CpState::VIS].p,
                                                   (const int2*)d[CpState::BEG].p, (const uint4*)c.epos.p, (uint32_t)E,
                                                   (pk_compact_entry*)c.ubuf.p);
@@ -1405,7 +1413,7 @@ extern "C" pk_status pk_copy_compacted(pk_job* j, void* keys, uint64_t* entry_of
   }
   if (ext_bases && c.ext_bases) {
     PK_TRY(cp_alloc(j, c.ubuf, c.ext_bases));
-    k_cp_unpack<<<blocks(E * 32, 256), 256, 0, st>>>((const uint64_t*)c.arena.p, (const uint64_t*)d[CpState::XOFF].p,
+    pk::note_launch(), k_cp_unpack<<<blocks(E * 32, 256), 256, 0, st>>>((const uint64_t*)c.arena.p, (const uint64_t*)d[CpState::XOFF].p,
                                                       (const uint32_t*)d[CpState::XLEN].p, nullptr,
                                                       (const uint4*)c.epos.p, (uint32_t)E, (uint8_t*)c.ubuf.p);
     PK_CUDA(cudaMemcpyAsync(ext_bases, c.ubuf.p, c.ext_bases, cudaMemcpyDeviceToHost, st));
@@ -1431,7 +1439,7 @@ extern "C" pk_status pk_copy_partial_contigs(pk_job* j, uint64_t* offsets, uint8
   }
   if (bases && c.ct_bases) {
     PK_TRY(cp_alloc(j, c.ubuf, c.ct_bases));
-    k_cp_unpack<<<blocks(c.C * 32, 256), 256, 0, st>>>((const uint64_t*)c.arena.p, nullptr, nullptr,
+    pk::note_launch(), k_cp_unpack<<<blocks(c.C * 32, 256), 256, 0, st>>>((const uint64_t*)c.arena.p, nullptr, nullptr,
                                                         (const Ct*)c.ct.p, (const uint4*)c.cpos.p, (uint32_t)c.C,
                                                         (uint8_t*)c.ubuf.p);
     PK_CUDA(cudaMemcpyAsync(bases, c.ubuf.p, c.ct_bases, cudaMemcpyDeviceToHost, st));

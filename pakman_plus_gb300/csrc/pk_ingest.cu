@@ -106,6 +106,8 @@ pk_status check_rank(int32_t rank, int32_t n_ranks) {
   return PK_OK;
 }
 
+pk_status stream_and_count(pk_job* j, Fd& f, const char* path, uint64_t off, uint64_t len, const pk_params* p);
+
 }  // namespace
 
 extern "C" pk_status pk_fasta_slice(const char* path, int32_t rank, int32_t n_ranks, int32_t read_length,
@@ -131,6 +133,29 @@ extern "C" pk_status pk_count_file(pk_job* j, const char* path, int32_t rank, in
   PK_TRY(slice_of(f.fd, size, rank, n_ranks, &off, &len));
   PK_TRY(set_device(j->ctx));
   for (int i = 0; i < ST_COUNT_; i++) j->ev_rec[i] = false;
+  // -b pieces (always, or when the slice does not fit at once): the slice is read into
+  // host memory and counted piece by piece
+  auto in_pieces = [&]() -> pk_status {
+    std::vector<char> host(len ? len : 1);
+    if (len && !read_at(f.fd, host.data(), len, off))
+      return set_error(PK_ERR_IO, std::string("reading the input FASTA file failed: ") + path);
+    const uint64_t b = p->batch_kmers ? p->batch_kmers : 100000000ull;
+    return count_pieces(j, host.data(), len, p, p->chunking == 1 ? b : std::min<uint64_t>(b, (len + 1) / 2));
+  };
+  if (p->chunking == 1) return in_pieces();
+  const pk_status whole = stream_and_count(j, f, path, off, len, p);
+  if ((whole == PK_ERR_NOMEM || whole == PK_ERR_LIMIT) && p->chunking == 0 && len > 1) {
+    PK_CUDA(cudaStreamSynchronize(j->stream));
+    job_free_all(j);
+    return in_pieces();
+  }
+  return whole;
+}
+
+namespace {
+
+// The whole slice streamed to the device and counted at once.
+pk_status stream_and_count(pk_job* j, Fd& f, const char* path, uint64_t off, uint64_t len, const pk_params* p) {
   PK_TRY(job_alloc(j, j->fasta, (size_t)len + 16));
   const uint64_t ntiles = (len + kTileBytes - 1) / kTileBytes;
   PK_TRY(job_alloc(j, j->tile_nl, sizeof(uint32_t) * (ntiles + 1)));
@@ -196,3 +221,5 @@ extern "C" pk_status pk_count_file(pk_job* j, const char* path, int32_t rank, in
   j->lines_ready = false;
   return s;
 }
+
+}  // namespace

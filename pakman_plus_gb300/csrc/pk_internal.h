@@ -13,6 +13,10 @@ namespace pk {
 // Records the calling thread's last-error text (pk_last_error) and returns s.
 pk_status set_error(pk_status s, const std::string& msg);
 
+// Counts one kernel launch made by this library (read by pk_kernel_launches); every
+// launch site calls it as `note_launch(), kernel<<<...>>>(...)`.
+void note_launch();
+
 // Device error word bits (pk_job error flag).
 enum : uint32_t {
   ERR_FORMAT = 1u,        // a record start is not '>' (reference asserts)
@@ -98,6 +102,7 @@ struct BucketArgs {
   const uint32_t* chunk_bucket;  // per chunk item: its bucket
   uint32_t* gdone;           // 2^bbits: chunk items of the bucket finished
   uint32_t* chunk_u;         // per chunk item: pairs it left, or kChunkRaw
+  int spin_limit;            // polls of a bounded wait before it gives up (0: default)
   Scalars* sc;
 };
 
@@ -117,6 +122,7 @@ struct FilterArgs {
   unsigned long long trows;  // rows the table count buffer holds (reads stay below)
   int k;
   int bbits;
+  int spin_limit;            // polls of a bounded wait before it gives up (0: default)
   Scalars* sc;
 };
 
@@ -135,6 +141,9 @@ struct MnArgs {
   int k;
   int bbits;
   int level;                 // node units cover 4^level table buckets (0: one bucket, split)
+  int spin_limit;            // polls of a bounded wait before it gives up (0: default)
+  int withhold_unit;         // a unit that publishes no look-back word (-1: none; tests of
+                             // the bounded waits)
   Scalars* sc;
 };
 

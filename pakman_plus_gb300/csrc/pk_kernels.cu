@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "pk_internal.h"
 
 namespace pk {
@@ -114,7 +116,8 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
 constexpr unsigned long long kLbAgg = 1ull << 62;
 constexpr unsigned long long kLbIncl = 2ull << 62;
 constexpr unsigned long long kLbVal = (1ull << 62) - 1;
-constexpr int kLbSpinLimit = 1 << 24;  // ~1-2 s with the back-off below
+constexpr int kLbSpinLimit = 1 << 24;  // ~1-2 s with the back-off below (the default)
+__device__ __forceinline__ int spin_limit(int limit) { return limit > 0 ? limit : kLbSpinLimit; }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
 #pragma unroll
@@ -128,7 +131,9 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 // aggregates up to the first word still unpublished and moves past them.  Waiting on
 // an unpublished word is bounded: on expiry the error bit is set and the partial sum
 // is returned.
-__device__ unsigned long long lookback_exclusive(unsigned long long* flags, int idx, uint32_t* err) {
+__device__ unsigned long long lookback_exclusive(unsigned long long* flags, int idx, uint32_t* err,
+                                                int limit) {
+  const int max_spins = spin_limit(limit);
   const int lane = threadIdx.x & 31;
   unsigned long long sum = 0;
   int top = idx - 1;  // nearest predecessor not yet added
@@ -151,7 +156,7 @@ __device__ unsigned long long lookback_exclusive(unsigned long long* flags, int 
       spins = 0;
       continue;
     }
-    if (++spins >= kLbSpinLimit) {
+    if (++spins >= max_spins) {
       if (lane == 0) atomicOr(err, ERR_LOOKBACK);
       return sum;
     }
@@ -433,6 +438,13 @@ __device__ __forceinline__ uint32_t window_bucket_hi(const Roll& s, int sh, int 
   return ((xh | (nh << 2)) >> shift_hi) & hmask;
 }
 
+template <typename KeyT>
+__device__ __forceinline__ void guarded_store(KeyT* __restrict__ out, uint32_t idx, KeyT v,
+                                              unsigned long long cap, uint32_t* err) {
+  if (idx < cap) out[idx] = v;
+  else atomicOr(err, ERR_BOUNDS);
+}
+
 // Counting-pass threads: 1024 for 64-bit keys (more warps hide the decode's latency),
 // 512 for 128-bit keys (whose windows need twice the registers)
 template <typename KeyT>
@@ -591,13 +603,6 @@ struct CoarseCfg {
                                                             // (T * BP keys between flushes)
   static constexpr size_t smem = sizeof(KeyT) * C * R;
 };
-
-template <typename KeyT>
-__device__ __forceinline__ void guarded_store(KeyT* __restrict__ out, uint32_t idx, KeyT v,
-                                              unsigned long long cap, uint32_t* err) {
-  if (idx < cap) out[idx] = v;
-  else atomicOr(err, ERR_BOUNDS);
-}
 
 template <typename KeyT>
 __device__ __forceinline__ void coarse_flush(KeyT* ring, uint32_t* w, uint32_t* f, const uint32_t* g,
@@ -1285,8 +1290,9 @@ __device__ __forceinline__ uint32_t giant_entries(const BucketArgs& a, uint32_t 
   const int tid = threadIdx.x;
   if (tid == 0) {
     int spins = 0;
+    const int max_spins = spin_limit(a.spin_limit);
     while (ld_acquire_u32(&a.gdone[beta]) < nch) {
-      if (++spins >= kLbSpinLimit) {
+      if (++spins >= max_spins) {
         atomicOr(&a.sc->err, ERR_LOOKBACK);
         *s_fail = 1;
         break;
@@ -1917,7 +1923,7 @@ __global__ void __launch_bounds__(256) k_filter_kept(FilterArgs a) {
     v = __reduce_add_sync(FULLMASK, v);
     if (lane == 0) st_release(&a.flags[beta], kLbAgg | (unsigned long long)v);
     __syncwarp();
-    unsigned long long K = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
+    unsigned long long K = lookback_exclusive(a.flags, (int)beta, &a.sc->err, a.spin_limit);
     if (lane == 0) {
       st_release(&a.flags[beta], kLbIncl | (K + v));
       if (beta == (uint32_t)B - 1) a.sc->n_kept_rows = K + v;
@@ -2161,11 +2167,14 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
           if (first) {
             if (tid < 32) {  // warp 0 looks back
               const unsigned long long mine = pass == 0 ? nodes : total;
-              if (tid == 0) st_release(&a.flags[beta], kLbAgg | mine);
+              // a withheld unit (bounded-wait tests) publishes nothing: its successors'
+              // waits run out and report ERR_LOOKBACK
+              const bool publish = (int)beta != a.withhold_unit;
+              if (tid == 0 && publish) st_release(&a.flags[beta], kLbAgg | mine);
               __syncwarp();
-              const unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err);
+              const unsigned long long ex = lookback_exclusive(a.flags, (int)beta, &a.sc->err, a.spin_limit);
               if (tid == 0) {
-                st_release(&a.flags[beta], kLbIncl | (ex + mine));
+                if (publish) st_release(&a.flags[beta], kLbIncl | (ex + mine));
                 s_NO = ex;
               }
             }
@@ -2242,6 +2251,9 @@ __global__ void __launch_bounds__(256) k_table_sizes(const uint32_t* bstart, int
 }
 
 // =================================================================== launchers =====
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 static int g_sms = 0;
 static int sm_count() {
   if (!g_sms) {
@@ -2262,13 +2274,13 @@ int mn_ctas_per_sm(int wide) { return wide ? 5 : 8; }
 
 cudaError_t launch_line_tiles(const uint8_t* buf, unsigned long long F, uint32_t* tile_nl, Scalars* sc,
                               unsigned long long tile0, unsigned long long ntiles, cudaStream_t st) {
-  if (ntiles > 0) k_line_scan<<<(unsigned)ntiles, 256, 0, st>>>(buf, F, tile_nl, sc, tile0);
+  if (ntiles > 0) pk::note_launch(), k_line_scan<<<(unsigned)ntiles, 256, 0, st>>>(buf, F, tile_nl, sc, tile0);
   return cudaGetLastError();
 }
 
 cudaError_t launch_tile_prefix(const CountArgs& a, cudaStream_t st) {
   const int ntiles = (int)((a.F + kTileBytes - 1) / kTileBytes);
-  k_tile_prefix<<<1, 1024, 0, st>>>(a.fasta, a.F, a.tile_nl, ntiles, a.sc);
+  pk::note_launch(), k_tile_prefix<<<1, 1024, 0, st>>>(a.fasta, a.F, a.tile_nl, ntiles, a.sc);
   return cudaGetLastError();
 }
 
@@ -2286,12 +2298,13 @@ static cudaError_t launch_extract_t(const CountArgs& a, cudaStream_t st) {
   // set to the largest histogram (15 partition digits), never to this launch's size
   static bool attr_set = false;  // same value from every thread, so a race is benign
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_extract<KeyT, FASTB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(sizeof(uint32_t) << 15));
+    cudaError_t e = cudaFuncSetAttribute(k_extract<KeyT, FASTB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(uint32_t) << kHistBits));
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  k_extract<KeyT, FASTB><<<a.grid, CountCfg<KeyT>::T, smem, st>>>(a);
+  pk::note_launch(), k_extract<KeyT, FASTB><<<a.grid, CountCfg<KeyT>::T, smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -2311,7 +2324,7 @@ static cudaError_t launch_coarse_t(const CountArgs& a, const uint32_t* coff, Key
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  k_scatter_coarse<KeyT><<<a.grid, CoarseCfg<KeyT>::T, smem, st>>>(a, coff, out);
+  pk::note_launch(), k_scatter_coarse<KeyT><<<a.grid, CoarseCfg<KeyT>::T, smem, st>>>(a, coff, out);
   return cudaGetLastError();
 }
 
@@ -2324,7 +2337,7 @@ cudaError_t launch_scatter_coarse(const CountArgs& a, const uint32_t* coff, void
 cudaError_t launch_coarse_offsets(const CountArgs& a, uint32_t* coff, uint32_t* cstart,
                                   uint32_t* slice_start, int slice_keys, cudaStream_t st) {
   const int sk = slice_keys;
-  k_coarse_offsets<<<a.grid, 256, 0, st>>>(a.counts, a.bstart, a.grid, a.bbits, a.cbits, coff, cstart,
+  pk::note_launch(), k_coarse_offsets<<<a.grid, 256, 0, st>>>(a.counts, a.bstart, a.grid, a.bbits, a.cbits, coff, cstart,
                                            slice_start, sk);
   return cudaGetLastError();
 }
@@ -2349,11 +2362,11 @@ static cudaError_t launch_fine_t(const KeyT* in, const uint32_t* cstart, const u
       if (e != cudaSuccess) return e;
       big_attr_set = true;
     }
-    k_scatter_fine_big<KeyT><<<sm_count(), FineBigCfg<KeyT>::T, bsmem, st>>>(in, cstart, slice_start, fcur, out, k,
+    pk::note_launch(), k_scatter_fine_big<KeyT><<<sm_count(), FineBigCfg<KeyT>::T, bsmem, st>>>(in, cstart, slice_start, fcur, out, k,
                                                                              bbits, cbits, ticket, cap, err);
     return cudaGetLastError();
   }
-  k_scatter_fine<KeyT><<<sm_count() * 2, FineCfg<KeyT>::T, smem, st>>>(in, cstart, slice_start, fcur, out,
+  pk::note_launch(), k_scatter_fine<KeyT><<<sm_count() * 2, FineCfg<KeyT>::T, smem, st>>>(in, cstart, slice_start, fcur, out,
                                                                         k, bbits, cbits, ticket, cap, err);
   return cudaGetLastError();
 }
@@ -2373,23 +2386,23 @@ cudaError_t launch_fine_count(const void* in, const uint32_t* cstart, const uint
                               cudaStream_t st) {
   const uint32_t sk = (uint32_t)fine_slice_keys(wide, bbits - cbits);
   if (wide)
-    k_fine_count<u128><<<sm_count() * 2, 512, 0, st>>>(reinterpret_cast<const u128*>(in), cstart, slice_start,
+    pk::note_launch(), k_fine_count<u128><<<sm_count() * 2, 512, 0, st>>>(reinterpret_cast<const u128*>(in), cstart, slice_start,
                                                       bcount, k, bbits, cbits, ticket, sk);
   else
-    k_fine_count<uint64_t><<<sm_count() * 2, 512, 0, st>>>(reinterpret_cast<const uint64_t*>(in), cstart,
+    pk::note_launch(), k_fine_count<uint64_t><<<sm_count() * 2, 512, 0, st>>>(reinterpret_cast<const uint64_t*>(in), cstart,
                                                           slice_start, bcount, k, bbits, cbits, ticket, sk);
   return cudaGetLastError();
 }
 
 cudaError_t launch_prefix(uint32_t* counts, int B, cudaStream_t st) {
-  k_bucket_prefix<<<1, 1024, 0, st>>>(counts, B);
+  pk::note_launch(), k_bucket_prefix<<<1, 1024, 0, st>>>(counts, B);
   return cudaGetLastError();
 }
 
 cudaError_t launch_bucket_offsets(const CountArgs& a, cudaStream_t st) {
   const int B = 1 << a.bbits;
-  k_col_prefix<<<(B + 31) / 32, 256, 0, st>>>(a.counts, a.grid, B, a.bstart);
-  k_bucket_prefix<<<1, 1024, 0, st>>>(a.bstart, B);
+  pk::note_launch(), k_col_prefix<<<(B + 31) / 32, 256, 0, st>>>(a.counts, a.grid, B, a.bstart);
+  pk::note_launch(), k_bucket_prefix<<<1, 1024, 0, st>>>(a.bstart, B);
   return cudaGetLastError();
 }
 
@@ -2408,8 +2421,8 @@ static cudaError_t launch_bucket_t(const BucketArgs& a, int grid, cudaStream_t s
   }
   if (grid <= 0) grid = sm_count() * bucket_ctas_per_sm(sizeof(KeyT) == 16);
   // exactly one of the two works (giant buckets present or not); the other returns
-  k_bucket_table<KeyT, false><<<grid, kBucketThreads, smem, st>>>(a);
-  k_bucket_table<KeyT, true><<<grid, kBucketThreads, smem, st>>>(a);
+  pk::note_launch(), k_bucket_table<KeyT, false><<<grid, kBucketThreads, smem, st>>>(a);
+  pk::note_launch(), k_bucket_table<KeyT, true><<<grid, kBucketThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -2420,7 +2433,7 @@ cudaError_t launch_bucket_table(const BucketArgs& a, int wide, int grid, cudaStr
 cudaError_t launch_giant_chunks(const uint32_t* bstart, int bbits, uint32_t* gfirst, uint32_t* gcount,
                                 uint32_t* chunk_bucket, uint32_t* gdone, Scalars* sc, cudaStream_t st) {
   const int B = 1 << bbits;
-  k_giant_chunks<<<(B + 255) / 256, 256, 0, st>>>(bstart, B, gfirst, gcount, chunk_bucket, gdone, sc);
+  pk::note_launch(), k_giant_chunks<<<(B + 255) / 256, 256, 0, st>>>(bstart, B, gfirst, gcount, chunk_bucket, gdone, sc);
   return cudaGetLastError();
 }
 
@@ -2429,19 +2442,19 @@ cudaError_t launch_histogram(const uint32_t* tcounts, unsigned long long u, int 
   int grid = (int)((u + 255) / 256);
   if (grid > sm_count() * 8) grid = sm_count() * 8;
   if (grid < 1) grid = 1;
-  k_histogram<<<grid, 256, 0, st>>>(tcounts, u, t, hist);
+  pk::note_launch(), k_histogram<<<grid, 256, 0, st>>>(tcounts, u, t, hist);
   return cudaGetLastError();
 }
 
 cudaError_t launch_cutoff(const unsigned long long* hist, int t, Scalars* sc, cudaStream_t st) {
-  k_cutoff<<<1, 1024, 0, st>>>(hist, t, sc);
+  pk::note_launch(), k_cutoff<<<1, 1024, 0, st>>>(hist, t, sc);
   return cudaGetLastError();
 }
 
 template <typename KeyT>
 static cudaError_t launch_filter_t(const FilterArgs& a, int grid, cudaStream_t st) {
   if (grid <= 0) grid = sm_count() * 8;
-  k_filter_kept<KeyT><<<grid, 256, 0, st>>>(a);
+  pk::note_launch(), k_filter_kept<KeyT><<<grid, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -2459,7 +2472,7 @@ static cudaError_t launch_mn_t(const MnArgs& a, int grid, cudaStream_t st) {
     attr_set = true;
   }
   if (grid <= 0) grid = sm_count() * mn_ctas_per_sm(sizeof(KeyT) == 16);
-  k_macro_nodes<KeyT><<<grid, kMnThreads, smem, st>>>(a);
+  pk::note_launch(), k_macro_nodes<KeyT><<<grid, kMnThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -2483,7 +2496,7 @@ __global__ void __launch_bounds__(1024) k_copy_prefix(const uint32_t* __restrict
 }
 
 cudaError_t launch_row_offsets(const uint32_t* tu, uint32_t* doff, int B, cudaStream_t st) {
-  k_copy_prefix<<<1, 1024, 0, st>>>(tu, doff, B);
+  pk::note_launch(), k_copy_prefix<<<1, 1024, 0, st>>>(tu, doff, B);
   return cudaGetLastError();
 }
 
@@ -2494,11 +2507,11 @@ cudaError_t launch_compact_rows(const void* tkeys, const uint32_t* tcounts, cons
   if (grid < 1) grid = 1;
   const int mode = packed ? 1 : 0;
   if (wide)
-    k_compact_rows<u128><<<grid, 256, 0, st>>>(reinterpret_cast<const u128*>(tkeys), tcounts, bstart,
+    pk::note_launch(), k_compact_rows<u128><<<grid, 256, 0, st>>>(reinterpret_cast<const u128*>(tkeys), tcounts, bstart,
                                                tu, doff, B, reinterpret_cast<u128*>(dkeys), dcounts,
                                                reinterpret_cast<uint32_t*>(packed), mode);
   else
-    k_compact_rows<uint64_t><<<grid, 256, 0, st>>>(reinterpret_cast<const uint64_t*>(tkeys), tcounts,
+    pk::note_launch(), k_compact_rows<uint64_t><<<grid, 256, 0, st>>>(reinterpret_cast<const uint64_t*>(tkeys), tcounts,
                                                    bstart, tu, doff, B,
                                                    reinterpret_cast<uint64_t*>(dkeys), dcounts,
                                                    reinterpret_cast<uint32_t*>(packed), mode);
@@ -2514,11 +2527,11 @@ cudaError_t launch_table_bounds(const void* keys, unsigned long long n, int bbit
   const int rem = 2 * k - bbits;
   const int grid = (B + 1 + 255) / 256;
   if (wide) {
-    k_table_bounds<u128><<<grid, 256, 0, st>>>((const u128*)keys, n, bbits, rem, bstart);
-    k_table_sizes<<<(B + 255) / 256, 256, 0, st>>>(bstart, B, tu);
+    pk::note_launch(), k_table_bounds<u128><<<grid, 256, 0, st>>>((const u128*)keys, n, bbits, rem, bstart);
+    pk::note_launch(), k_table_sizes<<<(B + 255) / 256, 256, 0, st>>>(bstart, B, tu);
   } else {
-    k_table_bounds<uint64_t><<<grid, 256, 0, st>>>((const uint64_t*)keys, n, bbits, rem, bstart);
-    k_table_sizes<<<(B + 255) / 256, 256, 0, st>>>(bstart, B, tu);
+    pk::note_launch(), k_table_bounds<uint64_t><<<grid, 256, 0, st>>>((const uint64_t*)keys, n, bbits, rem, bstart);
+    pk::note_launch(), k_table_sizes<<<(B + 255) / 256, 256, 0, st>>>(bstart, B, tu);
   }
   return cudaGetLastError();
 }
@@ -2568,8 +2581,8 @@ __global__ void __launch_bounds__(256) k_batch_copy(const unsigned long long* __
 cudaError_t launch_batch_emit(const Scalars* sc, unsigned long long* counter, unsigned long long cap,
                               unsigned long long* res, const void* nkeys, const void* nsuf, const void* npre,
                               int wide, void* okeys, void* osuf, void* opre, cudaStream_t st) {
-  k_batch_reserve<<<1, 32, 0, st>>>(sc, counter, cap, res);
-  k_batch_copy<<<sm_count() * 2, 256, 0, st>>>((const unsigned long long*)nkeys, (const uint4*)nsuf,
+  pk::note_launch(), k_batch_reserve<<<1, 32, 0, st>>>(sc, counter, cap, res);
+  pk::note_launch(), k_batch_copy<<<sm_count() * 2, 256, 0, st>>>((const unsigned long long*)nkeys, (const uint4*)nsuf,
                                                (const uint4*)npre, wide ? 2 : 1, res,
                                                (unsigned long long*)okeys, (uint4*)osuf, (uint4*)opre);
   return cudaGetLastError();
@@ -2683,8 +2696,10 @@ __global__ void __launch_bounds__(256) k_wire(const uint4* __restrict__ nsuf, co
 cudaError_t launch_wire(const void* nsuf, const void* npre, unsigned long long m, int coverage, WireRow* out,
                         cudaStream_t st) {
   if (m == 0) return cudaSuccess;
-  k_wire<<<(unsigned)((m + 255) / 256), 256, 0, st>>>((const uint4*)nsuf, (const uint4*)npre, m, coverage, out);
+  pk::note_launch(), k_wire<<<(unsigned)((m + 255) / 256), 256, 0, st>>>((const uint4*)nsuf, (const uint4*)npre, m, coverage, out);
   return cudaGetLastError();
 }
 
 }  // namespace pk
+
+extern "C" uint64_t pk_kernel_launches(void) { return pk::g_launches.load(std::memory_order_relaxed); }

@@ -109,12 +109,11 @@ extern "C" pk_status pk_cutoff_noalloc(const uint32_t* d_counts, uint64_t n_rows
     h = g_hist_addr[dev];
   }
   cudaStream_t st = (cudaStream_t)stream;
-  k_noalloc_clear<<<(num_buckets + 255) / 256, 256, 0, st>>>(h, num_buckets);
-  int grid = (int)((n_rows + 255) / 256);
-  if (grid > 1024) grid = 1024;
-  if (grid < 1) grid = 1;
-  k_noalloc_hist<<<grid, 256, 0, st>>>(d_counts, n_rows, num_buckets, h);
-  k_noalloc_cutoff<<<1, 1024, 0, st>>>(h, num_buckets, n_rows, d_cutoff, d_hist, d_kept);
+  pk::note_launch(), k_noalloc_clear<<<(num_buckets + 255) / 256, 256, 0, st>>>(h, num_buckets);
+  const uint64_t blocks = (n_rows + 255) / 256;  // clamped before narrowing
+  const int grid = blocks > 1024 ? 1024 : (blocks < 1 ? 1 : (int)blocks);
+  pk::note_launch(), k_noalloc_hist<<<grid, 256, 0, st>>>(d_counts, n_rows, num_buckets, h);
+  pk::note_launch(), k_noalloc_cutoff<<<1, 1024, 0, st>>>(h, num_buckets, n_rows, d_cutoff, d_hist, d_kept);
   e = cudaGetLastError();
   if (e != cudaSuccess) return pk::set_error(PK_ERR_CUDA, cudaGetErrorString(e));
   return PK_OK;

@@ -82,11 +82,18 @@ struct pk_job {
   DevBuf fasta, tile_nl, counts, bstart, hstart, keys, tkeys, tcounts, tu, flags_m, hist, hist2,
       nkeys, nsuf, npre, packed, doff, dkeys, dcounts, flags_f, kkeys, kcounts, kstart, kcount, ksub,
       coff, cstart, slice_start, fcur, wiring, gfirst, gcount, chunk_bucket, gdone, chunk_u;
+  // counting in pieces (pk_chunked.cu): the accumulated table (ping-pong) and the merge
+  DevBuf acc_keys[2], acc_counts[2], merge_keys, merge_counts, merge_part;
+  uint32_t pieces = 0;  // pieces the last count used (1: the whole input at once)
   bool dense_valid = false;
   bool wired = false;  // wiring matches the current macro-nodes
   pk::CpState* cp = nullptr;
   bool compacted = false;  // the compaction state matches the current macro-nodes
   bool timing = false;
+  // bounded device waits: polls before a wait gives up (0: the default, about 1-2 s), and
+  // a macro-node unit that withholds its look-back word (-1: none); see pk_job_set_wait_limit
+  uint32_t wait_limit = 0;
+  int32_t withhold_unit = -1;
   // graph mode (batch capture): no host synchronisation and no allocation; the
   // window count is bounded by ncap and scalars were initialised by the caller
   bool graph_mode = false;
@@ -112,9 +119,20 @@ int auto_bucket_bits(uint64_t F, int k, int wide);
 // device FASTA -> resident table; in graph mode no host synchronisation happens and
 // the window count is taken as j->ncap
 pk_status count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_params* p);
+// pk_count's body: a host buffer counted at once, or in -b pieces (pk_params.chunking)
+pk_status count_host(pk_job* j, const char* fasta, uint64_t n, const pk_params* p);
 pk_status sync_scalars(pk_job* j);
 pk_status cutoff_enqueue(pk_job* j, int t);
 pk_status mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound);
+// the resident table as dense ascending rows in j->dkeys / j->dcounts (built on demand)
+pk_status dense_table(pk_job* j);
+// counting a host buffer in record-aligned pieces of at most `piece` bytes, merged into
+// one table (pk_chunked.cu)
+pk_status count_pieces(pk_job* j, const char* host, uint64_t n, const pk_params* p, uint64_t piece);
+// frees every buffer of the counting stages except the table (tkeys, tcounts)
+void release_piece_buffers(pk_job* j);
+// every device buffer of a job, for freeing and accounting
+int job_buffers(pk_job* j, DevBuf** out, int cap);
 // per-stage CUDA events on the job's stream (when timing is on)
 void mark_begin(pk_job* j, int st);
 void mark_end(pk_job* j, int st);

@@ -200,10 +200,21 @@ void initiate_mnode_wiring(std::vector<std::pair<kmer_t, MacroNode>>& MN_map) {
     mn.suffixes_terminal.push_back(true);
     mn.suffix_count.push_back(std::make_pair(1, r.terminal_suffix_visit));
     const int nw = (int)(mn.prefixes.size() + mn.suffixes.size() + 1);
+    // a node has at most four prefixes and four suffixes plus the terminal entries, which
+    // is what pk_wiring holds; anything else means the map and the wiring disagree
+    const int max_wires = (int)(sizeof(r.wire) / sizeof(r.wire[0]));
+    const size_t max_prefixes = sizeof(r.prefix_begin) / sizeof(r.prefix_begin[0]);
+    if (nw > max_wires || mn.prefixes.size() > max_prefixes || r.n_wires > max_wires ||
+        r.n_prefixes != (int32_t)mn.prefixes.size() || r.n_suffixes != (int32_t)mn.suffixes.size()) {
+      fprintf(stderr, "initiate_mnode_wiring: node %zu has %zu prefixes and %zu suffixes, its wiring "
+                      "%d and %d (%d wires)\n", i, mn.prefixes.size(), mn.suffixes.size(), r.n_prefixes,
+              r.n_suffixes, r.n_wires);
+      die(PK_ERR_DEVICE, "pk_copy_wiring");
+    }
     mn.wiring_info.assign(nw, WireInfo{0, 0, 0});
-    for (int x = 0; x < nw && x < 9; x++) mn.wiring_info[x] = WireInfo{r.wire[x][0], r.wire[x][1], r.wire[x][2]};
+    for (int x = 0; x < nw; x++) mn.wiring_info[x] = WireInfo{r.wire[x][0], r.wire[x][1], r.wire[x][2]};
     mn.prefix_begin_info.assign(mn.prefixes.size(), PrefixInfo{0, 0});
-    for (size_t p = 0; p < mn.prefixes.size() && p < 5; p++)
+    for (size_t p = 0; p < mn.prefixes.size(); p++)
       mn.prefix_begin_info[p] = PrefixInfo{r.prefix_begin[p][0], r.prefix_begin[p][1]};
   }
 }

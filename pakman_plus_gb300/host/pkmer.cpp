@@ -4,7 +4,11 @@
 // parseCommandLine (src/distribute_kmers.cpp:217-313) and input reading
 // (src/input_reading.cpp:246-266):
 //   -f FILE  input FASTA (required; "Must specify an input FASTA file name with -f")
-//   -b N     batch size MAX_KMER_COUNT (default 100000000, with the reference's notice)
+//   -b N     batch size MAX_KMER_COUNT (default 100000000, with the reference's notice):
+//            an input that does not fit the GPU's memory budget at once is counted in
+//            record-aligned pieces of at most N bytes (so at most N k-mer windows) whose
+//            tables are merged on the device -- the reference's batch flush -- and the
+//            table is the same for any N
 //   -r N     read length (required, 100..250)
 //   -c N     coverage (required)
 //   -t N     histogram buckets num_buckets (default 21)
@@ -14,10 +18,12 @@
 // The reference's build knobs ksize and LMER_LENGTH are run-time options here:
 //   -k K     k-mer length, 2..64 (default 32)
 //   -l L     LMER_LENGTH (default 8)
-// and four options of this driver:
+// and five options of this driver:
 //   -o PFX   write PFX.table ("PKT1") and PFX.mn ("PKM1") binary dumps
 //   -d DEV   CUDA device (default 0)
 //   -N       drop k-mers spanning N (default: the reference's behaviour, kept)
+//   -M BYTES HBM budget of the run (default: the whole device); counting switches to -b
+//            pieces when the input does not fit it at once
 //   -g       contig generation, as the reference's PERFORM_CONTIG_GENERATION build
 //            (src/distribute_kmers.cpp:156-203): iterative compaction down to the -n
 //            threshold, the walk, and the contig files that build writes into the
@@ -93,8 +99,9 @@ int main(int argc, char** argv) {
   unsigned long max_kmer_count = 0;
   int read_length = 0, coverage = 0, num_buckets = 0, node_threshold = 0;
   int k = 32, lmer = 8, device = 0, drop_n = 0, gen = 0;
+  unsigned long long budget = 0;
   int ret;
-  while ((ret = getopt(argc, argv, "f:b:r:c:t:n:ip:k:l:o:d:Ng")) != -1) {
+  while ((ret = getopt(argc, argv, "f:b:r:c:t:n:ip:k:l:o:d:NgM:")) != -1) {
     switch (ret) {
       case 'f': input.assign(optarg); break;
       case 'b':
@@ -115,6 +122,9 @@ int main(int argc, char** argv) {
       case 'd': device = atoi(optarg); break;
       case 'N': drop_n = 1; break;
       case 'g': gen = 1; break;
+      case 'M':
+        if (sscanf(optarg, "%llu", &budget) != 1) abort_run("-M takes a byte count");
+        break;
       default:
         fprintf(stderr, "Should not reach here!!\n");
         abort();  // the reference asserts
@@ -156,7 +166,7 @@ int main(int argc, char** argv) {
 
   pk_ctx* ctx = nullptr;
   pk_job* job = nullptr;
-  if ((st = pk_ctx_create(device, 0, &ctx)) != PK_OK) die_pk("pk_ctx_create", st);
+  if ((st = pk_ctx_create(device, (uint64_t)budget, &ctx)) != PK_OK) die_pk("pk_ctx_create", st);
   if ((st = pk_job_create(ctx, nullptr, &job)) != PK_OK) die_pk("pk_job_create", st);
   pk_params p;
   pk_params_default(&p);
@@ -178,9 +188,12 @@ int main(int argc, char** argv) {
   if (st != PK_OK) die_pk("k-mer counting", st);
   uint64_t u = 0, nwin = 0, nreads = 0;
   pk_table_info(job, &u, &nwin, &nreads);
+  uint32_t pieces = 1;
+  pk_count_pieces(job, &pieces);
   double t3 = now_s();
   printf("input reading and k-mer counting (secs): %f, reads: %llu, k-mer instances: %llu, unique k-mers: %llu\n",
          t3 - t2, (unsigned long long)nreads, (unsigned long long)nwin, (unsigned long long)u);
+  printf("Number of batch iterations: %u\n", pieces);
   const int wide = k > 32;
   if (!out_prefix.empty()) {
     std::vector<uint64_t> keys((size_t)u * (wide ? 2 : 1) + 2);

@@ -18,7 +18,7 @@ ROOT = os.path.dirname(HERE)
 @pytest.mark.skipif(not os.path.isdir(po.REFERENCE_TREE), reason="reference sources not present")
 def test_reference_driver_links_with_the_dropin(tmp_path):
     pkbuild.build()
-    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "dropin", "K=32", "-j8"],
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "dropin", "K=32", f"REF={po.REFERENCE_TREE}", "-j8"],
                           stdout=subprocess.DEVNULL)
     exe = os.path.join(ROOT, "oracle", "_ref", "pkmer_dropin_k32")
     assert os.access(exe, os.X_OK)
@@ -45,7 +45,7 @@ def test_contig_generation_driver_links_with_the_dropin(tmp_path):
     COMPACT_PGRAGH) links with the drop-in in place of its wiring and compaction
     objects and keeps its own walk."""
     pkbuild.build()
-    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "dropin_contigs", "K=32",
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "dropin_contigs", "K=32", f"REF={po.REFERENCE_TREE}",
                            "-j8"], stdout=subprocess.DEVNULL)
     exe = os.path.join(ROOT, "oracle", "_ref", "pkmer_dropin_contigs_k32")
     syms = subprocess.run(["nm", "-C", exe], capture_output=True, text=True).stdout

@@ -1,4 +1,6 @@
 """GPU path against the reference's golden fixtures and the oracle (bit-exact)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -34,10 +36,12 @@ def test_golden_fixture(name):
     assert np.array_equal(mn.prefix_visits, g.mn_pre_visit)
 
 
-@pytest.mark.parametrize("bucket_bits", [2, 3, 6, 11, 16, 18])
+@pytest.mark.parametrize("bucket_bits", [2, 3, 6, 11, 15, 16, 18])
 @pytest.mark.parametrize("name", ["k32_basic", "k63_basic", "k11_dense", "k32_ragged"])
 def test_golden_with_forced_partition(name, bucket_bits):
-    """Few, large buckets force the multi-pass (split) path of the bucket kernel."""
+    """Few, large buckets force the multi-pass (split) path of the bucket kernel; deep
+    partitions (above 15 digits) take their fine bucket sizes from a count over the
+    coarse regions."""
     g = load(name)
     s, keys, counts, hist, mn, err = run_gpu(g.fasta, g.k, g.t, g.coverage, g.drop_n,
                                              bucket_bits=bucket_bits)
@@ -47,8 +51,8 @@ def test_golden_with_forced_partition(name, bucket_bits):
         assert_mn_equal(mn, g.mn_keys, g.mn_suf, g.mn_pre)
 
 
-def _compare_with_oracle(rs, t=21, bucket_bits=0):
-    ora = po.run(rs.fasta, rs.k, t, rs.drop_n)
+def _compare_with_oracle(rs, t=21, bucket_bits=0, threads=1):
+    ora = po.run(rs.fasta, rs.k, t, rs.drop_n, threads=threads)
     s, keys, counts, hist, mn, err = run_gpu(rs.fasta, rs.k, t, rs.coverage, rs.drop_n,
                                              bucket_bits=bucket_bits)
     assert_table_equal(keys, counts, ora.table.keys, ora.table.counts)
@@ -77,6 +81,15 @@ def test_bacterial_80x_k32_scaled():
 def test_longk_k63_dropn_scaled():
     """50 Mbp/40x k=63 workload scaled to 1 Mbp, N windows dropped."""
     _compare_with_oracle(synth.config3(0.02), t=21)
+
+
+@pytest.mark.slow
+def test_longk_k63_dropn_quarter_scale():
+    """The long-k workload at a quarter of its size (12.5 Mbp genome, 3.33M x 150 bp
+    reads at 40x, 0.3% substitutions, 0.05% N, k=63 as 128-bit keys, N windows dropped;
+    about 280M windows): table, histogram, cutoff and macro-nodes equal the oracle's
+    threaded restatement, which equals the serial oracle."""
+    _compare_with_oracle(synth.config3(0.25), t=21, threads=os.cpu_count() or 1)
 
 
 @pytest.mark.parametrize("k", [2, 5, 16, 17, 31, 33, 47, 48, 49, 50, 62, 64])
