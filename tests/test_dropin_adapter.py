@@ -162,4 +162,6 @@ def test_adapter_fills_the_reference_structures(tmp_path, name):
     for ln in open(tmp_path / "begins.txt"):
         a, b = ln.split()
         got.append((_key(a), int(b)))
-    assert got == want and len(got) > 0
+    assert got == want
+    if name != "k32_small":  # the small case compacts to nothing
+        assert len(got) > 0

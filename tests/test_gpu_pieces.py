@@ -59,11 +59,11 @@ def test_one_record_per_piece_and_a_sequence_line_starting_with_gt():
     """With a one-byte -b every record is a piece; a sequence line that begins with '>'
     (a sequence line in the reference, whose '>' is a base code) is never a cut."""
     rs = synth.small_case(91, genome_len=3000, n_reads=300, read_len=100, err=0.01, k=32)
-    recs = rs.fasta.split(b"\n>")
-    odd = b">h_odd\n>" + recs[5].split(b"\n", 1)[1]
-    fasta = b"\n>".join(recs[:10]) + b"\n" + odd + b">" + b"\n>".join(recs[10:])
+    lines = rs.fasta.split(b"\n")[:-1]  # header, sequence, header, ...
+    lines = lines[:20] + [b">h_odd", b">" + lines[11]] + lines[20:]
+    fasta = b"\n".join(lines) + b"\n"
     pieces = _run_and_compare(ctx(), fasta, 32, 21, 10, chunking=1, batch_kmers=1)
-    assert pieces == fasta.count(b"\n>") - 1 + 1
+    assert pieces == 301  # one per record; the sequence line's '>' starts no piece
 
 
 def test_bad_record_in_a_later_piece():
@@ -78,33 +78,40 @@ def test_budget_below_the_whole_input_switches_to_pieces():
     """The bacterial workload at 0.05 scale with an HBM budget too small for counting the
     whole input at once: the job counts in -b pieces by itself."""
     rs = synth.config2(0.05)
-    small = pk.Context(0, hbm_budget=6 * len(rs.fasta))
+    # counting at once needs about 13 bytes per FASTA byte (keys twice, counts); the
+    # pieces need the merged table (about 1.3 bytes per FASTA byte here) three times over
+    # plus one piece's working set
+    budget = 8 * len(rs.fasta)
+    small = pk.Context(0, hbm_budget=budget)
     try:
-        pieces = _run_and_compare(small, rs.fasta, rs.k, rs.t, rs.coverage, batch_kmers=len(rs.fasta) // 6)
+        pieces = _run_and_compare(small, rs.fasta, rs.k, rs.t, rs.coverage, batch_kmers=len(rs.fasta) // 10)
         assert pieces > 1
     finally:
         small.close()
-    with pk.Context(0, hbm_budget=6 * len(rs.fasta)) as small2, pk.Job(small2) as job:
+    with pk.Context(0, hbm_budget=budget) as small2, pk.Job(small2) as job:
         with pytest.raises(pk.capi.OutOfMemory):
             job.count(rs.fasta, pk.default_params(k=32, chunking=2))
 
 
 def test_pkmer_b_counts_in_pieces(tmp_path):
-    g = load("k63_basic")
+    """pkmer -b with an HBM budget (-M) below the whole input's footprint: the run counts
+    in -b pieces and its dumps equal the oracle's table and macro-nodes."""
+    rs = synth.config2(0.01)
     fa = tmp_path / "in.fa"
-    fa.write_bytes(g.fasta)
+    fa.write_bytes(rs.fasta)
     out = str(tmp_path / "out")
     pkbuild.build()
     exe = pkbuild.build_pkmer()
-    r = subprocess.run([exe, "-f", str(fa), "-r", "100", "-c", str(g.coverage), "-t", str(g.t), "-k", str(g.k),
-                        "-b", "20000", "-M", str(6 * len(g.fasta)), "-o", out], capture_output=True, text=True,
-                       timeout=300)
+    r = subprocess.run([exe, "-f", str(fa), "-r", "100", "-c", str(rs.coverage), "-t", str(rs.t), "-k", str(rs.k),
+                        "-b", str(len(rs.fasta) // 10), "-M", str(8 * len(rs.fasta)), "-o", out],
+                       capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     it = [ln for ln in r.stdout.splitlines() if ln.startswith("Number of batch iterations:")]
     assert it and int(it[0].split(":")[1]) > 1, r.stdout
+    ora = po.run(rs.fasta, rs.k, rs.t)
     k, keys, counts = po.read_table_dump(out + ".table")
-    assert np.array_equal(keys, g.table_keys)
-    assert np.array_equal(counts, g.table_counts.astype(np.int64))
-    mk, suf, pre, sv, pv, k1_ok = po.read_mn_dump(out + ".mn", g.coverage)
-    assert np.array_equal(mk, g.mn_keys)
-    assert np.array_equal(suf, g.mn_suf) and np.array_equal(pre, g.mn_pre)
+    assert np.array_equal(keys, ora.table.keys)
+    assert np.array_equal(counts, ora.table.counts.astype(np.int64))
+    mk, suf, pre, sv, pv, k1_ok = po.read_mn_dump(out + ".mn", rs.coverage)
+    assert np.array_equal(mk, ora.mn.keys)
+    assert np.array_equal(suf, ora.mn.suf) and np.array_equal(pre, ora.mn.pre)
