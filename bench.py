@@ -56,6 +56,8 @@ def parse():
                     help="batching benchmark: many read sets in one CUDA-graph launch")
     ap.add_argument("--batch-sets", type=int, default=256)
     ap.add_argument("--batch-branches", type=int, default=6)
+    ap.add_argument("--batch-check-every", type=int, default=8,
+                    help="every n-th set of the batch is checked against the oracle")
     ap.add_argument("--serve", action="store_true",
                     help="serving benchmark: Poisson stream of jobs through pk_submit, p50/p99 latency")
     ap.add_argument("--serve-jobs", type=int, default=5000)
@@ -358,12 +360,24 @@ def run_reference_arm(args, rank, world):
     return 0
 
 
+def _mn_digest(keys, suf, pre) -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for x in (keys, suf, pre):
+        h.update(memoryview(x).cast("B"))
+    return h.hexdigest()[:16]
+
+
 def run_serve(args, rank, world):
     """Serving workload: jobs (genome log-uniform 10 kb-20 Mbp, 100 bp reads at 30-80x,
     k in {31, 32, 63}) arrive as a Poisson stream and go through pk_submit/pk_wait
-    with HBM-budget admission; the same stream is then served one job at a time (the
-    plain one-job-per-launch path).  A pool of generated read sets stands in for the
-    stream's inputs (job i uses pool entry i mod P with that entry's k)."""
+    with HBM-budget admission and size-aware scheduling; the same stream is then served
+    one job at a time (the plain one-job-per-launch path), and both are run again with
+    every job submitted at once (capacity at saturation).  A pool of generated read sets
+    stands in for the stream's inputs (job i uses pool entry i mod P with that entry's
+    k).  Every pool entry's result is checked against the oracle (table and macro-nodes),
+    every served job's summary against its entry's, and one served table per entry
+    byte for byte."""
     if rank != 0:
         return 0
     import threading
@@ -372,6 +386,7 @@ def run_serve(args, rank, world):
     import torch
 
     import pakman_plus_gb300 as pk
+    from oracle import pk_oracle as po
     from pakman_plus_gb300 import build as pkbuild
     from pakman_plus_gb300 import synth
 
@@ -391,26 +406,60 @@ def run_serve(args, rank, world):
     t_gen = time.perf_counter() - t_gen
     budget = int(args.serve_budget_gb * 1e9)
     ctx = pk.Context(0, hbm_budget=budget)
-    # each pool entry alone, once: reference summaries and warm-up
+    # each pool entry alone, once: reference summaries, macro-node digests and warm-up
     # (a job whose k-mers all fall below the cutoff ends with PK_ERR_EMPTY, as the
     # reference aborts; that outcome must then be the same in the stream)
-    alone = []
+    alone, alone_digest, oracle_ok = [], [], []
+    t_ora = 0.0
+    threads = os.cpu_count() or 1
     with pk.Job(ctx) as job:
         for e, rs in enumerate(pool):
             t0 = time.perf_counter()
             status = 0
+            mn = None
             try:
                 job.run(pinned[e].numpy(), params[e])
-                job.macro_nodes()
+                mn = job.macro_nodes()
             except pk.EmptyAfterCutoff as ex:
                 status = ex.status
             alone.append((job.summary(), time.perf_counter() - t0, status))
+            keys, counts = job.table()
+            alone_digest.append(_mn_digest(mn.keys, mn.suffix_counts, mn.prefix_counts) if mn else None)
+            t1 = time.perf_counter()
+            ora = po.run(pinned[e].numpy().tobytes(), rs.k, 21, threads=threads)
+            t_ora += time.perf_counter() - t1
+            k128 = pk.to_key128(keys)
+            ok = k128.size == ora.table.keys.size and np.array_equal(k128, ora.table.keys) and \
+                np.array_equal(counts, ora.table.counts) and alone[-1][0].cutoff == ora.cutoff
+            if ora.mn is None:
+                ok = ok and status != 0
+            else:
+                ok = ok and mn is not None and np.array_equal(pk.to_key128(mn.keys), ora.mn.keys) and \
+                    np.array_equal(mn.suffix_counts, ora.mn.suf) and np.array_equal(mn.prefix_counts, ora.mn.pre)
+            oracle_ok.append(bool(ok))
+            del ora, keys, counts, mn
             job.reset()
+    # each entry's solo latency through the server (nothing else in flight), best of two
+    solo = []
+    srv = pk.Server(ctx, workers=args.serve_workers)
+    for e in range(len(pool)):
+        best = None
+        for _ in range(2):
+            tk = srv.submit(pinned[e].numpy(), params[e])
+            try:
+                srv.wait(tk)
+            except pk.PakmanError:
+                pass
+            lat = srv.poll(tk).latency_ms
+            srv.release(tk)
+            best = lat if best is None else min(best, lat)
+        solo.append(best)
+    srv.close()
     rng = np.random.Generator(np.random.PCG64(5_000_001))
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, args.serve_jobs))
     entries = [i % len(pool) for i in range(args.serve_jobs)]
 
-    def serve(workers):
+    def serve(workers, arrival):
         srv = pk.Server(ctx, workers=workers)
         tickets = [None] * args.serve_jobs
         ready = threading.Semaphore(0)
@@ -418,7 +467,7 @@ def run_serve(args, rank, world):
         def producer():
             t0 = time.perf_counter()
             for i, e in enumerate(entries):
-                dt = t0 + arrivals[i] - time.perf_counter()
+                dt = t0 + arrival[i] - time.perf_counter()
                 if dt > 0:
                     time.sleep(dt)
                 tickets[i] = srv.submit(pinned[e].numpy(), params[e])
@@ -426,38 +475,52 @@ def run_serve(args, rank, world):
 
         th = threading.Thread(target=producer, daemon=True)
         th.start()
-        lat, first_submit, last_end, windows, mismatches = [], None, 0, 0, 0
+        lat, ratio, first_submit, last_end, windows, mismatches = [], [], None, 0, 0, 0
+        checked, table_mismatch = set(), 0
         for i, e in enumerate(entries):
             ready.acquire()
             try:
                 srv.wait(tickets[i])
             except pk.PakmanError:
-                pass  # compared with the job run alone below
+                pass
             info = srv.poll(tickets[i])
-            srv.release(tickets[i])
             ref, _, ref_status = alone[e]
             s = info.summary
             if info.status != ref_status or (s.n_windows, s.n_unique, s.n_kept, s.cutoff) != (
                     ref.n_windows, ref.n_unique, ref.n_kept, ref.cutoff) or (
                     ref_status == 0 and s.n_nodes != ref.n_nodes):
                 mismatches += 1
+            if e not in checked and info.status == 0:
+                checked.add(e)
+                mn = srv.result(tickets[i])
+                if _mn_digest(mn.keys, mn.suffix_counts, mn.prefix_counts) != alone_digest[e]:
+                    table_mismatch += 1
+            srv.release(tickets[i])
             lat.append(info.latency_ms)
+            ratio.append(info.latency_ms / solo[e])
             first_submit = info.submit_ns if first_submit is None else min(first_submit, info.submit_ns)
             last_end = max(last_end, info.end_ns)
             windows += s.n_windows
         th.join()
         st = srv.stats()
         srv.close()
-        lat = np.array(lat)
+        lat, ratio = np.array(lat), np.array(ratio)
         span = (last_end - first_submit) / 1e9
         return {"workers": workers, "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
-                "max_ms": float(lat.max()), "kmers_per_s": windows / span, "span_s": span,
+                "max_ms": float(lat.max()), "p50_latency_over_solo": float(np.percentile(ratio, 50)),
+                "p99_latency_over_solo": float(np.percentile(ratio, 99)),
+                "jobs_within_2x_solo": float((ratio <= 2.0).mean()),
+                "kmers_per_s": windows / span, "span_s": span,
                 "peak_admitted_gb": st["peak_admitted_bytes"] / 1e9, "requeued": st["requeued"],
-                "results_differing_from_alone": mismatches}
+                "results_differing_from_alone": mismatches,
+                "macro_node_tables_checked": len(checked), "macro_node_tables_differing": table_mismatch}
 
-    served = serve(args.serve_workers)
-    plain = serve(1)
+    served = serve(args.serve_workers, arrivals)
+    plain = serve(1, arrivals)
+    at_once = np.zeros(args.serve_jobs)
+    served_sat = serve(args.serve_workers, at_once)
+    plain_sat = serve(1, at_once)
     total_windows = sum(alone[e][0].n_windows for e in entries)
     offered = total_windows / arrivals[-1]
     line = {"metric": "served p50/p99 latency of count + macro-node jobs", "impl": "serve",
@@ -470,10 +533,21 @@ def run_serve(args, rank, world):
                        "hbm_budget_gb": args.serve_budget_gb,
                        "offered_kmers_per_s": offered,
                        "alone_ms_by_entry": [round(a[1] * 1000, 2) for a in alone],
+                       "solo_served_ms_by_entry": [round(x, 2) for x in solo],
                        "entries_empty_after_cutoff": sum(1 for a in alone if a[2] != 0)},
-            "served": served, "plain_one_job_at_a_time": plain}
+            "oracle": {"entries_equal": sum(oracle_ok), "entries": len(oracle_ok), "seconds": t_ora,
+                       "against": "table, cutoff and macro-nodes of every pool entry against the oracle's "
+                                  f"threaded restatement ({threads} threads)"},
+            "served": served, "plain_one_job_at_a_time": plain,
+            "saturation": {"served": served_sat, "plain_one_job_at_a_time": plain_sat,
+                           "capacity_ratio": served_sat["kmers_per_s"] / plain_sat["kmers_per_s"]}}
     print(json.dumps(line), flush=True)
     ctx.close()
+    bad = sum(not x for x in oracle_ok) + sum(r["results_differing_from_alone"] + r["macro_node_tables_differing"]
+                                            for r in (served, plain, served_sat, plain_sat))
+    if bad:
+        print("bench: served results differ from the oracle or from the jobs run alone", file=sys.stderr)
+        return 3
     return 0
 
 
@@ -534,6 +608,27 @@ def run_batch(args, rank, world):
             torch.cuda.synchronize()
             plain_ms.append(1000 * (time.perf_counter() - t))
     med = sorted(graph_ms)[len(graph_ms) // 2]
+    # every 8th set (32 of 256, spread over the size range) against the oracle: summary,
+    # cutoff and the set's rows of the batch's macro-node table
+    from oracle import pk_oracle as po
+    threads = os.cpu_count() or 1
+    checked, equal = 0, 0
+    t_ora = time.perf_counter()
+    for i in range(0, len(sets), max(1, args.batch_check_every)):
+        f, p = sets[i]
+        ora = po.run(f.tobytes(), 32, 21, threads=threads)
+        r = res[i]
+        ok = r.summary.n_unique == ora.table.keys.size and r.summary.n_windows == ora.table.n_windows
+        if ora.mn is None:
+            ok = ok and r.status != 0
+        else:
+            mn = batch.macro_nodes(r, (keys, suf, pre), p.coverage)
+            ok = ok and r.status == 0 and r.summary.cutoff == ora.cutoff and \
+                np.array_equal(pk.to_key128(mn.keys), ora.mn.keys) and \
+                np.array_equal(mn.suffix_counts, ora.mn.suf) and np.array_equal(mn.prefix_counts, ora.mn.pre)
+        checked += 1
+        equal += bool(ok)
+    t_ora = time.perf_counter() - t_ora
     line = {"metric": "batched count + macro-node k-mers/s (one CUDA-graph launch per batch)", "impl": "batch",
             "value": windows / (med / 1000.0), "unit": "k-mers/s", "higher_is_better": True, "n_gpus": 1,
             "data": "synthetic", "dtype": "u64",
@@ -551,10 +646,16 @@ def run_batch(args, rank, world):
             "plain_one_job_at_a_time": {"kmers_per_s": windows / (min(plain_ms) / 1000.0),
                                         "ms": min(plain_ms)},
             "statuses": {str(s): sum(1 for r in res if r.status == s) for s in set(r.status for r in res)},
-            "total_nodes": st["total_nodes"]}
+            "total_nodes": st["total_nodes"],
+            "oracle": {"sets_checked": checked, "sets_equal": equal, "seconds": t_ora,
+                       "against": "summary, cutoff and macro-node rows of every "
+                                  f"{args.batch_check_every}th set against the oracle ({threads} threads)"}}
     print(json.dumps(line), flush=True)
     batch.close()
     ctx.close()
+    if equal != checked:
+        print("bench: batched results differ from the oracle", file=sys.stderr)
+        return 3
     return 0
 
 

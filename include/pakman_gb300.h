@@ -60,9 +60,10 @@ typedef enum pk_status {
                            on-chip capacity exceeded); results are not valid */
   PK_ERR_BUSY = 9,      /* serving: no capacity right now, retry later */
   PK_ERR_NO_DEVICE = 10, /* no usable CUDA device */
-  PK_ERR_IO = 11         /* the input file cannot be opened or read (the reference
+  PK_ERR_IO = 11,        /* the input file cannot be opened or read (the reference
                             prints "Couldn't open the input FASTA file" and exits 2,
                             src/input_reading.cpp:260-265) */
+  PK_ERR_CANCELLED = 12  /* serving: the request was cancelled (pk_cancel) */
 } pk_status;
 
 typedef struct pk_ctx pk_ctx;
@@ -346,13 +347,20 @@ uint64_t pk_kernel_launches(void);
 /* ---- Serving: many independent count -> cutoff -> macro-node jobs on one GPU ----
  *
  * The submit / poll interface of the serving design (there is no reference
- * counterpart: the reference runs one read set per MPI job).  A server owns
- * `workers` job slots on one context, each with its own CUDA stream, so one job's
- * host<->device copies and host synchronisations overlap other jobs' kernels.
- * Admission: a request starts only when the estimate of its device footprint fits
- * the context's free HBM budget (requests wait in FIFO order; the head of the queue
- * is never overtaken); a job that still runs out of device memory is put back at the
- * head of the queue and retried when another job has finished.  Results are
+ * counterpart: the reference runs one read set per MPI job).  A server owns `workers`
+ * worker threads on one context; a worker takes the next request as soon as its last
+ * one has finished (continuous batching), so one request's host<->device copies and
+ * host synchronisations overlap other requests' kernels.
+ * Scheduling: the queued request with the least estimated work (FASTA bytes, doubled
+ * for k > 32) starts first, so small requests are not queued behind large ones; a
+ * request that has waited longer than aging_ms starts first regardless of size (while
+ * it does not fit the budget only small requests start, in the memory it leaves).
+ * Requests of at most small_bytes are small: reserved_small workers take only small
+ * requests, and small requests run on high-priority CUDA streams.
+ * Admission: a request starts only when the estimate of its device footprint, added to
+ * the running requests' estimates and the device memory of kept results, fits the
+ * context's HBM budget; a request that still runs out of device memory goes back to
+ * the queue and starts again after another request has finished.  Results are
  * bit-identical to a job run alone. */
 typedef struct pk_server pk_server;
 
@@ -370,6 +378,12 @@ typedef struct pk_request {
   uint32_t* mn_suffix;
   uint32_t* mn_prefix;
   uint64_t mn_capacity;
+  /* 1: the finished request's job -- its k-mer table and macro-nodes resident in HBM --
+   * is kept for the caller (pk_result_job) until pk_result_release, and its device
+   * memory counts against the budget meanwhile; the macro-node buffers above are then
+   * optional (NULL: nothing is copied to the host). */
+  int32_t keep_on_device;
+  int32_t reserved[3];
 } pk_request;
 
 typedef struct pk_request_info {
@@ -386,14 +400,33 @@ typedef struct pk_request_info {
 typedef struct pk_server_stats {
   uint64_t submitted, completed, failed, queued, running;
   uint64_t admitted_bytes;       /* sum of the running jobs' footprint estimates */
-  uint64_t peak_admitted_bytes;
+  uint64_t peak_admitted_bytes;  /* peak of admitted_bytes + resident_bytes */
   uint64_t requeued;             /* jobs re-queued after running out of HBM */
+  uint64_t cancelled;
+  uint64_t resident_bytes;       /* device memory of results kept on the device */
+  uint64_t resident_jobs;
 } pk_server_stats;
 
+typedef struct pk_server_config {
+  uint64_t small_bytes;    /* requests of at most this estimated work are small (32 MiB) */
+  int32_t reserved_small;  /* workers that take only small requests (workers / 4) */
+  int32_t aging_ms;        /* a request waiting longer starts first (2000) */
+  int32_t reserved[4];
+} pk_server_config;
+
+void pk_server_config_default(pk_server_config* cfg, int32_t workers);
 pk_status pk_server_create(pk_ctx* ctx, int32_t workers, pk_server** out);
-/* Waits for running jobs, drops queued ones, frees every result. */
+/* cfg NULL: the defaults of pk_server_config_default. */
+pk_status pk_server_create_config(pk_ctx* ctx, int32_t workers, const pk_server_config* cfg,
+                                  pk_server** out);
+/* Cancels queued requests and ends running ones at their next stage boundary, waits for
+ * the workers, frees every result. */
 void pk_server_destroy(pk_server* s);
 pk_status pk_submit(pk_server* s, const pk_request* req, uint64_t* ticket);
+/* A queued request ends at once, a running one at its next stage boundary (after
+ * counting or after the cutoff), with status PK_ERR_CANCELLED; PK_ERR_STATE once the
+ * request has finished. */
+pk_status pk_cancel(pk_server* s, uint64_t ticket);
 /* Non-blocking: fills *info (info->done == 0 while queued or running). */
 pk_status pk_poll(pk_server* s, uint64_t ticket, pk_request_info* info);
 /* Blocks until the job is done or timeout_ms (< 0: no limit) passes; PK_ERR_BUSY on timeout. */
@@ -401,7 +434,12 @@ pk_status pk_wait(pk_server* s, uint64_t ticket, int64_t timeout_ms, pk_request_
 /* Server-kept macro-node table of a finished request (valid until pk_result_release). */
 pk_status pk_result_get(pk_server* s, uint64_t ticket, const void** keys, const uint32_t** suffix,
                         const uint32_t** prefix, uint64_t* n_nodes);
-/* Forgets a finished request and frees what the server kept for it. */
+/* The job of a finished keep_on_device request: its table and macro-nodes stay resident
+ * and every pk_* call on a job works on it (pk_copy_table, pk_wire_macro_nodes,
+ * pk_compact, pk_walk, ...).  The server owns it: valid until pk_result_release. */
+pk_status pk_result_job(pk_server* s, uint64_t ticket, pk_job** job);
+/* Forgets a finished request and frees what the server kept for it (host tables and a
+ * kept job's device memory). */
 pk_status pk_result_release(pk_server* s, uint64_t ticket);
 pk_status pk_server_get_stats(pk_server* s, pk_server_stats* out);
 /* Device footprint the admission control assumes for a request (bytes). */

@@ -231,14 +231,18 @@ class Job:
     """One read set on the device: count -> cutoff -> macro-nodes; buffers stay
     resident until :meth:`reset` or :meth:`close`."""
 
-    def __init__(self, ctx: Context, stream: Optional[int] = None):
+    def __init__(self, ctx: Context, stream: Optional[int] = None, _borrowed=None):
         self.ctx = ctx
+        self.params: Optional[capi.PkParams] = None
+        self._pin = None
+        self._owned = _borrowed is None
+        if _borrowed is not None:  # a job owned by a server (keep_on_device results)
+            self._h = _borrowed
+            return
         h = c_void_p()
         check(capi.lib().pk_job_create(ctx.handle, c_void_p(stream) if stream else None, byref(h)),
               "pk_job_create")
         self._h = h
-        self.params: Optional[capi.PkParams] = None
-        self._pin = None
 
     @property
     def handle(self):
@@ -410,7 +414,8 @@ class Job:
 
     def close(self):
         if getattr(self, "_h", None):
-            capi.lib().pk_job_destroy(self._h)
+            if self._owned:
+                capi.lib().pk_job_destroy(self._h)
             self._h = None
 
     def __enter__(self):
@@ -512,22 +517,36 @@ class Server:
     context's budget).  Each request's result equals that of the same read set run
     alone in a :class:`Job`."""
 
-    def __init__(self, ctx: Context, workers: int = 2):
+    def __init__(self, ctx: Context, workers: int = 2, small_bytes: Optional[int] = None,
+                 reserved_small: Optional[int] = None, aging_ms: Optional[int] = None):
+        """`small_bytes`, `reserved_small`, `aging_ms`: the scheduling knobs of
+        pk_server_config (None: the library's defaults for this many workers)."""
         self.ctx = ctx
+        cfg = capi.PkServerConfig()
+        capi.lib().pk_server_config_default(byref(cfg), workers)
+        if small_bytes is not None:
+            cfg.small_bytes = small_bytes
+        if reserved_small is not None:
+            cfg.reserved_small = reserved_small
+        if aging_ms is not None:
+            cfg.aging_ms = aging_ms
         h = c_void_p()
-        check(capi.lib().pk_server_create(ctx.handle, workers, byref(h)), "pk_server_create")
+        check(capi.lib().pk_server_create_config(ctx.handle, workers, byref(cfg), byref(h)),
+              "pk_server_create_config")
         self._h = h
         self._live: Dict[int, tuple] = {}  # ticket -> (input buffer, out arrays, params)
 
-    def submit(self, fasta, params: capi.PkParams, out=None) -> int:
+    def submit(self, fasta, params: capi.PkParams, out=None, keep_on_device: bool = False) -> int:
         """Queue one read set.  `fasta` stays referenced until :meth:`release`.  `out` =
         (keys, suffix, prefix) host arrays receiving the macro-node table (pinned memory
-        copies fastest); without it the server keeps the table for :meth:`result`."""
+        copies fastest); without it the server keeps the table for :meth:`result`, or,
+        with `keep_on_device`, keeps the whole job resident for :meth:`job`."""
         buf = _as_bytes_ptr(fasta)
         r = capi.PkRequest()
         r.fasta = buf[0]
         r.fasta_bytes = buf[1]
         r.params = params
+        r.keep_on_device = int(keep_on_device)
         if out is not None:
             keys, suf, pre = out
             r.mn_keys = keys.ctypes.data
@@ -578,6 +597,20 @@ class Server:
             if m else np.empty(0, np.uint32)
         return MacroNodeTable(keys.view(key_dtype(params.k)), suf.reshape(m, 4), pre.reshape(m, 4), cov,
                               params.k)
+
+    def cancel(self, ticket: int):
+        """Cancel a queued or running request (pk_cancel)."""
+        check(capi.lib().pk_cancel(self._h, ticket), "pk_cancel")
+
+    def job(self, ticket: int) -> "Job":
+        """The resident job of a finished keep_on_device request: its table and
+        macro-nodes stay in HBM for further calls (table, wire, compact, walk ...) until
+        :meth:`release`; the server owns it."""
+        h = c_void_p()
+        check(capi.lib().pk_result_job(self._h, ticket, byref(h)), "pk_result_job")
+        j = Job(self.ctx, _borrowed=h)
+        j.params = self._live[ticket][3]
+        return j
 
     def release(self, ticket: int):
         check(capi.lib().pk_result_release(self._h, ticket), "pk_result_release")

@@ -27,6 +27,7 @@ PK_ERR_DEVICE = 8
 PK_ERR_BUSY = 9
 PK_ERR_NO_DEVICE = 10
 PK_ERR_IO = 11
+PK_ERR_CANCELLED = 12
 
 
 class PkParams(ctypes.Structure):
@@ -45,7 +46,7 @@ class PkSummary(ctypes.Structure):
 class PkRequest(ctypes.Structure):
     _fields_ = [("fasta", c_void_p), ("fasta_bytes", c_uint64), ("params", PkParams),
                 ("mn_keys", c_void_p), ("mn_suffix", c_void_p), ("mn_prefix", c_void_p),
-                ("mn_capacity", c_uint64)]
+                ("mn_capacity", c_uint64), ("keep_on_device", c_int32), ("reserved", c_int32 * 3)]
 
 
 class PkRequestInfo(ctypes.Structure):
@@ -56,7 +57,13 @@ class PkRequestInfo(ctypes.Structure):
 
 class PkServerStats(ctypes.Structure):
     _fields_ = [(n, c_uint64) for n in ("submitted", "completed", "failed", "queued", "running",
-                                        "admitted_bytes", "peak_admitted_bytes", "requeued")]
+                                        "admitted_bytes", "peak_admitted_bytes", "requeued", "cancelled",
+                                        "resident_bytes", "resident_jobs")]
+
+
+class PkServerConfig(ctypes.Structure):
+    _fields_ = [("small_bytes", c_uint64), ("reserved_small", c_int32), ("aging_ms", c_int32),
+                ("reserved", c_int32 * 4)]
 
 
 class PkBatchSet(ctypes.Structure):
@@ -115,12 +122,17 @@ class Busy(PakmanError):
     pass
 
 
+class Cancelled(PakmanError):
+    """The served request was cancelled (pk_cancel)."""
+
+
 class InputFileError(PakmanError):
     """The FASTA file cannot be opened or read (the reference exits with status 2)."""
 
 
 _ERR_CLASSES = {PK_ERR_FORMAT: FormatError, PK_ERR_EMPTY: EmptyAfterCutoff,
-                PK_ERR_NOMEM: OutOfMemory, PK_ERR_BUSY: Busy, PK_ERR_IO: InputFileError}
+                PK_ERR_NOMEM: OutOfMemory, PK_ERR_BUSY: Busy, PK_ERR_IO: InputFileError,
+                PK_ERR_CANCELLED: Cancelled}
 
 _lib = None
 
@@ -174,6 +186,10 @@ _SIGS = {
     "pk_cutoff_noalloc": (c_int, [c_void_p, c_uint64, c_int32, c_void_p, c_void_p, c_void_p,
                                   c_void_p]),
     "pk_server_create": (c_int, [c_void_p, c_int32, POINTER(c_void_p)]),
+    "pk_server_config_default": (None, [POINTER(PkServerConfig), c_int32]),
+    "pk_server_create_config": (c_int, [c_void_p, c_int32, POINTER(PkServerConfig), POINTER(c_void_p)]),
+    "pk_cancel": (c_int, [c_void_p, c_uint64]),
+    "pk_result_job": (c_int, [c_void_p, c_uint64, POINTER(c_void_p)]),
     "pk_server_destroy": (None, [c_void_p]),
     "pk_submit": (c_int, [c_void_p, POINTER(PkRequest), POINTER(c_uint64)]),
     "pk_poll": (c_int, [c_void_p, c_uint64, POINTER(PkRequestInfo)]),

@@ -145,6 +145,7 @@ const char* pk_status_string(pk_status s) {
     case PK_ERR_BUSY: return "busy";
     case PK_ERR_NO_DEVICE: return "no CUDA device";
     case PK_ERR_IO: return "input file cannot be read";
+    case PK_ERR_CANCELLED: return "cancelled";
   }
   return "unknown status";
 }

@@ -1,20 +1,38 @@
-// Serving: a FIFO of independent count -> cutoff -> macro-node requests executed by
-// worker threads, each owning one pk_job (and its CUDA stream) on a shared context.
+// Serving: independent count -> cutoff -> macro-node requests run by worker threads on
+// one context, with continuous batching, size-aware scheduling and HBM-budget
+// admission.
 //
 // Continuous batching: a worker takes the next request as soon as its previous one
-// has finished, so jobs of different sizes and k overlap on the GPU (one job's host
-// to device copy and host synchronisations run while another job's kernels execute).
-// Admission control keeps the sum of the running jobs' footprint estimates within the
-// context's HBM budget; the budget itself is enforced exactly by the context's
-// allocator, and a job that hits it anyway goes back to the head of the queue.
+// has finished, so requests of different sizes and k overlap on the GPU (one request's
+// host-to-device copy and host synchronisations run while others' kernels execute).
+//
+// Scheduling.  Queued requests are not served first come, first served: a worker takes
+// the request with the least estimated work (FASTA bytes, doubled for 128-bit keys), so
+// a small request is never queued behind a large one.  A request that has waited longer
+// than the aging bound goes first regardless of size, and while it does not fit the
+// HBM budget no other large request is admitted, so memory drains for it and large
+// requests cannot starve.  Requests up to `small_bytes` are small: some workers
+// (`reserved_small`) take only small requests, so a burst of large ones never occupies
+// every worker, and small requests run on high-priority CUDA streams (the GPU's block
+// scheduler starts their blocks ahead of the large requests' pending blocks).
+//
+// Admission keeps the sum of the running requests' footprint estimates plus the device
+// memory of results kept on the device within the context's HBM budget; the budget is
+// enforced exactly by the context's allocator, and a request that hits it anyway goes
+// back to the queue and starts again after another request has finished.
+//
+// A request can be cancelled while queued (it ends at once) or while running (it ends
+// at its next stage boundary).  A request submitted with keep_on_device hands its job
+// -- the k-mer table and macro-nodes resident in HBM -- to the caller, who can run
+// further stages on it (pk_copy_table, pk_compact, pk_walk, ...) until releasing it.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
 #include <time.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
-#include <deque>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -23,6 +41,7 @@
 
 #include "../../include/pakman_gb300.h"
 #include "pk_internal.h"
+#include "pk_runtime.h"
 
 namespace {
 
@@ -36,13 +55,19 @@ struct Request {
   uint64_t ticket = 0;
   pk_request req{};
   uint64_t footprint = 0;
+  uint64_t cost = 0;         // estimated work: FASTA bytes, doubled for 128-bit keys
+  bool small = false;
   uint64_t retry_after = 0;  // re-queued: start again only after this many completions
+  bool cancel = false;       // cancellation asked while running
   pk_request_info info{};
   std::string error;
   // server-kept macro-node table (pinned host memory)
   void* own_keys = nullptr;
   uint32_t* own_suf = nullptr;
   uint32_t* own_pre = nullptr;
+  // keep_on_device: the finished job, handed to the caller, and its device bytes
+  pk_job* job = nullptr;
+  uint64_t resident = 0;
 };
 
 }  // namespace
@@ -50,15 +75,18 @@ struct Request {
 struct pk_server {
   pk_ctx* ctx = nullptr;
   uint64_t budget = 0;  // 0: no budget
+  int workers = 0;
+  pk_server_config cfg{};
   std::vector<std::thread> threads;
   std::mutex mu;
   std::condition_variable cv_work;  // queue changed / admission freed / stop
   std::condition_variable cv_done;  // a request finished
-  std::deque<Request*> queue;
+  std::vector<Request*> queue;      // waiting requests, in submission order
   std::unordered_map<uint64_t, Request*> reqs;
   uint64_t next_ticket = 1;
   bool stop = false;
   int running = 0;
+  uint64_t events = 0;  // requests finished and results released (re-queued requests wait for one)
   pk_server_stats st{};
   std::vector<std::pair<size_t, void*>> pinned_free;  // pinned host blocks for kept results
 };
@@ -78,6 +106,8 @@ uint64_t footprint(const pk_request& r) {
   const uint64_t fixed = 64ull << 20;  // per-bucket tables, histograms, look-back flags
   return F + N * (2 * W + 4) + V * (W + 4) + 2 * V * (W + 32) + fixed;
 }
+
+uint64_t cost_of(const pk_request& r) { return r.fasta_bytes * (r.params.k > 32 ? 2 : 1); }
 
 // Pinned host blocks for server-kept results, recycled between requests (page-locking
 // new memory costs far more than the copy into it).  Block sizes are rounded up to a
@@ -128,6 +158,47 @@ void pinned_release_all(pk_server* s) {
   s->pinned_free.clear();
 }
 
+// called with s->mu held
+bool fits(const pk_server* s, const Request* q, uint64_t reserve) {
+  if (s->budget == 0) return true;
+  return s->st.admitted_bytes + s->st.resident_bytes + reserve + q->footprint <= s->budget;
+}
+
+// The request a worker starts next, or null (called with s->mu held).  small_only:
+// a worker reserved for small requests.
+Request* pick(pk_server* s, bool small_only) {
+  const uint64_t now = now_ns();
+  const uint64_t done = s->events;
+  const uint64_t aging = (uint64_t)s->cfg.aging_ms * 1000000ull;
+  Request* aged = nullptr;
+  for (Request* q : s->queue)
+    if (now - q->info.submit_ns > aging && done >= q->retry_after) {
+      aged = q;  // the queue is in submission order: the first is the oldest
+      break;
+    }
+  uint64_t reserve = 0;
+  if (aged) {
+    const bool mine = !small_only || aged->small;
+    if (mine && (s->running == 0 || fits(s, aged, 0))) return aged;
+    // memory drains for it: meanwhile only small requests start, and only into the
+    // memory it leaves
+    if (!fits(s, aged, 0)) reserve = aged->footprint;
+  }
+  Request* best = nullptr;
+  for (Request* q : s->queue) {
+    if ((small_only || aged) && !q->small) continue;
+    if (done < q->retry_after) continue;
+    if (!(s->running == 0 && !aged) && !fits(s, q, reserve)) continue;
+    if (!best || q->cost < best->cost || (q->cost == best->cost && q->ticket < best->ticket)) best = q;
+  }
+  return best;
+}
+
+void remove_queued(pk_server* s, Request* q) {
+  s->queue.erase(std::find(s->queue.begin(), s->queue.end(), q));
+  s->st.queued = s->queue.size();
+}
+
 void finish(pk_server* s, Request* q, pk_status status, const pk_summary& sum, const std::string& err) {
   std::lock_guard<std::mutex> lk(s->mu);
   q->info.status = status;
@@ -138,58 +209,99 @@ void finish(pk_server* s, Request* q, pk_status status, const pk_summary& sum, c
   s->running--;
   s->st.running = (uint64_t)s->running;
   s->st.admitted_bytes -= q->footprint;
-  if (status == PK_OK) s->st.completed++; else s->st.failed++;
+  if (q->job) {
+    s->st.resident_bytes += q->resident;
+    s->st.resident_jobs++;
+  }
+  if (status == PK_OK) s->st.completed++;
+  else if (status == PK_ERR_CANCELLED) s->st.cancelled++;
+  else s->st.failed++;
+  s->events++;
   s->cv_done.notify_all();
   s->cv_work.notify_all();
 }
 
-void worker_main(pk_server* s) {
-  pk_job* job = nullptr;
-  pk_status cs = pk_job_create(s->ctx, nullptr, &job);
+bool cancelled(pk_server* s, Request* q) {
+  std::lock_guard<std::mutex> lk(s->mu);
+  return q->cancel;
+}
+
+// count -> cutoff -> macro-nodes of one request on `job`, ending early when it is
+// cancelled at a stage boundary
+pk_status run_request(pk_server* s, Request* q, pk_job* job, pk_summary* sum) {
+  const pk_params& p = q->req.params;
+  pk_status r = pk_count(job, q->req.fasta, q->req.fasta_bytes, &p);
+  if (r != PK_OK) return r;
+  if (cancelled(s, q)) return pk::set_error(PK_ERR_CANCELLED, "cancelled after counting");
+  uint32_t cut = 0;
+  uint64_t kept = 0;
+  r = pk_cutoff(job, p.num_buckets, &cut, nullptr, &kept);
+  if (r != PK_OK) {
+    pk_summary_get(job, sum);
+    return r;
+  }
+  if (cancelled(s, q)) return pk::set_error(PK_ERR_CANCELLED, "cancelled after the histogram cutoff");
+  uint64_t m = 0;
+  r = pk_build_macro_nodes(job, 0, &m);
+  if (r != PK_OK) return r;
+  return pk_summary_get(job, sum);
+}
+
+void worker_main(pk_server* s, bool small_only) {
+  // two jobs: small requests on a high-priority stream, the rest on a low-priority one
+  int least = 0, greatest = 0;
+  cudaSetDevice(s->ctx->device);
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  cudaStream_t st_hi = nullptr, st_lo = nullptr;
+  cudaStreamCreateWithPriority(&st_hi, cudaStreamNonBlocking, greatest);
+  cudaStreamCreateWithPriority(&st_lo, cudaStreamNonBlocking, least);
+  pk_job* job_hi = nullptr;
+  pk_job* job_lo = nullptr;
+  pk_status cs = pk_job_create(s->ctx, st_hi, &job_hi);
+  if (cs == PK_OK) cs = pk_job_create(s->ctx, st_lo, &job_lo);
+  const std::string cs_msg = cs == PK_OK ? std::string() : std::string(pk_last_error());
   while (true) {
     Request* q = nullptr;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      // FIFO: only the head may start, and only when its estimate fits the budget
-      // (or nothing else is running, so an oversized job still gets its chance)
       s->cv_work.wait(lk, [&] {
         if (s->stop) return true;
-        if (s->queue.empty()) return false;
-        const Request* h = s->queue.front();
-        if (s->running == 0) return true;
-        if (s->st.completed + s->st.failed < h->retry_after) return false;
-        return s->budget == 0 || s->st.admitted_bytes + h->footprint <= s->budget;
+        q = s->queue.empty() ? nullptr : pick(s, small_only);
+        return q != nullptr;
       });
       if (s->stop) break;
-      q = s->queue.front();
-      s->queue.pop_front();
+      remove_queued(s, q);
       s->running++;
       s->st.running = (uint64_t)s->running;
-      s->st.queued = s->queue.size();
       s->st.admitted_bytes += q->footprint;
-      if (s->st.admitted_bytes > s->st.peak_admitted_bytes) s->st.peak_admitted_bytes = s->st.admitted_bytes;
+      const uint64_t occ = s->st.admitted_bytes + s->st.resident_bytes;
+      if (occ > s->st.peak_admitted_bytes) s->st.peak_admitted_bytes = occ;
       if (q->info.start_ns == 0) q->info.start_ns = now_ns();
       q->info.attempts++;
     }
     pk_summary sum{};
     if (cs != PK_OK) {
-      finish(s, q, cs, sum, "worker could not create its job: " + std::string(pk_last_error()));
+      finish(s, q, cs, sum, "worker could not create its jobs: " + cs_msg);
       continue;
     }
-    pk_status r = pk_run(job, q->req.fasta, q->req.fasta_bytes, &q->req.params, &sum);
+    pk_job*& job = q->small ? job_hi : job_lo;
+    pk_status r = run_request(s, q, job, &sum);
     std::string err = r == PK_OK ? std::string() : std::string(pk_last_error());
     if (r == PK_ERR_NOMEM) {
       pk_job_reset(job);
       std::unique_lock<std::mutex> lk(s->mu);
-      if (s->running > 1) {
-        // others hold memory: back to the head of the queue, started again once
-        // another job has finished
+      if (s->running > 1 || s->st.resident_jobs > 0) {
+        // others hold memory: back to the queue, started again once another request
+        // has finished
         s->running--;
         s->st.running = (uint64_t)s->running;
         s->st.admitted_bytes -= q->footprint;
         s->st.requeued++;
-        q->retry_after = s->st.completed + s->st.failed + 1;
-        s->queue.push_front(q);
+        q->retry_after = s->events + 1;
+        // back in submission order, so it keeps its age
+        auto at = std::lower_bound(s->queue.begin(), s->queue.end(), q,
+                                   [](const Request* a, const Request* b) { return a->ticket < b->ticket; });
+        s->queue.insert(at, q);
         s->st.queued = s->queue.size();
         continue;
       }
@@ -209,7 +321,7 @@ void worker_main(pk_server* s) {
           r = pk_copy_macro_nodes(job, q->req.mn_keys, q->req.mn_suffix, q->req.mn_prefix, m);
           if (r != PK_OK) err = pk_last_error();
         }
-      } else {
+      } else if (!q->req.keep_on_device) {
         const size_t rows = m ? m : 1;
         q->own_keys = pinned_get(s, rows * W);
         q->own_suf = (uint32_t*)pinned_get(s, rows * 16);
@@ -224,12 +336,34 @@ void worker_main(pk_server* s) {
         }
       }
     }
+    if (r == PK_OK && q->req.keep_on_device) {
+      // the finished job goes to the request, on a stream of its own (its work is
+      // complete); the worker continues with a new job on its stream
+      pk_job* fresh = nullptr;
+      cudaStream_t own = nullptr;
+      if (pk_job_create(s->ctx, job == job_hi ? st_hi : st_lo, &fresh) == PK_OK &&
+          cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking) == cudaSuccess) {
+        job->stream = own;
+        job->own_stream = true;
+        pk_job_memory(job, &q->resident);
+        q->job = job;
+        job = fresh;
+      } else {
+        if (fresh) pk_job_destroy(fresh);
+        cudaGetLastError();
+        r = PK_ERR_NOMEM;
+        err = "a job for the next request";
+      }
+    }
     // the job's device buffers go back to the context's pool, so the budget
-    // accounting follows the running jobs only
-    pk_job_reset(job);
+    // accounting follows the running jobs (and the results kept on the device) only
+    if (job != q->job) pk_job_reset(job);
     finish(s, q, r, sum, err);
   }
-  if (job) pk_job_destroy(job);
+  if (job_hi) pk_job_destroy(job_hi);
+  if (job_lo) pk_job_destroy(job_lo);
+  if (st_hi) cudaStreamDestroy(st_hi);
+  if (st_lo) cudaStreamDestroy(st_lo);
 }
 
 // called with s->mu held
@@ -237,6 +371,11 @@ void free_request(pk_server* s, Request* q) {
   pinned_put(s, q->own_keys);
   pinned_put(s, q->own_suf);
   pinned_put(s, q->own_pre);
+  if (q->job) {
+    pk_job_destroy(q->job);
+    s->st.resident_bytes -= q->resident;
+    s->st.resident_jobs--;
+  }
   delete q;
 }
 
@@ -251,18 +390,37 @@ extern "C" {
 
 uint64_t pk_request_footprint(const pk_request* req) { return req ? footprint(*req) : 0; }
 
-pk_status pk_server_create(pk_ctx* ctx, int32_t workers, pk_server** out) {
+void pk_server_config_default(pk_server_config* c, int32_t workers) {
+  if (!c) return;
+  memset(c, 0, sizeof(*c));
+  c->small_bytes = 32ull << 20;
+  c->reserved_small = workers >= 4 ? workers / 4 : (workers >= 2 ? 1 : 0);
+  c->aging_ms = 2000;
+}
+
+pk_status pk_server_create_config(pk_ctx* ctx, int32_t workers, const pk_server_config* cfg, pk_server** out) {
   if (!ctx || !out) return pk::set_error(PK_ERR_INVALID, "ctx and out must not be null");
   if (workers < 1 || workers > 64) return pk::set_error(PK_ERR_INVALID, "workers must be in 1..64");
+  pk_server_config c;
+  pk_server_config_default(&c, workers);
+  if (cfg) c = *cfg;
+  if (c.reserved_small < 0 || c.reserved_small >= workers)
+    return pk::set_error(PK_ERR_INVALID, "reserved_small must be in 0..workers-1");
   uint64_t used = 0, budget = 0;
   pk_status st = pk_ctx_memory(ctx, &used, &budget);
   if (st != PK_OK) return st;
   pk_server* s = new pk_server();
   s->ctx = ctx;
   s->budget = budget;
-  for (int i = 0; i < workers; i++) s->threads.emplace_back(worker_main, s);
+  s->workers = workers;
+  s->cfg = c;
+  for (int i = 0; i < workers; i++) s->threads.emplace_back(worker_main, s, i < c.reserved_small);
   *out = s;
   return PK_OK;
+}
+
+pk_status pk_server_create(pk_ctx* ctx, int32_t workers, pk_server** out) {
+  return pk_server_create_config(ctx, workers, nullptr, out);
 }
 
 void pk_server_destroy(pk_server* s) {
@@ -270,6 +428,7 @@ void pk_server_destroy(pk_server* s) {
   {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
+    for (auto& kv : s->reqs) kv.second->cancel = true;
     s->cv_work.notify_all();
     s->cv_done.notify_all();
   }
@@ -285,6 +444,7 @@ pk_status pk_submit(pk_server* s, const pk_request* req, uint64_t* ticket) {
   Request* q = new Request();
   q->req = *req;
   q->footprint = footprint(*req);
+  q->cost = cost_of(*req);
   q->info.submit_ns = now_ns();
   q->info.status = PK_ERR_BUSY;
   std::lock_guard<std::mutex> lk(s->mu);
@@ -292,6 +452,7 @@ pk_status pk_submit(pk_server* s, const pk_request* req, uint64_t* ticket) {
     delete q;
     return pk::set_error(PK_ERR_STATE, "server is shutting down");
   }
+  q->small = q->cost <= s->cfg.small_bytes;
   q->ticket = s->next_ticket++;
   s->reqs[q->ticket] = q;
   s->queue.push_back(q);
@@ -299,6 +460,27 @@ pk_status pk_submit(pk_server* s, const pk_request* req, uint64_t* ticket) {
   s->st.queued = s->queue.size();
   *ticket = q->ticket;
   s->cv_work.notify_all();
+  return PK_OK;
+}
+
+pk_status pk_cancel(pk_server* s, uint64_t ticket) {
+  if (!s) return pk::set_error(PK_ERR_INVALID, "server is null");
+  std::lock_guard<std::mutex> lk(s->mu);
+  Request* q = find(s, ticket);
+  if (!q) return pk::set_error(PK_ERR_INVALID, "unknown ticket");
+  if (q->info.done) return pk::set_error(PK_ERR_STATE, "the request has finished");
+  if (std::find(s->queue.begin(), s->queue.end(), q) != s->queue.end()) {
+    remove_queued(s, q);
+    q->info.status = PK_ERR_CANCELLED;
+    q->info.done = 1;
+    q->info.end_ns = now_ns();
+    q->error = "cancelled while queued";
+    s->st.cancelled++;
+    s->cv_done.notify_all();
+    s->cv_work.notify_all();
+    return PK_OK;
+  }
+  q->cancel = true;  // running: it ends at its next stage boundary
   return PK_OK;
 }
 
@@ -339,11 +521,23 @@ pk_status pk_result_get(pk_server* s, uint64_t ticket, const void** keys, const 
   if (!q) return pk::set_error(PK_ERR_INVALID, "unknown ticket");
   if (!q->info.done) return pk::set_error(PK_ERR_BUSY, "request still queued or running");
   if (q->info.status != PK_OK) return pk::set_error(q->info.status, q->error);
-  if (!q->own_keys) return pk::set_error(PK_ERR_STATE, "the result was written to the caller's buffers");
+  if (!q->own_keys) return pk::set_error(PK_ERR_STATE, "the result is not kept in host memory by the server");
   if (keys) *keys = q->own_keys;
   if (suffix) *suffix = q->own_suf;
   if (prefix) *prefix = q->own_pre;
   if (n_nodes) *n_nodes = q->info.summary.n_nodes;
+  return PK_OK;
+}
+
+pk_status pk_result_job(pk_server* s, uint64_t ticket, pk_job** job) {
+  if (!s || !job) return pk::set_error(PK_ERR_INVALID, "server and job must not be null");
+  std::lock_guard<std::mutex> lk(s->mu);
+  Request* q = find(s, ticket);
+  if (!q) return pk::set_error(PK_ERR_INVALID, "unknown ticket");
+  if (!q->info.done) return pk::set_error(PK_ERR_BUSY, "request still queued or running");
+  if (q->info.status != PK_OK) return pk::set_error(q->info.status, q->error);
+  if (!q->job) return pk::set_error(PK_ERR_STATE, "the request was not submitted with keep_on_device");
+  *job = q->job;
   return PK_OK;
 }
 
@@ -354,7 +548,10 @@ pk_status pk_result_release(pk_server* s, uint64_t ticket) {
   if (!q) return pk::set_error(PK_ERR_INVALID, "unknown ticket");
   if (!q->info.done) return pk::set_error(PK_ERR_BUSY, "request still queued or running");
   s->reqs.erase(ticket);
+  const bool had_job = q->job != nullptr;
   free_request(s, q);
+  if (had_job) s->events++;
+  s->cv_work.notify_all();  // released device memory may admit a waiting request
   return PK_OK;
 }
 

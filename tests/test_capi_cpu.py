@@ -76,9 +76,16 @@ def test_no_cpu_fallback_without_device(lib):
 
 def test_serving_structs_and_footprint(lib):
     # pk_request: pointer, size, 64-byte params, three pointers, capacity
-    assert ctypes.sizeof(capi.PkRequest) == 8 + 8 + 64 + 8 * 3 + 8
+    assert ctypes.sizeof(capi.PkRequest) == 8 + 8 + 64 + 8 * 3 + 8 + 4 * 4
     assert ctypes.sizeof(capi.PkRequestInfo) == 8 + 48 + 8 * 3 + 8
-    assert ctypes.sizeof(capi.PkServerStats) == 64
+    assert ctypes.sizeof(capi.PkServerStats) == 11 * 8
+    assert ctypes.sizeof(capi.PkServerConfig) == 8 + 4 + 4 + 4 * 4
+    cfg = capi.PkServerConfig()
+    lib.pk_server_config_default(ctypes.byref(cfg), 8)
+    assert (cfg.small_bytes, cfg.reserved_small, cfg.aging_ms) == (32 << 20, 2, 2000)
+    assert lib.pk_cancel(None, 1) == capi.PK_ERR_INVALID
+    assert lib.pk_result_job(None, 1, None) == capi.PK_ERR_INVALID
+    assert capi.status_string(capi.PK_ERR_CANCELLED) == "cancelled"
     r = capi.PkRequest()
     r.params = capi.default_params(k=32)
     r.fasta_bytes = 1 << 20

@@ -106,3 +106,90 @@ def test_admission_stays_within_budget():
         assert st["completed"] == len(cases)
         used, _ = c.memory()
         assert used == 0
+
+
+def _sized(seed, glen, nreads, k=32):
+    rs = synth.small_case(seed, genome_len=glen, n_reads=nreads, read_len=100, err=0.005, k=k, coverage=20)
+    return rs.fasta
+
+
+def test_small_requests_overtake_queued_large_ones():
+    """One worker: after the first large request, the queued small ones start before the
+    second large one (least estimated work first), whatever the submission order."""
+    large = [_sized(9300 + i, 400000, 160000) for i in range(2)]
+    small = [_sized(9310 + i, 3000, 900) for i in range(4)]
+    p = _params(32, 21, 20)
+    with pk.Server(ctx(), workers=1, reserved_small=0) as srv:
+        tl = [srv.submit(f, p) for f in large]
+        ts = [srv.submit(f, p) for f in small]
+        infos = {t: srv.wait(t) for t in tl + ts}
+    assert max(infos[t].end_ns for t in ts) < infos[tl[1]].end_ns
+    assert infos[tl[0]].start_ns < min(infos[t].start_ns for t in ts)
+
+
+def test_aging_zero_serves_in_submission_order():
+    """An aging bound of 0 ms makes every queued request the oldest first: plain FIFO."""
+    fs = [_sized(9320 + i, 3000 + 4000 * (i % 3), 900 + 1200 * (i % 3)) for i in range(6)]
+    p = _params(32, 21, 20)
+    with pk.Server(ctx(), workers=1, reserved_small=0, aging_ms=0) as srv:
+        ts = [srv.submit(f, p) for f in reversed(fs)]
+        infos = [srv.wait(t) for t in ts]
+    starts = [i.start_ns for i in infos]
+    assert starts == sorted(starts)
+
+
+def test_cancel_queued_and_running_requests():
+    large = _sized(9330, 400000, 160000)
+    small = [_sized(9331 + i, 3000, 900) for i in range(3)]
+    p = _params(32, 21, 20)
+    ref = [run_gpu(f, 32, 21, 20)[0] for f in small]
+    with pk.Server(ctx(), workers=1, reserved_small=0) as srv:
+        t_run = srv.submit(large, p)
+        t_q = [srv.submit(f, p) for f in small]
+        srv.cancel(t_q[1])  # still queued behind the running large request
+        info = srv.poll(t_q[1])
+        assert info.done and info.status == pk.capi.PK_ERR_CANCELLED
+        with pytest.raises(pk.capi.Cancelled):
+            srv.wait(t_q[1])
+        srv.cancel(t_run)  # running: ends at its next stage boundary (or has finished)
+        try:
+            srv.wait(t_run)
+        except pk.capi.Cancelled:
+            pass
+        assert srv.poll(t_run).status in (0, pk.capi.PK_ERR_CANCELLED)
+        for i in (0, 2):
+            assert srv.wait(t_q[i]).summary.n_nodes == ref[i].n_nodes
+        with pytest.raises(pk.PakmanError) as e:
+            srv.cancel(t_q[0])  # finished
+        assert e.value.status == pk.capi.PK_ERR_STATE
+        st = srv.stats()
+        assert st["cancelled"] >= 1 and st["completed"] >= 2
+
+
+def test_keep_on_device_hands_over_the_resident_job():
+    """A keep_on_device request leaves its table and macro-nodes in HBM for further
+    calls on the returned job (here the table and a compaction), counted against the
+    budget until released."""
+    f, k, t, cov = _mix()[0]
+    s, keys, counts, hist, mn, err = run_gpu(f, k, t, cov)
+    with pk.Context(0) as c, pk.Server(c, workers=2) as srv:
+        tk = srv.submit(f, _params(k, t, cov), keep_on_device=True)
+        info = srv.wait(tk)
+        assert info.summary.n_nodes == s.n_nodes
+        st = srv.stats()
+        assert st["resident_jobs"] == 1 and st["resident_bytes"] > 0
+        used, _ = c.memory()
+        assert used >= st["resident_bytes"]
+        job = srv.job(tk)
+        k2, c2 = job.table()
+        assert np.array_equal(pk.to_key128(k2), keys) and np.array_equal(c2, counts)
+        got = job.macro_nodes(cov)
+        assert_mn_equal(got, pk.to_key128(mn.keys), mn.suffix_counts, mn.prefix_counts)
+        comp = job.compact(1000, cov)
+        assert comp.n_nodes <= 1000
+        with pytest.raises(pk.PakmanError):
+            srv.result(tk)  # not kept in host memory
+        srv.release(tk)
+        st = srv.stats()
+        assert st["resident_jobs"] == 0 and st["resident_bytes"] == 0
+    # another request still runs normally on the same server afterwards is covered above
