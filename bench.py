@@ -476,7 +476,6 @@ def run_serve(args, rank, world):
         th = threading.Thread(target=producer, daemon=True)
         th.start()
         lat, ratio, first_submit, last_end, windows, mismatches = [], [], None, 0, 0, 0
-        checked, table_mismatch = set(), 0
         for i, e in enumerate(entries):
             ready.acquire()
             try:
@@ -490,11 +489,6 @@ def run_serve(args, rank, world):
                     ref.n_windows, ref.n_unique, ref.n_kept, ref.cutoff) or (
                     ref_status == 0 and s.n_nodes != ref.n_nodes):
                 mismatches += 1
-            if e not in checked and info.status == 0:
-                checked.add(e)
-                mn = srv.result(tickets[i])
-                if _mn_digest(mn.keys, mn.suffix_counts, mn.prefix_counts) != alone_digest[e]:
-                    table_mismatch += 1
             srv.release(tickets[i])
             lat.append(info.latency_ms)
             ratio.append(info.latency_ms / solo[e])
@@ -513,9 +507,28 @@ def run_serve(args, rank, world):
                 "jobs_within_2x_solo": float((ratio <= 2.0).mean()),
                 "kmers_per_s": windows / span, "span_s": span,
                 "peak_admitted_gb": st["peak_admitted_bytes"] / 1e9, "requeued": st["requeued"],
-                "results_differing_from_alone": mismatches,
-                "macro_node_tables_checked": len(checked), "macro_node_tables_differing": table_mismatch}
+                "results_differing_from_alone": mismatches}
 
+    def tables_in_the_mix():
+        """Every pool entry served among the others (all submitted at once, twice over)
+        gives the macro-node table of the entry run alone, byte for byte."""
+        srv = pk.Server(ctx, workers=args.serve_workers)
+        order = list(range(len(pool))) * 2
+        tickets = [srv.submit(pinned[e].numpy(), params[e]) for e in order]
+        differing = 0
+        for tk, e in zip(tickets, order):
+            try:
+                srv.wait(tk)
+                mn = srv.result(tk)
+                d = _mn_digest(mn.keys, mn.suffix_counts, mn.prefix_counts)
+            except pk.EmptyAfterCutoff:
+                d = None
+            differing += d != alone_digest[e]
+            srv.release(tk)
+        srv.close()
+        return {"jobs": len(order), "macro_node_tables_differing": differing}
+
+    mix_check = tables_in_the_mix()
     served = serve(args.serve_workers, arrivals)
     plain = serve(1, arrivals)
     at_once = np.zeros(args.serve_jobs)
@@ -538,13 +551,14 @@ def run_serve(args, rank, world):
             "oracle": {"entries_equal": sum(oracle_ok), "entries": len(oracle_ok), "seconds": t_ora,
                        "against": "table, cutoff and macro-nodes of every pool entry against the oracle's "
                                   f"threaded restatement ({threads} threads)"},
+            "tables_in_the_mix": mix_check,
             "served": served, "plain_one_job_at_a_time": plain,
             "saturation": {"served": served_sat, "plain_one_job_at_a_time": plain_sat,
                            "capacity_ratio": served_sat["kmers_per_s"] / plain_sat["kmers_per_s"]}}
     print(json.dumps(line), flush=True)
     ctx.close()
-    bad = sum(not x for x in oracle_ok) + sum(r["results_differing_from_alone"] + r["macro_node_tables_differing"]
-                                            for r in (served, plain, served_sat, plain_sat))
+    bad = sum(not x for x in oracle_ok) + mix_check["macro_node_tables_differing"] + sum(
+        r["results_differing_from_alone"] for r in (served, plain, served_sat, plain_sat))
     if bad:
         print("bench: served results differ from the oracle or from the jobs run alone", file=sys.stderr)
         return 3

@@ -354,7 +354,7 @@ uint64_t pk_kernel_launches(void);
  * Scheduling: the queued request with the least estimated work (FASTA bytes, doubled
  * for k > 32) starts first, so small requests are not queued behind large ones; a
  * request that has waited longer than aging_ms starts first regardless of size (while
- * it does not fit the budget only small requests start, in the memory it leaves).
+ * it does not fit the budget, others start only in the memory it leaves).
  * Requests of at most small_bytes are small: reserved_small workers take only small
  * requests, and small requests run on high-priority CUDA streams.
  * Admission: a request starts only when the estimate of its device footprint, added to
@@ -409,7 +409,7 @@ typedef struct pk_server_stats {
 
 typedef struct pk_server_config {
   uint64_t small_bytes;    /* requests of at most this estimated work are small (32 MiB) */
-  int32_t reserved_small;  /* workers that take only small requests (workers / 4) */
+  int32_t reserved_small;  /* workers that take only small requests (one in eight) */
   int32_t aging_ms;        /* a request waiting longer starts first (2000) */
   int32_t reserved[4];
 } pk_server_config;
@@ -442,7 +442,9 @@ pk_status pk_result_job(pk_server* s, uint64_t ticket, pk_job** job);
  * kept job's device memory). */
 pk_status pk_result_release(pk_server* s, uint64_t ticket);
 pk_status pk_server_get_stats(pk_server* s, pk_server_stats* out);
-/* Device footprint the admission control assumes for a request (bytes). */
+/* Device footprint the admission control assumes for a request (bytes): the FASTA,
+ * keys and counts over the k-mer windows estimated from the first 256 KiB of the input,
+ * kept rows and macro-nodes for one kept k-mer in twelve windows. */
 uint64_t pk_request_footprint(const pk_request* req);
 
 /* ---- Batching: many independent read sets in one CUDA-graph launch ----------------

@@ -10,8 +10,8 @@
 // the request with the least estimated work (FASTA bytes, doubled for 128-bit keys), so
 // a small request is never queued behind a large one.  A request that has waited longer
 // than the aging bound goes first regardless of size, and while it does not fit the
-// HBM budget no other large request is admitted, so memory drains for it and large
-// requests cannot starve.  Requests up to `small_bytes` are small: some workers
+// HBM budget others start only in the memory it leaves, so memory drains for it and
+// large requests cannot starve.  Requests up to `small_bytes` are small: some workers
 // (`reserved_small`) take only small requests, so a burst of large ones never occupies
 // every worker, and small requests run on high-priority CUDA streams (the GPU's block
 // scheduler starts their blocks ahead of the large requests' pending blocks).
@@ -93,16 +93,41 @@ struct pk_server {
 
 namespace {
 
-// Device bytes a request may need: the FASTA, two key arrays and the count array
-// over N windows, kept rows and the macro-node arrays over V kept k-mers.  N is
-// bounded by the FASTA size (a window needs at least one byte); V, the k-mers at or
-// above the cutoff, is taken as N / 8 (a read set whose kept k-mers exceed that still
-// runs exactly, through the allocator's own budget check and a retry).
+// k-mer windows in a FASTA buffer, estimated from its first 256 KiB: lines alternate
+// header / sequence from the first '>', and a sequence line of L bytes holds L - k + 1
+// windows.  The count is scaled to the whole buffer with 5 % to spare; a buffer whose
+// later records are denser than its first ones still runs exactly, through the
+// allocator's own budget check and a retry.  Without a complete record in the sample
+// the bound N <= F (a window needs at least one byte) is used.
+uint64_t estimate_windows(const pk_request& r) {
+  const uint64_t F = r.fasta_bytes;
+  const uint64_t S = std::min<uint64_t>(F, 256ull << 10);
+  const char* b = r.fasta;
+  uint64_t p = 0, w = 0, end = 0;
+  while (p < S && b[p] != '>') p++;
+  bool seq = false;
+  while (p < S) {
+    const void* q = memchr(b + p, '\n', (size_t)(S - p));
+    if (!q) break;
+    const uint64_t e = (uint64_t)(static_cast<const char*>(q) - b);
+    if (seq && e - p >= (uint64_t)r.params.k) w += e - p - (uint64_t)r.params.k + 1;
+    seq = !seq;
+    p = e + 1;
+    if (!seq) end = p;  // a record ends here
+  }
+  if (end == 0 || S == F) return end == 0 ? F : w;
+  return std::min<uint64_t>(F, (uint64_t)((double)w / (double)end * (double)F * 1.05) + 1);
+}
+
+// Device bytes a request may need: the FASTA, two key arrays and the count array over
+// N windows, kept rows and the macro-node arrays over V kept k-mers.  V, the k-mers at
+// or above the cutoff, is taken as N / 12: read sets at 20x coverage or more keep about
+// one k-mer per genome position, one in 14 to 55 windows at 30-80x.
 uint64_t footprint(const pk_request& r) {
   const uint64_t F = r.fasta_bytes;
   const uint64_t W = r.params.k > 32 ? 16 : 8;
-  const uint64_t N = F;
-  const uint64_t V = N / 8;
+  const uint64_t N = r.fasta ? estimate_windows(r) : F;
+  const uint64_t V = N / 12;
   const uint64_t fixed = 64ull << 20;  // per-bucket tables, histograms, look-back flags
   return F + N * (2 * W + 4) + V * (W + 4) + 2 * V * (W + 32) + fixed;
 }
@@ -180,13 +205,12 @@ Request* pick(pk_server* s, bool small_only) {
   if (aged) {
     const bool mine = !small_only || aged->small;
     if (mine && (s->running == 0 || fits(s, aged, 0))) return aged;
-    // memory drains for it: meanwhile only small requests start, and only into the
-    // memory it leaves
+    // memory drains for it: meanwhile others start only in the memory it leaves
     if (!fits(s, aged, 0)) reserve = aged->footprint;
   }
   Request* best = nullptr;
   for (Request* q : s->queue) {
-    if ((small_only || aged) && !q->small) continue;
+    if (small_only && !q->small) continue;
     if (done < q->retry_after) continue;
     if (!(s->running == 0 && !aged) && !fits(s, q, reserve)) continue;
     if (!best || q->cost < best->cost || (q->cost == best->cost && q->ticket < best->ticket)) best = q;
@@ -226,25 +250,36 @@ bool cancelled(pk_server* s, Request* q) {
   return q->cancel;
 }
 
-// count -> cutoff -> macro-nodes of one request on `job`, ending early when it is
+void summary_of(const pk_job* j, pk_summary* o) {
+  const pk::Scalars& h = *j->h_sc;
+  o->n_reads = h.n_reads;
+  o->n_windows = h.n_windows;
+  o->n_unique = j->stage >= 1 ? h.n_unique : 0;
+  o->n_kept = j->stage >= 2 ? h.n_kept : 0;
+  o->n_nodes = j->stage >= 3 ? h.n_nodes : 0;
+  o->cutoff = j->stage >= 2 ? h.cutoff : 0;
+  o->key_bytes = j->wide ? 16 : 8;
+}
+
+// count -> cutoff -> macro-nodes of one request on `job` (the stages of pk_run, with one
+// host synchronisation after the cutoff and one at the end), ending early when it is
 // cancelled at a stage boundary
 pk_status run_request(pk_server* s, Request* q, pk_job* job, pk_summary* sum) {
   const pk_params& p = q->req.params;
   pk_status r = pk_count(job, q->req.fasta, q->req.fasta_bytes, &p);
   if (r != PK_OK) return r;
   if (cancelled(s, q)) return pk::set_error(PK_ERR_CANCELLED, "cancelled after counting");
-  uint32_t cut = 0;
-  uint64_t kept = 0;
-  r = pk_cutoff(job, p.num_buckets, &cut, nullptr, &kept);
-  if (r != PK_OK) {
-    pk_summary_get(job, sum);
-    return r;
-  }
+  PK_TRY(pk::cutoff_enqueue(job, p.num_buckets));
+  PK_TRY(pk::sync_scalars(job));
+  summary_of(job, sum);
+  if (job->h_sc->n_kept == 0)
+    return pk::set_error(PK_ERR_EMPTY, "no k-mer reaches the cutoff " + std::to_string(job->h_sc->cutoff) +
+                                           "; macro-node construction cannot proceed");
   if (cancelled(s, q)) return pk::set_error(PK_ERR_CANCELLED, "cancelled after the histogram cutoff");
-  uint64_t m = 0;
-  r = pk_build_macro_nodes(job, 0, &m);
-  if (r != PK_OK) return r;
-  return pk_summary_get(job, sum);
+  PK_TRY(pk::mn_enqueue(job, 0, job->h_sc->n_kept));
+  PK_TRY(pk::sync_scalars(job));
+  summary_of(job, sum);
+  return PK_OK;
 }
 
 void worker_main(pk_server* s, bool small_only) {
@@ -394,7 +429,7 @@ void pk_server_config_default(pk_server_config* c, int32_t workers) {
   if (!c) return;
   memset(c, 0, sizeof(*c));
   c->small_bytes = 32ull << 20;
-  c->reserved_small = workers >= 4 ? workers / 4 : (workers >= 2 ? 1 : 0);
+  c->reserved_small = workers >= 2 ? (workers + 7) / 8 : 0;
   c->aging_ms = 2000;
 }
 

@@ -82,7 +82,7 @@ def test_serving_structs_and_footprint(lib):
     assert ctypes.sizeof(capi.PkServerConfig) == 8 + 4 + 4 + 4 * 4
     cfg = capi.PkServerConfig()
     lib.pk_server_config_default(ctypes.byref(cfg), 8)
-    assert (cfg.small_bytes, cfg.reserved_small, cfg.aging_ms) == (32 << 20, 2, 2000)
+    assert (cfg.small_bytes, cfg.reserved_small, cfg.aging_ms) == (32 << 20, 1, 2000)
     assert lib.pk_cancel(None, 1) == capi.PK_ERR_INVALID
     assert lib.pk_result_job(None, 1, None) == capi.PK_ERR_INVALID
     assert capi.status_string(capi.PK_ERR_CANCELLED) == "cancelled"
@@ -97,6 +97,19 @@ def test_serving_structs_and_footprint(lib):
     assert small < big < wide
     assert big >= (1 << 24) * (1 + 2 * 8 + 4)  # FASTA + two key arrays + counts at N = F
     assert lib.pk_request_footprint(None) == 0
+    # with the input at hand the window count is estimated from its first records
+    reads = b"".join(b">r%d\n" % i + b"ACGT" * 25 + b"\n" for i in range(20000))
+    buf = ctypes.create_string_buffer(reads, len(reads))
+    r = capi.PkRequest()
+    r.params = capi.default_params(k=32)
+    r.fasta = ctypes.cast(buf, ctypes.c_void_p)
+    r.fasta_bytes = len(reads)
+    sampled = lib.pk_request_footprint(ctypes.byref(r))
+    r.fasta = None
+    bound = lib.pk_request_footprint(ctypes.byref(r))
+    windows = 20000 * 69
+    assert sampled < bound
+    assert sampled >= len(reads) + windows * (2 * 8 + 4)
     assert lib.pk_server_create(None, 2, None) == capi.PK_ERR_INVALID
     assert lib.pk_submit(None, None, None) == capi.PK_ERR_INVALID
 

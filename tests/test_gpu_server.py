@@ -118,7 +118,7 @@ def test_small_requests_overtake_queued_large_ones():
     second large one (least estimated work first), whatever the submission order."""
     large = [_sized(9300 + i, 400000, 160000) for i in range(2)]
     small = [_sized(9310 + i, 3000, 900) for i in range(4)]
-    p = _params(32, 21, 20)
+    p = _params(32, 5, 20)
     with pk.Server(ctx(), workers=1, reserved_small=0) as srv:
         tl = [srv.submit(f, p) for f in large]
         ts = [srv.submit(f, p) for f in small]
@@ -130,7 +130,7 @@ def test_small_requests_overtake_queued_large_ones():
 def test_aging_zero_serves_in_submission_order():
     """An aging bound of 0 ms makes every queued request the oldest first: plain FIFO."""
     fs = [_sized(9320 + i, 3000 + 4000 * (i % 3), 900 + 1200 * (i % 3)) for i in range(6)]
-    p = _params(32, 21, 20)
+    p = _params(32, 5, 20)
     with pk.Server(ctx(), workers=1, reserved_small=0, aging_ms=0) as srv:
         ts = [srv.submit(f, p) for f in reversed(fs)]
         infos = [srv.wait(t) for t in ts]
@@ -141,8 +141,8 @@ def test_aging_zero_serves_in_submission_order():
 def test_cancel_queued_and_running_requests():
     large = _sized(9330, 400000, 160000)
     small = [_sized(9331 + i, 3000, 900) for i in range(3)]
-    p = _params(32, 21, 20)
-    ref = [run_gpu(f, 32, 21, 20)[0] for f in small]
+    p = _params(32, 5, 20)
+    ref = [run_gpu(f, 32, 5, 20)[0] for f in small]
     with pk.Server(ctx(), workers=1, reserved_small=0) as srv:
         t_run = srv.submit(large, p)
         t_q = [srv.submit(f, p) for f in small]
