@@ -91,14 +91,7 @@ typedef struct pk_params {
                            batch_kmers k-mer windows each) whose tables are merged on the
                            device; 1 = always in such pieces; 2 = never.  The table is the
                            same for any piece size, as the reference's is for any -b. */
-  int32_t sample_stride; /* coarse regions of the key partition: 0 = automatic -- inputs of
-                           64 MiB or more with partitions of 8 to 14 digits size them from a
-                           sample of every (tiles / 256)-th 64 KiB tile instead of an exact
-                           counting pass, and fall back to that pass when a region outgrows
-                           its sampled size; -1 = always the exact counting pass; n > 0 = a
-                           sample of every n-th tile wherever the partition allows.  The
-                           table is the same either way. */
-  int32_t reserved[4];
+  int32_t reserved[5];
 } pk_params;
 
 /* Counts reported by a run. */
@@ -143,10 +136,6 @@ pk_status pk_table_info(pk_job* job, uint64_t* n_unique, uint64_t* n_windows, ui
  * was counted in -b pieces (the reference's batch flush, src/kmer_counting.cpp:3022-3139)
  * and their tables merged. */
 pk_status pk_count_pieces(pk_job* job, uint32_t* pieces);
-/* How the last count partitioned its keys: the partition digits, whether the coarse
- * regions were sized from a sample (pk_params.sample_stride), and whether a region
- * outgrew its sampled size so that the exact counting pass ran instead. */
-pk_status pk_partition_info(pk_job* job, int32_t* bucket_bits, int32_t* sampled, int32_t* fell_back);
 
 /* ---- file ingest: replaces perform_input_reading ----------------------------------
  * The slice of a FASTA file that MPI rank `rank` of `n_ranks` reads in the reference

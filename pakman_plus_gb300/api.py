@@ -17,7 +17,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import byref, c_float, c_int, c_int32, c_uint32, c_uint64, c_void_p
+from ctypes import byref, c_float, c_int, c_uint32, c_uint64, c_void_p
 from dataclasses import dataclass
 from typing import Dict, List, Optional, Tuple
 
@@ -274,13 +274,6 @@ class Job:
         counts = np.ascontiguousarray(counts, dtype=np.uint32)
         check(capi.lib().pk_table_load(self._h, keys.ctypes.data, counts.ctypes.data, counts.size,
                                        byref(params)), "pk_table_load")
-
-    def partition_info(self) -> Tuple[int, bool, bool]:
-        """(partition digits, coarse regions sized from a sample, fell back to the exact
-        counting pass) of the last count."""
-        b, s, f = c_int32(), c_int32(), c_int32()
-        check(capi.lib().pk_partition_info(self._h, byref(b), byref(s), byref(f)), "pk_partition_info")
-        return b.value, bool(s.value), bool(f.value)
 
     def table_info(self) -> Tuple[int, int, int]:
         u, w, r = c_uint64(), c_uint64(), c_uint64()

@@ -34,8 +34,7 @@ class PkParams(ctypes.Structure):
     _fields_ = [("k", c_int32), ("lmer_length", c_int32), ("num_buckets", c_int32),
                 ("coverage", c_int32), ("read_length", c_int32), ("drop_n", c_int32),
                 ("batch_kmers", c_uint64), ("bucket_bits", c_int32), ("mn_units", c_int32),
-                ("chunking", c_int32), ("sample_stride", c_int32),
-                ("reserved", c_int32 * 4)]
+                ("chunking", c_int32), ("reserved", c_int32 * 5)]
 
 
 class PkSummary(ctypes.Structure):
@@ -159,7 +158,6 @@ _SIGS = {
     "pk_table_load": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64, POINTER(PkParams)]),
     "pk_table_info": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64)]),
     "pk_count_pieces": (c_int, [c_void_p, POINTER(c_uint32)]),
-    "pk_partition_info": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_int32), POINTER(c_int32)]),
     "pk_copy_table": (c_int, [c_void_p, c_void_p, c_void_p, c_uint64]),
     "pk_copy_table_packed": (c_int, [c_void_p, c_void_p, c_uint64]),
     "pk_table_device": (c_int, [c_void_p, POINTER(c_void_p), POINTER(c_void_p)]),

@@ -82,8 +82,7 @@ int pk::job_buffers(pk_job* j, DevBuf** out, int cap) {
                    &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring,
                    &j->gfirst, &j->gcount, &j->chunk_bucket, &j->gdone,
                    &j->chunk_u, &j->acc_keys[0], &j->acc_keys[1], &j->acc_counts[0], &j->acc_counts[1],
-                   &j->merge_keys, &j->merge_counts, &j->merge_part, &j->rstart, &j->rcap, &j->gcur,
-                   &j->cend, &j->fcount};
+                   &j->merge_keys, &j->merge_counts, &j->merge_part};
   const int n = (int)(sizeof(all) / sizeof(all[0]));
   for (int i = 0; i < n && i < cap; i++) out[i] = all[i];
   return n;
@@ -278,15 +277,6 @@ pk_status pk_job_memory(pk_job* j, uint64_t* bytes) {
   return PK_OK;
 }
 
-pk_status pk_partition_info(pk_job* j, int32_t* bucket_bits, int32_t* sampled, int32_t* fell_back) {
-  if (!j) return fail(PK_ERR_INVALID, "job is null");
-  if (j->stage < 1) return fail(PK_ERR_STATE, "no table: call pk_count first");
-  if (bucket_bits) *bucket_bits = j->bbits;
-  if (sampled) *sampled = j->sampled ? 1 : 0;
-  if (fell_back) *fell_back = j->resampled ? 1 : 0;
-  return PK_OK;
-}
-
 pk_status pk_job_set_wait_limit(pk_job* j, uint32_t spins, int32_t withhold_unit) {
   if (!j) return fail(PK_ERR_INVALID, "job is null");
   if (spins > (1u << 30)) return fail(PK_ERR_INVALID, "spins must be at most 2^30");
@@ -333,7 +323,6 @@ pk_status pk::check_params(const pk_params* p) {
   if (p->num_buckets < 1) return fail(PK_ERR_INVALID, "num_buckets (-t) must be >= 1");
   if (p->mn_units < 0 || p->mn_units > 16) return fail(PK_ERR_INVALID, "mn_units must be in 0..16");
   if (p->chunking < 0 || p->chunking > 2) return fail(PK_ERR_INVALID, "chunking must be 0, 1 or 2");
-  if (p->sample_stride < -1) return fail(PK_ERR_INVALID, "sample_stride must be -1, 0 or positive");
   if (p->bucket_bits < 0 || p->bucket_bits > kMaxPartitionBits)
     return fail(PK_ERR_INVALID, "bucket_bits must be in 0.." + std::to_string(kMaxPartitionBits));
   return PK_OK;
@@ -355,113 +344,6 @@ int pk::auto_bucket_bits(uint64_t F, int k, int wide) {
 }
 
 static pk_status table_impl(pk_job* j, uint64_t N, int t);
-
-// Inputs of at least this many line-scan tiles (64 MiB) use the sampled coarse regions;
-// below, a sample of enough tiles would cost about as much as the counting pass.
-constexpr uint64_t kSampledMinTiles = 1024;
-constexpr int kSampleTiles = 256;  // tiles in the sample
-
-// The partition without the exact counting pass.  Every stride-th 64 KiB tile is counted
-// by coarse region; region capacities are that sample scaled to the input plus a margin
-// (k_region_caps); the coarse scatter reads and decodes the FASTA once, reserves room in
-// each region per flushed run, counts the windows, checks the records and histograms the
-// fine buckets; the fine pass then reads the regions where they ended.  When a region
-// outgrows its capacity (*redo), nothing of the scatter is used and the caller runs the
-// exact counting pass instead.
-static pk_status count_sampled(pk_job* j, CountArgs a, uint64_t n, const pk_params* p, bool* redo) {
-  const int k = p->k;
-  const int W = j->wide ? 16 : 8;
-  const int B = 1 << j->bbits;
-  const int Cn = 1 << a.cbits;
-  const uint64_t ntiles = (n + kTileBytes - 1) / kTileBytes;
-  const int stride = p->sample_stride > 0 ? (int)std::min<uint64_t>((uint64_t)p->sample_stride, std::max<uint64_t>(ntiles, 1))
-                                          : (int)std::max<uint64_t>(1, ntiles / kSampleTiles);
-  const int rows = (int)((ntiles + stride - 1) / stride);
-  *redo = false;
-  // the sample: tiles 0, stride, 2 stride, ... counted by coarse region
-  CountArgs sa = a;
-  sa.bbits = a.cbits;
-  sa.grid = rows;
-  sa.chunk = kTileBytes;
-  sa.tile_stride = stride;
-  PK_TRY(job_alloc(j, j->counts, sizeof(uint32_t) * (size_t)rows * Cn));
-  sa.counts = (uint32_t*)j->counts.p;
-  PK_TRY(job_alloc(j, j->rstart, sizeof(uint32_t) * (Cn + 1)));
-  PK_TRY(job_alloc(j, j->rcap, sizeof(uint32_t) * Cn));
-  PK_TRY(job_alloc(j, j->gcur, sizeof(uint32_t) * Cn));
-  PK_TRY(job_alloc(j, j->cend, sizeof(uint32_t) * Cn));
-  PK_TRY(job_alloc(j, j->fcount, sizeof(uint32_t) * (B + 1)));
-  PK_TRY(job_alloc(j, j->slice_start, sizeof(uint32_t) * (Cn + 1)));
-  mark_begin(j, ST_BUCKET_COUNT);
-  PK_CUDA(launch_bucket_count(sa, j->wide, j->stream));
-  mark_end(j, ST_BUCKET_COUNT);
-  mark_begin(j, ST_OFFSETS);
-  PK_CUDA(launch_region_caps(sa.counts, rows, a.cbits, stride, (uint32_t*)j->rstart.p, (uint32_t*)j->rcap.p,
-                             (uint32_t*)j->gcur.p, j->stream));
-  PK_CUDA(cudaMemsetAsync(j->fcount.p, 0, sizeof(uint32_t) * (B + 1), j->stream));
-  mark_end(j, ST_OFFSETS);
-  // the coarse buffer holds every region at its capacity: a sample of tiles holds at most
-  // their bytes in windows, so the capacities add up to at most 9/8 of (F + one stride of
-  // tiles) plus 4096 keys a region
-  const uint64_t cap = (n + (uint64_t)stride * kTileBytes) / 8 * 9 + 4096ull * Cn + 16;
-  if (cap >= 0xffffffffull) {  // region offsets are 32-bit: the exact pass sizes by N
-    *redo = true;
-    return PK_OK;
-  }
-  PK_TRY(job_alloc(j, j->tkeys, (size_t)W * cap));
-  a.fbits = j->bbits;
-  a.gcur = (uint32_t*)j->gcur.p;
-  a.rstart = (const uint32_t*)j->rstart.p;
-  a.rcap = (const uint32_t*)j->rcap.p;
-  a.fcount = (uint32_t*)j->fcount.p;
-  a.n_keys = cap;
-  mark_begin(j, ST_SCATTER);
-  PK_CUDA(launch_scatter_sampled(a, j->tkeys.p, j->wide, j->stream));
-  mark_end(j, ST_SCATTER);
-  PK_CUDA(launch_region_slices((const uint32_t*)j->rstart.p, (const uint32_t*)j->gcur.p, (const uint32_t*)j->rcap.p,
-                               (uint32_t*)j->cend.p, a.cbits, fine_slice_keys(j->wide, j->bbits - a.cbits),
-                               (uint32_t*)j->slice_start.p, j->stream));
-  PK_CUDA(cudaMemcpyAsync(j->h_sc, j->d_sc, sizeof(Scalars), cudaMemcpyDeviceToHost, j->stream));
-  PK_CUDA(cudaStreamSynchronize(j->stream));
-  if (j->h_sc->err & ERR_FORMAT)
-    return fail(PK_ERR_FORMAT, "a FASTA record start is not '>' (one '>' header line and one "
-                               "sequence line per record expected)");
-  if (j->h_sc->err & ERR_REGION) {
-    // back to the exact counting pass: the windows are counted again, and no error bit
-    // of this attempt may remain
-    PK_CUDA(cudaMemsetAsync(&j->d_sc->n_windows, 0, sizeof(unsigned long long), j->stream));
-    PK_CUDA(cudaMemsetAsync(&j->d_sc->err, 0, sizeof(uint32_t), j->stream));
-    *redo = true;
-    return PK_OK;
-  }
-  const uint64_t N = j->h_sc->n_windows;
-  if (N >= (1ull << 32) - 1)
-    return fail(PK_ERR_LIMIT, "more than 2^32-2 k-mer windows in one job; split the input");
-  j->N = N;
-  j->sampled = true;
-  PK_TRY(job_alloc(j, j->keys, (size_t)W * N));
-  PK_TRY(job_alloc(j, j->tcounts, sizeof(uint32_t) * (N ? N : 1)));
-  PK_TRY(job_alloc(j, j->tu, sizeof(uint32_t) * (size_t)B));
-  PK_TRY(job_alloc(j, j->bstart, sizeof(uint32_t) * (B + 1)));
-  PK_TRY(job_alloc(j, j->fcur, sizeof(uint32_t) * (size_t)B));
-  const int t = p->num_buckets;
-  PK_TRY(job_alloc(j, j->hist, sizeof(unsigned long long) * (size_t)t));
-  PK_CUDA(cudaMemsetAsync(j->hist.p, 0, sizeof(unsigned long long) * (size_t)t, j->stream));
-  j->t_hist = t;
-  j->dense_valid = false;
-  mark_begin(j, ST_SCATTER_FINE);
-  PK_CUDA(cudaMemcpyAsync(j->bstart.p, j->fcount.p, sizeof(uint32_t) * (size_t)B, cudaMemcpyDeviceToDevice,
-                          j->stream));
-  PK_CUDA(launch_prefix((uint32_t*)j->bstart.p, B, j->stream));
-  PK_CUDA(cudaMemcpyAsync(j->fcur.p, j->bstart.p, sizeof(uint32_t) * (size_t)B, cudaMemcpyDeviceToDevice,
-                          j->stream));
-  PK_CUDA(cudaMemsetAsync(&j->d_sc->ticket_fine, 0, sizeof(uint32_t), j->stream));
-  PK_CUDA(launch_scatter_fine(j->tkeys.p, (const uint32_t*)j->rstart.p, (const uint32_t*)j->cend.p,
-                              (const uint32_t*)j->slice_start.p, (uint32_t*)j->fcur.p, j->keys.p, k, j->bbits,
-                              a.cbits, j->wide, &j->d_sc->ticket_fine, N, &j->d_sc->err, j->stream));
-  mark_end(j, ST_SCATTER_FINE);
-  return table_impl(j, N, t);
-}
 
 // Stages 1-5: device FASTA -> sorted (k-mer, count) table, resident.
 pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_params* p) {
@@ -521,17 +403,6 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   if (j->lines_ready) PK_CUDA(launch_tile_prefix(a, j->stream));
   else PK_CUDA(launch_line_scan(a, j->stream));
   mark_end(j, ST_LINES);
-  // large inputs whose partition fits the sampled coarse scatter skip the exact counting
-  // pass (a region that outgrows its sampled capacity sends the job back here)
-  j->sampled = false;
-  j->resampled = false;
-  if (!j->graph_mode && p->sample_stride >= 0 && j->bbits > kCoarseBits && j->bbits <= kSampledMaxBits &&
-      (p->sample_stride > 0 || ntiles >= kSampledMinTiles)) {
-    bool redo = false;
-    PK_TRY(count_sampled(j, a, n, p, &redo));
-    if (!redo) return PK_OK;
-    j->resampled = true;
-  }
   mark_begin(j, ST_BUCKET_COUNT);
   PK_CUDA(launch_bucket_count(a, j->wide, j->stream));
   mark_end(j, ST_BUCKET_COUNT);
@@ -591,9 +462,9 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
     PK_CUDA(cudaMemcpyAsync(j->fcur.p, j->bstart.p, sizeof(uint32_t) * (size_t)B, cudaMemcpyDeviceToDevice,
                             j->stream));
     PK_CUDA(cudaMemsetAsync(&j->d_sc->ticket_fine, 0, sizeof(uint32_t), j->stream));
-    PK_CUDA(launch_scatter_fine(j->tkeys.p, (const uint32_t*)j->cstart.p, (const uint32_t*)j->cstart.p + 1,
-                                (const uint32_t*)j->slice_start.p, (uint32_t*)j->fcur.p, j->keys.p, k, j->bbits,
-                                a.cbits, j->wide, &j->d_sc->ticket_fine, N, &j->d_sc->err, j->stream));
+    PK_CUDA(launch_scatter_fine(j->tkeys.p, (const uint32_t*)j->cstart.p, (const uint32_t*)j->slice_start.p,
+                                (uint32_t*)j->fcur.p, j->keys.p, k, j->bbits, a.cbits, j->wide,
+                                &j->d_sc->ticket_fine, N, &j->d_sc->err, j->stream));
   }
   mark_end(j, ST_SCATTER_FINE);
   return table_impl(j, N, t);

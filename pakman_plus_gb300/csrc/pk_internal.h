@@ -25,8 +25,6 @@ enum : uint32_t {
   ERR_MN_CAPACITY = 8u,   // a macro-node segment exceeded on-chip capacity
   ERR_TICKET = 16u,       // work ticket overrun (should not happen)
   ERR_BOUNDS = 32u,       // a computed index fell outside its buffer (write skipped)
-  ERR_REGION = 64u,       // a coarse region outgrew its sampled capacity (the host redoes
-                          // the partition with exact counts)
 };
 
 constexpr int kTileBytes = 65536;   // line-scan tile; chunk boundaries are multiples of it
@@ -82,15 +80,6 @@ struct CountArgs {
   uint32_t* counts;          // grid x 2^bbits  (per-chunk bucket counts, then prefixes)
   uint32_t* bstart;          // 2^bbits + 1 bucket starts
   unsigned long long n_keys; // capacity of the bucketed key buffer (scatter pass)
-  int tile_stride;           // sampling pass: chunk c is tile c * tile_stride (chunk =
-                             // one tile; windows are not added to n_windows); 0 = off
-  // sampled coarse regions: the coarse scatter reserves room in region g at every
-  // flush instead of writing to per-chunk offsets from an exact counting pass
-  uint32_t* gcur;            // 2^cbits: keys placed in region g so far (zeroed)
-  const uint32_t* rstart;    // 2^cbits: region starts in the coarse buffer
-  const uint32_t* rcap;      // 2^cbits: region capacities
-  uint32_t* fcount;          // 2^fbits: fine bucket sizes (zeroed)
-  int fbits;                 // digits of the whole partition
   Scalars* sc;
 };
 
@@ -196,23 +185,9 @@ cudaError_t launch_coarse_offsets(const CountArgs& a, uint32_t* coff, uint32_t* 
                                   uint32_t* slice_start, int slice_keys, cudaStream_t st);
 cudaError_t launch_scatter_coarse(const CountArgs& a, const uint32_t* coff, void* out, int wide,
                                   cudaStream_t st);
-// Sampled coarse regions (partitions of at most kSampledMaxBits digits): a counting pass
-// over every tile_stride-th tile (launch_bucket_count with a.tile_stride, a.bbits =
-// cbits), then region capacities from that sample, then the coarse scatter, which counts
-// windows, checks the records and histograms the fine buckets itself.
-constexpr int kSampledMaxBits = 14;
-cudaError_t launch_region_caps(const uint32_t* counts, int rows, int cbits, int stride, uint32_t* rstart,
-                               uint32_t* rcap, uint32_t* gcur, cudaStream_t st);
-cudaError_t launch_scatter_sampled(const CountArgs& a, void* out, int wide, cudaStream_t st);
-// Slices of the coarse regions [cstart[g], cend[g]) for the fine pass (one block).
-// Ends of the sampled regions (cend[g] = cstart[g] + min(gcur[g], rcap[g])) and the first
-// fine-pass slice of every region (one block).
-cudaError_t launch_region_slices(const uint32_t* cstart, const uint32_t* gcur, const uint32_t* rcap, uint32_t* cend,
-                                 int cbits, int slice_keys, uint32_t* slice_start, cudaStream_t st);
-cudaError_t launch_scatter_fine(const void* in, const uint32_t* cstart, const uint32_t* cend,
-                                const uint32_t* slice_start, uint32_t* fcur, void* out, int k, int bbits,
-                                int cbits, int wide, uint32_t* ticket, unsigned long long cap, uint32_t* err,
-                                cudaStream_t st);
+cudaError_t launch_scatter_fine(const void* in, const uint32_t* cstart, const uint32_t* slice_start,
+                                uint32_t* fcur, void* out, int k, int bbits, int cbits, int wide,
+                                uint32_t* ticket, unsigned long long cap, uint32_t* err, cudaStream_t st);
 cudaError_t launch_bucket_table(const BucketArgs& a, int wide, int grid, cudaStream_t st);
 // bstart / tu of a dense ascending table (pk_table_load)
 cudaError_t launch_table_bounds(const void* keys, unsigned long long n, int bbits, int k, uint32_t* bstart,

@@ -476,9 +476,7 @@ k_extract(CountArgs a) {
   for (int i = tid; i < B; i += NT) s_bins[i] = 0;
   __syncthreads();
 
-  // a sampling pass takes every tile_stride-th tile (one tile per chunk)
-  const unsigned long long c0 = a.tile_stride ? (unsigned long long)c * a.tile_stride * kTileBytes
-                                              : (unsigned long long)c * a.chunk;
+  const unsigned long long c0 = (unsigned long long)c * a.chunk;
   const unsigned long long c1 = min(c0 + a.chunk, F);
   uint32_t local = 0;
   const int warm_units = (k - 1 + 15) / 16;
@@ -547,9 +545,9 @@ k_extract(CountArgs a) {
           while (ends) {
             int q = __ffs(ends) - 1;
             ends &= ends - 1;
-            uint8_t next;
-            if (q < 15) next = (uint8_t)(w[u][(q + 1) >> 2] >> (8 * ((q + 1) & 3)));
-            else next = p + 16 < F ? buf[p + 16] : (uint8_t)'>';
+            // the byte after the newline, read from memory (it is in L1): picking it out of
+            // w by a run-time index would keep w in local memory for the whole loop
+            const uint8_t next = p + q + 1 < F ? __ldg(buf + p + q + 1) : (uint8_t)'>';
             check_record_start(buf, F, a.lmer_m, p + q, next, &a.sc->err);
           }
         }
@@ -583,7 +581,7 @@ k_extract(CountArgs a) {
     if (tid == 0) {
       unsigned long long tsum = 0;
       for (int i = 0; i < NW; i++) tsum += s_red[i];
-      if (tsum && !a.tile_stride) atomicAdd(&a.sc->n_windows, tsum);
+      if (tsum) atomicAdd(&a.sc->n_windows, tsum);
     }
   }
 }
@@ -606,23 +604,10 @@ struct CoarseCfg {
   static constexpr size_t smem = sizeof(KeyT) * C * R;
 };
 
-// A key of sampled coarse region b at place `at` of the region (beyond its capacity:
-// ERR_REGION, the write is skipped and the host redoes the partition exactly).
 template <typename KeyT>
-__device__ __forceinline__ void region_store(KeyT* __restrict__ out, const CountArgs& a, uint32_t b, uint32_t at,
-                                             KeyT v) {
-  if (at < a.rcap[b]) out[a.rstart[b] + at] = v;
-  else atomicOr(&a.sc->err, ERR_REGION);
-}
-
-// Flush of the shared-memory rings: whole 128-byte lines (and at the end every key) go
-// to the chunk's segment of their coarse region (offsets g from the counting pass), or,
-// for sampled regions (SAMPLED), to room reserved in the region by one atomic per
-// flushed run.
-template <typename KeyT, bool SAMPLED>
 __device__ __forceinline__ void coarse_flush(KeyT* ring, uint32_t* w, uint32_t* f, const uint32_t* g,
                                              KeyT* __restrict__ out, bool final_flush,
-                                             unsigned long long cap, uint32_t* err, const CountArgs& a) {
+                                             unsigned long long cap, uint32_t* err) {
   using CF = CoarseCfg<KeyT>;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int NW = CF::T / 32;
@@ -630,33 +615,23 @@ __device__ __forceinline__ void coarse_flush(KeyT* ring, uint32_t* w, uint32_t* 
     const uint32_t W = w[b];
     uint32_t Fv = f[b];
     KeyT* rb = ring + b * CF::R;
-    const uint32_t gb = SAMPLED ? 0u : g[b];
-    // n keys of the ring from ring position `first` (n <= 32)
-    auto put = [&](uint32_t first, uint32_t n) {
-      if (SAMPLED) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&a.gcur[b], n);
-        base = __shfl_sync(FULLMASK, base, 0);
-        if ((uint32_t)lane < n) region_store(out, a, (uint32_t)b, base + lane, rb[(first + lane) & (CF::R - 1)]);
-      } else if ((uint32_t)lane < n) {
-        guarded_store(out, gb + first + lane, rb[(first + lane) & (CF::R - 1)], cap, err);
-      }
-    };
+    const uint32_t gb = g[b];
     if (W - Fv > (uint32_t)CF::R) {
       // the ring overflowed this batch: keys past Fv+R went straight to global memory
-      for (uint32_t x = 0; x < (uint32_t)CF::R; x += 32) put(Fv + x, 32);
+      for (uint32_t x = lane; x < (uint32_t)CF::R; x += 32)
+        guarded_store(out, gb + Fv + x, rb[(Fv + x) & (CF::R - 1)], cap, err);
       Fv = W;
     } else {
       while (W - Fv >= 32) {
-        put(Fv, 32);
+        guarded_store(out, gb + Fv + lane, rb[(Fv + lane) & (CF::R - 1)], cap, err);
         Fv += 32;
       }
       if (W - Fv >= (uint32_t)CF::FU) {
-        put(Fv, CF::FU);
+        if (lane < CF::FU) guarded_store(out, gb + Fv + lane, rb[(Fv + lane) & (CF::R - 1)], cap, err);
         Fv += CF::FU;
       }
       if (final_flush && W > Fv) {
-        put(Fv, W - Fv);
+        if ((uint32_t)lane < W - Fv) guarded_store(out, gb + Fv + lane, rb[(Fv + lane) & (CF::R - 1)], cap, err);
         Fv = W;
       }
     }
@@ -665,20 +640,14 @@ __device__ __forceinline__ void coarse_flush(KeyT* ring, uint32_t* w, uint32_t* 
   }
 }
 
-// SAMPLED: the regions were sized from a sample (launch_region_caps), so a flush reserves
-// its room in the region with one atomic; the kernel then also counts the windows,
-// checks the record starts and histograms the fine buckets (2^fbits bins in shared
-// memory, after the rings), which the counting pass does otherwise.
-template <typename KeyT, bool SAMPLED>
+template <typename KeyT>
 __global__ void __launch_bounds__(CoarseCfg<KeyT>::T, 1)
 k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restrict__ out) {
   using CF = CoarseCfg<KeyT>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   KeyT* ring = reinterpret_cast<KeyT*>(smem_raw);
-  uint32_t* s_fh = reinterpret_cast<uint32_t*>(smem_raw + CF::smem);  // SAMPLED: fine histogram
   __shared__ uint32_t s_w[CF::C], s_f[CF::C], s_g[CF::C];
   __shared__ uint32_t s_wpar[CF::T / 32];
-  __shared__ uint32_t s_red[CF::T / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int NW = CF::T / 32;
   const int k = a.k;
@@ -690,15 +659,11 @@ k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restric
   const unsigned long long s0 = a.sc->s0;
   const int c = blockIdx.x;
   const int Cn = 1 << a.cbits;
-  const int fshift = 2 * k - a.fbits;  // fine bucket = leading fbits bits
   for (int i = tid; i < CF::C; i += CF::T) {
     s_w[i] = 0;
     s_f[i] = 0;
-    s_g[i] = (!SAMPLED && i < Cn) ? coff[(size_t)c * Cn + i] : 0;
+    s_g[i] = i < Cn ? coff[(size_t)c * Cn + i] : 0;
   }
-  if (SAMPLED)
-    for (int i = tid; i < (1 << a.fbits); i += CF::T) s_fh[i] = 0;
-  uint32_t local = 0;  // SAMPLED: windows of this thread
   __syncthreads();
   const unsigned long long c0 = (unsigned long long)c * a.chunk;
   const unsigned long long c1 = min(c0 + a.chunk, F);
@@ -768,17 +733,6 @@ k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restric
           v = odd & in & ~ub.nl;
           all_clear = k + 15 <= 64 ? window_clear(s, 0, k + 15)
                                    : (s.h0 == 0 && (s.h1 & ((1ull << (k + 15 - 64)) - 1ull)) == 0);
-          if (SAMPLED) {  // no counting pass ran: the record-start rule is checked here
-            uint32_t ends = ub.nl & odd & in;  // newlines that end sequence lines
-            while (ends) {
-              const int q = __ffs(ends) - 1;
-              ends &= ends - 1;
-              uint8_t next;
-              if (q < 15) next = (uint8_t)(w[u][(q + 1) >> 2] >> (8 * ((q + 1) & 3)));
-              else next = p + 16 < F ? buf[p + 16] : (uint8_t)'>';
-              check_record_start(buf, F, a.lmer_m, p + q, next, &a.sc->err);
-            }
-          }
         }
 #pragma unroll
         for (int half = 0; half < 16 / CF::BP; half++) {
@@ -790,82 +744,19 @@ k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restric
             if (!all_clear && !window_clear(s, age, k)) continue;
             const KeyT key = window_key<KeyT>(s, 2 * age, kmask);
             const uint32_t b = (uint32_t)(key >> cshift);
-            if (SAMPLED) {
-              atomicAdd(&s_fh[(uint32_t)(key >> fshift)], 1u);
-              local++;
-            }
             const uint32_t pos = atomicAdd(&s_w[b], 1u);
             if (pos - s_f[b] < (uint32_t)CF::R) ring[b * CF::R + (pos & (CF::R - 1))] = key;
-            else if (SAMPLED) region_store(out, a, b, atomicAdd(&a.gcur[b], 1u), key);
             else guarded_store(out, s_g[b] + pos, key, a.n_keys, &a.sc->err);
           }
           __syncthreads();
-          coarse_flush<KeyT, SAMPLED>(ring, s_w, s_f, s_g, out, false, a.n_keys, &a.sc->err, a);
+          coarse_flush<KeyT>(ring, s_w, s_f, s_g, out, false, a.n_keys, &a.sc->err);
           __syncthreads();
         }
       }
     }
   }
   __syncthreads();
-  coarse_flush<KeyT, SAMPLED>(ring, s_w, s_f, s_g, out, true, a.n_keys, &a.sc->err, a);
-  if (SAMPLED) {
-    for (int i = tid; i < (1 << a.fbits); i += CF::T)
-      if (s_fh[i]) atomicAdd(&a.fcount[i], s_fh[i]);
-    uint32_t x = __reduce_add_sync(FULLMASK, local);
-    if (lane == 0) s_red[warp] = x;
-    __syncthreads();
-    if (tid == 0) {
-      unsigned long long tsum = 0;
-      for (int i = 0; i < NW; i++) tsum += s_red[i];
-      if (tsum) atomicAdd(&a.sc->n_windows, tsum);
-    }
-  }
-}
-
-// Capacities of sampled coarse regions: every tile_stride-th tile was counted by coarse
-// region (counts[row][g]); a region gets its sampled share scaled to the whole input,
-// one eighth more, and 4096 keys, and the regions are laid out one after another.
-__global__ void __launch_bounds__(256) k_region_caps(const uint32_t* __restrict__ counts, int rows, int cbits,
-                                                     int stride, uint32_t* rstart, uint32_t* rcap, uint32_t* gcur) {
-  __shared__ uint32_t s_cap[1 << kCoarseBits];
-  const int Cn = 1 << cbits;
-  for (int g = threadIdx.x; g < Cn; g += blockDim.x) {
-    unsigned long long n = 0;
-    for (int r = 0; r < rows; r++) n += counts[(size_t)r * Cn + g];
-    n *= (unsigned long long)stride;
-    n += n / 8 + 4096;
-    s_cap[g] = (uint32_t)min(n, 0x7fffffffull);
-    gcur[g] = 0;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long acc = 0;
-    for (int g = 0; g < Cn; g++) {
-      rstart[g] = (uint32_t)min(acc, 0xffffffffull);
-      const unsigned long long room = acc < 0xffffffffull ? 0xffffffffull - acc : 0ull;
-      rcap[g] = (uint32_t)min((unsigned long long)s_cap[g], room);
-      acc += s_cap[g];
-    }
-    rstart[Cn] = (uint32_t)min(acc, 0xffffffffull);
-  }
-}
-
-// Ends of the sampled coarse regions (cend[g] = cstart[g] + keys placed, at most the
-// capacity) and the first fine-pass slice of every region.
-__global__ void __launch_bounds__(32) k_region_slices(const uint32_t* __restrict__ cstart,
-                                                      const uint32_t* __restrict__ gcur,
-                                                      const uint32_t* __restrict__ rcap, uint32_t* cend,
-                                                      int cbits, int slice_keys, uint32_t* slice_start) {
-  if (threadIdx.x != 0) return;
-  const int Cn = 1 << cbits;
-  uint32_t acc = 0;
-  for (int g = 0; g < Cn; g++) {
-    const uint32_t n = min(gcur[g], rcap[g]);
-    cend[g] = cstart[g] + n;
-    slice_start[g] = acc;
-    acc += (n + (uint32_t)slice_keys - 1) / (uint32_t)slice_keys;
-  }
-  slice_start[Cn] = acc;
+  coarse_flush<KeyT>(ring, s_w, s_f, s_g, out, true, a.n_keys, &a.sc->err);
 }
 
 // Coarse offsets: coff[c][g] = start of chunk c's segment in coarse region g (the
@@ -919,7 +810,6 @@ struct FineCfg {
 template <typename KeyT>
 __global__ void __launch_bounds__(512, 2) k_scatter_fine(const KeyT* __restrict__ in,
                                                         const uint32_t* __restrict__ cstart,
-                                                        const uint32_t* __restrict__ cend,
                                                         const uint32_t* __restrict__ slice_start,
                                                         uint32_t* fcur, KeyT* __restrict__ out,
                                                         int k, int bbits, int cbits, uint32_t* ticket,
@@ -953,7 +843,7 @@ __global__ void __launch_bounds__(512, 2) k_scatter_fine(const KeyT* __restrict_
     if (sl >= nslices) break;
     const uint32_t g = s_g;
     const uint32_t r0 = cstart[g] + (sl - slice_start[g]) * FC::S;
-    const uint32_t r1 = min(r0 + (uint32_t)FC::S, cend[g]);
+    const uint32_t r1 = min(r0 + (uint32_t)FC::S, cstart[g + 1]);
     const uint32_t m = r1 - r0;
     KeyT xs[FC::PT];
     uint32_t fs[FC::PT];
@@ -1022,7 +912,6 @@ struct FineBigCfg {
 template <typename KeyT>
 __global__ void __launch_bounds__(1024, 1) k_scatter_fine_big(const KeyT* __restrict__ in,
                                                              const uint32_t* __restrict__ cstart,
-                                                             const uint32_t* __restrict__ cend,
                                                              const uint32_t* __restrict__ slice_start,
                                                              uint32_t* fcur, KeyT* __restrict__ out,
                                                              int k, int bbits, int cbits, uint32_t* ticket,
@@ -1039,11 +928,10 @@ __global__ void __launch_bounds__(1024, 1) k_scatter_fine_big(const KeyT* __rest
   const int fshift = 2 * k - bbits;
   // the region tables live in shared memory: the slice -> region search of every slice
   // reads no global memory
-  __shared__ uint32_t s_ss[(1 << kCoarseBits) + 1], s_cs[(1 << kCoarseBits) + 1], s_ce[1 << kCoarseBits];
+  __shared__ uint32_t s_ss[(1 << kCoarseBits) + 1], s_cs[(1 << kCoarseBits) + 1];
   for (int i = tid; i <= Cn; i += FC::T) {
     s_ss[i] = slice_start[i];
     s_cs[i] = cstart[i];
-    if (i < Cn) s_ce[i] = cend[i];
   }
   const uint32_t nslices = slice_start[Cn];
   while (true) {
@@ -1065,7 +953,7 @@ __global__ void __launch_bounds__(1024, 1) k_scatter_fine_big(const KeyT* __rest
     if (sl >= nslices) break;
     const uint32_t g = s_g;
     const uint32_t r0 = s_cs[g] + (sl - s_ss[g]) * FC::S;
-    const uint32_t r1 = min(r0 + (uint32_t)FC::S, s_ce[g]);
+    const uint32_t r1 = min(r0 + (uint32_t)FC::S, s_cs[g + 1]);
     const uint32_t m = r1 - r0;
     for (uint32_t i0 = 0; i0 < m; i0 += FC::PR * FC::T) {
       KeyT xs[FC::PR];
@@ -2427,45 +2315,23 @@ cudaError_t launch_bucket_count(const CountArgs& a, int wide, cudaStream_t st) {
   return launch_extract_t<uint64_t, false>(a, st);
 }
 
-template <typename KeyT, bool SAMPLED>
+template <typename KeyT>
 static cudaError_t launch_coarse_t(const CountArgs& a, const uint32_t* coff, KeyT* out, cudaStream_t st) {
-  // the sampled kernel keeps the fine histogram after the rings: the attribute is set
-  // once to the largest (kSampledMaxBits digits), never to this launch's size
-  const size_t fh_max = SAMPLED ? sizeof(uint32_t) << kSampledMaxBits : 0;
-  const size_t smem = CoarseCfg<KeyT>::smem + (SAMPLED ? sizeof(uint32_t) << a.fbits : 0);
+  const size_t smem = CoarseCfg<KeyT>::smem;
   static bool attr_set = false;  // a constant, so concurrent first calls agree
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_scatter_coarse<KeyT, SAMPLED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(CoarseCfg<KeyT>::smem + fh_max));
+    cudaError_t e = cudaFuncSetAttribute(k_scatter_coarse<KeyT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  pk::note_launch(), k_scatter_coarse<KeyT, SAMPLED><<<a.grid, CoarseCfg<KeyT>::T, smem, st>>>(a, coff, out);
+  pk::note_launch(), k_scatter_coarse<KeyT><<<a.grid, CoarseCfg<KeyT>::T, smem, st>>>(a, coff, out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_scatter_coarse(const CountArgs& a, const uint32_t* coff, void* out, int wide,
                                   cudaStream_t st) {
-  return wide ? launch_coarse_t<u128, false>(a, coff, reinterpret_cast<u128*>(out), st)
-              : launch_coarse_t<uint64_t, false>(a, coff, reinterpret_cast<uint64_t*>(out), st);
-}
-
-cudaError_t launch_scatter_sampled(const CountArgs& a, void* out, int wide, cudaStream_t st) {
-  if (a.fbits > kSampledMaxBits || a.fbits <= a.cbits) return cudaErrorInvalidValue;
-  return wide ? launch_coarse_t<u128, true>(a, nullptr, reinterpret_cast<u128*>(out), st)
-              : launch_coarse_t<uint64_t, true>(a, nullptr, reinterpret_cast<uint64_t*>(out), st);
-}
-
-cudaError_t launch_region_caps(const uint32_t* counts, int rows, int cbits, int stride, uint32_t* rstart,
-                               uint32_t* rcap, uint32_t* gcur, cudaStream_t st) {
-  pk::note_launch(), k_region_caps<<<1, 256, 0, st>>>(counts, rows, cbits, stride, rstart, rcap, gcur);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_region_slices(const uint32_t* cstart, const uint32_t* gcur, const uint32_t* rcap, uint32_t* cend,
-                                 int cbits, int slice_keys, uint32_t* slice_start, cudaStream_t st) {
-  pk::note_launch(), k_region_slices<<<1, 32, 0, st>>>(cstart, gcur, rcap, cend, cbits, slice_keys, slice_start);
-  return cudaGetLastError();
+  return wide ? launch_coarse_t<u128>(a, coff, reinterpret_cast<u128*>(out), st)
+              : launch_coarse_t<uint64_t>(a, coff, reinterpret_cast<uint64_t*>(out), st);
 }
 
 cudaError_t launch_coarse_offsets(const CountArgs& a, uint32_t* coff, uint32_t* cstart,
@@ -2477,9 +2343,9 @@ cudaError_t launch_coarse_offsets(const CountArgs& a, uint32_t* coff, uint32_t* 
 }
 
 template <typename KeyT>
-static cudaError_t launch_fine_t(const KeyT* in, const uint32_t* cstart, const uint32_t* cend,
-                                 const uint32_t* slice_start, uint32_t* fcur, KeyT* out, int k, int bbits, int cbits,
-                                 uint32_t* ticket, unsigned long long cap, uint32_t* err, cudaStream_t st) {
+static cudaError_t launch_fine_t(const KeyT* in, const uint32_t* cstart, const uint32_t* slice_start,
+                                 uint32_t* fcur, KeyT* out, int k, int bbits, int cbits, uint32_t* ticket,
+                                 unsigned long long cap, uint32_t* err, cudaStream_t st) {
   const size_t smem = FineCfg<KeyT>::smem;
   static bool attr_set = false;  // a constant, so concurrent first calls agree
   if (!attr_set) {
@@ -2496,22 +2362,21 @@ static cudaError_t launch_fine_t(const KeyT* in, const uint32_t* cstart, const u
       if (e != cudaSuccess) return e;
       big_attr_set = true;
     }
-    pk::note_launch(), k_scatter_fine_big<KeyT><<<sm_count(), FineBigCfg<KeyT>::T, bsmem, st>>>(in, cstart, cend, slice_start, fcur, out, k,
+    pk::note_launch(), k_scatter_fine_big<KeyT><<<sm_count(), FineBigCfg<KeyT>::T, bsmem, st>>>(in, cstart, slice_start, fcur, out, k,
                                                                              bbits, cbits, ticket, cap, err);
     return cudaGetLastError();
   }
-  pk::note_launch(), k_scatter_fine<KeyT><<<sm_count() * 2, FineCfg<KeyT>::T, smem, st>>>(in, cstart, cend, slice_start, fcur, out,
+  pk::note_launch(), k_scatter_fine<KeyT><<<sm_count() * 2, FineCfg<KeyT>::T, smem, st>>>(in, cstart, slice_start, fcur, out,
                                                                         k, bbits, cbits, ticket, cap, err);
   return cudaGetLastError();
 }
 
-cudaError_t launch_scatter_fine(const void* in, const uint32_t* cstart, const uint32_t* cend,
-                                const uint32_t* slice_start, uint32_t* fcur, void* out, int k, int bbits,
-                                int cbits, int wide, uint32_t* ticket, unsigned long long cap, uint32_t* err,
-                                cudaStream_t st) {
-  return wide ? launch_fine_t<u128>(reinterpret_cast<const u128*>(in), cstart, cend, slice_start, fcur,
+cudaError_t launch_scatter_fine(const void* in, const uint32_t* cstart, const uint32_t* slice_start,
+                                uint32_t* fcur, void* out, int k, int bbits, int cbits, int wide,
+                                uint32_t* ticket, unsigned long long cap, uint32_t* err, cudaStream_t st) {
+  return wide ? launch_fine_t<u128>(reinterpret_cast<const u128*>(in), cstart, slice_start, fcur,
                                     reinterpret_cast<u128*>(out), k, bbits, cbits, ticket, cap, err, st)
-              : launch_fine_t<uint64_t>(reinterpret_cast<const uint64_t*>(in), cstart, cend, slice_start, fcur,
+              : launch_fine_t<uint64_t>(reinterpret_cast<const uint64_t*>(in), cstart, slice_start, fcur,
                                         reinterpret_cast<uint64_t*>(out), k, bbits, cbits, ticket, cap, err,
                                         st);
 }

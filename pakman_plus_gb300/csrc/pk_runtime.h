@@ -84,10 +84,6 @@ struct pk_job {
       coff, cstart, slice_start, fcur, wiring, gfirst, gcount, chunk_bucket, gdone, chunk_u;
   // counting in pieces (pk_chunked.cu): the accumulated table (ping-pong) and the merge
   DevBuf acc_keys[2], acc_counts[2], merge_keys, merge_counts, merge_part;
-  // sampled coarse regions: starts, capacities, fill cursors, ends, fine bucket sizes
-  DevBuf rstart, rcap, gcur, cend, fcount;
-  bool sampled = false;   // the last count placed its coarse regions by a sample
-  bool resampled = false; // ... or tried to, and fell back to the exact counting pass
   uint32_t pieces = 0;  // pieces the last count used (1: the whole input at once)
   bool dense_valid = false;
   bool wired = false;  // wiring matches the current macro-nodes

@@ -239,62 +239,3 @@ def test_golden_with_macro_node_units(name, bucket_bits, mn_units):
         job.build_macro_nodes(0)
         mn = job.macro_nodes(g.coverage)
     assert_mn_equal(mn, g.mn_keys, g.mn_suf, g.mn_pre)
-
-
-@pytest.mark.parametrize("bucket_bits", [8, 11, 14])
-@pytest.mark.parametrize("name", ["k32_basic", "k63_basic", "k31_lower_n", "k32_ragged", "k63_dropn"])
-def test_sampled_coarse_regions_on_fixtures(name, bucket_bits):
-    """Coarse regions sized from a sample of every tile (sample_stride 1): the coarse
-    scatter counts, checks records and histograms the fine buckets itself."""
-    g = load(name)
-    p = pk.default_params(k=g.k, num_buckets=g.t, coverage=g.coverage, drop_n=int(g.drop_n),
-                          bucket_bits=bucket_bits, sample_stride=1)
-    with pk.Job(ctx()) as job:
-        job.count(g.fasta, p)
-        assert job.partition_info() == (bucket_bits, True, False)
-        keys, counts = job.table()
-        assert_table_equal(pk.to_key128(keys), counts, g.table_keys, g.table_counts)
-        assert job.summary().n_windows == g.n_windows
-        if g.expect == "ok":
-            cut, hist, kept = job.cutoff(g.t)
-            assert cut == g.cutoff and np.array_equal(hist, g.hist)
-            job.build_macro_nodes(0)
-            assert_mn_equal(job.macro_nodes(g.coverage), g.mn_keys, g.mn_suf, g.mn_pre)
-
-
-def test_sampled_regions_report_a_bad_record():
-    g = load("k32_bad_record")
-    p = pk.default_params(k=g.k, num_buckets=g.t, coverage=g.coverage, bucket_bits=10, sample_stride=1)
-    with pk.Job(ctx()) as job:
-        with pytest.raises(pk.FormatError):
-            job.count(g.fasta, p)
-
-
-def test_sampled_regions_fall_back_when_the_sample_misleads():
-    """Only the first tile is sampled and it holds random reads; the rest is homopolymer
-    and dinucleotide repeats whose k-mers all fall in a few coarse regions.  Those regions
-    outgrow their sampled size, the job redoes the partition with the exact counting
-    pass, and the result is the oracle's."""
-    rs = synth.small_case(4321, genome_len=50000, n_reads=700, read_len=100, err=0.0, k=32)
-    head = rs.fasta
-    tail = _low_complexity_fasta(40000, seed=8)
-    fasta = head + tail
-    ntiles = (len(fasta) + 65535) // 65536
-    ora = po.run(fasta, 32, 21)
-    p = pk.default_params(k=32, num_buckets=21, coverage=10, bucket_bits=12, sample_stride=ntiles)
-    with pk.Job(ctx()) as job:
-        job.count(fasta, p)
-        assert job.partition_info() == (12, False, True)
-        keys, counts = job.table()
-        assert_table_equal(pk.to_key128(keys), counts, ora.table.keys, ora.table.counts)
-        cut, hist, kept = job.cutoff(21)
-        assert cut == ora.cutoff and np.array_equal(hist, ora.hist)
-        job.build_macro_nodes(0)
-        assert_mn_equal(job.macro_nodes(10), ora.mn.keys, ora.mn.suf, ora.mn.pre)
-    # the same input with the exact pass asked for
-    p2 = pk.default_params(k=32, num_buckets=21, coverage=10, bucket_bits=12, sample_stride=-1)
-    with pk.Job(ctx()) as job:
-        job.count(fasta, p2)
-        assert job.partition_info() == (12, False, False)
-        keys, counts = job.table()
-        assert_table_equal(pk.to_key128(keys), counts, ora.table.keys, ora.table.counts)
