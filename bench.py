@@ -462,7 +462,7 @@ def run_serve(args, rank, world):
     def serve(workers, arrival):
         srv = pk.Server(ctx, workers=workers)
         tickets = [None] * args.serve_jobs
-        ready = threading.Semaphore(0)
+        by_ticket = {}
 
         def producer():
             t0 = time.perf_counter()
@@ -470,26 +470,28 @@ def run_serve(args, rank, world):
                 dt = t0 + arrival[i] - time.perf_counter()
                 if dt > 0:
                     time.sleep(dt)
-                tickets[i] = srv.submit(pinned[e].numpy(), params[e])
-                ready.release()
+                t = srv.submit(pinned[e].numpy(), params[e])
+                tickets[i] = t
+                by_ticket[t] = i
 
         th = threading.Thread(target=producer, daemon=True)
         th.start()
         lat, ratio, first_submit, last_end, windows, mismatches = [], [], None, 0, 0, 0
-        for i, e in enumerate(entries):
-            ready.acquire()
-            try:
-                srv.wait(tickets[i])
-            except pk.PakmanError:
-                pass
-            info = srv.poll(tickets[i])
+        # results are taken in completion order and released at once, so the server's
+        # pinned result blocks are recycled whatever order it ran the jobs in
+        for _ in entries:
+            info = srv.next_done()
+            while info.ticket not in by_ticket:  # the producer has not recorded it yet
+                time.sleep(0.0002)
+            i = by_ticket[info.ticket]
+            e = entries[i]
             ref, _, ref_status = alone[e]
             s = info.summary
             if info.status != ref_status or (s.n_windows, s.n_unique, s.n_kept, s.cutoff) != (
                     ref.n_windows, ref.n_unique, ref.n_kept, ref.cutoff) or (
                     ref_status == 0 and s.n_nodes != ref.n_nodes):
                 mismatches += 1
-            srv.release(tickets[i])
+            srv.release(info.ticket)
             lat.append(info.latency_ms)
             ratio.append(info.latency_ms / solo[e])
             first_submit = info.submit_ns if first_submit is None else min(first_submit, info.submit_ns)

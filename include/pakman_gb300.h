@@ -429,6 +429,11 @@ pk_status pk_submit(pk_server* s, const pk_request* req, uint64_t* ticket);
 pk_status pk_cancel(pk_server* s, uint64_t ticket);
 /* Non-blocking: fills *info (info->done == 0 while queued or running). */
 pk_status pk_poll(pk_server* s, uint64_t ticket, pk_request_info* info);
+/* Completion order: the next finished (or cancelled) request not handed out before, its
+ * ticket and state; blocks up to timeout_ms (< 0: no limit), PK_ERR_BUSY on timeout.  A
+ * caller that consumes results as they finish releases each one promptly, whatever
+ * order the scheduler ran them in. */
+pk_status pk_next_done(pk_server* s, int64_t timeout_ms, uint64_t* ticket, pk_request_info* info);
 /* Blocks until the job is done or timeout_ms (< 0: no limit) passes; PK_ERR_BUSY on timeout. */
 pk_status pk_wait(pk_server* s, uint64_t ticket, int64_t timeout_ms, pk_request_info* info);
 /* Server-kept macro-node table of a finished request (valid until pk_result_release). */

@@ -598,6 +598,15 @@ class Server:
         return MacroNodeTable(keys.view(key_dtype(params.k)), suf.reshape(m, 4), pre.reshape(m, 4), cov,
                               params.k)
 
+    def next_done(self, timeout: Optional[float] = None) -> RequestInfo:
+        """The next request to finish, in completion order (pk_next_done); its own
+        status is in the returned info (not raised)."""
+        t = c_uint64()
+        i = capi.PkRequestInfo()
+        ms = -1 if timeout is None else int(timeout * 1000)
+        check(capi.lib().pk_next_done(self._h, ms, byref(t), byref(i)), "pk_next_done")
+        return self._info(t.value, i)
+
     def cancel(self, ticket: int):
         """Cancel a queued or running request (pk_cancel)."""
         check(capi.lib().pk_cancel(self._h, ticket), "pk_cancel")

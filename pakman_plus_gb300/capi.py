@@ -189,6 +189,7 @@ _SIGS = {
     "pk_server_config_default": (None, [POINTER(PkServerConfig), c_int32]),
     "pk_server_create_config": (c_int, [c_void_p, c_int32, POINTER(PkServerConfig), POINTER(c_void_p)]),
     "pk_cancel": (c_int, [c_void_p, c_uint64]),
+    "pk_next_done": (c_int, [c_void_p, ctypes.c_int64, POINTER(c_uint64), POINTER(PkRequestInfo)]),
     "pk_result_job": (c_int, [c_void_p, c_uint64, POINTER(c_void_p)]),
     "pk_server_destroy": (None, [c_void_p]),
     "pk_submit": (c_int, [c_void_p, POINTER(PkRequest), POINTER(c_uint64)]),

@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <deque>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -83,6 +84,7 @@ struct pk_server {
   std::condition_variable cv_done;  // a request finished
   std::vector<Request*> queue;      // waiting requests, in submission order
   std::unordered_map<uint64_t, Request*> reqs;
+  std::deque<uint64_t> done_q;      // finished requests not yet handed out by pk_next_done
   uint64_t next_ticket = 1;
   bool stop = false;
   int running = 0;
@@ -241,6 +243,7 @@ void finish(pk_server* s, Request* q, pk_status status, const pk_summary& sum, c
   else if (status == PK_ERR_CANCELLED) s->st.cancelled++;
   else s->st.failed++;
   s->events++;
+  s->done_q.push_back(q->ticket);
   s->cv_done.notify_all();
   s->cv_work.notify_all();
 }
@@ -511,6 +514,7 @@ pk_status pk_cancel(pk_server* s, uint64_t ticket) {
     q->info.end_ns = now_ns();
     q->error = "cancelled while queued";
     s->st.cancelled++;
+    s->done_q.push_back(q->ticket);
     s->cv_done.notify_all();
     s->cv_work.notify_all();
     return PK_OK;
@@ -531,6 +535,26 @@ pk_status pk_poll(pk_server* s, uint64_t ticket, pk_request_info* info) {
   Request* q = find(s, ticket);
   if (!q) return pk::set_error(PK_ERR_INVALID, "unknown ticket");
   return report(q, info);
+}
+
+pk_status pk_next_done(pk_server* s, int64_t timeout_ms, uint64_t* ticket, pk_request_info* info) {
+  if (!s || !ticket) return pk::set_error(PK_ERR_INVALID, "server and ticket must not be null");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto ready = [&] {
+    while (!s->done_q.empty() && !s->reqs.count(s->done_q.front())) s->done_q.pop_front();  // released
+    return !s->done_q.empty() || s->stop;
+  };
+  if (timeout_ms < 0) {
+    s->cv_done.wait(lk, ready);
+  } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
+    return pk::set_error(PK_ERR_BUSY, "no request finished in time");
+  }
+  if (s->done_q.empty()) return pk::set_error(PK_ERR_STATE, "server is shutting down");
+  *ticket = s->done_q.front();
+  s->done_q.pop_front();
+  Request* q = find(s, *ticket);
+  if (info) *info = q->info;
+  return PK_OK;
 }
 
 pk_status pk_wait(pk_server* s, uint64_t ticket, int64_t timeout_ms, pk_request_info* info) {

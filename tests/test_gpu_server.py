@@ -193,3 +193,20 @@ def test_keep_on_device_hands_over_the_resident_job():
         st = srv.stats()
         assert st["resident_jobs"] == 0 and st["resident_bytes"] == 0
     # another request still runs normally on the same server afterwards is covered above
+
+
+def test_next_done_hands_out_every_request_once_in_completion_order():
+    cases = _mix()
+    with pk.Server(ctx(), workers=3) as srv:
+        tickets = [srv.submit(f, _params(k, t, cov)) for f, k, t, cov in cases]
+        got = []
+        for _ in tickets:
+            info = srv.next_done()
+            assert info.done
+            got.append(info)
+            srv.release(info.ticket)
+        assert sorted(i.ticket for i in got) == sorted(tickets)
+        ends = [i.end_ns for i in got]
+        assert ends == sorted(ends)
+        with pytest.raises(pk.capi.Busy):
+            srv.next_done(timeout=0.05)
