@@ -624,6 +624,13 @@ def run_batch(args, rank, world):
             torch.cuda.synchronize()
             plain_ms.append(1000 * (time.perf_counter() - t))
     med = sorted(graph_ms)[len(graph_ms) // 2]
+    tuned_shapes = {}
+    for f, _ in sets:
+        cls = "%d KiB" % ((1 << (len(f).bit_length() - 1)) >> 10)
+        try:
+            tuned_shapes[cls] = "digits %d, chunk x%d, table CTAs/SM %d" % batch.tuned_shape(len(f), 32)
+        except pk.PakmanError:
+            tuned_shapes[cls] = "not tuned"
     # every 8th set (32 of 256, spread over the size range) against the oracle: summary,
     # cutoff and the set's rows of the batch's macro-node table
     from oracle import pk_oracle as po
@@ -656,6 +663,7 @@ def run_batch(args, rank, world):
             "kernels_per_launch": st["kernels_per_launch"], "captures": st["graph_captures"],
             "reruns": st["reruns"], "tuned_classes": st["tuned_classes"], "tune_ms": st["tune_ms"],
             "first_run_ms": st0["last_graph_ms"],
+            "tuned_shapes": tuned_shapes,
             "e2e": {"value": windows / wall, "unit": "k-mers/s", "ms_per_step": 1000 * wall,
                     "h2d_bytes_per_step": total_bytes,
                     "note": "pk_batch_run: host input copy, graph launch, per-set results (table copy separate)"},

@@ -502,6 +502,11 @@ pk_status pk_batch_copy_macro_nodes(pk_batch* b, void* keys, uint32_t* suffix_co
 pk_status pk_batch_get_stats(pk_batch* b, pk_batch_stats* out);
 /* Autotuned partition digits for a set of this size and k (0 if not tuned yet). */
 int32_t pk_batch_tuned_bits(pk_batch* b, uint64_t fasta_bytes, int32_t k);
+/* The whole tuned launch shape of that size class: partition digits, counting/scatter
+ * chunks as a multiple of the one-chunk-per-SM size, table CTAs per SM; PK_ERR_STATE
+ * if the class has not been tuned. */
+pk_status pk_batch_tuned_shape(pk_batch* b, uint64_t fasta_bytes, int32_t k, int32_t* digits,
+                               int32_t* chunk_mult, int32_t* table_ctas);
 
 #ifdef __cplusplus
 }

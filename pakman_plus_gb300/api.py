@@ -717,6 +717,13 @@ class Batch:
     def tuned_bits(self, fasta_bytes: int, k: int) -> int:
         return int(capi.lib().pk_batch_tuned_bits(self._h, fasta_bytes, k))
 
+    def tuned_shape(self, fasta_bytes: int, k: int) -> Tuple[int, int, int]:
+        """(partition digits, chunk multiple, table CTAs per SM) tuned for this size class."""
+        d, c, t = c_int32(), c_int32(), c_int32()
+        check(capi.lib().pk_batch_tuned_shape(self._h, fasta_bytes, k, byref(d), byref(c), byref(t)),
+              "pk_batch_tuned_shape")
+        return d.value, c.value, t.value
+
     def close(self):
         if getattr(self, "_h", None):
             capi.lib().pk_batch_destroy(self._h)

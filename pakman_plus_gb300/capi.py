@@ -206,6 +206,8 @@ _SIGS = {
     "pk_batch_copy_macro_nodes": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
     "pk_batch_get_stats": (c_int, [c_void_p, POINTER(PkBatchStats)]),
     "pk_batch_tuned_bits": (c_int32, [c_void_p, c_uint64, c_int32]),
+    "pk_batch_tuned_shape": (c_int, [c_void_p, c_uint64, c_int32, POINTER(c_int32), POINTER(c_int32),
+                                     POINTER(c_int32)]),
     "pk_host_alloc": (c_int, [c_uint64, POINTER(c_void_p)]),
     "pk_host_free": (None, [c_void_p]),
 }

@@ -48,6 +48,16 @@ struct HostTable {      // rows of sets run on their own
 
 int size_class(uint64_t bytes) { return bytes ? 63 - __builtin_clzll(bytes) : 0; }
 
+// What the autotuner picks for a size class: the partition digits (radix width), the
+// counting/scatter chunk size (a multiple of one chunk per SM: fewer, longer chunks leave
+// SMs to the other graph branches) and the table kernel's CTAs per SM (how the buckets are
+// dealt to CTAs).
+struct Shape {
+  int digits = 0;
+  int chunk_mult = 1;
+  int table_ctas = 2;
+};
+
 }  // namespace
 
 struct pk_batch {
@@ -68,7 +78,7 @@ struct pk_batch {
   std::vector<SetPlan> plan;
   std::vector<Scalars> h_scal;
   std::vector<unsigned long long> h_res;
-  std::map<std::pair<int, int>, int> tuned;  // (size class, k) -> partition digits
+  std::map<std::pair<int, int>, Shape> tuned;  // (size class, k) -> launch shape
   std::vector<HostTable> extra;         // per set run on its own (empty otherwise)
   uint64_t device_rows = 0;
   pk_batch_stats st{};
@@ -153,8 +163,20 @@ pk_status presize(pk_job* j, uint64_t fmax, int k, int bbits, int t, int sms) {
 int digits_for(pk_batch* b, const pk_params& p, uint64_t bytes) {
   if (p.bucket_bits) return std::min(p.bucket_bits, std::min(kMaxPartBits, 2 * p.k - 2));
   auto it = b->tuned.find({size_class(bytes), p.k});
-  if (it != b->tuned.end()) return it->second;
+  if (it != b->tuned.end()) return it->second.digits;
   return auto_bucket_bits(bytes, p.k, p.k > 32);
+}
+
+Shape shape_for(pk_batch* b, const pk_params& p, uint64_t bytes) {
+  auto it = b->tuned.find({size_class(bytes), p.k});
+  Shape s = it != b->tuned.end() ? it->second : Shape{};
+  s.digits = digits_for(b, p, bytes);
+  return s;
+}
+
+void apply(pk_job* j, const Shape& s) {
+  j->chunk_mult = s.chunk_mult;
+  j->table_ctas = s.table_ctas;
 }
 
 // Time the whole path of one set on a branch job (outside any capture).
@@ -184,9 +206,10 @@ pk_status time_set(pk_job* j, const void* d_fasta, uint64_t bytes, const pk_para
   return PK_OK;
 }
 
-// Autotune the partition digits of every (size class, k) of the batch that has
-// automatic digits: the fastest of the automatic choice and its two neighbours on
-// the class's largest set.
+// Autotune the launch shape of every (size class, k) of the batch that has automatic
+// digits, on the class's largest set: first the partition digits (the fastest of the
+// automatic choice and its two neighbours), then with those the chunk size (one or two
+// times the one-chunk-per-SM size) and the table CTAs per SM (one or two).
 pk_status autotune(pk_batch* b, const std::vector<SetPlan>& plan) {
   std::map<std::pair<int, int>, int> largest;  // class -> set index
   for (size_t i = 0; i < plan.size(); i++) {
@@ -216,7 +239,23 @@ pk_status autotune(pk_batch* b, const std::vector<SetPlan>& plan) {
         best_bits = bits;
       }
     }
-    b->tuned[kv.first] = best_bits;
+    Shape best{best_bits, 1, 2};
+    for (int cm = 1; cm <= 2; cm++)
+      for (int tc = 1; tc <= 2; tc++) {
+        if (cm == 1 && tc == 2) continue;  // timed above
+        pk_params p = sp.params;
+        p.bucket_bits = best_bits;
+        apply(j, Shape{best_bits, cm, tc});
+        double ms = 0;
+        const pk_status r = time_set(j, (const char*)b->input.p + sp.off, sp.bytes, p, &ms);
+        apply(j, Shape{});
+        PK_TRY(r);
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = Shape{best_bits, cm, tc};
+        }
+      }
+    b->tuned[kv.first] = best;
   }
   pk_job_reset(j);
   b->st.tuned_classes = b->tuned.size();
@@ -268,6 +307,7 @@ pk_status capture(pk_batch* b) {
     j->graph_mode = true;
     j->ncap = sp.bytes;
     j->d_sc = scal + i;
+    apply(j, shape_for(b, sp.params, sp.bytes));
     st = count_impl(j, (const char*)b->input.p + sp.off, sp.bytes, &sp.params);
     if (st == PK_OK) st = cutoff_enqueue(j, sp.params.num_buckets);
     if (st == PK_OK) st = mn_enqueue(j, 0, b->vcap[sp.branch]);
@@ -279,6 +319,7 @@ pk_status capture(pk_batch* b) {
     }
     j->graph_mode = false;
     j->d_sc = own;
+    apply(j, Shape{});
   }
   for (int r = 0; r < b->branches; r++) {
     cudaEventRecord(b->join[r], b->jobs[r]->stream);
@@ -539,8 +580,19 @@ pk_status pk_batch_get_stats(pk_batch* b, pk_batch_stats* out) {
   return PK_OK;
 }
 
+pk_status pk_batch_tuned_shape(pk_batch* b, uint64_t fasta_bytes, int32_t k, int32_t* digits, int32_t* chunk_mult,
+                               int32_t* table_ctas) {
+  if (!b) return set_error(PK_ERR_INVALID, "batch is null");
+  auto it = b->tuned.find({size_class(fasta_bytes), k});
+  if (it == b->tuned.end()) return set_error(PK_ERR_STATE, "no tuned shape for this size and k");
+  if (digits) *digits = it->second.digits;
+  if (chunk_mult) *chunk_mult = it->second.chunk_mult;
+  if (table_ctas) *table_ctas = it->second.table_ctas;
+  return PK_OK;
+}
+
 int32_t pk_batch_tuned_bits(pk_batch* b, uint64_t fasta_bytes, int32_t k) {
   if (!b) return 0;
   auto it = b->tuned.find({size_class(fasta_bytes), k});
-  return it == b->tuned.end() ? 0 : it->second;
+  return it == b->tuned.end() ? 0 : it->second.digits;
 }

@@ -367,6 +367,7 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   int grid = (int)std::min<uint64_t>((uint64_t)j->ctx->sms, std::max<uint64_t>(ntiles, 1));
   unsigned long long chunk = (ntiles + grid - 1) / grid * (unsigned long long)kTileBytes;
   if (chunk == 0) chunk = kTileBytes;
+  if (j->chunk_mult > 1) chunk *= (unsigned long long)j->chunk_mult;  // fewer, longer chunks
   grid = (int)std::max<uint64_t>(1, (n + chunk - 1) / chunk);
   j->grid = grid;
   j->chunk = chunk;
@@ -502,7 +503,7 @@ static pk_status table_impl(pk_job* j, uint64_t N, int t) {
   b.cap = N;
   b.spin_limit = (int)j->wait_limit;
   b.sc = j->d_sc;
-  PK_CUDA(launch_bucket_table(b, j->wide, 0, j->stream));
+  PK_CUDA(launch_bucket_table(b, j->wide, j->table_ctas > 0 ? j->table_ctas * j->ctx->sms : 0, j->stream));
   mark_end(j, ST_TABLE);
   j->pieces = 1;
   j->stage = 1;

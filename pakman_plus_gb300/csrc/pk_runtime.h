@@ -90,6 +90,10 @@ struct pk_job {
   pk::CpState* cp = nullptr;
   bool compacted = false;  // the compaction state matches the current macro-nodes
   bool timing = false;
+  // launch shapes chosen by the batch autotuner (0: the defaults): counting/scatter chunks
+  // of chunk_mult times the one-chunk-per-SM size, and table CTAs per SM
+  int chunk_mult = 0;
+  int table_ctas = 0;
   // bounded device waits: polls before a wait gives up (0: the default, about 1-2 s), and
   // a macro-node unit that withholds its look-back word (-1: none); see pk_job_set_wait_limit
   uint32_t wait_limit = 0;
