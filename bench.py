@@ -509,6 +509,8 @@ def run_serve(args, rank, world):
                 "jobs_within_2x_solo": float((ratio <= 2.0).mean()),
                 "kmers_per_s": windows / span, "span_s": span,
                 "peak_admitted_gb": st["peak_admitted_bytes"] / 1e9, "requeued": st["requeued"],
+                "worker_s_by_phase": {ph: round(st[ph + "_ns"] / 1e9, 3)
+                                      for ph in ("count", "cutoff", "mn", "copyout", "release")},
                 "results_differing_from_alone": mismatches}
 
     def tables_in_the_mix():
@@ -872,7 +874,7 @@ def main():
         job.macro_nodes(out=outs[0])
     serial_ms = 1000.0 * (time.perf_counter() - t0) / 2
     job.reset()
-    srv = pk.Server(ctx, workers=depth)
+    srv = pk.Server(ctx, workers=depth, reserved_small=0)  # every worker takes this size
     for tk in [srv.submit(pin_np, params, out=outs[i]) for i in range(depth)]:  # warm-up
         srv.wait(tk)
         srv.release(tk)

@@ -405,6 +405,10 @@ typedef struct pk_server_stats {
   uint64_t cancelled;
   uint64_t resident_bytes;       /* device memory of results kept on the device */
   uint64_t resident_jobs;
+  /* worker wall time summed over finished requests, by phase: counting (input copy
+   * included), histogram cutoff, macro-nodes, copying the result out, releasing the
+   * job's device buffers */
+  uint64_t count_ns, cutoff_ns, mn_ns, copyout_ns, release_ns;
 } pk_server_stats;
 
 typedef struct pk_server_config {

@@ -58,7 +58,8 @@ class PkRequestInfo(ctypes.Structure):
 class PkServerStats(ctypes.Structure):
     _fields_ = [(n, c_uint64) for n in ("submitted", "completed", "failed", "queued", "running",
                                         "admitted_bytes", "peak_admitted_bytes", "requeued", "cancelled",
-                                        "resident_bytes", "resident_jobs")]
+                                        "resident_bytes", "resident_jobs", "count_ns", "cutoff_ns", "mn_ns",
+                                        "copyout_ns", "release_ns")]
 
 
 class PkServerConfig(ctypes.Structure):

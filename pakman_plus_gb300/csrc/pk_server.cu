@@ -69,6 +69,9 @@ struct Request {
   // keep_on_device: the finished job, handed to the caller, and its device bytes
   pk_job* job = nullptr;
   uint64_t resident = 0;
+  // worker wall time by phase: counting, cutoff, macro-nodes, copy-out, releasing the
+  // job's buffers (added to the server's stats when the request finishes)
+  uint64_t phase_ns[5] = {0, 0, 0, 0, 0};
 };
 
 }  // namespace
@@ -239,6 +242,11 @@ void finish(pk_server* s, Request* q, pk_status status, const pk_summary& sum, c
     s->st.resident_bytes += q->resident;
     s->st.resident_jobs++;
   }
+  s->st.count_ns += q->phase_ns[0];
+  s->st.cutoff_ns += q->phase_ns[1];
+  s->st.mn_ns += q->phase_ns[2];
+  s->st.copyout_ns += q->phase_ns[3];
+  s->st.release_ns += q->phase_ns[4];
   if (status == PK_OK) s->st.completed++;
   else if (status == PK_ERR_CANCELLED) s->st.cancelled++;
   else s->st.failed++;
@@ -269,11 +277,16 @@ void summary_of(const pk_job* j, pk_summary* o) {
 // cancelled at a stage boundary
 pk_status run_request(pk_server* s, Request* q, pk_job* job, pk_summary* sum) {
   const pk_params& p = q->req.params;
+  const uint64_t t0 = now_ns();
   pk_status r = pk_count(job, q->req.fasta, q->req.fasta_bytes, &p);
+  const uint64_t t1 = now_ns();
+  q->phase_ns[0] += t1 - t0;
   if (r != PK_OK) return r;
   if (cancelled(s, q)) return pk::set_error(PK_ERR_CANCELLED, "cancelled after counting");
   PK_TRY(pk::cutoff_enqueue(job, p.num_buckets));
   PK_TRY(pk::sync_scalars(job));
+  const uint64_t t2 = now_ns();
+  q->phase_ns[1] += t2 - t1;
   summary_of(job, sum);
   if (job->h_sc->n_kept == 0)
     return pk::set_error(PK_ERR_EMPTY, "no k-mer reaches the cutoff " + std::to_string(job->h_sc->cutoff) +
@@ -281,6 +294,7 @@ pk_status run_request(pk_server* s, Request* q, pk_job* job, pk_summary* sum) {
   if (cancelled(s, q)) return pk::set_error(PK_ERR_CANCELLED, "cancelled after the histogram cutoff");
   PK_TRY(pk::mn_enqueue(job, 0, job->h_sc->n_kept));
   PK_TRY(pk::sync_scalars(job));
+  q->phase_ns[2] += now_ns() - t2;
   summary_of(job, sum);
   return PK_OK;
 }
@@ -344,6 +358,7 @@ void worker_main(pk_server* s, bool small_only) {
         continue;
       }
     }
+    const uint64_t t_copy = now_ns();
     if (r == PK_OK) {
       const uint64_t m = sum.n_nodes;
       const uint64_t W = q->req.params.k > 32 ? 16 : 8;
@@ -393,9 +408,12 @@ void worker_main(pk_server* s, bool small_only) {
         err = "a job for the next request";
       }
     }
+    const uint64_t t_reset = now_ns();
+    q->phase_ns[3] += t_reset - t_copy;
     // the job's device buffers go back to the context's pool, so the budget
     // accounting follows the running jobs (and the results kept on the device) only
     if (job != q->job) pk_job_reset(job);
+    q->phase_ns[4] += now_ns() - t_reset;
     finish(s, q, r, sum, err);
   }
   if (job_hi) pk_job_destroy(job_hi);
