@@ -477,6 +477,7 @@ def run_serve(args, rank, world):
         th = threading.Thread(target=producer, daemon=True)
         th.start()
         lat, ratio, first_submit, last_end, windows, mismatches = [], [], None, 0, 0, 0
+        small_ratio, large_ratio = [], []
         # results are taken in completion order and released at once, so the server's
         # pinned result blocks are recycled whatever order it ran the jobs in
         for _ in entries:
@@ -494,6 +495,8 @@ def run_serve(args, rank, world):
             srv.release(info.ticket)
             lat.append(info.latency_ms)
             ratio.append(info.latency_ms / solo[e])
+            (small_ratio if pinned[e].numel() * (2 if params[e].k > 32 else 1) <= (32 << 20)
+             else large_ratio).append(ratio[-1])
             first_submit = info.submit_ns if first_submit is None else min(first_submit, info.submit_ns)
             last_end = max(last_end, info.end_ns)
             windows += s.n_windows
@@ -507,6 +510,12 @@ def run_serve(args, rank, world):
                 "max_ms": float(lat.max()), "p50_latency_over_solo": float(np.percentile(ratio, 50)),
                 "p99_latency_over_solo": float(np.percentile(ratio, 99)),
                 "jobs_within_2x_solo": float((ratio <= 2.0).mean()),
+                "small_jobs": {"jobs": len(small_ratio),
+                               "p50_latency_over_solo": float(np.percentile(small_ratio, 50)) if small_ratio else None,
+                               "p99_latency_over_solo": float(np.percentile(small_ratio, 99)) if small_ratio else None},
+                "large_jobs": {"jobs": len(large_ratio),
+                               "p50_latency_over_solo": float(np.percentile(large_ratio, 50)) if large_ratio else None,
+                               "p99_latency_over_solo": float(np.percentile(large_ratio, 99)) if large_ratio else None},
                 "kmers_per_s": windows / span, "span_s": span,
                 "peak_admitted_gb": st["peak_admitted_bytes"] / 1e9, "requeued": st["requeued"],
                 "worker_s_by_phase": {ph: round(st[ph + "_ns"] / 1e9, 3)
