@@ -17,7 +17,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import byref, c_float, c_int, c_uint32, c_uint64, c_void_p
+from ctypes import byref, c_float, c_int, c_int32, c_uint32, c_uint64, c_void_p
 from dataclasses import dataclass
 from typing import Dict, List, Optional, Tuple
 
