@@ -519,7 +519,7 @@ def run_serve(args, rank, world):
                 "kmers_per_s": windows / span, "span_s": span,
                 "peak_admitted_gb": st["peak_admitted_bytes"] / 1e9, "requeued": st["requeued"],
                 "worker_s_by_phase": {ph: round(st[ph + "_ns"] / 1e9, 3)
-                                      for ph in ("count", "cutoff", "mn", "copyout", "release")},
+                                      for ph in ("count", "cutoff", "mn", "copyout", "release", "pin")},
                 "results_differing_from_alone": mismatches}
 
     def tables_in_the_mix():

@@ -409,6 +409,7 @@ typedef struct pk_server_stats {
    * included), histogram cutoff, macro-nodes, copying the result out, releasing the
    * job's device buffers */
   uint64_t count_ns, cutoff_ns, mn_ns, copyout_ns, release_ns;
+  uint64_t pin_ns;               /* of copyout_ns: page-locking new host blocks for results */
 } pk_server_stats;
 
 typedef struct pk_server_config {
@@ -448,8 +449,11 @@ pk_status pk_result_get(pk_server* s, uint64_t ticket, const void** keys, const 
  * pk_compact, pk_walk, ...).  The server owns it: valid until pk_result_release. */
 pk_status pk_result_job(pk_server* s, uint64_t ticket, pk_job** job);
 /* Forgets a finished request and frees what the server kept for it (host tables and a
- * kept job's device memory). */
+ * kept job's device memory).  The pinned host blocks of server-kept tables are recycled
+ * by every server of the process (up to 32 GiB of free blocks are kept). */
 pk_status pk_result_release(pk_server* s, uint64_t ticket);
+/* Frees the recycled pinned host blocks no request holds. */
+void pk_server_cache_release(void);
 pk_status pk_server_get_stats(pk_server* s, pk_server_stats* out);
 /* Device footprint the admission control assumes for a request (bytes): the FASTA,
  * keys and counts over the k-mer windows estimated from the first 256 KiB of the input,

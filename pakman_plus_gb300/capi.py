@@ -59,7 +59,7 @@ class PkServerStats(ctypes.Structure):
     _fields_ = [(n, c_uint64) for n in ("submitted", "completed", "failed", "queued", "running",
                                         "admitted_bytes", "peak_admitted_bytes", "requeued", "cancelled",
                                         "resident_bytes", "resident_jobs", "count_ns", "cutoff_ns", "mn_ns",
-                                        "copyout_ns", "release_ns")]
+                                        "copyout_ns", "release_ns", "pin_ns")]
 
 
 class PkServerConfig(ctypes.Structure):
@@ -190,6 +190,7 @@ _SIGS = {
     "pk_server_config_default": (None, [POINTER(PkServerConfig), c_int32]),
     "pk_server_create_config": (c_int, [c_void_p, c_int32, POINTER(PkServerConfig), POINTER(c_void_p)]),
     "pk_cancel": (c_int, [c_void_p, c_uint64]),
+    "pk_server_cache_release": (None, []),
     "pk_next_done": (c_int, [c_void_p, ctypes.c_int64, POINTER(c_uint64), POINTER(PkRequestInfo)]),
     "pk_result_job": (c_int, [c_void_p, c_uint64, POINTER(c_void_p)]),
     "pk_server_destroy": (None, [c_void_p]),

@@ -31,6 +31,7 @@
 #include <time.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -93,7 +94,7 @@ struct pk_server {
   int running = 0;
   uint64_t events = 0;  // requests finished and results released (re-queued requests wait for one)
   pk_server_stats st{};
-  std::vector<std::pair<size_t, void*>> pinned_free;  // pinned host blocks for kept results
+  std::atomic<uint64_t> pin_ns{0};  // time spent page-locking new result blocks
 };
 
 namespace {
@@ -139,25 +140,31 @@ uint64_t footprint(const pk_request& r) {
 
 uint64_t cost_of(const pk_request& r) { return r.fasta_bytes * (r.params.k > 32 ? 2 : 1); }
 
-// Pinned host blocks for server-kept results, recycled between requests (page-locking
-// new memory costs far more than the copy into it).  Block sizes are rounded up to a
-// power of two so blocks fit later requests of similar size.
+// Pinned host blocks for server-kept results, recycled between requests and between
+// servers of the process (page-locking new memory costs far more than the copy into it).
+// Block sizes are rounded up to a power of two so blocks fit later requests of similar
+// size; at most kPinnedCache bytes of free blocks are kept.
+constexpr uint64_t kPinnedCache = 32ull << 30;
 std::mutex g_block_mu;
 std::unordered_map<void*, size_t> g_block_size;
+std::vector<std::pair<size_t, void*>> g_pinned_free;
+uint64_t g_pinned_free_bytes = 0;
 
 void* pinned_get(pk_server* s, size_t bytes) {
   size_t sz = 4096;
   while (sz < bytes) sz <<= 1;
   {
-    std::lock_guard<std::mutex> lk(s->mu);
-    for (size_t i = 0; i < s->pinned_free.size(); i++)
-      if (s->pinned_free[i].first == sz) {
-        void* p = s->pinned_free[i].second;
-        s->pinned_free[i] = s->pinned_free.back();
-        s->pinned_free.pop_back();
+    std::lock_guard<std::mutex> lk(g_block_mu);
+    for (size_t i = 0; i < g_pinned_free.size(); i++)
+      if (g_pinned_free[i].first == sz) {
+        void* p = g_pinned_free[i].second;
+        g_pinned_free[i] = g_pinned_free.back();
+        g_pinned_free.pop_back();
+        g_pinned_free_bytes -= sz;
         return p;
       }
   }
+  const uint64_t t0 = now_ns();
   void* p = nullptr;
   if (cudaMallocHost(&p, sz) != cudaSuccess) {
     cudaGetLastError();
@@ -165,27 +172,21 @@ void* pinned_get(pk_server* s, size_t bytes) {
   }
   std::lock_guard<std::mutex> lk(g_block_mu);
   g_block_size[p] = sz;
+  s->pin_ns += now_ns() - t0;  // read under s->mu by the stats; a relaxed count is enough
   return p;
 }
 
-// called with s->mu held
-void pinned_put(pk_server* s, void* p) {
+void pinned_put(pk_server*, void* p) {
   if (!p) return;
-  size_t sz;
-  {
-    std::lock_guard<std::mutex> lk(g_block_mu);
-    sz = g_block_size[p];
+  std::lock_guard<std::mutex> lk(g_block_mu);
+  const size_t sz = g_block_size[p];
+  if (g_pinned_free_bytes + sz > kPinnedCache) {
+    cudaFreeHost(p);
+    g_block_size.erase(p);
+    return;
   }
-  s->pinned_free.emplace_back(sz, p);
-}
-
-void pinned_release_all(pk_server* s) {
-  for (auto& b : s->pinned_free) {
-    cudaFreeHost(b.second);
-    std::lock_guard<std::mutex> lk(g_block_mu);
-    g_block_size.erase(b.second);
-  }
-  s->pinned_free.clear();
+  g_pinned_free.emplace_back(sz, p);
+  g_pinned_free_bytes += sz;
 }
 
 // called with s->mu held
@@ -490,7 +491,6 @@ void pk_server_destroy(pk_server* s) {
   }
   for (auto& t : s->threads) t.join();
   for (auto& kv : s->reqs) free_request(s, kv.second);
-  pinned_release_all(s);
   delete s;
 }
 
@@ -636,7 +636,18 @@ pk_status pk_server_get_stats(pk_server* s, pk_server_stats* out) {
   if (!s || !out) return pk::set_error(PK_ERR_INVALID, "server and out must not be null");
   std::lock_guard<std::mutex> lk(s->mu);
   *out = s->st;
+  out->pin_ns = s->pin_ns.load();
   return PK_OK;
+}
+
+void pk_server_cache_release(void) {
+  std::lock_guard<std::mutex> lk(g_block_mu);
+  for (auto& b : g_pinned_free) {
+    cudaFreeHost(b.second);
+    g_block_size.erase(b.second);
+  }
+  g_pinned_free.clear();
+  g_pinned_free_bytes = 0;
 }
 
 }  // extern "C"

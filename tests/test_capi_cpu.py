@@ -78,7 +78,7 @@ def test_serving_structs_and_footprint(lib):
     # pk_request: pointer, size, 64-byte params, three pointers, capacity
     assert ctypes.sizeof(capi.PkRequest) == 8 + 8 + 64 + 8 * 3 + 8 + 4 * 4
     assert ctypes.sizeof(capi.PkRequestInfo) == 8 + 48 + 8 * 3 + 8
-    assert ctypes.sizeof(capi.PkServerStats) == 16 * 8
+    assert ctypes.sizeof(capi.PkServerStats) == 17 * 8
     assert ctypes.sizeof(capi.PkServerConfig) == 8 + 4 + 4 + 4 * 4
     cfg = capi.PkServerConfig()
     lib.pk_server_config_default(ctypes.byref(cfg), 8)
