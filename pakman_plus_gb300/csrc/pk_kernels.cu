@@ -1036,7 +1036,7 @@ __global__ void __launch_bounds__(512, 2) k_fine_count(const KeyT* __restrict__ 
   // the region tables live in shared memory: the slice -> region search of every slice
   // reads no global memory
   __shared__ uint32_t s_ss[(1 << kCoarseBits) + 1], s_cs[(1 << kCoarseBits) + 1];
-  for (int i = tid; i <= Cn; i += FC::T) {
+  for (int i = tid; i <= Cn; i += (int)blockDim.x) {
     s_ss[i] = slice_start[i];
     s_cs[i] = cstart[i];
   }
@@ -1054,17 +1054,17 @@ __global__ void __launch_bounds__(512, 2) k_fine_count(const KeyT* __restrict__ 
         s_g = lo;
       }
     }
-    for (int i = tid; i < FB; i += FC::T) s_hist[i] = 0;
+    for (int i = tid; i < FB; i += (int)blockDim.x) s_hist[i] = 0;
     __syncthreads();
     const uint32_t sl = s_slice;
     if (sl >= nslices) break;
     const uint32_t g = s_g;
     const uint32_t r0 = s_cs[g] + (sl - s_ss[g]) * slice_keys;
     const uint32_t r1 = min(r0 + slice_keys, s_cs[g + 1]);
-    for (uint32_t i = r0 + tid; i < r1; i += FC::T)
+    for (uint32_t i = r0 + tid; i < r1; i += blockDim.x)
       atomicAdd(&s_hist[(uint32_t)(in[i] >> fshift) & (uint32_t)(FB - 1)], 1u);
     __syncthreads();
-    for (int f = tid; f < FB; f += FC::T)
+    for (int f = tid; f < FB; f += (int)blockDim.x)
       if (s_hist[f]) atomicAdd(&bcount[((uint32_t)g << fb) + f], s_hist[f]);
   }
 }
