@@ -82,7 +82,7 @@ int pk::job_buffers(pk_job* j, DevBuf** out, int cap) {
                    &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring,
                    &j->gfirst, &j->gcount, &j->chunk_bucket, &j->gdone,
                    &j->chunk_u, &j->acc_keys[0], &j->acc_keys[1], &j->acc_counts[0], &j->acc_counts[1],
-                   &j->merge_keys, &j->merge_counts, &j->merge_part};
+                   &j->merge_keys, &j->merge_counts, &j->merge_part, &j->units};
   const int n = (int)(sizeof(all) / sizeof(all[0]));
   for (int i = 0; i < n && i < cap; i++) out[i] = all[i];
   return n;
@@ -374,6 +374,10 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
 
   PK_TRY(job_alloc(j, j->tile_nl, sizeof(uint32_t) * (ntiles + 1)));
   PK_TRY(job_alloc(j, j->counts, sizeof(uint32_t) * (size_t)grid * HB));
+  // packed units: 4 x nseg codes, 4 x nseg bit-2 planes, nseg window masks (10 bytes per
+  // 16 input bytes)
+  const uint64_t nseg = (n + kSegBytes - 1) / kSegBytes;
+  PK_TRY(job_alloc(j, j->units, (size_t)40 * nseg));
   PK_TRY(job_alloc(j, j->bstart, sizeof(uint32_t) * (B + 1)));
   if (hb < j->bbits) PK_TRY(job_alloc(j, j->hstart, sizeof(uint32_t) * (HB + 1)));
   uint32_t* hstart = (uint32_t*)(hb < j->bbits ? j->hstart.p : j->bstart.p);
@@ -399,6 +403,10 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   a.counts = (uint32_t*)j->counts.p;
   a.bstart = hstart;
   a.sc = j->d_sc;
+  a.nseg = nseg;
+  a.unit_codes = (uint32_t*)j->units.p;
+  a.unit_nbits = a.unit_codes + 4 * nseg;
+  a.unit_windows = (unsigned long long*)(a.unit_nbits + 4 * nseg);
 
   mark_begin(j, ST_LINES);
   if (j->lines_ready) PK_CUDA(launch_tile_prefix(a, j->stream));

@@ -81,6 +81,14 @@ struct CountArgs {
   uint32_t* bstart;          // 2^bbits + 1 bucket starts
   unsigned long long n_keys; // capacity of the bucketed key buffer (scatter pass)
   Scalars* sc;
+  // Packed units written by the counting pass and rolled again by the coarse scatter.
+  // Unit u (0..3) of kSegBytes-byte segment g (its bytes 16u..16u+15) sits at
+  // [u * nseg + g] of the code and bit-2 planes; windows[g] has bit 16u + j set iff the
+  // window whose newest byte is byte j of that unit was counted.
+  uint32_t* unit_codes;      // 4 x nseg
+  uint32_t* unit_nbits;      // 4 x nseg
+  unsigned long long* unit_windows;  // nseg
+  unsigned long long nseg;   // ceil(F / kSegBytes)
 };
 
 // The table is kept "sparse": the u rows of bucket b sit at [bstart[b], bstart[b] + u),

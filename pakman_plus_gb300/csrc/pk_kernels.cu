@@ -381,6 +381,17 @@ __device__ __forceinline__ void roll_push(Roll& s, const UnitBits& u, bool drop_
   s.h0 = (s.h0 << 16) | (uint64_t)rev;
 }
 
+// The same roll from a packed unit (the coarse scatter: the counting pass already
+// decided which windows count, so no breaker history is kept).
+__device__ __forceinline__ void roll_push_codes(Roll& s, uint32_t codes, uint32_t nbits) {
+  s.r2 = (s.r2 << 32) | (s.r1 >> 32);
+  s.r1 = (s.r1 << 32) | (s.r0 >> 32);
+  s.r0 = (s.r0 << 32) | (uint64_t)codes;
+  s.n2 = (s.n2 << 32) | (s.n1 >> 32);
+  s.n1 = (s.n1 << 32) | (s.n0 >> 32);
+  s.n0 = (s.n0 << 32) | (uint64_t)nbits;
+}
+
 // The k-mer whose newest byte has age sh/2: kmer_shift ORs a byte's code bit 2 into
 // the previous base's low bit, so only bytes inside the window (age >= sh/2)
 // contribute their bit-2 plane, shifted up by one base.
@@ -525,12 +536,16 @@ k_extract(CountArgs a) {
         load_unit(buf, F, (unsigned long long)p, ww);
         roll_push(s, decode_unit(ww, drop_n), drop_n);
       }
+      const unsigned long long g = seg / kSegBytes;
+      unsigned long long counted = 0;  // windows counted, bit 16u + j
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         const unsigned long long p = seg + 16ull * u;
         if (p >= c1) break;
         const UnitBits ub = decode_unit(w[u], drop_n);
         roll_push(s, ub, drop_n);
+        a.unit_codes[u * a.nseg + g] = ub.codes;
+        a.unit_nbits[u * a.nseg + g] = ub.nbits;
         // line parity per byte: exclusive prefix XOR of the newline bits
         uint32_t x = ub.nl;
         x ^= x << 1; x ^= x << 2; x ^= x << 4; x ^= x << 8;
@@ -567,8 +582,10 @@ k_extract(CountArgs a) {
           else beta = (uint32_t)(window_key<KeyT>(s, 2 * age, kmask) >> shift);
           atomicAdd(&s_bins[beta], 1u);
           local++;
+          counted |= 1ull << (16 * u + j);
         }
       }
+      a.unit_windows[g] = counted;
     }
   }
   __syncthreads();
@@ -647,14 +664,10 @@ k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restric
   extern __shared__ __align__(16) unsigned char smem_raw[];
   KeyT* ring = reinterpret_cast<KeyT*>(smem_raw);
   __shared__ uint32_t s_w[CF::C], s_f[CF::C], s_g[CF::C];
-  __shared__ uint32_t s_wpar[CF::T / 32];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int NW = CF::T / 32;
+  const int tid = threadIdx.x;
   const int k = a.k;
   const int cshift = 2 * k - a.cbits;  // coarse bucket = leading cbits bits
   const KeyT kmask = KeyOps<KeyT>::mask(2 * k);
-  const bool drop_n = a.drop_n != 0;
-  const uint8_t* __restrict__ buf = a.fasta;
   const unsigned long long F = a.F;
   const unsigned long long s0 = a.sc->s0;
   const int c = blockIdx.x;
@@ -667,72 +680,36 @@ k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restric
   __syncthreads();
   const unsigned long long c0 = (unsigned long long)c * a.chunk;
   const unsigned long long c1 = min(c0 + a.chunk, F);
-  const int warm_units = (k - 1 + 15) / 16;
+  const int warm_units = (k - 1 + 15) / 16;  // <= 4 (k <= 64): all in the previous segment
+  const unsigned long long nseg = a.nseg;
   if (c0 < c1 && s0 < F) {
-    uint32_t carry = (a.tile_nl[c0 / kTileBytes] ^ a.sc->nl_before_s0) & 1u;
     for (unsigned long long base = c0; base < c1; base += (unsigned long long)CF::T * kSegBytes) {
       const unsigned long long seg = base + (unsigned long long)tid * kSegBytes;
       const bool active = seg < c1;
-      uint32_t w[4][4];
-      uint32_t nlc = 0;
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        unsigned long long p = seg + 16ull * u;
-        if (active && p < c1) {
-          load_unit(buf, F, p, w[u]);
-#pragma unroll
-          for (int i = 0; i < 4; i++) nlc += __popc(__vcmpeq4(w[u][i], 0x0A0A0A0Au)) >> 3;
-        } else {
-          w[u][0] = w[u][1] = w[u][2] = w[u][3] = 0;
-        }
-      }
-      const unsigned bal = __ballot_sync(FULLMASK, nlc & 1u);
-      if (lane == 0) s_wpar[warp] = __popc(bal) & 1u;
-      __syncthreads();
-      uint32_t wp = 0, tot = 0;
-#pragma unroll
-      for (int i = 0; i < NW; i++) {
-        uint32_t x = s_wpar[i];
-        tot ^= x;
-        if (i < warp) wp ^= x;
-      }
-      __syncthreads();
-      uint32_t pin = carry ^ wp ^ (__popc(bal & lanemask_lt()) & 1u);
-      carry ^= tot;
-
+      const unsigned long long g = seg / kSegBytes;
+      // the counting pass's packed units: codes, bit-2 plane and the windows it counted
+      // (no FASTA decode, no line parity, no window checks here)
       Roll s;
       s.r0 = s.r1 = s.r2 = 0;
       s.n0 = s.n1 = s.n2 = 0;
       s.h0 = s.h1 = 0;
+      unsigned long long counted = 0;
       if (active) {
-        for (int u = warm_units; u >= 1; u--) {
-          long long p = (long long)seg - 16ll * u;
-          if (p < 0) continue;
-          uint32_t ww[4];
-          load_unit(buf, F, (unsigned long long)p, ww);
-          roll_push(s, decode_unit(ww, drop_n), drop_n);
-        }
+        counted = __ldg(a.unit_windows + g);
+        if (g > 0)
+          for (int wu = warm_units; wu >= 1; wu--) {
+            const unsigned long long q = (unsigned long long)(4 - wu) * nseg + g - 1;
+            roll_push_codes(s, __ldg(a.unit_codes + q), __ldg(a.unit_nbits + q));
+          }
       }
 #pragma unroll
       for (int u = 0; u < 4; u++) {
-        const unsigned long long p = seg + 16ull * u;
-        const bool live = active && p < c1;
+        const bool live = active && seg + 16ull * u < c1;
         uint32_t v = 0;
-        bool all_clear = false;
         if (live) {
-          const UnitBits ub = decode_unit(w[u], drop_n);
-          roll_push(s, ub, drop_n);
-          uint32_t x = ub.nl;
-          x ^= x << 1; x ^= x << 2; x ^= x << 4; x ^= x << 8;
-          const uint32_t ex = (x << 1) & 0xffffu;
-          const uint32_t odd = (pin ? ~ex : ex) & 0xffffu;
-          pin ^= __popc(ub.nl) & 1u;
-          uint32_t in = 0xffffu;
-          if (p + 16 > F) in &= (1u << (uint32_t)(F - p)) - 1u;
-          if (p < s0) in &= s0 - p >= 16 ? 0u : ~((1u << (uint32_t)(s0 - p)) - 1u);
-          v = odd & in & ~ub.nl;
-          all_clear = k + 15 <= 64 ? window_clear(s, 0, k + 15)
-                                   : (s.h0 == 0 && (s.h1 & ((1ull << (k + 15 - 64)) - 1ull)) == 0);
+          const unsigned long long q = (unsigned long long)u * nseg + g;
+          roll_push_codes(s, __ldg(a.unit_codes + q), __ldg(a.unit_nbits + q));
+          v = (uint32_t)(counted >> (16 * u)) & 0xffffu;
         }
 #pragma unroll
         for (int half = 0; half < 16 / CF::BP; half++) {
@@ -741,7 +718,6 @@ k_scatter_coarse(CountArgs a, const uint32_t* __restrict__ coff, KeyT* __restric
             const int j = half * CF::BP + jj;
             if (!((v >> j) & 1u)) continue;
             const int age = 15 - j;
-            if (!all_clear && !window_clear(s, age, k)) continue;
             const KeyT key = window_key<KeyT>(s, 2 * age, kmask);
             const uint32_t b = (uint32_t)(key >> cshift);
             const uint32_t pos = atomicAdd(&s_w[b], 1u);

@@ -135,7 +135,9 @@ uint64_t footprint(const pk_request& r) {
   const uint64_t N = r.fasta ? estimate_windows(r) : F;
   const uint64_t V = N / 12;
   const uint64_t fixed = 64ull << 20;  // per-bucket tables, histograms, look-back flags
-  return F + N * (2 * W + 4) + V * (W + 4) + 2 * V * (W + 32) + fixed;
+  // FASTA, its packed units (10 bytes per 16), two key arrays and the counts, kept rows,
+  // macro-nodes
+  return F + F / 16 * 10 + N * (2 * W + 4) + V * (W + 4) + 2 * V * (W + 32) + fixed;
 }
 
 uint64_t cost_of(const pk_request& r) { return r.fasta_bytes * (r.params.k > 32 ? 2 : 1); }
