@@ -147,9 +147,11 @@ def stage_bytes(stage: str, F: int, N: int, U: int, V: int, M: int, W: int, t: i
     """Algorithmic bytes one launch of a stage must move (read + write)."""
     return {
         "line_scan": F,
-        "bucket_count": F + 4 * G * B,
+        # the counting pass also writes each 16-byte unit packed (10 bytes), which the
+        # coarse scatter reads instead of the FASTA
+        "bucket_count": F + 5 * F // 8 + 4 * G * B,
         "bucket_offsets": 3 * 4 * G * B,
-        "scatter_coarse": F + N * W,
+        "scatter_coarse": 5 * F // 8 + N * W,
         "scatter_fine": 2 * N * W,
         "bucket_table": N * W + U * (W + 4),
         "cutoff": 8 * t,
