@@ -32,6 +32,9 @@ constexpr int kSegBytes = 64;       // bytes per thread per extraction step
 constexpr int kBucketThreads = 512;
 constexpr int kMnThreads = 128;
 constexpr int kMnCap = 1536;        // items (k-mer records) per macro-node segment on chip
+constexpr int kMnBinBits = 8;       // counting-sort bins of a macro-node segment
+constexpr int kMnBins = 1 << kMnBinBits;
+constexpr int kMnBinMax = 32;       // largest bin ranked within itself (else merge ranks)
 constexpr int kHistSmem = 1024;     // count-histogram bins kept in shared memory
 constexpr int kBucketStack = 256;   // pending sub-ranges of one bucket
 constexpr int kSplitWays = 4;      // pieces an overflowing sub-range is cut into

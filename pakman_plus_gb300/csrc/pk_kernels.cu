@@ -1987,6 +1987,8 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
   __shared__ uint32_t s_warp[33];
   __shared__ uint32_t s_beta, s_off[6], s_cur[5], s_end[5], s_segend[5], s_beg[5], s_last;
   __shared__ unsigned long long s_NO;
+  // counting-sort bins of a segment: offset (low 16 bits) and fill (high 16 bits)
+  __shared__ uint32_t s_bin[kMnBins];
 
   const int tid = threadIdx.x;
   const int Bu = 1 << (a.bbits - 2 * a.level);  // node units
@@ -1997,6 +1999,13 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
   const KeyT* __restrict__ kk = reinterpret_cast<const KeyT*>(a.kkeys);
   KeyT* __restrict__ nkeys = reinterpret_cast<KeyT*>(a.nkeys);
   constexpr uint32_t CAP = kMnCap - 16;  // rows per segment before ties
+  // every node key of a unit shares its top pbits bits; the sort bins are the next
+  // (at most kMnBinBits) bits
+  const int pbits = a.bbits - 2 * a.level;
+  const int rbits = nb - pbits > 0 ? nb - pbits : 0;
+  const int dbits = rbits < kMnBinBits ? rbits : kMnBinBits;
+  const int bsh = rbits - dbits;
+  const uint32_t bmask = (1u << dbits) - 1u;
 
   // kept rows beyond the kept buffers were not written: nothing to merge (every CTA
   // reads the same flag, so all of them leave)
@@ -2107,18 +2116,66 @@ __global__ void __launch_bounds__(kMnThreads, 8) k_macro_nodes(MnArgs a) {
           icnt[i] = a.kcounts[row];
         }
         __syncthreads();
-        // ---- merge rank of every item across the five runs
-        for (uint32_t i = tid; i < mm; i += kMnThreads) {
-          int st = 0;
-          while (i >= s_off[st + 1]) st++;
-          const KeyT x = ikey[i];
-          uint32_t rank = i - s_off[st];
-          for (int b = 0; b < 5; b++) {
-            if (b == st) continue;
-            const uint32_t lo = s_off[b], hi = s_off[b + 1];
-            rank += (b < st ? upper_bound_s(ikey, lo, hi, x) : lower_bound_s(ikey, lo, hi, x)) - lo;
+        // ---- order of the items by node key, ties by run and then position (the stable
+        //      merge of the five runs): a counting sort on the key bits below the unit's
+        //      common prefix, then each item's rank among its bin, which holds a few items.
+        //      A crowded bin falls back to merge ranks across the runs.
+        for (int b = tid; b < kMnBins; b += kMnThreads) s_bin[b] = 0;
+        __syncthreads();
+        for (uint32_t i = tid; i < mm; i += kMnThreads)
+          atomicAdd(&s_bin[(uint32_t)KeyOps<KeyT>::shr(ikey[i], bsh) & bmask], 1u);
+        __syncthreads();
+        {
+          constexpr int BPT = kMnBins / kMnThreads;
+          uint32_t hv[BPT], hs = 0, hm = 0;
+#pragma unroll
+          for (int q = 0; q < BPT; q++) {
+            hv[q] = s_bin[tid * BPT + q];
+            hs += hv[q];
+            hm = max(hm, hv[q]);
           }
-          ord[rank] = (uint16_t)i;
+          uint32_t tot;
+          uint32_t ex = block_exclusive_sum(hs, s_warp, tot);
+#pragma unroll
+          for (int q = 0; q < BPT; q++) {
+            s_bin[tid * BPT + q] = ex;
+            ex += hv[q];
+          }
+          const bool crowded = __syncthreads_or(hm > (uint32_t)kMnBinMax) != 0;
+          if (!crowded) {
+            uint16_t* binned = nid;  // scratch until the node ids are computed
+            for (uint32_t i = tid; i < mm; i += kMnThreads) {
+              const uint32_t o = atomicAdd(&s_bin[(uint32_t)KeyOps<KeyT>::shr(ikey[i], bsh) & bmask], 1u << 16);
+              binned[(o & 0xffffu) + (o >> 16)] = (uint16_t)i;
+            }
+            __syncthreads();
+            for (uint32_t p = tid; p < mm; p += kMnThreads) {
+              const uint32_t i = binned[p];
+              const KeyT x = ikey[i];
+              const uint32_t o = s_bin[(uint32_t)KeyOps<KeyT>::shr(x, bsh) & bmask];
+              const uint32_t b0 = o & 0xffffu, b1 = b0 + (o >> 16);
+              uint32_t rank = 0;
+              for (uint32_t j = b0; j < b1; j++) {
+                const uint32_t ij = binned[j];
+                const KeyT y = ikey[ij];
+                rank += (y < x || (!(x < y) && ij < i)) ? 1u : 0u;
+              }
+              ord[b0 + rank] = (uint16_t)i;
+            }
+          } else {
+            for (uint32_t i = tid; i < mm; i += kMnThreads) {
+              int st = 0;
+              while (i >= s_off[st + 1]) st++;
+              const KeyT x = ikey[i];
+              uint32_t rank = i - s_off[st];
+              for (int b = 0; b < 5; b++) {
+                if (b == st) continue;
+                const uint32_t lo = s_off[b], hi = s_off[b + 1];
+                rank += (b < st ? upper_bound_s(ikey, lo, hi, x) : lower_bound_s(ikey, lo, hi, x)) - lo;
+              }
+              ord[rank] = (uint16_t)i;
+            }
+          }
         }
         __syncthreads();
         // ---- node boundaries and node index per merged position: each thread takes
