@@ -415,7 +415,6 @@ def run_serve(args, rank, world):
     t_ora = 0.0
     threads = os.cpu_count() or 1
     device_ms = []  # kernel time of each entry alone (CUDA events around its stages)
-    h2d_ms = []  # its input copy alone
     with pk.Job(ctx) as job:
         for e, rs in enumerate(pool):
             t0 = time.perf_counter()
@@ -450,30 +449,34 @@ def run_serve(args, rank, world):
                 pass
             stages = job.stage_times()
             device_ms.append(sum(v for k, v in stages.items() if k != "h2d"))
-            h2d_ms.append(stages.get("h2d", 0.0))
             job.enable_timing(False)
             job.reset()
-    # each entry's solo latency through the server (nothing else in flight), best of two
-    solo = []
+    # each entry's solo latency through the server (nothing else in flight), best of two,
+    # with the table copied to pinned host memory and with it kept on the device
+    solo, solo_res = [], []
     srv = pk.Server(ctx, workers=args.serve_workers)
     for e in range(len(pool)):
-        best = None
-        for _ in range(2):
-            tk = srv.submit(pinned[e].numpy(), params[e])
-            try:
-                srv.wait(tk)
-            except pk.PakmanError:
-                pass
-            lat = srv.poll(tk).latency_ms
-            srv.release(tk)
-            best = lat if best is None else min(best, lat)
-        solo.append(best)
+        for keep, out in ((False, solo), (True, solo_res)):
+            best = None
+            for _ in range(2):
+                tk = srv.submit(pinned[e].numpy(), params[e], keep_on_device=keep)
+                try:
+                    srv.wait(tk)
+                except pk.PakmanError:
+                    pass
+                lat = srv.poll(tk).latency_ms
+                srv.release(tk)
+                best = lat if best is None else min(best, lat)
+            out.append(best)
     srv.close()
     rng = np.random.Generator(np.random.PCG64(5_000_001))
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, args.serve_jobs))
     entries = [i % len(pool) for i in range(args.serve_jobs)]
 
-    def serve(workers, arrival):
+    def serve(workers, arrival, resident=False):
+        """The stream through a server of `workers` workers; `resident`: every table stays
+        on the device (keep_on_device) until the consumer releases it, instead of the
+        macro-node table crossing to pinned host memory."""
         srv = pk.Server(ctx, workers=workers)
         tickets = [None] * args.serve_jobs
         by_ticket = {}
@@ -484,7 +487,7 @@ def run_serve(args, rank, world):
                 dt = t0 + arrival[i] - time.perf_counter()
                 if dt > 0:
                     time.sleep(dt)
-                t = srv.submit(pinned[e].numpy(), params[e])
+                t = srv.submit(pinned[e].numpy(), params[e], keep_on_device=resident)
                 tickets[i] = t
                 by_ticket[t] = i
 
@@ -508,7 +511,7 @@ def run_serve(args, rank, world):
                 mismatches += 1
             srv.release(info.ticket)
             lat.append(info.latency_ms)
-            ratio.append(info.latency_ms / solo[e])
+            ratio.append(info.latency_ms / (solo_res[e] if resident else solo[e]))
             (small_ratio if pinned[e].numel() * (2 if params[e].k > 32 else 1) <= (32 << 20)
              else large_ratio).append(ratio[-1])
             first_submit = info.submit_ns if first_submit is None else min(first_submit, info.submit_ns)
@@ -519,7 +522,8 @@ def run_serve(args, rank, world):
         srv.close()
         lat, ratio = np.array(lat), np.array(ratio)
         span = (last_end - first_submit) / 1e9
-        return {"workers": workers, "p50_ms": float(np.percentile(lat, 50)),
+        return {"workers": workers, "results": "resident on the device" if resident else "pinned host memory",
+                "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
                 "max_ms": float(lat.max()), "p50_latency_over_solo": float(np.percentile(ratio, 50)),
                 "p99_latency_over_solo": float(np.percentile(ratio, 99)),
@@ -579,6 +583,10 @@ def run_serve(args, rank, world):
     served_sat = serve(args.serve_workers, at_once)
     plain_sat = serve(1, at_once)
     link_after = link_gbps()
+    # tables kept on the device: no macro-node table crosses the host link
+    served_res = serve(args.serve_workers, arrivals, resident=True)
+    served_res_sat = serve(args.serve_workers, at_once, resident=True)
+    plain_res_sat = serve(1, at_once, resident=True)
     total_windows = sum(alone[e][0].n_windows for e in entries)
     offered = total_windows / arrivals[-1]
     # what the GPU could serve if the stream's kernels ran back to back with nothing
@@ -597,9 +605,8 @@ def run_serve(args, rank, world):
                        "offered_kmers_per_s": offered,
                        "alone_ms_by_entry": [round(a[1] * 1000, 2) for a in alone],
                        "solo_served_ms_by_entry": [round(x, 2) for x in solo],
+                       "solo_resident_ms_by_entry": [round(x, 2) for x in solo_res],
                        "device_ms_by_entry": [round(x, 3) for x in device_ms],
-                       "h2d_gbps_alone": pool_bytes / 1e6 / max(sum(h2d_ms), 1e-9),
-                       "h2d_ms_by_entry": [round(x, 3) for x in h2d_ms],
                        "link_h2d_gbps_before_after_streams": [round(link_before, 1), round(link_after, 1)],
                        "device_bound_kmers_per_s": device_bound,
                        "small_jobs_kmer_share": small_windows / total_windows,
@@ -611,11 +618,16 @@ def run_serve(args, rank, world):
             "served": served, "plain_one_job_at_a_time": plain,
             "saturation": {"served": served_sat, "plain_one_job_at_a_time": plain_sat,
                            "capacity_ratio": served_sat["kmers_per_s"] / plain_sat["kmers_per_s"],
-                           "served_over_device_bound": served_sat["kmers_per_s"] / device_bound}}
+                           "served_over_device_bound": served_sat["kmers_per_s"] / device_bound},
+            "resident": {"served": served_res,
+                         "saturation": {"served": served_res_sat, "plain_one_job_at_a_time": plain_res_sat,
+                                        "capacity_ratio": served_res_sat["kmers_per_s"] / plain_res_sat["kmers_per_s"],
+                                        "served_over_device_bound": served_res_sat["kmers_per_s"] / device_bound}}}
     print(json.dumps(line), flush=True)
     ctx.close()
     bad = sum(not x for x in oracle_ok) + mix_check["macro_node_tables_differing"] + sum(
-        r["results_differing_from_alone"] for r in (served, plain, served_sat, plain_sat))
+        r["results_differing_from_alone"] for r in (served, plain, served_sat, plain_sat, served_res,
+                                                    served_res_sat, plain_res_sat))
     if bad:
         print("bench: served results differ from the oracle or from the jobs run alone", file=sys.stderr)
         return 3

@@ -95,6 +95,11 @@ struct pk_server {
   uint64_t events = 0;  // requests finished and results released (re-queued requests wait for one)
   pk_server_stats st{};
   std::atomic<uint64_t> pin_ns{0};  // time spent page-locking new result blocks
+  // idle jobs with streams of their own: a request kept on the device takes its
+  // worker's job and the worker continues with one of these; a released resident
+  // job is reset and comes back here (creating and destroying jobs page-locks and
+  // frees memory, which can wait for the whole device)
+  std::vector<pk_job*> spare;
 };
 
 namespace {
@@ -393,19 +398,23 @@ void worker_main(pk_server* s, bool small_only) {
       }
     }
     if (r == PK_OK && q->req.keep_on_device) {
-      // the finished job goes to the request, on a stream of its own (its work is
-      // complete); the worker continues with a new job on its stream
+      // the finished job goes to the request (its work is complete) on the stream of
+      // a spare job, which takes the worker's stream and the worker's place
       pk_job* fresh = nullptr;
-      cudaStream_t own = nullptr;
-      if (pk_job_create(s->ctx, job == job_hi ? st_hi : st_lo, &fresh) == PK_OK &&
-          cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking) == cudaSuccess) {
-        job->stream = own;
-        job->own_stream = true;
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (!s->spare.empty()) {
+          fresh = s->spare.back();
+          s->spare.pop_back();
+        }
+      }
+      if (fresh || pk_job_create(s->ctx, nullptr, &fresh) == PK_OK) {
+        std::swap(job->stream, fresh->stream);
+        std::swap(job->own_stream, fresh->own_stream);
         pk_job_memory(job, &q->resident);
         q->job = job;
         job = fresh;
       } else {
-        if (fresh) pk_job_destroy(fresh);
         cudaGetLastError();
         r = PK_ERR_NOMEM;
         err = "a job for the next request";
@@ -431,7 +440,12 @@ void free_request(pk_server* s, Request* q) {
   pinned_put(s, q->own_suf);
   pinned_put(s, q->own_pre);
   if (q->job) {
-    pk_job_destroy(q->job);
+    // its device buffers go back to the context's pool; the job itself is kept for
+    // the next request kept on the device
+    if (!s->stop && s->spare.size() < (size_t)(2 * s->workers) && pk_job_reset(q->job) == PK_OK)
+      s->spare.push_back(q->job);
+    else
+      pk_job_destroy(q->job);
     s->st.resident_bytes -= q->resident;
     s->st.resident_jobs--;
   }
@@ -493,6 +507,7 @@ void pk_server_destroy(pk_server* s) {
   }
   for (auto& t : s->threads) t.join();
   for (auto& kv : s->reqs) free_request(s, kv.second);
+  for (pk_job* j : s->spare) pk_job_destroy(j);
   delete s;
 }
 
