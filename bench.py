@@ -63,8 +63,14 @@ def parse():
     ap.add_argument("--serve-jobs", type=int, default=5000)
     ap.add_argument("--serve-rate", type=float, default=200.0, help="mean arrivals per second")
     ap.add_argument("--serve-pool", type=int, default=32, help="distinct generated read sets")
-    ap.add_argument("--serve-workers", type=int, default=8)
+    ap.add_argument("--serve-workers", type=int, default=12)
     ap.add_argument("--serve-budget-gb", type=float, default=160.0)
+    ap.add_argument("--serve-small-sms", type=int, default=16,
+                    help="SMs set aside for small requests in the SM-partition run")
+    ap.add_argument("--serve-reserved-small", type=int, default=4,
+                    help="workers that take only small requests (-1: the library's default)")
+    ap.add_argument("--serve-modes", default="host,resident,partition",
+                    help="which streams to run: host (tables to pinned host memory), resident, partition")
     ap.add_argument("--ingest", action="store_true",
                     help="file ingest benchmark: FASTA file -> macro-node table on the host, read "
                          "into memory then counted, against streamed by pk_count_file")
@@ -473,11 +479,14 @@ def run_serve(args, rank, world):
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, args.serve_jobs))
     entries = [i % len(pool) for i in range(args.serve_jobs)]
 
-    def serve(workers, arrival, resident=False):
+    def serve(workers, arrival, resident=False, small_sms=0):
         """The stream through a server of `workers` workers; `resident`: every table stays
         on the device (keep_on_device) until the consumer releases it, instead of the
-        macro-node table crossing to pinned host memory."""
-        srv = pk.Server(ctx, workers=workers)
+        macro-node table crossing to pinned host memory; `small_sms`: SMs set aside for
+        small requests (an SM partition)."""
+        rsv = args.serve_reserved_small if args.serve_reserved_small >= 0 and workers > 1 else None
+        srv = pk.Server(ctx, workers=workers, small_sms=small_sms, reserved_small=rsv)
+        partition = srv.partition()
         tickets = [None] * args.serve_jobs
         by_ticket = {}
 
@@ -523,6 +532,7 @@ def run_serve(args, rank, world):
         lat, ratio = np.array(lat), np.array(ratio)
         span = (last_end - first_submit) / 1e9
         return {"workers": workers, "results": "resident on the device" if resident else "pinned host memory",
+                "sm_partition": {"small_requests": partition[0], "others": partition[1]} if small_sms else None,
                 "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
                 "max_ms": float(lat.max()), "p50_latency_over_solo": float(np.percentile(ratio, 50)),
@@ -575,18 +585,35 @@ def run_serve(args, rank, world):
         del dst
         return pinned[e].numel() / best / 1e9
 
+    modes = set(args.serve_modes.split(","))
+    skipped = {"skipped": "not in --serve-modes"}
     mix_check = tables_in_the_mix()
     link_before = link_gbps()
-    served = serve(args.serve_workers, arrivals)
-    plain = serve(1, arrivals)
     at_once = np.zeros(args.serve_jobs)
-    served_sat = serve(args.serve_workers, at_once)
-    plain_sat = serve(1, at_once)
+    served = plain = served_sat = plain_sat = skipped
+    if "host" in modes:
+        served = serve(args.serve_workers, arrivals)
+        plain = serve(1, arrivals)
+        served_sat = serve(args.serve_workers, at_once)
+        plain_sat = serve(1, at_once)
     link_after = link_gbps()
     # tables kept on the device: no macro-node table crosses the host link
-    served_res = serve(args.serve_workers, arrivals, resident=True)
-    served_res_sat = serve(args.serve_workers, at_once, resident=True)
-    plain_res_sat = serve(1, at_once, resident=True)
+    served_res = served_res_sat = plain_res_sat = skipped
+    if "resident" in modes:
+        served_res = serve(args.serve_workers, arrivals, resident=True)
+        served_res_sat = serve(args.serve_workers, at_once, resident=True)
+        plain_res_sat = serve(1, at_once, resident=True)
+    # small requests on SMs of their own (green contexts), tables resident
+    part = part_sat = skipped
+    if "partition" in modes:
+        try:
+            part = serve(args.serve_workers, arrivals, resident=True, small_sms=args.serve_small_sms)
+            part_sat = serve(args.serve_workers, at_once, resident=True, small_sms=args.serve_small_sms)
+        except pk.PakmanError as ex:
+            part = part_sat = {"unavailable": str(ex)}
+
+    def ratio_of(a, b):
+        return a["kmers_per_s"] / b["kmers_per_s"] if "kmers_per_s" in a and "kmers_per_s" in b else None
     total_windows = sum(alone[e][0].n_windows for e in entries)
     offered = total_windows / arrivals[-1]
     # what the GPU could serve if the stream's kernels ran back to back with nothing
@@ -594,8 +621,9 @@ def run_serve(args, rank, world):
     device_bound = total_windows / (sum(device_ms[e] for e in entries) / 1e3)
     small_windows = sum(alone[e][0].n_windows for e in entries
                         if pinned[e].numel() * (2 if params[e].k > 32 else 1) <= (32 << 20))
+    headline = served if "p99_ms" in served else served_res
     line = {"metric": "served p50/p99 latency of count + macro-node jobs", "impl": "serve",
-            "value": served["p99_ms"], "unit": "ms (p99)", "higher_is_better": False,
+            "value": headline.get("p99_ms"), "unit": "ms (p99)", "higher_is_better": False,
             "n_gpus": 1, "data": "synthetic",
             "config": {"workload": "serving: Poisson arrivals, genome log-uniform 10 kb-20 Mbp, 100 bp reads "
                                    "at 30-80x, 0.5% errors, k in {31,32,63}",
@@ -617,17 +645,20 @@ def run_serve(args, rank, world):
             "tables_in_the_mix": mix_check,
             "served": served, "plain_one_job_at_a_time": plain,
             "saturation": {"served": served_sat, "plain_one_job_at_a_time": plain_sat,
-                           "capacity_ratio": served_sat["kmers_per_s"] / plain_sat["kmers_per_s"],
-                           "served_over_device_bound": served_sat["kmers_per_s"] / device_bound},
+                           "capacity_ratio": ratio_of(served_sat, plain_sat),
+                           "served_over_device_bound": served_sat["kmers_per_s"] / device_bound
+                           if "kmers_per_s" in served_sat else None},
+            "resident_sm_partition": {"served": part, "saturation": part_sat},
             "resident": {"served": served_res,
                          "saturation": {"served": served_res_sat, "plain_one_job_at_a_time": plain_res_sat,
-                                        "capacity_ratio": served_res_sat["kmers_per_s"] / plain_res_sat["kmers_per_s"],
-                                        "served_over_device_bound": served_res_sat["kmers_per_s"] / device_bound}}}
+                                        "capacity_ratio": ratio_of(served_res_sat, plain_res_sat),
+                                        "served_over_device_bound": served_res_sat["kmers_per_s"] / device_bound
+                                        if "kmers_per_s" in served_res_sat else None}}}
     print(json.dumps(line), flush=True)
     ctx.close()
     bad = sum(not x for x in oracle_ok) + mix_check["macro_node_tables_differing"] + sum(
-        r["results_differing_from_alone"] for r in (served, plain, served_sat, plain_sat, served_res,
-                                                    served_res_sat, plain_res_sat))
+        r.get("results_differing_from_alone", 0) for r in (served, plain, served_sat, plain_sat, served_res,
+                                                           served_res_sat, plain_res_sat, part, part_sat))
     if bad:
         print("bench: served results differ from the oracle or from the jobs run alone", file=sys.stderr)
         return 3

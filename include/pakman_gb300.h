@@ -416,7 +416,13 @@ typedef struct pk_server_config {
   uint64_t small_bytes;    /* requests of at most this estimated work are small (32 MiB) */
   int32_t reserved_small;  /* workers that take only small requests (one in eight) */
   int32_t aging_ms;        /* a request waiting longer starts first (2000) */
-  int32_t reserved[4];
+  /* SMs set aside for small requests (0: none).  When > 0 the device is split into two
+   * SM partitions (green contexts): small requests run on their own SMs (rounded up to
+   * the device's partition granularity) and the rest on the others, so a small request
+   * never waits for a large one's kernels; pk_server_create_config fails with
+   * PK_ERR_CUDA when the driver cannot partition the device. */
+  int32_t small_sms;
+  int32_t reserved[3];
 } pk_server_config;
 
 void pk_server_config_default(pk_server_config* cfg, int32_t workers);
@@ -424,6 +430,9 @@ pk_status pk_server_create(pk_ctx* ctx, int32_t workers, pk_server** out);
 /* cfg NULL: the defaults of pk_server_config_default. */
 pk_status pk_server_create_config(pk_ctx* ctx, int32_t workers, const pk_server_config* cfg,
                                   pk_server** out);
+/* The SMs of the server's partitions: small requests' and the others' (both the whole
+ * device's count when the server has no partition). */
+pk_status pk_server_partition(pk_server* s, int32_t* small_sms, int32_t* large_sms);
 /* Cancels queued requests and ends running ones at their next stage boundary, waits for
  * the workers, frees every result. */
 void pk_server_destroy(pk_server* s);

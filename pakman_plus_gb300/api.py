@@ -518,9 +518,11 @@ class Server:
     alone in a :class:`Job`."""
 
     def __init__(self, ctx: Context, workers: int = 2, small_bytes: Optional[int] = None,
-                 reserved_small: Optional[int] = None, aging_ms: Optional[int] = None):
+                 reserved_small: Optional[int] = None, aging_ms: Optional[int] = None,
+                 small_sms: int = 0):
         """`small_bytes`, `reserved_small`, `aging_ms`: the scheduling knobs of
-        pk_server_config (None: the library's defaults for this many workers)."""
+        pk_server_config (None: the library's defaults for this many workers);
+        `small_sms` > 0: SMs set aside for small requests (an SM partition)."""
         self.ctx = ctx
         cfg = capi.PkServerConfig()
         capi.lib().pk_server_config_default(byref(cfg), workers)
@@ -530,11 +532,19 @@ class Server:
             cfg.reserved_small = reserved_small
         if aging_ms is not None:
             cfg.aging_ms = aging_ms
+        cfg.small_sms = small_sms
         h = c_void_p()
         check(capi.lib().pk_server_create_config(ctx.handle, workers, byref(cfg), byref(h)),
               "pk_server_create_config")
         self._h = h
         self._live: Dict[int, tuple] = {}  # ticket -> (input buffer, out arrays, params)
+
+    def partition(self) -> tuple:
+        """(SMs of small requests, SMs of the others): the SM partition, or the whole
+        device's count twice."""
+        a, b = c_int32(), c_int32()
+        check(capi.lib().pk_server_partition(self._h, byref(a), byref(b)), "pk_server_partition")
+        return a.value, b.value
 
     def submit(self, fasta, params: capi.PkParams, out=None, keep_on_device: bool = False) -> int:
         """Queue one read set.  `fasta` stays referenced until :meth:`release`.  `out` =

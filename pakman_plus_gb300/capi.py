@@ -64,7 +64,7 @@ class PkServerStats(ctypes.Structure):
 
 class PkServerConfig(ctypes.Structure):
     _fields_ = [("small_bytes", c_uint64), ("reserved_small", c_int32), ("aging_ms", c_int32),
-                ("reserved", c_int32 * 4)]
+                ("small_sms", c_int32), ("reserved", c_int32 * 3)]
 
 
 class PkBatchSet(ctypes.Structure):
@@ -191,6 +191,7 @@ _SIGS = {
     "pk_server_create_config": (c_int, [c_void_p, c_int32, POINTER(PkServerConfig), POINTER(c_void_p)]),
     "pk_cancel": (c_int, [c_void_p, c_uint64]),
     "pk_server_cache_release": (None, []),
+    "pk_server_partition": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_int32)]),
     "pk_next_done": (c_int, [c_void_p, ctypes.c_int64, POINTER(c_uint64), POINTER(PkRequestInfo)]),
     "pk_result_job": (c_int, [c_void_p, c_uint64, POINTER(c_void_p)]),
     "pk_server_destroy": (None, [c_void_p]),

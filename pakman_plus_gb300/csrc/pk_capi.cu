@@ -364,7 +364,7 @@ pk_status pk::count_impl(pk_job* j, const void* d_fasta, uint64_t n, const pk_pa
   const int hb = std::min(j->bbits, kHistBits);
   const int HB = 1 << hb;
   const uint64_t ntiles = (n + kTileBytes - 1) / kTileBytes;
-  int grid = (int)std::min<uint64_t>((uint64_t)j->ctx->sms, std::max<uint64_t>(ntiles, 1));
+  int grid = (int)std::min<uint64_t>((uint64_t)thread_sms(j->ctx->sms), std::max<uint64_t>(ntiles, 1));
   unsigned long long chunk = (ntiles + grid - 1) / grid * (unsigned long long)kTileBytes;
   if (chunk == 0) chunk = kTileBytes;
   if (j->chunk_mult > 1) chunk *= (unsigned long long)j->chunk_mult;  // fewer, longer chunks
@@ -511,7 +511,7 @@ static pk_status table_impl(pk_job* j, uint64_t N, int t) {
   b.cap = N;
   b.spin_limit = (int)j->wait_limit;
   b.sc = j->d_sc;
-  PK_CUDA(launch_bucket_table(b, j->wide, j->table_ctas > 0 ? j->table_ctas * j->ctx->sms : 0, j->stream));
+  PK_CUDA(launch_bucket_table(b, j->wide, j->table_ctas > 0 ? j->table_ctas * thread_sms(j->ctx->sms) : 0, j->stream));
   mark_end(j, ST_TABLE);
   j->pieces = 1;
   j->stage = 1;

@@ -166,6 +166,11 @@ struct WireRow {
 };
 
 // Launchers (all stream-ordered, no host synchronisation).
+// SM count the calling thread's launches are sized for (a serving worker on an SM
+// partition sets its partition's count; 0 restores the whole device)
+void set_thread_sms(int n);
+int thread_sms(int device_sms);
+
 cudaError_t launch_line_scan(const CountArgs& a, cudaStream_t st);
 // chunk items of the giant buckets (n_b >= kGiantKeys): floor(n_b / kChunkKeys)
 // consecutive items each, from gfirst[b], gcount[b] of them; chunk_bucket maps an item

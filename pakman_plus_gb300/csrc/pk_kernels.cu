@@ -2288,7 +2288,14 @@ static std::atomic<unsigned long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static int g_sms = 0;
+// SM count the calling thread's launches are sized for: a serving worker running a
+// request on an SM partition sets it to the partition's SMs (0: the whole device)
+static thread_local int t_sms = 0;
+void set_thread_sms(int n) { t_sms = n > 0 ? n : 0; }
+int thread_sms(int device_sms) { return t_sms > 0 ? t_sms : device_sms; }
+
 static int sm_count() {
+  if (t_sms > 0) return t_sms;
   if (!g_sms) {
     int dev = 0;
     cudaGetDevice(&dev);

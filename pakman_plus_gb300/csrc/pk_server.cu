@@ -25,6 +25,8 @@
 // at its next stage boundary).  A request submitted with keep_on_device hands its job
 // -- the k-mer table and macro-nodes resident in HBM -- to the caller, who can run
 // further stages on it (pk_copy_table, pk_compact, pk_walk, ...) until releasing it.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -100,6 +102,13 @@ struct pk_server {
   // job is reset and comes back here (creating and destroying jobs page-locks and
   // frees memory, which can wait for the whole device)
   std::vector<pk_job*> spare;
+  // SM partition (cfg.small_sms > 0): small requests on green context g_small's SMs,
+  // the others on g_large's; the driver calls come through the runtime's entry-point
+  // query, so the library does not link the driver library itself
+  CUgreenCtx g_small = nullptr, g_large = nullptr;
+  int sms_small = 0, sms_large = 0;
+  PFN_cuGreenCtxStreamCreate_v12050 green_stream = nullptr;
+  PFN_cuGreenCtxDestroy_v12040 green_destroy = nullptr;
 };
 
 namespace {
@@ -313,8 +322,14 @@ void worker_main(pk_server* s, bool small_only) {
   cudaSetDevice(s->ctx->device);
   cudaDeviceGetStreamPriorityRange(&least, &greatest);
   cudaStream_t st_hi = nullptr, st_lo = nullptr;
-  cudaStreamCreateWithPriority(&st_hi, cudaStreamNonBlocking, greatest);
-  cudaStreamCreateWithPriority(&st_lo, cudaStreamNonBlocking, least);
+  if (s->g_small) {
+    // small requests on the small partition's SMs, the others on the rest
+    s->green_stream(&st_hi, s->g_small, CU_STREAM_NON_BLOCKING, greatest);
+    s->green_stream(&st_lo, s->g_large, CU_STREAM_NON_BLOCKING, least);
+  } else {
+    cudaStreamCreateWithPriority(&st_hi, cudaStreamNonBlocking, greatest);
+    cudaStreamCreateWithPriority(&st_lo, cudaStreamNonBlocking, least);
+  }
   pk_job* job_hi = nullptr;
   pk_job* job_lo = nullptr;
   pk_status cs = pk_job_create(s->ctx, st_hi, &job_hi);
@@ -345,6 +360,8 @@ void worker_main(pk_server* s, bool small_only) {
       continue;
     }
     pk_job*& job = q->small ? job_hi : job_lo;
+    // grids sized for the partition the request runs on
+    pk::set_thread_sms(s->g_small ? (q->small ? s->sms_small : s->sms_large) : 0);
     pk_status r = run_request(s, q, job, &sum);
     std::string err = r == PK_OK ? std::string() : std::string(pk_last_error());
     if (r == PK_ERR_NOMEM) {
@@ -459,6 +476,62 @@ Request* find(pk_server* s, uint64_t ticket) {
 
 }  // namespace
 
+namespace {
+
+template <typename F>
+bool driver_fn(const char* name, F* fn) {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+  if (cudaGetDriverEntryPointByVersion(name, &p, 12050, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !p) {
+    cudaGetLastError();
+    return false;
+  }
+  *fn = reinterpret_cast<F>(p);
+  return true;
+}
+
+// Splits the device into `small_sms` SMs (rounded up by the driver) for small requests
+// and the rest for the others, one green context each.
+pk_status make_partition(pk_server* s, int small_sms) {
+  PFN_cuDeviceGet_v2000 device_get = nullptr;
+  PFN_cuDeviceGetDevResource_v12040 get_resource = nullptr;
+  PFN_cuDevSmResourceSplitByCount_v12040 split = nullptr;
+  PFN_cuDevResourceGenerateDesc_v12040 make_desc = nullptr;
+  PFN_cuGreenCtxCreate_v12040 green_create = nullptr;
+  if (!driver_fn("cuDeviceGet", &device_get) || !driver_fn("cuDeviceGetDevResource", &get_resource) ||
+      !driver_fn("cuDevSmResourceSplitByCount", &split) || !driver_fn("cuDevResourceGenerateDesc", &make_desc) ||
+      !driver_fn("cuGreenCtxCreate", &green_create) || !driver_fn("cuGreenCtxDestroy", &s->green_destroy) ||
+      !driver_fn("cuGreenCtxStreamCreate", &s->green_stream))
+    return pk::set_error(PK_ERR_CUDA, "SM partitions: the driver has no green-context entry points");
+  CUdevice dev = 0;
+  CUdevResource all{}, part{}, rest{};
+  unsigned int groups = 1;
+  CUdevResourceDesc d_small = nullptr, d_large = nullptr;
+  CUresult r = device_get(&dev, s->ctx->device);
+  if (r == CUDA_SUCCESS) r = get_resource(dev, &all, CU_DEV_RESOURCE_TYPE_SM);
+  if (r == CUDA_SUCCESS && (unsigned)small_sms >= all.sm.smCount)
+    return pk::set_error(PK_ERR_INVALID, "small_sms must be below the device's " +
+                                             std::to_string(all.sm.smCount) + " SMs");
+  if (r == CUDA_SUCCESS) r = split(&part, &groups, &all, &rest, 0, (unsigned)small_sms);
+  if (r == CUDA_SUCCESS && (groups != 1 || rest.sm.smCount == 0)) r = CUDA_ERROR_INVALID_VALUE;
+  if (r == CUDA_SUCCESS) r = make_desc(&d_small, &part, 1);
+  if (r == CUDA_SUCCESS) r = make_desc(&d_large, &rest, 1);
+  if (r == CUDA_SUCCESS) r = green_create(&s->g_small, d_small, dev, CU_GREEN_CTX_DEFAULT_STREAM);
+  if (r == CUDA_SUCCESS) r = green_create(&s->g_large, d_large, dev, CU_GREEN_CTX_DEFAULT_STREAM);
+  if (r != CUDA_SUCCESS) {
+    if (s->g_small) s->green_destroy(s->g_small);
+    if (s->g_large) s->green_destroy(s->g_large);
+    s->g_small = s->g_large = nullptr;
+    return pk::set_error(PK_ERR_CUDA, "SM partitions: driver error " + std::to_string((int)r));
+  }
+  s->sms_small = (int)part.sm.smCount;
+  s->sms_large = (int)rest.sm.smCount;
+  return PK_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 uint64_t pk_request_footprint(const pk_request* req) { return req ? footprint(*req) : 0; }
@@ -479,6 +552,7 @@ pk_status pk_server_create_config(pk_ctx* ctx, int32_t workers, const pk_server_
   if (cfg) c = *cfg;
   if (c.reserved_small < 0 || c.reserved_small >= workers)
     return pk::set_error(PK_ERR_INVALID, "reserved_small must be in 0..workers-1");
+  if (c.small_sms < 0) return pk::set_error(PK_ERR_INVALID, "small_sms must be >= 0");
   uint64_t used = 0, budget = 0;
   pk_status st = pk_ctx_memory(ctx, &used, &budget);
   if (st != PK_OK) return st;
@@ -487,6 +561,14 @@ pk_status pk_server_create_config(pk_ctx* ctx, int32_t workers, const pk_server_
   s->budget = budget;
   s->workers = workers;
   s->cfg = c;
+  if (c.small_sms > 0) {
+    pk::set_device(ctx);
+    const pk_status ps = make_partition(s, c.small_sms);
+    if (ps != PK_OK) {
+      delete s;
+      return ps;
+    }
+  }
   for (int i = 0; i < workers; i++) s->threads.emplace_back(worker_main, s, i < c.reserved_small);
   *out = s;
   return PK_OK;
@@ -508,6 +590,8 @@ void pk_server_destroy(pk_server* s) {
   for (auto& t : s->threads) t.join();
   for (auto& kv : s->reqs) free_request(s, kv.second);
   for (pk_job* j : s->spare) pk_job_destroy(j);
+  if (s->g_small) s->green_destroy(s->g_small);
+  if (s->g_large) s->green_destroy(s->g_large);
   delete s;
 }
 
@@ -654,6 +738,13 @@ pk_status pk_server_get_stats(pk_server* s, pk_server_stats* out) {
   std::lock_guard<std::mutex> lk(s->mu);
   *out = s->st;
   out->pin_ns = s->pin_ns.load();
+  return PK_OK;
+}
+
+pk_status pk_server_partition(pk_server* s, int32_t* small_sms, int32_t* large_sms) {
+  if (!s || !small_sms || !large_sms) return pk::set_error(PK_ERR_INVALID, "null argument");
+  *small_sms = s->g_small ? s->sms_small : s->ctx->sms;
+  *large_sms = s->g_small ? s->sms_large : s->ctx->sms;
   return PK_OK;
 }
 

@@ -82,7 +82,8 @@ def test_serving_structs_and_footprint(lib):
     assert ctypes.sizeof(capi.PkServerConfig) == 8 + 4 + 4 + 4 * 4
     cfg = capi.PkServerConfig()
     lib.pk_server_config_default(ctypes.byref(cfg), 8)
-    assert (cfg.small_bytes, cfg.reserved_small, cfg.aging_ms) == (32 << 20, 1, 2000)
+    assert (cfg.small_bytes, cfg.reserved_small, cfg.aging_ms, cfg.small_sms) == (32 << 20, 1, 2000, 0)
+    assert lib.pk_server_partition(None, None, None) == capi.PK_ERR_INVALID
     assert lib.pk_cancel(None, 1) == capi.PK_ERR_INVALID
     assert lib.pk_result_job(None, 1, None) == capi.PK_ERR_INVALID
     assert capi.status_string(capi.PK_ERR_CANCELLED) == "cancelled"

@@ -210,3 +210,34 @@ def test_next_done_hands_out_every_request_once_in_completion_order():
         assert ends == sorted(ends)
         with pytest.raises(pk.capi.Busy):
             srv.next_done(timeout=0.05)
+
+
+def test_sm_partition_for_small_requests():
+    """With small_sms the device is split into two SM partitions (green contexts): small
+    requests run on their own SMs, the others on the rest, and every result still equals
+    the read set run alone (results copied out and kept on the device alike)."""
+    cases = _mix()
+    alone = [run_gpu(f, k, t, cov) for f, k, t, cov in cases]
+    with pk.Server(ctx(), workers=2) as whole:  # no partition: the device's SMs twice
+        total, again = whole.partition()
+        assert total == again and total > 16
+    try:
+        srv = pk.Server(ctx(), workers=3, small_bytes=1 << 20, small_sms=16)
+    except pk.PakmanError as ex:
+        if ex.status == pk.capi.PK_ERR_CUDA:
+            pytest.skip(f"SM partitions unavailable here: {ex}")
+        raise
+    with srv:
+        small, large = srv.partition()
+        assert small >= 16 and large > 0
+        assert small + large <= total
+        tickets = [srv.submit(f, _params(k, t, cov), keep_on_device=(i % 2 == 1))
+                   for i, (f, k, t, cov) in enumerate(cases)]
+        for i, (tk, (s, _, _, _, mn, err)) in enumerate(zip(tickets, alone)):
+            info = srv.wait(tk)
+            assert info.status == 0
+            assert (info.summary.n_windows, info.summary.n_unique, info.summary.cutoff, info.summary.n_nodes) == \
+                (s.n_windows, s.n_unique, s.cutoff, s.n_nodes)
+            if i % 2 == 0:
+                assert_mn_equal(srv.result(tk), pk.to_key128(mn.keys), mn.suffix_counts, mn.prefix_counts)
+            srv.release(tk)
