@@ -692,7 +692,9 @@ def run_batch(args, rank, world):
                                                     read_length=rs.read_len)))
     t_gen = time.perf_counter() - t_gen
     ctx = pk.Context(0)
-    batch = pk.Batch(ctx, branches=args.batch_branches)
+    # device value: the sets copied before the graph, so the launch runs with its inputs
+    # in HBM
+    batch = pk.Batch(ctx, branches=args.batch_branches, input_in_graph=False)
     res = batch.run(sets)  # autotune + capture + first launch
     st0 = batch.stats()
     windows = sum(r.summary.n_windows for r in res)
@@ -703,6 +705,14 @@ def run_batch(args, rank, world):
     for _ in range(args.steps):
         res = batch.run(sets)
         graph_ms.append(batch.stats()["last_graph_ms"])
+    wall_before = (time.perf_counter() - t0) / args.steps
+    # end to end: the graph copies each pinned set itself, overlapping other branches
+    batch.set_input_in_graph(True)
+    for _ in range(max(1, args.warmup)):
+        batch.run(sets)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = batch.run(sets)
     wall = (time.perf_counter() - t0) / args.steps
     keys, suf, pre = batch.table()
     st = batch.stats()
@@ -764,7 +774,9 @@ def run_batch(args, rank, world):
             "tuned_shapes": tuned_shapes,
             "e2e": {"value": windows / wall, "unit": "k-mers/s", "ms_per_step": 1000 * wall,
                     "h2d_bytes_per_step": total_bytes,
-                    "note": "pk_batch_run: host input copy, graph launch, per-set results (table copy separate)"},
+                    "note": "pk_batch_run from pinned host buffers: the graph copies each set on its branch "
+                            "ahead of its kernels, per-set results (table copy separate)",
+                    "copied_before_the_graph": {"value": windows / wall_before, "ms_per_step": 1000 * wall_before}},
             "plain_one_job_at_a_time": {"kmers_per_s": windows / (min(plain_ms) / 1000.0),
                                         "ms": min(plain_ms)},
             "statuses": {str(s): sum(1 for r in res if r.status == s) for s in set(r.status for r in res)},

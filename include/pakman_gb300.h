@@ -517,6 +517,15 @@ pk_status pk_batch_run(pk_batch* b, const pk_batch_set* sets, int32_t n_sets, pk
 pk_status pk_batch_copy_macro_nodes(pk_batch* b, void* keys, uint32_t* suffix_counts,
                                     uint32_t* prefix_counts, uint64_t capacity);
 pk_status pk_batch_get_stats(pk_batch* b, pk_batch_stats* out);
+/* Where the sets' inputs are copied to the device.  PK_BATCH_INPUT_IN_GRAPH (the
+ * default): when every set's FASTA is in page-locked host memory, the graph copies each
+ * set itself, on the set's branch ahead of its kernels, so the copies overlap the other
+ * branches' work (the graph reads the host buffers at every launch; new buffers
+ * recapture it); otherwise, as with PK_BATCH_INPUT_BEFORE, all sets are copied before
+ * the graph is launched. */
+#define PK_BATCH_INPUT_IN_GRAPH 0
+#define PK_BATCH_INPUT_BEFORE 1
+pk_status pk_batch_set_input_mode(pk_batch* b, int32_t mode);
 /* Autotuned partition digits for a set of this size and k (0 if not tuned yet). */
 int32_t pk_batch_tuned_bits(pk_batch* b, uint64_t fasta_bytes, int32_t k);
 /* The whole tuned launch shape of that size class: partition digits, counting/scatter

@@ -674,13 +674,20 @@ class Batch:
     graph is captured on the first run of a batch shape and replayed while the shape
     stays the same; partition digits are autotuned per size class."""
 
-    def __init__(self, ctx: Context, branches: int = 4):
+    def __init__(self, ctx: Context, branches: int = 4, input_in_graph: bool = True):
+        """`input_in_graph`: when every set is in page-locked host memory the graph copies
+        each set itself, overlapping the other branches' work (pk_batch_set_input_mode)."""
         self.ctx = ctx
         h = c_void_p()
         check(capi.lib().pk_batch_create(ctx.handle, branches, byref(h)), "pk_batch_create")
         self._h = h
         self._keep = None
         self._k = 32
+        self.set_input_in_graph(input_in_graph)
+
+    def set_input_in_graph(self, on: bool):
+        mode = capi.PK_BATCH_INPUT_IN_GRAPH if on else capi.PK_BATCH_INPUT_BEFORE
+        check(capi.lib().pk_batch_set_input_mode(self._h, mode), "pk_batch_set_input_mode")
 
     def run(self, sets) -> list:
         """`sets`: sequence of (fasta, params).  Returns one BatchResult per set."""

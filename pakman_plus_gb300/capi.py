@@ -29,6 +29,10 @@ PK_ERR_NO_DEVICE = 10
 PK_ERR_IO = 11
 PK_ERR_CANCELLED = 12
 
+# pk_batch_set_input_mode
+PK_BATCH_INPUT_IN_GRAPH = 0
+PK_BATCH_INPUT_BEFORE = 1
+
 
 class PkParams(ctypes.Structure):
     _fields_ = [("k", c_int32), ("lmer_length", c_int32), ("num_buckets", c_int32),
@@ -192,6 +196,7 @@ _SIGS = {
     "pk_cancel": (c_int, [c_void_p, c_uint64]),
     "pk_server_cache_release": (None, []),
     "pk_server_partition": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_int32)]),
+    "pk_batch_set_input_mode": (c_int, [c_void_p, c_int32]),
     "pk_next_done": (c_int, [c_void_p, ctypes.c_int64, POINTER(c_uint64), POINTER(PkRequestInfo)]),
     "pk_result_job": (c_int, [c_void_p, c_uint64, POINTER(c_void_p)]),
     "pk_server_destroy": (None, [c_void_p]),

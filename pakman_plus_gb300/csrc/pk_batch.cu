@@ -38,6 +38,7 @@ struct SetPlan {
   pk_params params{};
   int branch = 0;
   bool in_graph = true;  // false: too large for the graph bounds, run on its own
+  const void* host = nullptr;  // the set's FASTA in host memory
 };
 
 struct HostTable {      // rows of sets run on their own
@@ -75,6 +76,8 @@ struct pk_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<uint64_t> signature;      // shape of the captured batch
+  bool copy_in_graph = false;           // the graph copies each set's input itself
+  int input_mode = PK_BATCH_INPUT_IN_GRAPH;
   std::vector<SetPlan> plan;
   std::vector<Scalars> h_scal;
   std::vector<unsigned long long> h_res;
@@ -211,7 +214,8 @@ pk_status time_set(pk_job* j, const void* d_fasta, uint64_t bytes, const pk_para
 // digits, on the class's largest set: first the partition digits (the fastest of the
 // automatic choice and its two neighbours), then with those the chunk size (one or two
 // times the one-chunk-per-SM size) and the table CTAs per SM (one or two).
-pk_status autotune(pk_batch* b, const std::vector<SetPlan>& plan) {
+// size classes not tuned yet -> their largest set
+std::map<std::pair<int, int>, int> untuned(const pk_batch* b, const std::vector<SetPlan>& plan) {
   std::map<std::pair<int, int>, int> largest;  // class -> set index
   for (size_t i = 0; i < plan.size(); i++) {
     if (plan[i].params.bucket_bits || !plan[i].in_graph) continue;
@@ -220,6 +224,11 @@ pk_status autotune(pk_batch* b, const std::vector<SetPlan>& plan) {
     auto it = largest.find(key);
     if (it == largest.end() || plan[it->second].bytes < plan[i].bytes) largest[key] = (int)i;
   }
+  return largest;
+}
+
+pk_status autotune(pk_batch* b, const std::vector<SetPlan>& plan) {
+  const std::map<std::pair<int, int>, int> largest = untuned(b, plan);
   if (largest.empty()) return PK_OK;
   const auto t0 = std::chrono::steady_clock::now();
   pk_job* j = b->solo;
@@ -309,7 +318,14 @@ pk_status capture(pk_batch* b) {
     j->ncap = sp.bytes;
     j->d_sc = scal + i;
     apply(j, shape_for(b, sp.params, sp.bytes));
-    st = count_impl(j, (const char*)b->input.p + sp.off, sp.bytes, &sp.params);
+    if (b->copy_in_graph && sp.bytes) {
+      // the set's input, on its branch ahead of its kernels: other branches compute
+      // meanwhile
+      cudaError_t e = cudaMemcpyAsync((char*)b->input.p + sp.off, sp.host, sp.bytes, cudaMemcpyHostToDevice,
+                                      j->stream);
+      if (e != cudaSuccess) st = set_error(PK_ERR_CUDA, std::string("batch input copy: ") + cudaGetErrorString(e));
+    }
+    if (st == PK_OK) st = count_impl(j, (const char*)b->input.p + sp.off, sp.bytes, &sp.params);
     if (st == PK_OK) st = cutoff_enqueue(j, sp.params.num_buckets);
     if (st == PK_OK) st = mn_enqueue(j, 0, b->vcap[sp.branch]);
     if (st == PK_OK) {
@@ -450,16 +466,29 @@ pk_status pk_batch_run(pk_batch* b, const pk_batch_set* sets, int32_t n, pk_batc
     plan[i].bytes = sets[i].fasta_bytes;
     plan[i].params = sets[i].params;
     plan[i].in_graph = sets[i].fasta_bytes > 0 && sets[i].fasta_bytes < (1ull << 32) - 1;
+    plan[i].host = sets[i].fasta;
     off += (sets[i].fasta_bytes + kAlign - 1) / kAlign * kAlign;
     out_rows += kept_cap(sets[i].fasta_bytes) / 2;
   }
-  // ---- input to the device (outside the graph)
+  // ---- input to the device.  When every set is in page-locked host memory the graph
+  //      copies each set itself, on the set's branch ahead of its kernels, so the copies
+  //      overlap the other branches' work; otherwise (and for the size classes still to
+  //      be tuned, which are timed on their largest set) the sets are copied first.
   PK_TRY(dev_alloc(b->ctx, b->input, off + kAlign, b->origin));
-  for (int i = 0; i < n; i++)
-    if (sets[i].fasta_bytes)
-      PK_CUDA(cudaMemcpyAsync((char*)b->input.p + plan[i].off, sets[i].fasta, sets[i].fasta_bytes,
-                              cudaMemcpyHostToDevice, b->origin));
-  PK_CUDA(cudaStreamSynchronize(b->origin));
+  bool pinned = n > 0 && b->input_mode == PK_BATCH_INPUT_IN_GRAPH;
+  for (int i = 0; i < n && pinned; i++) {
+    if (!sets[i].fasta_bytes) continue;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, sets[i].fasta) != cudaSuccess || at.type != cudaMemoryTypeHost) pinned = false;
+  }
+  cudaGetLastError();
+  if (!pinned || !untuned(b, plan).empty()) {
+    for (int i = 0; i < n; i++)
+      if (sets[i].fasta_bytes)
+        PK_CUDA(cudaMemcpyAsync((char*)b->input.p + plan[i].off, sets[i].fasta, sets[i].fasta_bytes,
+                                cudaMemcpyHostToDevice, b->origin));
+    PK_CUDA(cudaStreamSynchronize(b->origin));
+  }
   // ---- autotune digit widths of new size classes, then fix every set's digits
   PK_TRY(autotune(b, plan));
   for (int i = 0; i < n; i++) plan[i].params.bucket_bits = digits_for(b, plan[i].params, plan[i].bytes);
@@ -475,14 +504,17 @@ pk_status pk_batch_run(pk_batch* b, const pk_batch_set* sets, int32_t n, pk_batc
   // ---- (re)capture when the shape changed
   std::vector<uint64_t> sig;
   sig.push_back((uint64_t)n);
+  sig.push_back(pinned ? 1 : 0);
   for (int i = 0; i < n; i++) {
     sig.push_back(plan[i].bytes);
     sig.push_back(plan[i].off);
+    if (pinned) sig.push_back((uint64_t)(uintptr_t)plan[i].host);  // the graph reads these buffers
     const uint64_t* pw = (const uint64_t*)&plan[i].params;
     for (size_t w = 0; w < sizeof(pk_params) / 8; w++) sig.push_back(pw[w]);
   }
   const bool same = b->exec && sig == b->signature;
   b->plan = plan;
+  b->copy_in_graph = pinned;
   b->out_cap = std::max<uint64_t>(1, out_rows);
   PK_TRY(dev_alloc(b->ctx, b->scal, sizeof(Scalars) * (size_t)std::max(1, n), b->origin));
   PK_TRY(dev_alloc(b->ctx, b->res, 24 * (size_t)std::max(1, n), b->origin));
@@ -549,6 +581,14 @@ pk_status pk_batch_run(pk_batch* b, const pk_batch_set* sets, int32_t n, pk_batc
       next += b->extra[i].rows;
     }
   b->st.total_nodes = next;
+  return PK_OK;
+}
+
+pk_status pk_batch_set_input_mode(pk_batch* b, int32_t mode) {
+  if (!b) return set_error(PK_ERR_INVALID, "batch is null");
+  if (mode != PK_BATCH_INPUT_IN_GRAPH && mode != PK_BATCH_INPUT_BEFORE)
+    return set_error(PK_ERR_INVALID, "unknown batch input mode");
+  b->input_mode = mode;
   return PK_OK;
 }
 
