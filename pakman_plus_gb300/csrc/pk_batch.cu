@@ -135,6 +135,7 @@ pk_status presize(pk_job* j, uint64_t fmax, int k, int bbits, int t, int sms) {
   PK_TRY(job_alloc(j, j->tile_nl, 4 * (ntiles + 1)));
   PK_TRY(job_alloc(j, j->counts, 4 * (size_t)sms * HB));
   PK_TRY(job_alloc(j, j->units, 40 * ((fmax + kSegBytes - 1) / kSegBytes)));
+  PK_TRY(job_alloc(j, j->bsmall, 4 * kSmallCounts * (size_t)B));
   PK_TRY(job_alloc(j, j->bstart, 4 * (size_t)(B + 1)));
   PK_TRY(job_alloc(j, j->hstart, 4 * (size_t)(HB + 1)));
   PK_TRY(job_alloc(j, j->keys, W * fmax));

@@ -82,7 +82,7 @@ int pk::job_buffers(pk_job* j, DevBuf** out, int cap) {
                    &j->ksub,  &j->coff,    &j->cstart,  &j->slice_start, &j->fcur, &j->wiring,
                    &j->gfirst, &j->gcount, &j->chunk_bucket, &j->gdone,
                    &j->chunk_u, &j->acc_keys[0], &j->acc_keys[1], &j->acc_counts[0], &j->acc_counts[1],
-                   &j->merge_keys, &j->merge_counts, &j->merge_part, &j->units};
+                   &j->merge_keys, &j->merge_counts, &j->merge_part, &j->units, &j->bsmall};
   const int n = (int)(sizeof(all) / sizeof(all[0]));
   for (int i = 0; i < n && i < cap; i++) out[i] = all[i];
   return n;
@@ -92,6 +92,7 @@ void pk::job_free_all(pk_job* j) {
   DevBuf* all[64];
   const int n = job_buffers(j, all, 64);
   for (int i = 0; i < n; i++) job_free(j, *all[i]);
+  j->bsmall_valid = false;
   cp_free(j);
   j->compacted = false;
   j->dense_valid = false;
@@ -493,8 +494,10 @@ static pk_status table_impl(pk_job* j, uint64_t N, int t) {
   PK_CUDA(launch_giant_chunks((const uint32_t*)j->bstart.p, j->bbits, (uint32_t*)j->gfirst.p,
                               (uint32_t*)j->gcount.p, (uint32_t*)j->chunk_bucket.p, (uint32_t*)j->gdone.p,
                               j->d_sc, j->stream));
+  PK_TRY(job_alloc(j, j->bsmall, sizeof(uint32_t) * kSmallCounts * (size_t)B));
   BucketArgs b{};
   b.keys = j->keys.p;
+  b.bsmall = (uint32_t*)j->bsmall.p;
   b.gfirst = (const uint32_t*)j->gfirst.p;
   b.gcount = (const uint32_t*)j->gcount.p;
   b.chunk_bucket = (const uint32_t*)j->chunk_bucket.p;
@@ -513,6 +516,7 @@ static pk_status table_impl(pk_job* j, uint64_t N, int t) {
   b.sc = j->d_sc;
   PK_CUDA(launch_bucket_table(b, j->wide, j->table_ctas > 0 ? j->table_ctas * thread_sms(j->ctx->sms) : 0, j->stream));
   mark_end(j, ST_TABLE);
+  j->bsmall_valid = true;
   j->pieces = 1;
   j->stage = 1;
   return PK_OK;
@@ -565,6 +569,7 @@ pk_status pk_table_load(pk_job* j, const void* keys, const uint32_t* counts, uin
   PK_TRY(check_params(p));
   if (n && (!keys || !counts)) return fail(PK_ERR_INVALID, "keys and counts must not be null");
   if (n >= 0xffffffffull) return fail(PK_ERR_LIMIT, "tables of 2^32-1 rows or more are not supported");
+  j->bsmall_valid = false;  // the loaded table did not come from the table kernel
   const int k = p->k;
   const bool wide = k > 32;
   const uint64_t* kw = (const uint64_t*)keys;
@@ -777,6 +782,7 @@ pk_status pk::mn_enqueue(pk_job* j, uint32_t min_count, uint64_t kept_bound) {
   f.ksub = (uint32_t*)j->ksub.p;
   f.cap = kcap;
   f.trows = j->tcounts.bytes / sizeof(uint32_t);
+  f.bsmall = j->bsmall_valid ? (const uint32_t*)j->bsmall.p : nullptr;
   f.k = j->params.k;
   f.bbits = j->bbits;
   f.spin_limit = (int)j->wait_limit;

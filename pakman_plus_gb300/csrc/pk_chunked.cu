@@ -304,6 +304,7 @@ pk_status pk::count_pieces(pk_job* j, const char* host, uint64_t n, const pk_par
   std::swap(j->tkeys, j->acc_keys[cur]);
   std::swap(j->tcounts, j->acc_counts[cur]);
   release_piece_buffers(j);
+  j->bsmall_valid = false;  // the merged table has no per-bucket small-count histogram
   const int k = p->k;
   int bb = p->bucket_bits;
   if (!bb) {  // about 4000 rows per bucket, as for a loaded table

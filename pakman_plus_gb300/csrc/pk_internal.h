@@ -31,6 +31,7 @@ constexpr int kTileBytes = 65536;   // line-scan tile; chunk boundaries are mult
 constexpr int kSegBytes = 64;       // bytes per thread per extraction step
 constexpr int kBucketThreads = 512;
 constexpr int kMnThreads = 128;
+constexpr int kSmallCounts = 16;    // per-bucket histogram of the table kernel: counts 0..15
 constexpr int kMnCap = 1536;        // items (k-mer records) per macro-node segment on chip
 constexpr int kMnBinBits = 8;       // counting-sort bins of a macro-node segment
 constexpr int kMnBins = 1 << kMnBinBits;
@@ -113,6 +114,7 @@ struct BucketArgs {
   const uint32_t* chunk_bucket;  // per chunk item: its bucket
   uint32_t* gdone;           // 2^bbits: chunk items of the bucket finished
   uint32_t* chunk_u;         // per chunk item: pairs it left, or kChunkRaw
+  uint32_t* bsmall;          // kSmallCounts x 2^bbits: rows of each bucket by count < kSmallCounts
   int spin_limit;            // polls of a bounded wait before it gives up (0: default)
   Scalars* sc;
 };
@@ -131,6 +133,9 @@ struct FilterArgs {
   uint32_t* ksub;            // 3 * 2^bbits
   unsigned long long cap;    // kept-row capacity
   unsigned long long trows;  // rows the table count buffer holds (reads stay below)
+  // the table kernel's rows per bucket by count below kSmallCounts (null: not known);
+  // with a cutoff <= kSmallCounts a bucket's kept rows follow from them and its row count
+  const uint32_t* bsmall;
   int k;
   int bbits;
   int spin_limit;            // polls of a bounded wait before it gives up (0: default)

@@ -1140,17 +1140,20 @@ __device__ __forceinline__ int hash_insert(KeyT* skey, uint32_t* scnt, uint32_t 
   return 2;
 }
 
-// One table row, plus its count in the count histogram (counts below t).
+// One table row, plus its count in the bucket's histogram of small counts (sbsmall, folded
+// into the count histogram when the bucket ends) or in the count histogram (counts below t).
 template <typename KeyT>
 __device__ __forceinline__ void emit_row(const BucketArgs& a, KeyT* __restrict__ tkeys, unsigned long long row,
-                                         KeyT key, uint32_t cnt, uint32_t* shist) {
+                                         KeyT key, uint32_t cnt, uint32_t* shist, uint32_t* sbsmall) {
   if (row < a.cap) {
     tkeys[row] = key;
     a.tcounts[row] = cnt;
   } else {
     atomicOr(&a.sc->err, ERR_BOUNDS);
   }
-  if (cnt < (uint32_t)a.t) {
+  if (cnt < (uint32_t)kSmallCounts) {
+    atomicAdd(&sbsmall[cnt], 1u);
+  } else if (cnt < (uint32_t)a.t) {
     if (cnt < (uint32_t)kHistSmem) atomicAdd(&shist[cnt], 1u);
     else atomicAdd(&a.hist[cnt], 1ull);
   }
@@ -1160,10 +1163,10 @@ __device__ __forceinline__ void emit_row(const BucketArgs& a, KeyT* __restrict__
 template <typename KeyT>
 __device__ void write_bucket_rows(const KeyT* sk, const uint32_t* sc, uint32_t u, const BucketArgs& a,
                                   uint32_t beta, int rem, uint32_t base, uint32_t acc,
-                                  KeyT* __restrict__ tkeys, uint32_t* shist) {
+                                  KeyT* __restrict__ tkeys, uint32_t* shist, uint32_t* sbsmall) {
   const KeyT hi_bits = KeyOps<KeyT>::shl((KeyT)beta, rem);
   for (uint32_t i = threadIdx.x; i < u; i += kBucketThreads)
-    emit_row<KeyT>(a, tkeys, (unsigned long long)base + acc + i, hi_bits | sk[i], sc[i], shist);
+    emit_row<KeyT>(a, tkeys, (unsigned long long)base + acc + i, hi_bits | sk[i], sc[i], shist, sbsmall);
 }
 
 // Chunk items of the giant buckets (one thread per bucket): a bucket of at least
@@ -1346,6 +1349,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   __shared__ KeyT s_stk_hi[kBucketStack];
   __shared__ KeyT s_split[kSplitWays];
   __shared__ float s_ratio;
+  __shared__ uint32_t s_bsmall[kSmallCounts];  // the current bucket's rows by small count
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int B = 1 << a.bbits;
@@ -1357,6 +1361,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
   KeyT* __restrict__ tkeys = reinterpret_cast<KeyT*>(a.tkeys);
   const int hbins = a.t < kHistSmem ? a.t : kHistSmem;
   for (int i = tid; i < hbins; i += kBucketThreads) shist[i] = 0;
+  if (tid < kSmallCounts) s_bsmall[tid] = 0;
   // running distinct/keys ratio of this CTA's buckets; read sets at 20x-80x coverage
   // with sub-percent errors start near 0.2 (a high guess splits the first buckets
   // needlessly, a low one costs one overflowing pass)
@@ -1423,6 +1428,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
     if (tid == 0) s_fail = 0;
     if (n == 0) {
       if (tid == 0) a.tu[beta] = 0;
+      if (tid < kSmallCounts && a.bsmall) a.bsmall[(size_t)beta * kSmallCounts + tid] = 0;
       continue;
     }
     // a giant bucket reads its chunks' pairs (or keys, where a chunk stayed raw) and the
@@ -1636,7 +1642,8 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
             const uint32_t b0 = bh[bi], b1 = b0 + bf[bi];
             uint32_t rank = 0;
             for (uint32_t j = b0; j < b1; j++) rank += skey[j] < x;
-            emit_row<KeyT>(a, tkeys, (unsigned long long)base + acc + b0 + rank, hi_bits | x, scnt[i], shist);
+            emit_row<KeyT>(a, tkeys, (unsigned long long)base + acc + b0 + rank, hi_bits | x, scnt[i], shist,
+                           s_bsmall);
           }
         } else {
           // stable LSD radix sort of the binned run in [0, u) through [H/2, H/2 + u)
@@ -1716,7 +1723,7 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
             KeyT* tk = sk; sk = dk; dk = tk;
             uint32_t* tc = sc; sc = dc; dc = tc;
           }
-          write_bucket_rows<KeyT>(sk, sc, u, a, beta, rem, base, acc, tkeys, shist);
+          write_bucket_rows<KeyT>(sk, sc, u, a, beta, rem, base, acc, tkeys, shist, s_bsmall);
         }
       }
       acc += u;
@@ -1727,6 +1734,15 @@ __global__ void __launch_bounds__(kBucketThreads, 2) k_bucket_table(BucketArgs a
       acc = 0;
     }
     __syncthreads();
+    // the bucket's rows by small count: stored for the kept filter and folded into the
+    // count histogram (counts below t); zeroed for the next bucket, whose rows come after
+    // the barrier at the top of the loop
+    if (tid < kSmallCounts) {
+      const uint32_t c = s_bsmall[tid];
+      if (a.bsmall) a.bsmall[(size_t)beta * kSmallCounts + tid] = c;
+      if (c && tid < a.t) atomicAdd(&shist[tid], c);
+      s_bsmall[tid] = 0;
+    }
     if (tid == 0) {
       a.tu[beta] = acc;
       atomicAdd(&a.sc->n_unique, (unsigned long long)acc);
@@ -1892,11 +1908,18 @@ __global__ void __launch_bounds__(256) k_filter_kept(FilterArgs a) {
     const uint32_t r0 = a.bstart[beta], e = r0 + a.tu[beta];
     const uint32_t g0 = r0 & ~3u;
     uint32_t v = 0;
-    for (uint32_t g = g0; g < e; g += 128) {
-      uint32_t c[4];
-      v += __popc(kept_group(a, g + 4 * lane, r0, e, cut, c));
+    if (a.bsmall && cut <= (uint32_t)kSmallCounts) {
+      // kept rows = the bucket's rows minus those counted fewer than cut times
+      uint32_t below = (lane >= 1 && (uint32_t)lane < cut) ? a.bsmall[(size_t)beta * kSmallCounts + lane] : 0u;
+      below = __reduce_add_sync(FULLMASK, below);
+      v = (e - r0) - below;
+    } else {
+      for (uint32_t g = g0; g < e; g += 128) {
+        uint32_t c[4];
+        v += __popc(kept_group(a, g + 4 * lane, r0, e, cut, c));
+      }
+      v = __reduce_add_sync(FULLMASK, v);
     }
-    v = __reduce_add_sync(FULLMASK, v);
     if (lane == 0) st_release(&a.flags[beta], kLbAgg | (unsigned long long)v);
     __syncwarp();
     unsigned long long K = lookback_exclusive(a.flags, (int)beta, &a.sc->err, a.spin_limit);

@@ -82,7 +82,9 @@ struct pk_job {
   DevBuf fasta, tile_nl, counts, bstart, hstart, keys, tkeys, tcounts, tu, flags_m, hist, hist2,
       nkeys, nsuf, npre, packed, doff, dkeys, dcounts, flags_f, kkeys, kcounts, kstart, kcount, ksub,
       coff, cstart, slice_start, fcur, wiring, gfirst, gcount, chunk_bucket, gdone, chunk_u,
-      units;  // packed units of the counting pass, rolled again by the coarse scatter
+      units,   // packed units of the counting pass, rolled again by the coarse scatter
+      bsmall;  // rows of each table bucket by count below kSmallCounts (the table kernel's)
+  bool bsmall_valid = false;  // bsmall describes the current table
   // counting in pieces (pk_chunked.cu): the accumulated table (ping-pong) and the merge
   DevBuf acc_keys[2], acc_counts[2], merge_keys, merge_counts, merge_part;
   uint32_t pieces = 0;  // pieces the last count used (1: the whole input at once)
