@@ -11,8 +11,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <mutex>
-
 #include "../../include/pakman_gb300.h"
 #include "pk_internal.h"
 
@@ -21,10 +19,6 @@ namespace {
 // Histogram bins shared by every call in the process.  Any GPU that loads this
 // library holds these PK_NOALLOC_MAX_BUCKETS x 8 bytes until the process exits.
 static __device__ __align__(256) unsigned long long g_noalloc_hist[PK_NOALLOC_MAX_BUCKETS];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-unsigned long long* g_hist_addr[kMaxDevices] = {};
 
 __global__ void __launch_bounds__(256) k_noalloc_clear(unsigned long long* h, int t) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < t; i += gridDim.x * blockDim.x) h[i] = 0;
@@ -93,21 +87,12 @@ extern "C" pk_status pk_cutoff_noalloc(const uint32_t* d_counts, uint64_t n_rows
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return pk::set_error(PK_ERR_NO_DEVICE, cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return pk::set_error(PK_ERR_INVALID, "device index out of range");
+  // the device address of the static scratch in the current context, looked up on every
+  // call (a host-side query), so a reset or recreated context never leaves a stale
+  // address behind; host code must not use the symbol itself as a device pointer
   unsigned long long* h = nullptr;
-  {
-    // first call on this device (with it current): look up the device address of the
-    // static scratch; host code must not use the symbol itself as a device pointer
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_hist_addr[dev]) {
-      e = cudaGetSymbolAddress((void**)&g_hist_addr[dev], g_noalloc_hist);
-      if (e != cudaSuccess) {
-        g_hist_addr[dev] = nullptr;
-        return pk::set_error(PK_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      }
-    }
-    h = g_hist_addr[dev];
-  }
+  e = cudaGetSymbolAddress((void**)&h, g_noalloc_hist);
+  if (e != cudaSuccess) return pk::set_error(PK_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
   cudaStream_t st = (cudaStream_t)stream;
   pk::note_launch(), k_noalloc_clear<<<(num_buckets + 255) / 256, 256, 0, st>>>(h, num_buckets);
   const uint64_t blocks = (n_rows + 255) / 256;  // clamped before narrowing
