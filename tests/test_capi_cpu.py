@@ -84,6 +84,9 @@ def test_serving_structs_and_footprint(lib):
     lib.pk_server_config_default(ctypes.byref(cfg), 8)
     assert (cfg.small_bytes, cfg.reserved_small, cfg.aging_ms, cfg.small_sms) == (32 << 20, 1, 2000, 0)
     assert lib.pk_server_partition(None, None, None) == capi.PK_ERR_INVALID
+    # batch input modes: copies inside the graph (default) or before it
+    assert (capi.PK_BATCH_INPUT_IN_GRAPH, capi.PK_BATCH_INPUT_BEFORE) == (0, 1)
+    assert lib.pk_batch_set_input_mode(None, capi.PK_BATCH_INPUT_BEFORE) == capi.PK_ERR_INVALID
     assert lib.pk_cancel(None, 1) == capi.PK_ERR_INVALID
     assert lib.pk_result_job(None, 1, None) == capi.PK_ERR_INVALID
     assert capi.status_string(capi.PK_ERR_CANCELLED) == "cancelled"
