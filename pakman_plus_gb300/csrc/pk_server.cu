@@ -322,19 +322,24 @@ void worker_main(pk_server* s, bool small_only) {
   cudaSetDevice(s->ctx->device);
   cudaDeviceGetStreamPriorityRange(&least, &greatest);
   cudaStream_t st_hi = nullptr, st_lo = nullptr;
+  pk_status cs = PK_OK;
+  std::string cs_msg;
   if (s->g_small) {
     // small requests on the small partition's SMs, the others on the rest
-    s->green_stream(&st_hi, s->g_small, CU_STREAM_NON_BLOCKING, greatest);
-    s->green_stream(&st_lo, s->g_large, CU_STREAM_NON_BLOCKING, least);
+    if (s->green_stream(&st_hi, s->g_small, CU_STREAM_NON_BLOCKING, greatest) != CUDA_SUCCESS ||
+        s->green_stream(&st_lo, s->g_large, CU_STREAM_NON_BLOCKING, least) != CUDA_SUCCESS) {
+      cs = PK_ERR_CUDA;
+      cs_msg = "a stream on an SM partition";
+    }
   } else {
     cudaStreamCreateWithPriority(&st_hi, cudaStreamNonBlocking, greatest);
     cudaStreamCreateWithPriority(&st_lo, cudaStreamNonBlocking, least);
   }
   pk_job* job_hi = nullptr;
   pk_job* job_lo = nullptr;
-  pk_status cs = pk_job_create(s->ctx, st_hi, &job_hi);
+  if (cs == PK_OK) cs = pk_job_create(s->ctx, st_hi, &job_hi);
   if (cs == PK_OK) cs = pk_job_create(s->ctx, st_lo, &job_lo);
-  const std::string cs_msg = cs == PK_OK ? std::string() : std::string(pk_last_error());
+  if (cs != PK_OK && cs_msg.empty()) cs_msg = pk_last_error();
   while (true) {
     Request* q = nullptr;
     {
